@@ -1,0 +1,400 @@
+"""ctypes loader for the CPU oracle -- TEST INFRASTRUCTURE ONLY.
+
+Only tests/, ``__graft_entry__.smoke()`` and bench.py's CPU-baseline leg import
+this module; the product package never does.  Two libraries sit behind it:
+
+* ``liboracle.so`` -- the plain-C restatement (pmmc_oracle.c) of the
+  reference's CPU annealers, arc marking and HCM lines;
+* ``_ref/libpmmc_ref.so`` -- the reference's own CPU code (built from its
+  sources by oracle/Makefile, present only where the reference tree exists).
+
+Arrays are numpy; positions are (n, 3) float32.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+from dataclasses import dataclass, field
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "liboracle.so")
+REF_PATH = os.path.join(HERE, "_ref", "libpmmc_ref.so")
+
+RNG_LIBC = 0
+RNG_PHILOX = 1
+
+
+class OrcParams(C.Structure):
+    _fields_ = [
+        ("max_temp", C.c_float),
+        ("dt_temp", C.c_float),
+        ("jump_scale", C.c_float),
+        ("jump_coef", C.c_float),
+        ("improvement", C.c_float),
+        ("min_successes", C.c_int),
+        ("milestone_steps", C.c_int),
+        ("k_stretch", C.c_float),
+        ("k_squeeze", C.c_float),
+        ("k_angle", C.c_float),
+        ("w_dist", C.c_float),
+        ("w_angle", C.c_float),
+        ("sphere_radius", C.c_float),
+        ("use2d", C.c_int),
+        ("max_moves", C.c_int64),
+    ]
+
+
+class OrcRng(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int),
+        ("seed", C.c_uint64),
+        ("chain", C.c_uint32),
+        ("move", C.c_uint64),
+    ]
+
+
+class OrcResult(C.Structure):
+    _fields_ = [
+        ("score", C.c_double),
+        ("moves", C.c_int64),
+        ("accepted", C.c_int64),
+        ("proposals", C.c_int64),
+    ]
+
+
+@dataclass
+class Params:
+    """Annealing parameters with the reference's Settings defaults
+    (src/include/Settings.hpp:479-505)."""
+
+    max_temp: float = 20.0
+    dt_temp: float = 0.99995
+    jump_scale: float = 50.0
+    jump_coef: float = 20.0
+    improvement: float = 0.995
+    min_successes: int = 5
+    milestone_steps: int = 10000
+    k_stretch: float = 1.0
+    k_squeeze: float = 1.0
+    k_angle: float = 0.1
+    w_dist: float = 1.0
+    w_angle: float = 1.0
+    sphere_radius: float = 0.0
+    use2d: int = 0
+    max_moves: int = 0
+
+    def c(self) -> OrcParams:
+        return OrcParams(*[getattr(self, f[0]) for f in OrcParams._fields_])
+
+
+def build() -> None:
+    """Compile liboracle.so (and _ref when the reference tree exists)."""
+    subprocess.run(["make", "-C", HERE, "-s"], check=True)
+
+
+def _p(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def _u8(a):
+    return None if a is None else np.ascontiguousarray(a, dtype=np.uint8)
+
+
+_lib = None
+_ref = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            build()
+        L = C.CDLL(LIB_PATH)
+        v = C.c_void_p
+        L.orc_arcs_full_score.restype = C.c_double
+        L.orc_arcs_spring_score.restype = C.c_double
+        L.orc_arcs_repulsion.restype = C.c_double
+        L.orc_arcs_local_score.restype = C.c_double
+        L.orc_heatmap_score.restype = C.c_double
+        L.orc_smooth_full_score.restype = C.c_double
+        L.orc_smooth_local_score.restype = C.c_double
+        L.orc_u01.restype = C.c_float
+        L.orc_u01.argtypes = [C.c_uint32]
+        for name in ("orc_arcs_full_score", "orc_arcs_spring_score",
+                     "orc_arcs_local_score", "orc_arcs_anneal"):
+            pass
+        _lib = L
+        del v
+    return _lib
+
+
+def ref_available() -> bool:
+    return os.path.exists(REF_PATH)
+
+
+def ref():
+    global _ref
+    if _ref is None:
+        if not os.path.exists(REF_PATH):
+            raise FileNotFoundError(REF_PATH)
+        R = C.CDLL(REF_PATH)
+        R.ref_arcs_score.restype = C.c_double
+        R.ref_heatmap_score.restype = C.c_double
+        R.ref_smooth_score.restype = C.c_double
+        _ref = R
+    return _ref
+
+
+# ---------------------------------------------------------------------------
+# Problems
+# ---------------------------------------------------------------------------
+@dataclass
+class ArcsProblem:
+    """One arc-level active region in the reference layout: positions, fixed
+    flags, the dense n x n expected-distance matrix (-1 = no arc, 0 on the
+    diagonal) and loop constraints (cluster_i, cluster_j, stiffness, r0)."""
+
+    pos: np.ndarray
+    exp_dist: np.ndarray
+    fixed: np.ndarray | None = None
+    loops_i: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    loops_j: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    loops_k: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
+    loops_r0: np.ndarray = field(default_factory=lambda: np.zeros(0, np.float32))
+
+    @property
+    def n(self):
+        return int(self.pos.shape[0])
+
+    def loop_args(self):
+        return (len(self.loops_i), _p(_i32(self.loops_i)), _p(_i32(self.loops_j)),
+                _p(_f32(self.loops_k)), _p(_f32(self.loops_r0)))
+
+
+def _loops(pr):
+    li, lj, lk, lr = _i32(pr.loops_i), _i32(pr.loops_j), _f32(pr.loops_k), _f32(pr.loops_r0)
+    return (len(li), _p(li), _p(lj), _p(lk), _p(lr)), (li, lj, lk, lr)
+
+
+def arcs_full(pr: ArcsProblem, prm: Params, pos=None, repulsion=True) -> float:
+    pos = _f32(pr.pos if pos is None else pos)
+    ed = _f32(pr.exp_dist)
+    la, keep = _loops(pr)
+    f = lib().orc_arcs_full_score if repulsion else lib().orc_arcs_spring_score
+    return f(pr.n, _p(pos), _p(ed), *la, C.byref(prm.c()))
+
+
+def arcs_repulsion(pr: ArcsProblem, pos=None) -> float:
+    pos = _f32(pr.pos if pos is None else pos)
+    return lib().orc_arcs_repulsion(pr.n, _p(pos), _p(_f32(pr.exp_dist)))
+
+
+def arcs_local(pr: ArcsProblem, prm: Params, moved: int, pos=None) -> float:
+    pos = _f32(pr.pos if pos is None else pos)
+    ed = _f32(pr.exp_dist)
+    la, keep = _loops(pr)
+    return lib().orc_arcs_local_score(pr.n, _p(pos), _p(ed), *la, C.byref(prm.c()),
+                                      int(moved))
+
+
+def arcs_anneal(pr: ArcsProblem, prm: Params, step: float, seed: int,
+                rng=RNG_LIBC, chain=0):
+    pos = _f32(pr.pos).copy()
+    ed = _f32(pr.exp_dist)
+    fx = _u8(pr.fixed)
+    la, keep = _loops(pr)
+    r = OrcRng(rng, seed, chain, 0)
+    res = OrcResult()
+    lib().orc_arcs_anneal(pr.n, _p(pos), _p(fx), _p(ed), *la, C.byref(prm.c()),
+                          C.c_float(step), C.byref(r), C.byref(res))
+    return pos, res
+
+
+def ref_arcs_anneal(pr: ArcsProblem, prm: Params, step: float, seed: int):
+    pos = _f32(pr.pos).copy()
+    ed = _f32(pr.exp_dist)
+    fx = _u8(pr.fixed)
+    la, keep = _loops(pr)
+    sc = C.c_double()
+    mv = C.c_longlong()
+    ref().ref_arcs_anneal(pr.n, _p(pos), _p(fx), _p(ed), *la, C.byref(prm.c()),
+                          C.c_float(step), C.c_uint(seed), C.byref(sc), C.byref(mv))
+    return pos, sc.value, mv.value
+
+
+def ref_arcs_score(pr: ArcsProblem, prm: Params, moved: int, pos=None) -> float:
+    pos = _f32(pr.pos if pos is None else pos)
+    ed = _f32(pr.exp_dist)
+    la, keep = _loops(pr)
+    return ref().ref_arcs_score(pr.n, _p(pos), _p(ed), *la, C.byref(prm.c()), int(moved))
+
+
+@dataclass
+class HeatmapProblem:
+    pos: np.ndarray
+    heat: np.ndarray
+    diag: int = 1
+    bounds: np.ndarray = field(default_factory=lambda: np.zeros(0, np.int32))
+    fixed: np.ndarray | None = None
+
+    @property
+    def n(self):
+        return int(self.pos.shape[0])
+
+
+def heatmap_score(pr: HeatmapProblem, moved=-1, pos=None) -> float:
+    pos = _f32(pr.pos if pos is None else pos)
+    b = _i32(pr.bounds)
+    return lib().orc_heatmap_score(pr.n, _p(pos), _p(_f32(pr.heat)), int(pr.diag),
+                                   len(b), _p(b), int(moved))
+
+
+def heatmap_anneal(pr: HeatmapProblem, prm: Params, step: float, seed: int,
+                   rng=RNG_LIBC, incremental=False, chain=0):
+    pos = _f32(pr.pos).copy()
+    b = _i32(pr.bounds)
+    fx = _u8(pr.fixed)
+    r = OrcRng(rng, seed, chain, 0)
+    res = OrcResult()
+    lib().orc_heatmap_anneal(pr.n, _p(pos), _p(fx), _p(_f32(pr.heat)), int(pr.diag),
+                             len(b), _p(b), C.byref(prm.c()), C.c_float(step),
+                             int(bool(incremental)), C.byref(r), C.byref(res))
+    return pos, res
+
+
+def ref_heatmap_anneal(pr: HeatmapProblem, prm: Params, step: float, seed: int):
+    pos = _f32(pr.pos).copy()
+    b = _i32(pr.bounds)
+    fx = _u8(pr.fixed)
+    sc = C.c_double()
+    mv = C.c_longlong()
+    ref().ref_heatmap_anneal(pr.n, _p(pos), _p(fx), _p(_f32(pr.heat)), int(pr.diag),
+                             len(b), _p(b), C.byref(prm.c()), C.c_float(step),
+                             C.c_uint(seed), C.byref(sc), C.byref(mv))
+    return pos, sc.value, mv.value
+
+
+def ref_heatmap_score(pr: HeatmapProblem, moved=-1, pos=None) -> float:
+    pos = _f32(pr.pos if pos is None else pos)
+    b = _i32(pr.bounds)
+    return ref().ref_heatmap_score(pr.n, _p(pos), _p(_f32(pr.heat)), int(pr.diag),
+                                   len(b), _p(b), int(moved))
+
+
+@dataclass
+class SmoothProblem:
+    pos: np.ndarray
+    dist_to_next: np.ndarray
+    fixed: np.ndarray | None = None
+
+    @property
+    def n(self):
+        return int(self.pos.shape[0])
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def smooth_full(pr: SmoothProblem, prm: Params, pos=None) -> float:
+    pos = _f32(pr.pos if pos is None else pos)
+    return lib().orc_smooth_full_score(pr.n, _p(pos), _p(_f64(pr.dist_to_next)),
+                                       C.byref(prm.c()))
+
+
+def smooth_local(pr: SmoothProblem, prm: Params, moved: int, pos=None) -> float:
+    pos = _f32(pr.pos if pos is None else pos)
+    return lib().orc_smooth_local_score(pr.n, _p(pos), _p(_f64(pr.dist_to_next)),
+                                        C.byref(prm.c()), int(moved))
+
+
+def smooth_anneal(pr: SmoothProblem, prm: Params, step: float, seed: int,
+                  rng=RNG_LIBC, chain=0):
+    pos = _f32(pr.pos).copy()
+    fx = _u8(pr.fixed)
+    r = OrcRng(rng, seed, chain, 0)
+    res = OrcResult()
+    lib().orc_smooth_anneal(pr.n, _p(pos), _p(fx), _p(_f64(pr.dist_to_next)),
+                            C.byref(prm.c()), C.c_float(step), C.byref(r), C.byref(res))
+    return pos, res
+
+
+def ref_smooth_anneal(pr: SmoothProblem, prm: Params, step: float, seed: int):
+    pos = _f32(pr.pos).copy()
+    fx = _u8(pr.fixed)
+    sc = C.c_double()
+    mv = C.c_longlong()
+    ref().ref_smooth_anneal(pr.n, _p(pos), _p(fx), _p(_f64(pr.dist_to_next)),
+                            C.byref(prm.c()), C.c_float(step), C.c_uint(seed),
+                            C.byref(sc), C.byref(mv))
+    return pos, sc.value, mv.value
+
+
+def ref_smooth_score(pr: SmoothProblem, prm: Params, moved=-1, pos=None) -> float:
+    pos = _f32(pr.pos if pos is None else pos)
+    return ref().ref_smooth_score(pr.n, _p(pos), _p(_f64(pr.dist_to_next)),
+                                  C.byref(prm.c()), int(moved))
+
+
+# ---------------------------------------------------------------------------
+# Arc marking, HCM lines, Philox
+# ---------------------------------------------------------------------------
+def _mark(fn, anchors, raw):
+    a = _i32(anchors).reshape(-1, 2)
+    r = _i32(raw).reshape(-1, 4)
+    a_s, a_e = _i32(a[:, 0]), _i32(a[:, 1])
+    r_s, r_e, r_sc, r_f = (_i32(r[:, k]) for k in range(4))
+    cap = 2 * len(r) + 8
+    out = np.zeros((cap, 7), np.int32)
+    nm = C.c_int()
+    cnt = fn(len(a), _p(a_s), _p(a_e), len(r), _p(r_s), _p(r_e), _p(r_sc), _p(r_f),
+             _p(out), cap, C.byref(nm))
+    if cnt < 0:
+        raise RuntimeError("mark_arcs output capacity exceeded")
+    return out[:cnt].copy()
+
+
+def mark_arcs(anchors, raw):
+    """anchors: (A,2) [start,end]; raw: (R,4) [start,end,score,factor] ->
+    (M,7) [start end genomic_start genomic_end score eff_score factor]."""
+    return _mark(lib().orc_mark_arcs, anchors, raw)
+
+
+def ref_mark_arcs(anchors, raw):
+    return _mark(ref().ref_mark_arcs, anchors, raw)
+
+
+def hcm_cluster_line(start, end, orient, xyz, children=(), use_ref=False) -> str:
+    buf = C.create_string_buffer(4096)
+    ch = _i32(list(children) if len(children) else [0])
+    fn = ref().ref_hcm_cluster_line if use_ref else lib().orc_hcm_cluster_line
+    fn(buf, 4096, int(start), int(end), C.c_char(orient.encode()),
+       C.c_float(xyz[0]), C.c_float(xyz[1]), C.c_float(xyz[2]), len(children), _p(ch))
+    return buf.value.decode()
+
+
+def hcm_arc_line(a7, use_ref=False) -> str:
+    buf = C.create_string_buffer(256)
+    a = _i32(a7)
+    fn = ref().ref_hcm_arc_line if use_ref else lib().orc_hcm_arc_line
+    fn(buf, 256, _p(a))
+    return buf.value.decode()
+
+
+def philox(ctr, key):
+    c = (C.c_uint32 * 4)(*ctr)
+    k = (C.c_uint32 * 2)(*key)
+    o = (C.c_uint32 * 4)()
+    lib().orc_philox4x32_10(c, k, o)
+    return [o[i] for i in range(4)]

@@ -1,0 +1,908 @@
+/*
+ * pmmc_oracle.c -- plain-C restatement of the reference's CPU annealers.
+ *
+ * TEST INFRASTRUCTURE ONLY (see pmmc_oracle.h): the checker for the CUDA
+ * path, never part of it.  Each function names the reference file:line it
+ * restates.  Types follow the reference expression by expression: vector3 is
+ * three floats (src/thirdparty/mtxlib.h:84-123) whose length() is a float
+ * (mtxlib.cpp:322), scores accumulate in double, and a float-typed
+ * subexpression such as `(v.length() - e) / e` stays float before it is
+ * widened.  Compile with -ffp-contract=off.
+ */
+#include "pmmc_oracle.h"
+
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+/* ------------------------------------------------------------------ */
+/* vector3 helpers (mtxlib.cpp:322-345, common.cpp:39-46)             */
+/* ------------------------------------------------------------------ */
+static float v_len(float x, float y, float z) {
+  float s = x * x + y * y;
+  s = s + z * z;
+  return (float)sqrt((double)s);
+}
+
+/* angle(v1, v2) = 1 - (dot(n1, n2) + 1) / 2 with both vectors normalised. */
+static float v_angle(const float a[3], const float b[3]) {
+  float ma = v_len(a[0], a[1], a[2]);
+  ma = ma > 0.0f ? 1.0f / ma : 0.0f;
+  float mb = v_len(b[0], b[1], b[2]);
+  mb = mb > 0.0f ? 1.0f / mb : 0.0f;
+  float ax = a[0] * ma, ay = a[1] * ma, az = a[2] * ma;
+  float bx = b[0] * mb, by = b[1] * mb, bz = b[2] * mb;
+  float dot = ax * bx + ay * by;
+  dot = dot + az * bz;
+  return 1.0f - (dot + 1.0f) / 2.0f;
+}
+
+/* SphericalContainer::boundaryPenalty (src/include/SphericalContainer.hpp:
+ * 109-122), centre at the origin. */
+static float sphere_pen(const float *p, float radius) {
+  float ds = p[0] * p[0] + p[1] * p[1];
+  ds = ds + p[2] * p[2];
+  float rs = radius * radius;
+  if (ds <= rs)
+    return 0.0f;
+  float d = sqrtf(ds);
+  float o = d - radius;
+  return o * o;
+}
+
+/* ------------------------------------------------------------------ */
+/* Philox4x32-10 (J. Salmon, M. Moraes, R. Dror, D. Shaw, "Parallel    */
+/* random numbers: as easy as 1, 2, 3", SC'11).                        */
+/* ------------------------------------------------------------------ */
+#define PHILOX_M0 0xD2511F53u
+#define PHILOX_M1 0xCD9E8D57u
+#define PHILOX_W0 0x9E3779B9u
+#define PHILOX_W1 0xBB67AE85u
+
+void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2],
+                       uint32_t out[4]) {
+  uint32_t c0 = ctr[0], c1 = ctr[1], c2 = ctr[2], c3 = ctr[3];
+  uint32_t k0 = key[0], k1 = key[1];
+  for (int r = 0; r < 10; ++r) {
+    uint64_t p0 = (uint64_t)PHILOX_M0 * c0;
+    uint64_t p1 = (uint64_t)PHILOX_M1 * c2;
+    uint32_t hi0 = (uint32_t)(p0 >> 32), lo0 = (uint32_t)p0;
+    uint32_t hi1 = (uint32_t)(p1 >> 32), lo1 = (uint32_t)p1;
+    c0 = hi1 ^ c1 ^ k0;
+    c1 = lo1;
+    c2 = hi0 ^ c3 ^ k1;
+    c3 = lo0;
+    k0 += PHILOX_W0;
+    k1 += PHILOX_W1;
+  }
+  out[0] = c0;
+  out[1] = c1;
+  out[2] = c2;
+  out[3] = c3;
+}
+
+float orc_u01(uint32_t x) { return (float)(x >> 8) * (1.0f / 16777216.0f); }
+
+/* ------------------------------------------------------------------ */
+/* Random-number source                                                */
+/* ------------------------------------------------------------------ */
+typedef struct {
+  orc_rng *r;
+  const int *movable; /* philox: indices of non-fixed beads */
+  int n_movable;
+  float disp_u[3];    /* philox: cached displacement draws of the move */
+} rng_ctx;
+
+/* libc draws, common.cpp:10-18: random(range) = rand() % range,
+ * random_uniform() = rand() / (float)RAND_MAX. */
+static float libc_uniform(void) { return (float)rand() / (float)RAND_MAX; }
+
+static void philox_block(const orc_rng *r, uint32_t tag, uint32_t out[4]) {
+  uint32_t ctr[4] = {(uint32_t)r->move, (uint32_t)(r->move >> 32), r->chain,
+                     tag};
+  uint32_t key[2] = {(uint32_t)r->seed, (uint32_t)(r->seed >> 32)};
+  orc_philox4x32_10(ctr, key, out);
+}
+
+/* Bead draw.  libc: rand() % size (the caller skips fixed beads as the
+ * reference does).  philox: one of the movable beads, uniformly. */
+static int draw_bead(rng_ctx *c, int size) {
+  if (c->r->kind == ORC_RNG_LIBC)
+    return rand() % size;
+  uint32_t o[4];
+  philox_block(c->r, 0u, o);
+  c->disp_u[0] = orc_u01(o[1]);
+  c->disp_u[1] = orc_u01(o[2]);
+  c->disp_u[2] = orc_u01(o[3]);
+  uint32_t k = (uint32_t)(((uint64_t)o[0] * (uint32_t)c->n_movable) >> 32);
+  return c->movable[k];
+}
+
+/* random_vector(max, in2D) (common.cpp:20-25).  GCC evaluates the vector3
+ * constructor's arguments right to left, so the first libc draw is z. */
+static void draw_disp(rng_ctx *c, float max, int in2d, float d[3]) {
+  if (c->r->kind == ORC_RNG_LIBC) {
+    if (in2d) {
+      d[2] = 0.0f;
+      d[1] = (2.0f * libc_uniform() - 1.0f) * max;
+      d[0] = (2.0f * libc_uniform() - 1.0f) * max;
+    } else {
+      d[2] = (2.0f * libc_uniform() - 1.0f) * max;
+      d[1] = (2.0f * libc_uniform() - 1.0f) * max;
+      d[0] = (2.0f * libc_uniform() - 1.0f) * max;
+    }
+    return;
+  }
+  d[0] = (2.0f * c->disp_u[0] - 1.0f) * max;
+  d[1] = (2.0f * c->disp_u[1] - 1.0f) * max;
+  d[2] = in2d ? 0.0f : (2.0f * c->disp_u[2] - 1.0f) * max;
+}
+
+/* withChance(chance) = random_uniform() < chance (common.cpp:326). */
+static int draw_chance(rng_ctx *c, float chance) {
+  if (c->r->kind == ORC_RNG_LIBC)
+    return libc_uniform() < chance;
+  uint32_t o[4];
+  philox_block(c->r, 1u, o);
+  return orc_u01(o[0]) < chance;
+}
+
+static void end_move(rng_ctx *c) {
+  if (c->r->kind == ORC_RNG_PHILOX)
+    c->r->move++;
+}
+
+static int *movable_list(int n, const unsigned char *fixed, int *cnt) {
+  int *m = (int *)malloc(sizeof(int) * (n > 0 ? n : 1));
+  int k = 0;
+  for (int i = 0; i < n; ++i)
+    if (!fixed || !fixed[i])
+      m[k++] = i;
+  *cnt = k;
+  return m;
+}
+
+static void rng_begin(rng_ctx *c, orc_rng *r, int n,
+                      const unsigned char *fixed) {
+  c->r = r;
+  c->movable = NULL;
+  c->n_movable = 0;
+  if (r->kind == ORC_RNG_LIBC) {
+    srand((unsigned)r->seed);
+  } else {
+    c->movable = movable_list(n, fixed, &c->n_movable);
+  }
+}
+
+static void rng_end(rng_ctx *c) { free((void *)c->movable); }
+
+/* ------------------------------------------------------------------ */
+/* Loop constraints: rebuildActiveLoopMap (LooperSolver.hpp:3318-3337)  */
+/* keys (min,max) in std::map order, the last constraint of a key wins. */
+/* ------------------------------------------------------------------ */
+typedef struct {
+  int a, b;
+  float k, r0;
+} loop_ent;
+
+static int loop_cmp(const void *x, const void *y) {
+  const loop_ent *p = (const loop_ent *)x, *q = (const loop_ent *)y;
+  if (p->a != q->a)
+    return p->a < q->a ? -1 : 1;
+  if (p->b != q->b)
+    return p->b < q->b ? -1 : 1;
+  return 0;
+}
+
+static loop_ent *build_loops(int n, int n_loops, const int *li, const int *lj,
+                             const float *lk, const float *lr0, int *cnt) {
+  loop_ent *e = (loop_ent *)malloc(sizeof(loop_ent) * (n_loops > 0 ? n_loops : 1));
+  int m = 0;
+  for (int c = 0; c < n_loops; ++c) {
+    int i = li[c], j = lj[c];
+    if (i < 0 || i >= n || j < 0 || j >= n)
+      continue;
+    loop_ent x;
+    x.a = i < j ? i : j;
+    x.b = i < j ? j : i;
+    x.k = lk[c];
+    x.r0 = lr0[c];
+    int found = -1;
+    for (int t = 0; t < m; ++t)
+      if (e[t].a == x.a && e[t].b == x.b)
+        found = t;
+    if (found >= 0)
+      e[found] = x; /* active_loop_map[key] = c : the later one wins */
+    else
+      e[m++] = x;
+  }
+  qsort(e, m, sizeof(loop_ent), loop_cmp);
+  *cnt = m;
+  return e;
+}
+
+static double loop_energy(const float *pos, const loop_ent *e, int m,
+                          int moved) {
+  double sc = 0.0;
+  for (int t = 0; t < m; ++t) {
+    if (moved >= 0 && e[t].a != moved && e[t].b != moved)
+      continue;
+    const float *pa = pos + 3 * e[t].a, *pb = pos + 3 * e[t].b;
+    double d = v_len(pa[0] - pb[0], pa[1] - pb[1], pa[2] - pb[2]);
+    double delta = d - e[t].r0;
+    sc += e[t].k * delta * delta;
+  }
+  return sc;
+}
+
+/* ------------------------------------------------------------------ */
+/* Arc level                                                           */
+/* ------------------------------------------------------------------ */
+/* calcScoreDistancesActiveRegion() (LooperSolver.hpp:3215-3246). */
+static double arcs_dist_full(int n, const float *pos, const float *ed,
+                             const orc_params *p, int with_springs,
+                             int with_repulsion) {
+  double sc = 0.0;
+  for (int i = 0; i < n; ++i) {
+    for (int j = i + 1; j < n; ++j) {
+      const float *a = pos + 3 * i, *b = pos + 3 * j;
+      float len = v_len(a[0] - b[0], a[1] - b[1], a[2] - b[2]);
+      float e = ed[(size_t)i * n + j];
+      if (e < 0.0f) {
+        if (with_repulsion)
+          sc += 1.0f / len;
+        continue;
+      }
+      if (e < 1e-6)
+        continue;
+      if (!with_springs)
+        continue;
+      float t = (len - e) / e;
+      double diff = t;
+      sc += diff * diff * (diff >= 0.0f ? p->k_stretch : p->k_squeeze);
+    }
+  }
+  return sc;
+}
+
+/* calcScoreDistancesActiveRegion(int) (LooperSolver.hpp:3250-3281). */
+static double arcs_dist_local(int n, const float *pos, const float *ed,
+                              const orc_params *p, int moved) {
+  double sc = 0.0;
+  const float *m = pos + 3 * moved;
+  for (int i = 0; i < n; ++i) {
+    if (i == moved)
+      continue;
+    const float *b = pos + 3 * i;
+    float e = ed[(size_t)i * n + moved];
+    if (e < 0.0f)
+      continue;
+    if (e < 1e-6)
+      continue;
+    float len = v_len(m[0] - b[0], m[1] - b[1], m[2] - b[2]);
+    float t = (len - e) / e;
+    double diff = t;
+    sc += diff * diff * (diff >= 0.0f ? p->k_stretch : p->k_squeeze);
+  }
+  return sc;
+}
+
+double orc_arcs_full_score(int n, const float *pos, const float *exp_dist,
+                           int n_loops, const int *loop_i, const int *loop_j,
+                           const float *loop_k, const float *loop_r0,
+                           const orc_params *p) {
+  int m;
+  loop_ent *e = build_loops(n, n_loops, loop_i, loop_j, loop_k, loop_r0, &m);
+  double sc = arcs_dist_full(n, pos, exp_dist, p, 1, 1) + loop_energy(pos, e, m, -1);
+  if (p->sphere_radius > 0.0f)
+    for (int k = 0; k < n; ++k)
+      sc += sphere_pen(pos + 3 * k, p->sphere_radius);
+  free(e);
+  return sc;
+}
+
+double orc_arcs_spring_score(int n, const float *pos, const float *exp_dist,
+                             int n_loops, const int *loop_i, const int *loop_j,
+                             const float *loop_k, const float *loop_r0,
+                             const orc_params *p) {
+  int m;
+  loop_ent *e = build_loops(n, n_loops, loop_i, loop_j, loop_k, loop_r0, &m);
+  double sc = arcs_dist_full(n, pos, exp_dist, p, 1, 0) + loop_energy(pos, e, m, -1);
+  if (p->sphere_radius > 0.0f)
+    for (int k = 0; k < n; ++k)
+      sc += sphere_pen(pos + 3 * k, p->sphere_radius);
+  free(e);
+  return sc;
+}
+
+double orc_arcs_repulsion(int n, const float *pos, const float *exp_dist) {
+  orc_params p;
+  memset(&p, 0, sizeof(p));
+  return arcs_dist_full(n, pos, exp_dist, &p, 0, 1);
+}
+
+double orc_arcs_local_score(int n, const float *pos, const float *exp_dist,
+                            int n_loops, const int *loop_i, const int *loop_j,
+                            const float *loop_k, const float *loop_r0,
+                            const orc_params *p, int moved) {
+  int m;
+  loop_ent *e = build_loops(n, n_loops, loop_i, loop_j, loop_k, loop_r0, &m);
+  double sc = arcs_dist_local(n, pos, exp_dist, p, moved) + loop_energy(pos, e, m, moved);
+  if (p->sphere_radius > 0.0f)
+    sc += sphere_pen(pos + 3 * moved, p->sphere_radius);
+  free(e);
+  return sc;
+}
+
+/* LooperSolver::MonteCarloArcs (LooperSolver.hpp:4670-4796).  Differences
+ * only where the reference has no counterpart: the Philox source picks among
+ * movable beads directly and keeps the pre-move position on rejection (as the
+ * CUDA kernels do) instead of subtracting the displacement back. */
+void orc_arcs_anneal(int n, float *pos, const unsigned char *fixed,
+                     const float *exp_dist, int n_loops, const int *loop_i,
+                     const int *loop_j, const float *loop_k,
+                     const float *loop_r0, const orc_params *p,
+                     float step_size, orc_rng *rng, orc_result *res) {
+  int m;
+  loop_ent *e = build_loops(n, n_loops, loop_i, loop_j, loop_k, loop_r0, &m);
+  rng_ctx c;
+  rng_begin(&c, rng, n, fixed);
+  memset(res, 0, sizeof(*res));
+
+  double T = p->max_temp, dt = p->dt_temp, tp;
+  double score_curr = arcs_dist_full(n, pos, exp_dist, p, 1, 1) + loop_energy(pos, e, m, -1);
+  if (p->sphere_radius > 0.0f)
+    for (int k = 0; k < n; ++k)
+      score_curr += sphere_pen(pos + 3 * k, p->sphere_radius);
+  double score_prev = score_curr, milestone_score = score_curr;
+  int64_t success = 0, milestone_success = 0, i = 1;
+  int philox = rng->kind == ORC_RNG_PHILOX;
+
+  if (philox && c.n_movable == 0) { /* nothing can move */
+    res->score = score_curr;
+    goto done;
+  }
+  for (;;) {
+    int pb = draw_bead(&c, n);
+    res->proposals++;
+    if (fixed && fixed[pb]) {
+      /* the reference stops the program here (error(), :4718-4719) */
+      fprintf(stderr, "oracle: cluster fixed during arcs\n");
+      res->score = score_curr;
+      res->moves = -1;
+      goto done;
+    }
+    float *q = pos + 3 * pb;
+    double lp = arcs_dist_local(n, pos, exp_dist, p, pb) + loop_energy(pos, e, m, pb);
+    if (p->sphere_radius > 0.0f)
+      lp += sphere_pen(q, p->sphere_radius);
+    float d[3], old[3] = {q[0], q[1], q[2]};
+    draw_disp(&c, step_size, p->use2d, d);
+    q[0] += d[0];
+    q[1] += d[1];
+    q[2] += d[2];
+    double lc = arcs_dist_local(n, pos, exp_dist, p, pb) + loop_energy(pos, e, m, pb);
+    if (p->sphere_radius > 0.0f)
+      lc += sphere_pen(q, p->sphere_radius);
+    score_curr = score_curr - lp + lc;
+    int ok = score_curr <= score_prev;
+    if (!ok) {
+      tp = p->jump_scale * exp(-p->jump_coef * (score_curr / score_prev) / T);
+      ok = draw_chance(&c, (float)tp);
+    }
+    if (ok) {
+      success++;
+      milestone_success++;
+    } else {
+      if (philox) {
+        q[0] = old[0];
+        q[1] = old[1];
+        q[2] = old[2];
+      } else {
+        q[0] -= d[0];
+        q[1] -= d[1];
+        q[2] -= d[2];
+      }
+      score_curr = score_prev;
+    }
+    end_move(&c);
+    T *= dt;
+    if (i % p->milestone_steps == 0) {
+      if ((score_curr > p->improvement * milestone_score &&
+           milestone_success < p->min_successes) ||
+          score_curr < 1e-5 || score_curr / milestone_score > 0.9999)
+        break;
+      milestone_score = score_curr;
+      milestone_success = 0;
+    }
+    if (p->max_moves > 0 && i >= p->max_moves)
+      break;
+    score_prev = score_curr;
+    i++;
+  }
+  res->score = score_curr;
+  res->moves = i;
+  res->accepted = success;
+done:
+  rng_end(&c);
+  free(e);
+}
+
+/* ------------------------------------------------------------------ */
+/* Heatmap level                                                       */
+/* ------------------------------------------------------------------ */
+/* getChromosomeHeatmapBoundary (LooperSolver.hpp:6034-6050). */
+static void hm_bounds(int n_bounds, const int *b, int p, int *st, int *en) {
+  if (n_bounds == 0)
+    return;
+  if (p < 0 || p > b[n_bounds - 1])
+    return;
+  for (int i = 0; i + 1 < n_bounds; ++i)
+    if (b[i] <= p && p < b[i + 1]) {
+      *st = b[i];
+      *en = b[i + 1] - 1;
+      return;
+    }
+}
+
+static double hm_local(int n, const float *pos, const float *h, int diag,
+                       int n_bounds, const int *bounds, int moved) {
+  double err = 0.0;
+  int st = 0, en = n - 1;
+  if (n_bounds > 0)
+    hm_bounds(n_bounds, bounds, moved, &st, &en);
+  const float *m = pos + 3 * moved;
+  for (int i = st; i <= en; ++i) {
+    if (abs(i - moved) >= diag) {
+      float hv = h[(size_t)i * n + moved];
+      if (hv < 1e-6)
+        continue;
+      const float *b = pos + 3 * i;
+      float d = v_len(b[0] - m[0], b[1] - m[1], b[2] - m[2]);
+      float ce = (d - hv) / hv;
+      double cerr = ce;
+      err += cerr * cerr;
+    }
+  }
+  return err;
+}
+
+/* calcScoreHeatmapActiveRegion (LooperSolver.hpp:3583-3617). */
+double orc_heatmap_score(int n, const float *pos, const float *heat, int diag,
+                         int n_bounds, const int *bounds, int moved) {
+  if (moved >= 0)
+    return hm_local(n, pos, heat, diag, n_bounds, bounds, moved);
+  double err = 0.0;
+  for (int i = 0; i < n; ++i)
+    err += hm_local(n, pos, heat, diag, n_bounds, bounds, i);
+  return err;
+}
+
+/* MonteCarloHeatmap (LooperSolver.hpp:1424-1565). */
+void orc_heatmap_anneal(int n, float *pos, const unsigned char *fixed,
+                        const float *heat, int diag, int n_bounds,
+                        const int *bounds, const orc_params *p,
+                        float step_size, int incremental, orc_rng *rng,
+                        orc_result *res) {
+  memset(res, 0, sizeof(*res));
+  step_size *= 0.5;
+  if (n <= 1)
+    return;
+  rng_ctx c;
+  rng_begin(&c, rng, n, fixed);
+  int philox = rng->kind == ORC_RNG_PHILOX;
+  double T = p->max_temp, tp;
+  double score_curr = orc_heatmap_score(n, pos, heat, diag, n_bounds, bounds, -1);
+  int sph = p->sphere_radius > 0.0f;
+  double boundary_sum = 0.0;
+  if (sph) {
+    for (int k = 0; k < n; ++k)
+      boundary_sum += sphere_pen(pos + 3 * k, p->sphere_radius);
+    score_curr += boundary_sum;
+  }
+  double score_prev = score_curr, milestone_score = score_curr;
+  int64_t success = 0, milestone_success = 0, i = 1;
+  if (score_curr != score_curr || score_curr < 1e-6 ||
+      (philox && c.n_movable == 0)) {
+    res->score = 0.0;
+    rng_end(&c);
+    return;
+  }
+  for (;;) {
+    int pb = draw_bead(&c, n);
+    res->proposals++;
+    if (fixed && fixed[pb])
+      continue;
+    float *q = pos + 3 * pb;
+    double old_pen = 0.0, before = 0.0;
+    if (sph)
+      old_pen = sphere_pen(q, p->sphere_radius);
+    if (incremental)
+      before = hm_local(n, pos, heat, diag, n_bounds, bounds, pb);
+    float d[3], old[3] = {q[0], q[1], q[2]};
+    draw_disp(&c, step_size, p->use2d, d);
+    q[0] += d[0];
+    q[1] += d[1];
+    q[2] += d[2];
+    if (incremental) {
+      double after = hm_local(n, pos, heat, diag, n_bounds, bounds, pb);
+      score_curr = (score_prev - (sph ? boundary_sum : 0.0)) + 2.0 * (after - before);
+    } else {
+      score_curr = orc_heatmap_score(n, pos, heat, diag, n_bounds, bounds, -1);
+    }
+    if (sph) {
+      double new_pen = sphere_pen(q, p->sphere_radius);
+      score_curr += boundary_sum - old_pen + new_pen;
+    }
+    int ok = score_curr <= score_prev;
+    if (!ok && T > 0.0) {
+      tp = p->jump_scale * exp(-p->jump_coef * (score_curr / score_prev) / T);
+      ok = draw_chance(&c, (float)tp);
+    }
+    if (ok) {
+      success++;
+      milestone_success++;
+      if (sph) {
+        double new_pen = sphere_pen(q, p->sphere_radius);
+        boundary_sum = boundary_sum - old_pen + new_pen;
+      }
+    } else {
+      if (philox) {
+        q[0] = old[0];
+        q[1] = old[1];
+        q[2] = old[2];
+      } else {
+        q[0] -= d[0];
+        q[1] -= d[1];
+        q[2] -= d[2];
+      }
+      score_curr = score_prev;
+    }
+    end_move(&c);
+    T *= p->dt_temp;
+    if (i % p->milestone_steps == 0) {
+      if ((score_curr > p->improvement * milestone_score &&
+           milestone_success < p->min_successes) ||
+          score_curr < 1e-6)
+        break;
+      milestone_score = score_curr;
+      milestone_success = 0;
+    }
+    if (p->max_moves > 0 && i >= p->max_moves)
+      break;
+    score_prev = score_curr;
+    i++;
+  }
+  res->score = score_curr;
+  res->moves = i;
+  res->accepted = success;
+  rng_end(&c);
+}
+
+/* ------------------------------------------------------------------ */
+/* Subanchor smoothing                                                 */
+/* ------------------------------------------------------------------ */
+static double bond_term(const float *a, const float *b, double dtn,
+                        const orc_params *p) {
+  if (dtn < 1e-6)
+    dtn = 1e-6;
+  float len = v_len(a[0] - b[0], a[1] - b[1], a[2] - b[2]);
+  double diff = (len - dtn) / dtn;
+  return diff * diff * (diff >= 0.0f ? p->k_stretch : p->k_squeeze);
+}
+
+/* calcScoreStructureSmooth(true, true) (LooperSolver.hpp:3414-3451). */
+static double smooth_structure(int n, const float *pos, const double *dtn,
+                               const orc_params *p) {
+  double sca = 0.0, scb = 0.0;
+  float v2[3] = {0, 0, 0};
+  for (int i = 0; i + 1 < n; ++i) {
+    const float *a = pos + 3 * i, *b = pos + 3 * (i + 1);
+    float v[3] = {a[0] - b[0], a[1] - b[1], a[2] - b[2]};
+    sca += bond_term(a, b, dtn[i], p);
+    if (i > 0) {
+      double ang = v_angle(v, v2);
+      scb += ang * ang * ang * p->k_angle;
+    }
+    v2[0] = v[0];
+    v2[1] = v[1];
+    v2[2] = v[2];
+  }
+  return sca * p->w_dist + scb * p->w_angle;
+}
+
+double orc_smooth_full_score(int n, const float *pos, const double *dist_to_next,
+                             const orc_params *p) {
+  double sc = smooth_structure(n, pos, dist_to_next, p);
+  if (p->sphere_radius > 0.0f)
+    for (int k = 0; k < n; ++k)
+      sc += sphere_pen(pos + 3 * k, p->sphere_radius);
+  return sc;
+}
+
+/* calcScoreStructureSmooth(moved, true, true) (LooperSolver.hpp:3453-3495). */
+static double smooth_local(int n, const float *pos, const double *dtn,
+                           const orc_params *p, int moved) {
+  double sca = 0.0, scb = 0.0;
+  float v2[3] = {0, 0, 0};
+  for (int i = moved - 2; i < moved + 2; i++) {
+    if (i < 0 || i + 1 >= n)
+      continue;
+    const float *a = pos + 3 * i, *b = pos + 3 * (i + 1);
+    float v[3] = {a[0] - b[0], a[1] - b[1], a[2] - b[2]};
+    if (i == moved - 1 || i == moved)
+      sca += bond_term(a, b, dtn[i], p);
+    if (i > moved - 2 && i > 0) {
+      double ang = v_angle(v, v2);
+      scb += ang * ang * ang * p->k_angle;
+    }
+    v2[0] = v[0];
+    v2[1] = v[1];
+    v2[2] = v[2];
+  }
+  return sca + scb;
+}
+
+double orc_smooth_local_score(int n, const float *pos,
+                              const double *dist_to_next, const orc_params *p,
+                              int moved) {
+  double sc = smooth_local(n, pos, dist_to_next, p, moved);
+  if (p->sphere_radius > 0.0f)
+    sc += sphere_pen(pos + 3 * moved, p->sphere_radius);
+  return sc;
+}
+
+/* MonteCarloArcsSmooth (LooperSolver.hpp:4798-5047), orientation and
+ * subanchor-heatmap terms off. */
+void orc_smooth_anneal(int n, float *pos, const unsigned char *fixed,
+                       const double *dist_to_next, const orc_params *p,
+                       float step_size, orc_rng *rng, orc_result *res) {
+  memset(res, 0, sizeof(*res));
+  rng_ctx c;
+  rng_begin(&c, rng, n, fixed);
+  int philox = rng->kind == ORC_RNG_PHILOX;
+  double T = p->max_temp, dt = p->dt_temp, tp;
+  double curr_structure = orc_smooth_full_score(n, pos, dist_to_next, p);
+  double prev_structure = curr_structure;
+  double score_curr = curr_structure + 0.0 + 0.0;
+  double score_prev = score_curr, milestone_score = score_curr;
+  int64_t success = 0, milestone_success = 0, i = 1;
+  if (philox && c.n_movable == 0) {
+    res->score = score_curr;
+    rng_end(&c);
+    return;
+  }
+  for (;;) {
+    int pb = draw_bead(&c, n);
+    res->proposals++;
+    if (fixed && fixed[pb])
+      continue;
+    float *q = pos + 3 * pb;
+    double lp = orc_smooth_local_score(n, pos, dist_to_next, p, pb);
+    float d[3], old[3] = {q[0], q[1], q[2]};
+    draw_disp(&c, step_size, p->use2d, d);
+    q[0] += d[0];
+    q[1] += d[1];
+    q[2] += d[2];
+    double lc = orc_smooth_local_score(n, pos, dist_to_next, p, pb);
+    curr_structure = curr_structure - lp + lc;
+    score_curr = curr_structure + 0.0 + 0.0;
+    int ok = score_curr < score_prev;
+    if (!ok && T > 0.0) {
+      tp = p->jump_scale * exp(-p->jump_coef * (score_curr / score_prev) / T);
+      ok = draw_chance(&c, (float)tp);
+    }
+    if (ok) {
+      success++;
+      milestone_success++;
+      score_prev = score_curr;
+      prev_structure = curr_structure;
+    } else {
+      if (philox) {
+        q[0] = old[0];
+        q[1] = old[1];
+        q[2] = old[2];
+      } else {
+        q[0] -= d[0];
+        q[1] -= d[1];
+        q[2] -= d[2];
+      }
+      score_curr = score_prev;
+      curr_structure = prev_structure;
+    }
+    end_move(&c);
+    if (i % p->milestone_steps == 0) {
+      if ((score_curr > p->improvement * milestone_score &&
+           milestone_success < p->min_successes) ||
+          score_curr < 1e-6)
+        break;
+      milestone_score = score_curr;
+      milestone_success = 0;
+    }
+    T *= dt;
+    if (p->max_moves > 0 && i >= p->max_moves)
+      break;
+    i++;
+  }
+  res->score = score_curr;
+  res->moves = i;
+  res->accepted = success;
+  rng_end(&c);
+}
+
+/* ------------------------------------------------------------------ */
+/* Arc marking: InteractionArcs::markArcs (InteractionArcs.hpp:207-336) */
+/* ------------------------------------------------------------------ */
+typedef struct {
+  int start, end, gstart, gend, score, eff, factor;
+  int order; /* input position: ties keep input order */
+} arc_t;
+
+/* InteractionArc::operator< (InteractionArc.hpp:74-84): start, end, factor. */
+static int arc_cmp(const void *x, const void *y) {
+  const arc_t *a = (const arc_t *)x, *b = (const arc_t *)y;
+  if (a->start != b->start)
+    return a->start < b->start ? -1 : 1;
+  if (a->end != b->end)
+    return a->end < b->end ? -1 : 1;
+  if (a->factor != b->factor)
+    return a->factor < b->factor ? -1 : 1;
+  return a->order < b->order ? -1 : (a->order > b->order);
+}
+
+static int emit(int *out, int cap, int *cnt, const arc_t *a) {
+  if (*cnt < cap) {
+    int *o = out + 7 * (*cnt);
+    o[0] = a->start;
+    o[1] = a->end;
+    o[2] = a->gstart;
+    o[3] = a->gend;
+    o[4] = a->score;
+    o[5] = a->eff;
+    o[6] = a->factor;
+  }
+  (*cnt)++;
+  return 0;
+}
+
+/* Flush the arcs gathered for one start anchor: tmp_arcs is a std::map keyed
+ * by the end anchor, iterated in ascending key order (:263-316). */
+static void flush_group(arc_t *g, int ng, int *out, int cap, int *cnt) {
+  /* order by end anchor (std::map key), keeping arrival order within a key */
+  for (int a = 1; a < ng; ++a) { /* insertion sort: stable */
+    arc_t x = g[a];
+    int b = a - 1;
+    while (b >= 0 && g[b].end > x.end) {
+      g[b + 1] = g[b];
+      b--;
+    }
+    g[b + 1] = x;
+  }
+  int s = 0;
+  while (s < ng) {
+    int e = s;
+    while (e < ng && g[e].end == g[s].end)
+      e++;
+    int sz = e - s;
+    arc_t *el = g + s;
+    if (sz == 1) {
+      emit(out, cap, cnt, &el[0]);
+    } else {
+      /* std::sort by (start, end, factor); equal keys keep arrival order */
+      qsort(el, sz, sizeof(arc_t), arc_cmp);
+      int multiple = 0;
+      for (int j = 1; j < sz; ++j)
+        if (el[j].factor != el[j - 1].factor)
+          multiple = 1;
+      int total = 0, fscore = 0, first = 0;
+      for (int j = 0; j <= sz; ++j) {
+        if (j == sz || (j > 0 && el[j].factor != el[j - 1].factor)) {
+          arc_t r = el[first];
+          r.score = fscore;
+          r.eff = multiple ? 0 : fscore;
+          emit(out, cap, cnt, &r);
+          first = j;
+          total += fscore;
+          fscore = 0;
+        }
+        if (j < sz)
+          fscore += el[j].score;
+      }
+      if (multiple) {
+        /* InteractionArc(start, end, 0, -1) with eff_score = total */
+        arc_t r;
+        r.start = el[0].start;
+        r.end = el[0].end;
+        r.gstart = -1;
+        r.gend = -1;
+        r.score = 0;
+        r.eff = total;
+        r.factor = -1;
+        emit(out, cap, cnt, &r);
+      }
+    }
+    s = e;
+  }
+}
+
+int orc_mark_arcs(int n_anchors, const int *a_start, const int *a_end,
+                  int n_raw, const int *r_start, const int *r_end,
+                  const int *r_score, const int *r_factor, int *out, int cap,
+                  int *non_matching) {
+  arc_t *raw = (arc_t *)malloc(sizeof(arc_t) * (n_raw > 0 ? n_raw : 1));
+  arc_t *grp = (arc_t *)malloc(sizeof(arc_t) * (n_raw > 0 ? n_raw : 1));
+  for (int i = 0; i < n_raw; ++i) {
+    raw[i].start = r_start[i];
+    raw[i].end = r_end[i];
+    raw[i].score = r_score[i];
+    raw[i].factor = r_factor[i];
+    raw[i].order = i;
+  }
+  qsort(raw, n_raw, sizeof(arc_t), arc_cmp);
+  int cnt = 0, ng = 0, nm = 0, last_start = -1;
+  for (int i = 0; i <= n_raw; ++i) {
+    int st = -1, en = -1;
+    if (i < n_raw) {
+      /* every anchor of length > 1 that contains the position; last wins
+       * (Anchor::length / contains, Anchor.hpp:81-87) */
+      for (int j = 0; j < n_anchors; ++j) {
+        int len = (a_start[j] == 0 && a_end[j] == 0) ? 0 : a_end[j] - a_start[j] + 1;
+        if (len > 1) {
+          if (raw[i].start >= a_start[j] && raw[i].start <= a_end[j])
+            st = j;
+          if (raw[i].end >= a_start[j] && raw[i].end <= a_end[j])
+            en = j;
+        }
+      }
+      if (st == -1 || en == -1) {
+        ++nm;
+        continue;
+      }
+      if (st == en)
+        continue;
+    }
+    if (st != last_start || i == n_raw) {
+      flush_group(grp, ng, out, cap, &cnt);
+      ng = 0;
+      last_start = st;
+    }
+    if (i < n_raw) {
+      arc_t a;
+      a.start = st;
+      a.end = en;
+      a.gstart = raw[i].start;
+      a.gend = raw[i].end;
+      a.score = raw[i].score;
+      a.eff = raw[i].score;
+      a.factor = raw[i].factor;
+      a.order = ng;
+      grp[ng++] = a;
+    }
+  }
+  free(raw);
+  free(grp);
+  if (non_matching)
+    *non_matching = nm;
+  return cnt <= cap ? cnt : -cnt - 1;
+}
+
+/* ------------------------------------------------------------------ */
+/* HCM lines                                                           */
+/* ------------------------------------------------------------------ */
+int orc_hcm_cluster_line(char *buf, int cap, int start, int end, char orient,
+                         float x, float y, float z, int n_children,
+                         const int *children) {
+  int w = snprintf(buf, cap, "%d %d %c %f %f %f %zu", start, end, orient,
+                   (double)x, (double)y, (double)z, (size_t)n_children);
+  for (int i = 0; i < n_children; ++i)
+    w += snprintf(buf + (w < cap ? w : cap), w < cap ? cap - w : 0, " %d",
+                  children[i]);
+  w += snprintf(buf + (w < cap ? w : cap), w < cap ? cap - w : 0, "\n");
+  return w;
+}
+
+int orc_hcm_arc_line(char *buf, int cap, const int a[7]) {
+  return snprintf(buf, cap, "%d %d %d %d %d %d %d\n", a[0], a[1], a[2], a[3],
+                  a[4], a[5], a[6]);
+}

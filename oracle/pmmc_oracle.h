@@ -1,0 +1,158 @@
+/*
+ * pmmc_oracle.h -- CPU oracle for the pMMC simulated-annealing hot path.
+ *
+ * TEST INFRASTRUCTURE ONLY.  Nothing in the product (the pmmc_gb300 package,
+ * its CUDA library or its C ABI) links, loads or calls this code.  It is the
+ * checker: a plain-C restatement of the reference's CPU algorithms, used by
+ * tests/, by __graft_entry__.smoke() and by bench.py's CPU-baseline leg.
+ *
+ * Every function cites the reference file:line it restates (paths relative to
+ * the SFGLab/pMMC source tree).  The restatement keeps the reference's
+ * floating-point types and operation order (float vs double per expression)
+ * so that, driven by the same libc rand() stream, it reproduces the
+ * reference's CPU annealers bit for bit; tests pin it against the reference
+ * itself (oracle/_ref, built from the reference sources by oracle/Makefile)
+ * and against committed golden vectors generated from it.
+ *
+ * Build flags matter: compile with -ffp-contract=off so that no platform
+ * fuses a*b+c into an FMA that the reference's x86-64 build does not use.
+ */
+#ifndef PMMC_ORACLE_H_
+#define PMMC_ORACLE_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Annealing parameters; every field mirrors a reference Settings:: static
+ * (src/include/Settings.hpp:242-328) and keeps its C type (float / int). */
+typedef struct orc_params {
+  float max_temp;      /* maxTemp / maxTempHeatmap / maxTempSmooth          */
+  float dt_temp;       /* dtTemp* : T *= dt after every counted move        */
+  float jump_scale;    /* tempJumpScale*                                    */
+  float jump_coef;     /* tempJumpCoef*                                     */
+  float improvement;   /* MCstopConditionImprovement*                       */
+  int min_successes;   /* MCstopConditionMinSuccesses*                      */
+  int milestone_steps; /* MCstopConditionSteps*                             */
+  float k_stretch;     /* springConstantStretch(Arcs)                       */
+  float k_squeeze;     /* springConstantSqueeze(Arcs)                       */
+  float k_angle;       /* springAngularConstant                             */
+  float w_dist;        /* weightDistSmooth                                  */
+  float w_angle;       /* weightAngleSmooth                                 */
+  float sphere_radius; /* sphere_radius (0 = no container)                  */
+  int use2d;           /* use2D                                             */
+  int64_t max_moves;   /* oracle-only safety cap on counted moves (0: none) */
+} orc_params;
+
+/* Random-number source of an oracle annealer.
+ *  ORC_RNG_LIBC   : the reference's own stream -- libc rand() after
+ *                   srand(seed) (src/thirdparty/common.cpp:10-24).
+ *  ORC_RNG_PHILOX : the counter-based Philox4x32-10 stream the CUDA kernels
+ *                   draw from (same key/counter layout, see orc_philox_*). */
+enum { ORC_RNG_LIBC = 0, ORC_RNG_PHILOX = 1 };
+
+typedef struct orc_rng {
+  int kind;
+  uint64_t seed;    /* libc: srand(seed); philox: key                    */
+  uint32_t chain;   /* philox: chain id (counter word 1)                 */
+  uint64_t move;    /* philox: proposal counter (counter words 2,3)      */
+} orc_rng;
+
+/* Result of one annealing run. */
+typedef struct orc_result {
+  double score;        /* final running (incremental) score             */
+  int64_t moves;       /* counted moves (the reference's loop index i)  */
+  int64_t accepted;    /* accepted moves                                */
+  int64_t proposals;   /* proposals drawn, incl. skipped fixed beads    */
+} orc_result;
+
+/* ---------------- Philox4x32-10 (Salmon et al., SC'11) ---------------- */
+void orc_philox4x32_10(const uint32_t ctr[4], const uint32_t key[2],
+                       uint32_t out[4]);
+/* u32 -> float in [0,1): top 24 bits times 2^-24. */
+float orc_u01(uint32_t x);
+
+/* ---------------- arc level (anchor) ---------------- */
+/* Full score: LooperSolver::calcScoreDistancesActiveRegion()
+ * (src/include/LooperSolver.hpp:3215-3246, incl. 1/d repulsion for e<0)
+ * + calcScoreLoopEnergy() (:3339-3353) + sphere penalty for every bead
+ * (:4700-4705).  exp_dist is the dense n*n row-major target matrix. */
+double orc_arcs_full_score(int n, const float *pos, const float *exp_dist,
+                           int n_loops, const int *loop_i, const int *loop_j,
+                           const float *loop_k, const float *loop_r0,
+                           const orc_params *p);
+/* Same without the repulsion term (the energy the incremental updates track). */
+double orc_arcs_spring_score(int n, const float *pos, const float *exp_dist,
+                             int n_loops, const int *loop_i, const int *loop_j,
+                             const float *loop_k, const float *loop_r0,
+                             const orc_params *p);
+/* The repulsion term alone: sum over pairs i<j with e_ij<0 of 1.0f/|d_ij|. */
+double orc_arcs_repulsion(int n, const float *pos, const float *exp_dist);
+/* Local score of bead `moved`: calcScoreDistancesActiveRegion(int)
+ * (:3250-3281) + calcScoreLoopEnergy(int) (:3355-3371) + sphere penalty of
+ * the bead (:4721-4723). */
+double orc_arcs_local_score(int n, const float *pos, const float *exp_dist,
+                            int n_loops, const int *loop_i, const int *loop_j,
+                            const float *loop_k, const float *loop_r0,
+                            const orc_params *p, int moved);
+/* LooperSolver::MonteCarloArcs (:4670-4796).  pos is updated in place. */
+void orc_arcs_anneal(int n, float *pos, const unsigned char *fixed,
+                     const float *exp_dist, int n_loops, const int *loop_i,
+                     const int *loop_j, const float *loop_k,
+                     const float *loop_r0, const orc_params *p,
+                     float step_size, orc_rng *rng, orc_result *res);
+
+/* ---------------- heatmap level (chromosome / segment) ---------------- */
+/* calcScoreHeatmapActiveRegion(moved) (:3583-3617); moved = -1 -> full. */
+double orc_heatmap_score(int n, const float *pos, const float *heat, int diag,
+                         int n_bounds, const int *bounds, int moved);
+/* MonteCarloHeatmap (:1424-1565).  incremental = 0 re-scores O(N^2) after
+ * every move exactly as the reference does; incremental = 1 updates the
+ * score with 2*(local_after - local_before) (valid for the symmetric
+ * matrices createDistanceHeatmap builds, :3042-3085). */
+void orc_heatmap_anneal(int n, float *pos, const unsigned char *fixed,
+                        const float *heat, int diag, int n_bounds,
+                        const int *bounds, const orc_params *p,
+                        float step_size, int incremental, orc_rng *rng,
+                        orc_result *res);
+
+/* ---------------- subanchor smoothing ---------------- */
+/* calcScoreStructureSmooth(true,true) (:3414-3451), weighted, + sphere. */
+double orc_smooth_full_score(int n, const float *pos, const double *dist_to_next,
+                             const orc_params *p);
+/* calcScoreStructureSmooth(moved,true,true) (:3453-3495), unweighted, +
+ * sphere penalty of the moved bead (:4939-4941). */
+double orc_smooth_local_score(int n, const float *pos,
+                              const double *dist_to_next, const orc_params *p,
+                              int moved);
+/* MonteCarloArcsSmooth(step, false) (:4798-5047) without the CTCF and
+ * subanchor-heatmap terms (both off by default, Settings.hpp:401,405). */
+void orc_smooth_anneal(int n, float *pos, const unsigned char *fixed,
+                       const double *dist_to_next, const orc_params *p,
+                       float step_size, orc_rng *rng, orc_result *res);
+
+/* ---------------- arc marking ---------------- */
+/* InteractionArcs::markArcs (src/include/InteractionArcs.hpp:207-336) for one
+ * chromosome.  Anchors {start,end}; raw arcs {start,end,score,factor}.
+ * Writes up to cap output arcs (7 ints each: start end genomic_start
+ * genomic_end score eff_score factor) and returns the count (or -count-1 if
+ * cap was too small).  *non_matching receives the skipped-arc count. */
+int orc_mark_arcs(int n_anchors, const int *a_start, const int *a_end,
+                  int n_raw, const int *r_start, const int *r_end,
+                  const int *r_score, const int *r_factor, int *out, int cap,
+                  int *non_matching);
+
+/* ---------------- HCM text lines ---------------- */
+/* Cluster::toFile (src/include/Cluster.hpp:175-181). Returns bytes written. */
+int orc_hcm_cluster_line(char *buf, int cap, int start, int end, char orient,
+                         float x, float y, float z, int n_children,
+                         const int *children);
+/* InteractionArc::toFile (src/include/InteractionArc.hpp:122-125). */
+int orc_hcm_arc_line(char *buf, int cap, const int arc7[7]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PMMC_ORACLE_H_ */

@@ -1,0 +1,383 @@
+/*
+ * ref_harness.cpp -- drives the REFERENCE's own CPU code (SFGLab/pMMC,
+ * header-only LooperSolver / InteractionArcs) through a C ABI.
+ *
+ * TEST INFRASTRUCTURE ONLY.  oracle/Makefile compiles this file together with
+ * the reference's sources where they lie (its src/include headers and
+ * src/thirdparty/*.cpp) into oracle/_ref/libpmmc_ref.so.  Tests use it to pin
+ * the plain-C oracle (pmmc_oracle.c) bit for bit, and
+ * tests/golden/gen_golden.py uses it to write the golden fixtures that travel
+ * with the repository.  No reference source is copied here: this file only
+ * fills the reference's data structures and calls its functions.
+ *
+ * The header-only classes keep their state private; the harness opens them
+ * with `#define private public` after including every standard header first
+ * (the reference's common.h defines `epsilon`, which would break <random>).
+ */
+#include <algorithm>
+#include <array>
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <fstream>
+#include <iostream>
+#include <map>
+#include <numeric>
+#include <queue>
+#include <random>
+#include <set>
+#include <sstream>
+#include <unordered_map>
+#include <vector>
+
+#include <fcntl.h>
+#include <unistd.h>
+
+#define private public
+#define protected public
+#include <AppCommon.hpp>
+#include <Static.hpp>
+#include <LooperSolver.hpp>
+#undef private
+#undef protected
+
+#include "pmmc_oracle.h"
+
+/* The CPU-only harness holds no device resources; LooperSolver's destructor
+ * still references this member of its GPU cache. */
+void GpuResourceCache::cleanup() {}
+
+namespace {
+
+/* Silence the reference's progress printing for the duration of a call. */
+struct Quiet {
+  int saved = -1;
+  Quiet() {
+    fflush(stdout);
+    std::cout.flush();
+    saved = dup(1);
+    int dn = open("/dev/null", O_WRONLY);
+    if (dn >= 0) {
+      dup2(dn, 1);
+      close(dn);
+    }
+  }
+  ~Quiet() {
+    fflush(stdout);
+    std::cout.flush();
+    if (saved >= 0) {
+      dup2(saved, 1);
+      close(saved);
+    }
+  }
+};
+
+std::string segments_file() {
+  static std::string path;
+  if (path.empty()) {
+    char tmpl[] = "/tmp/pmmc_ref_segXXXXXX";
+    int fd = mkstemp(tmpl);
+    if (fd >= 0) {
+      const char *line = "chr1\t0\t1000000\n";
+      if (write(fd, line, strlen(line)) < 0) {
+      }
+      close(fd);
+    }
+    path = tmpl;
+  }
+  return path;
+}
+
+void apply_settings(const orc_params *p, int level) {
+  static Settings st;
+  static bool inited = false;
+  if (!inited) {
+    st.init();
+    inited = true;
+  }
+  Settings::dataSegmentsSplit = segments_file();
+  Settings::outputLevel = 0;
+  Settings::energyTraceEnabled = false;
+  Settings::use2D = p->use2d != 0;
+  Settings::sphere_radius = p->sphere_radius;
+  Settings::springAngularConstant = p->k_angle;
+  Settings::weightDistSmooth = p->w_dist;
+  Settings::weightAngleSmooth = p->w_angle;
+  if (level == 0) { /* arcs */
+    Settings::maxTemp = p->max_temp;
+    Settings::dtTemp = p->dt_temp;
+    Settings::tempJumpScale = p->jump_scale;
+    Settings::tempJumpCoef = p->jump_coef;
+    Settings::MCstopConditionImprovement = p->improvement;
+    Settings::MCstopConditionMinSuccesses = p->min_successes;
+    Settings::MCstopConditionSteps = p->milestone_steps;
+    Settings::springConstantStretchArcs = p->k_stretch;
+    Settings::springConstantSqueezeArcs = p->k_squeeze;
+  } else if (level == 1) { /* heatmap */
+    Settings::maxTempHeatmap = p->max_temp;
+    Settings::dtTempHeatmap = p->dt_temp;
+    Settings::tempJumpScaleHeatmap = p->jump_scale;
+    Settings::tempJumpCoefHeatmap = p->jump_coef;
+    Settings::MCstopConditionImprovementHeatmap = p->improvement;
+    Settings::MCstopConditionMinSuccessesHeatmap = p->min_successes;
+    Settings::MCstopConditionStepsHeatmap = p->milestone_steps;
+  } else { /* smooth */
+    Settings::maxTempSmooth = p->max_temp;
+    Settings::dtTempSmooth = p->dt_temp;
+    Settings::tempJumpScaleSmooth = p->jump_scale;
+    Settings::tempJumpCoefSmooth = p->jump_coef;
+    Settings::MCstopConditionImprovementSmooth = p->improvement;
+    Settings::MCstopConditionMinSuccessesSmooth = p->min_successes;
+    Settings::MCstopConditionStepsSmooth = p->milestone_steps;
+    Settings::springConstantStretch = p->k_stretch;
+    Settings::springConstantSqueeze = p->k_squeeze;
+  }
+}
+
+void load_clusters(LooperSolver &s, int n, const float *pos,
+                   const unsigned char *fixed, const double *dtn) {
+  s.clusters.assign(n, Cluster());
+  s.active_region.clear();
+  for (int i = 0; i < n; ++i) {
+    s.clusters[i].pos.set(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
+    s.clusters[i].is_fixed = fixed ? fixed[i] != 0 : false;
+    s.clusters[i].dist_to_next = dtn ? dtn[i] : 0.0;
+    s.active_region.push_back(i);
+  }
+}
+
+void store_positions(const LooperSolver &s, int n, float *pos) {
+  for (int i = 0; i < n; ++i) {
+    pos[3 * i] = s.clusters[i].pos.x;
+    pos[3 * i + 1] = s.clusters[i].pos.y;
+    pos[3 * i + 2] = s.clusters[i].pos.z;
+  }
+}
+
+void load_dense(Heatmap &h, int n, const float *m) {
+  h.init(n);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j)
+      h.v[i][j] = m[(size_t)i * n + j];
+}
+
+void load_loops(LooperSolver &s, int n_loops, const int *li, const int *lj,
+                const float *lk, const float *lr0) {
+  s.loop_constraints.clear();
+  for (int c = 0; c < n_loops; ++c) {
+    LooperSolver::LoopConstraint lc;
+    lc.cluster_i = li[c];
+    lc.cluster_j = lj[c];
+    lc.stiffness = lk[c];
+    lc.eq_distance = lr0[c];
+    s.loop_constraints.push_back(lc);
+  }
+  s.rebuildActiveLoopMap();
+}
+
+} // namespace
+
+extern "C" {
+
+/* LooperSolver::MonteCarloArcs (src/include/LooperSolver.hpp:4670-4796). */
+void ref_arcs_anneal(int n, float *pos, const unsigned char *fixed,
+                     const float *exp_dist, int n_loops, const int *li,
+                     const int *lj, const float *lk, const float *lr0,
+                     const orc_params *p, float step, unsigned seed,
+                     double *score, long long *moves) {
+  Quiet q;
+  apply_settings(p, 0);
+  LooperSolver s("ref", "/tmp/");
+  load_clusters(s, n, pos, fixed, nullptr);
+  load_dense(s.heatmap_exp_dist_anchor, n, exp_dist);
+  load_loops(s, n_loops, li, lj, lk, lr0);
+  srand(seed);
+  *score = s.MonteCarloArcs(step);
+  *moves = s.total_mc_steps;
+  store_positions(s, n, pos);
+}
+
+/* moved < 0: calcScoreDistancesActiveRegion() + calcScoreLoopEnergy() +
+ * sphere over all beads; moved >= 0: the local score MonteCarloArcs uses. */
+double ref_arcs_score(int n, const float *pos, const float *exp_dist,
+                      int n_loops, const int *li, const int *lj,
+                      const float *lk, const float *lr0, const orc_params *p,
+                      int moved) {
+  Quiet q;
+  apply_settings(p, 0);
+  LooperSolver s("ref", "/tmp/");
+  load_clusters(s, n, pos, nullptr, nullptr);
+  load_dense(s.heatmap_exp_dist_anchor, n, exp_dist);
+  load_loops(s, n_loops, li, lj, lk, lr0);
+  double sc;
+  if (moved < 0) {
+    sc = s.calcScoreDistancesActiveRegion() + s.calcScoreLoopEnergy();
+    if (s.spherical_container)
+      for (int k = 0; k < n; k++)
+        sc += s.spherical_container->boundaryPenalty(s.clusters[k].pos);
+  } else {
+    sc = s.calcScoreDistancesActiveRegion(moved) + s.calcScoreLoopEnergy(moved);
+    if (s.spherical_container)
+      sc += s.spherical_container->boundaryPenalty(s.clusters[moved].pos);
+  }
+  return sc;
+}
+
+/* LooperSolver::MonteCarloHeatmap (:1424-1565). */
+void ref_heatmap_anneal(int n, float *pos, const unsigned char *fixed,
+                        const float *heat, int diag, int n_bounds,
+                        const int *bounds, const orc_params *p, float step,
+                        unsigned seed, double *score, long long *moves) {
+  Quiet q;
+  apply_settings(p, 1);
+  LooperSolver s("ref", "/tmp/");
+  load_clusters(s, n, pos, fixed, nullptr);
+  load_dense(s.heatmap_dist, n, heat);
+  s.heatmap_dist.diagonal_size = diag;
+  s.heatmap_chromosome_boundaries.assign(bounds, bounds + n_bounds);
+  srand(seed);
+  *score = s.MonteCarloHeatmap(step);
+  *moves = s.total_mc_steps;
+  store_positions(s, n, pos);
+}
+
+/* calcScoreHeatmapActiveRegion(moved) (:3583-3617). */
+double ref_heatmap_score(int n, const float *pos, const float *heat, int diag,
+                         int n_bounds, const int *bounds, int moved) {
+  Quiet q;
+  orc_params p{};
+  apply_settings(&p, 1);
+  LooperSolver s("ref", "/tmp/");
+  load_clusters(s, n, pos, nullptr, nullptr);
+  load_dense(s.heatmap_dist, n, heat);
+  s.heatmap_dist.diagonal_size = diag;
+  s.heatmap_chromosome_boundaries.assign(bounds, bounds + n_bounds);
+  return s.calcScoreHeatmapActiveRegion(moved);
+}
+
+/* LooperSolver::MonteCarloArcsSmooth(step, false) (:4798-5047). */
+void ref_smooth_anneal(int n, float *pos, const unsigned char *fixed,
+                       const double *dtn, const orc_params *p, float step,
+                       unsigned seed, double *score, long long *moves) {
+  Quiet q;
+  apply_settings(p, 2);
+  LooperSolver s("ref", "/tmp/");
+  load_clusters(s, n, pos, fixed, dtn);
+  srand(seed);
+  *score = s.MonteCarloArcsSmooth(step, false);
+  *moves = s.total_mc_steps;
+  store_positions(s, n, pos);
+}
+
+/* moved < 0: calcScoreStructureSmooth(true,true) + sphere over all beads (the
+ * initial score of MonteCarloArcsSmooth, :4880-4884); moved >= 0: the local
+ * score calcScoreStructureSmooth(moved,true,true) + sphere of that bead. */
+double ref_smooth_score(int n, const float *pos, const double *dtn,
+                        const orc_params *p, int moved) {
+  Quiet q;
+  apply_settings(p, 2);
+  LooperSolver s("ref", "/tmp/");
+  load_clusters(s, n, pos, nullptr, dtn);
+  double sc;
+  if (moved < 0) {
+    sc = s.calcScoreStructureSmooth(true, true);
+    if (s.spherical_container)
+      for (int k = 0; k < n; k++)
+        sc += s.spherical_container->boundaryPenalty(s.clusters[k].pos);
+  } else {
+    sc = s.calcScoreStructureSmooth(moved, true, true);
+    if (s.spherical_container)
+      sc += s.spherical_container->boundaryPenalty(s.clusters[moved].pos);
+  }
+  return sc;
+}
+
+/* InteractionArcs::markArcs (src/include/InteractionArcs.hpp:207-336) on a
+ * single chromosome "chr1".  Output layout as orc_mark_arcs. */
+int ref_mark_arcs(int n_anchors, const int *a_start, const int *a_end,
+                  int n_raw, const int *r_start, const int *r_end,
+                  const int *r_score, const int *r_factor, int *out, int cap,
+                  int *non_matching) {
+  Quiet q;
+  InteractionArcs ia;
+  std::string chr = "chr1";
+  ia.chrs.push_back(chr);
+  for (int i = 0; i < n_anchors; ++i)
+    ia.anchors[chr].push_back(Anchor(chr, a_start[i], a_end[i], 'N'));
+  ia.anchors_cnt[chr] = n_anchors;
+  for (int i = 0; i < n_raw; ++i) {
+    InteractionArc a(r_start[i], r_end[i], r_score[i], r_factor[i]);
+    ia.raw_arcs[chr].push_back(a);
+  }
+  ia.markArcs(false);
+  const std::vector<InteractionArc> &v = ia.arcs[chr];
+  *non_matching = 0; /* printed, not stored, by the reference */
+  int cnt = (int)v.size();
+  if (cnt > cap)
+    return -cnt - 1;
+  for (int i = 0; i < cnt; ++i) {
+    int *o = out + 7 * i;
+    o[0] = v[i].start;
+    o[1] = v[i].end;
+    o[2] = v[i].genomic_start;
+    o[3] = v[i].genomic_end;
+    o[4] = v[i].score;
+    o[5] = v[i].eff_score;
+    o[6] = v[i].factor;
+  }
+  return cnt;
+}
+
+/* Cluster::toFile (src/include/Cluster.hpp:175-181) into a buffer. */
+int ref_hcm_cluster_line(char *buf, int cap, int start, int end, char orient,
+                         float x, float y, float z, int n_children,
+                         const int *children) {
+  Cluster c(start, end);
+  c.orientation = orient;
+  c.pos.set(x, y, z);
+  c.children.assign(children, children + n_children);
+  char *mem = nullptr;
+  size_t sz = 0;
+  FILE *f = open_memstream(&mem, &sz);
+  c.toFile(f);
+  fclose(f);
+  int w = (int)sz < cap - 1 ? (int)sz : cap - 1;
+  memcpy(buf, mem, w);
+  buf[w] = 0;
+  free(mem);
+  return (int)sz;
+}
+
+/* InteractionArc::toFile (src/include/InteractionArc.hpp:122-125). */
+int ref_hcm_arc_line(char *buf, int cap, const int *a7) {
+  InteractionArc a(a7[0], a7[1], a7[4], a7[6]);
+  a.genomic_start = a7[2];
+  a.genomic_end = a7[3];
+  a.eff_score = a7[5];
+  char *mem = nullptr;
+  size_t sz = 0;
+  FILE *f = open_memstream(&mem, &sz);
+  a.toFile(f);
+  fclose(f);
+  int w = (int)sz < cap - 1 ? (int)sz : cap - 1;
+  memcpy(buf, mem, w);
+  buf[w] = 0;
+  free(mem);
+  return (int)sz;
+}
+
+/* random_vector (src/thirdparty/common.cpp:20-25) after srand(seed): records
+ * which of the three rand() draws lands in x, y and z with this compiler. */
+void ref_random_vectors(unsigned seed, int count, float max_size, int in2d,
+                        float *out) {
+  srand(seed);
+  for (int i = 0; i < count; ++i) {
+    vector3 v = random_vector(max_size, in2d != 0);
+    out[3 * i] = v.x;
+    out[3 * i + 1] = v.y;
+    out[3 * i + 2] = v.z;
+  }
+}
+
+} /* extern "C" */

@@ -1,0 +1,197 @@
+"""Seeded synthetic inputs with the shapes of the benchmark workloads.
+
+The reference's example inputs (ChIA-PET / Hi-C files) are not available, so
+every workload is generated here from a seed:
+
+* ``arcs_region``      -- one anchor-level active region: a 3D random walk
+  with unit steps, arcs between beads i<j with |i-j| log-uniform in
+  [3, n-1], PET counts geometric with mean 8, target distance
+  count^-0.5 * |i-j|^0.25.  Returned both as the reference's dense n x n
+  matrix (-1 = no arc, 0 on the diagonal, LooperSolver.hpp:5498-5538) and as
+  per-bead arc lists (CSR) that the CUDA kernels consume.
+* ``heatmap_region``   -- symmetric contact map c_ij = |i-j|^-1 x
+  lognormal(0, 0.5), 20 TAD diagonal blocks boosted x3, expected distance
+  c^-1/3 (createDistanceHeatmap with freq_dist_scale 1, power -1/3).
+* ``smooth_genome``    -- 23 chromosomes with lengths proportional to human
+  chr1..22,X at 10 kb per bead, anchors every Poisson(10) beads fixed.
+* ``arcs_ensemble``    -- structures x blocks of arc regions with
+  log-uniform block sizes.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+# Human chromosome lengths in Mb (chr1..chr22, chrX), used only for the
+# relative sizes of the genome-scale smoothing workload.
+HUMAN_CHR_MB = [248, 242, 198, 190, 181, 171, 159, 145, 138, 134, 135, 133,
+                114, 107, 102, 90, 83, 80, 59, 64, 47, 51, 156]
+
+
+def random_walk(n: int, rng: np.random.Generator, step: float = 1.0) -> np.ndarray:
+    """3D random walk with steps of fixed length `step` (float32, (n,3))."""
+    d = rng.normal(size=(n, 3))
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    d[0] = 0.0
+    return (np.cumsum(d * step, axis=0)).astype(np.float32)
+
+
+@dataclass
+class ArcsRegion:
+    pos: np.ndarray          # (n,3) float32
+    arcs: np.ndarray         # (m,2) int32, i<j
+    target: np.ndarray       # (m,) float32 expected distance
+    count: np.ndarray        # (m,) int32 PET counts
+
+    @property
+    def n(self) -> int:
+        return int(self.pos.shape[0])
+
+    def dense(self) -> np.ndarray:
+        """The reference layout: -1 everywhere, 0 on the diagonal, targets on
+        arc pairs (both triangles)."""
+        n = self.n
+        m = np.full((n, n), -1.0, np.float32)
+        np.fill_diagonal(m, 0.0)
+        m[self.arcs[:, 0], self.arcs[:, 1]] = self.target
+        m[self.arcs[:, 1], self.arcs[:, 0]] = self.target
+        return m
+
+
+def arcs_region(n: int = 256, n_arcs: int = 400, seed: int = 42,
+                mean_count: float = 8.0, arcs_per_bead: float | None = None) -> ArcsRegion:
+    rng = np.random.default_rng(seed)
+    pos = random_walk(n, rng)
+    if arcs_per_bead is not None:
+        n_arcs = int(round(arcs_per_bead * n))
+    max_sep = n - 1
+    n_arcs = min(n_arcs, n * (n - 1) // 2 - (n - 1) * 2)
+    seen = {}
+    p_geo = 1.0 / mean_count
+    tries = 0
+    while len(seen) < n_arcs and tries < 50 * n_arcs + 1000:
+        tries += 1
+        if max_sep < 3:
+            sep = max(1, max_sep)
+        else:
+            sep = int(round(np.exp(rng.uniform(np.log(3), np.log(max_sep)))))
+            sep = min(max(sep, 3), max_sep)
+        i = int(rng.integers(0, n - sep))
+        j = i + sep
+        if (i, j) in seen:
+            continue
+        cnt = int(rng.geometric(p_geo))
+        seen[(i, j)] = cnt
+    keys = sorted(seen)
+    arcs = np.array(keys, np.int32).reshape(-1, 2)
+    count = np.array([seen[k] for k in keys], np.int32)
+    sep = (arcs[:, 1] - arcs[:, 0]).astype(np.float64)
+    target = (count.astype(np.float64) ** -0.5 * sep ** 0.25).astype(np.float32)
+    return ArcsRegion(pos, arcs, target, count)
+
+
+@dataclass
+class HeatmapRegion:
+    pos: np.ndarray      # (n,3) float32
+    heat: np.ndarray     # (n,n) float32 expected distances (0 = ignore)
+    diag: int
+    bounds: np.ndarray   # chromosome boundaries ([] = one block)
+
+    @property
+    def n(self) -> int:
+        return int(self.pos.shape[0])
+
+
+def heatmap_region(n: int = 2048, seed: int = 7, n_tads: int = 20,
+                   tad_min: int = 40, tad_max: int = 200, sigma: float = 0.5,
+                   diag: int = 1) -> HeatmapRegion:
+    rng = np.random.default_rng(seed)
+    pos = random_walk(n, rng)
+    i = np.arange(n)
+    sep = np.abs(i[:, None] - i[None, :]).astype(np.float64)
+    noise = rng.lognormal(0.0, sigma, size=(n, n))
+    noise = np.triu(noise, 1)
+    noise = noise + noise.T
+    with np.errstate(divide="ignore"):
+        c = np.where(sep > 0, 1.0 / np.maximum(sep, 1.0), 0.0) * noise
+    # TAD blocks: non-overlapping diagonal blocks boosted x3
+    placed = []
+    tries = 0
+    while len(placed) < n_tads and tries < 10000:
+        tries += 1
+        size = int(rng.integers(tad_min, tad_max + 1))
+        if size >= n:
+            continue
+        s = int(rng.integers(0, n - size))
+        if any(not (s + size <= a or b <= s) for a, b in placed):
+            continue
+        placed.append((s, s + size))
+    for a, b in placed:
+        c[a:b, a:b] *= 3.0
+    with np.errstate(divide="ignore"):
+        h = np.where(c > 0, c ** (-1.0 / 3.0), 0.0)
+    h = h.astype(np.float32)
+    np.fill_diagonal(h, 0.0)
+    return HeatmapRegion(pos, h, diag, np.zeros(0, np.int32))
+
+
+@dataclass
+class SmoothChain:
+    pos: np.ndarray          # (n,3) float32
+    fixed: np.ndarray        # (n,) uint8
+    dist_to_next: np.ndarray # (n,) float64
+    chrom_start: np.ndarray  # chromosome first-bead offsets (+ total at end)
+
+    @property
+    def n(self) -> int:
+        return int(self.pos.shape[0])
+
+
+def smooth_chain(n: int, seed: int = 3, gap_mean: float = 10.0,
+                 bond: float = 1.0) -> SmoothChain:
+    """One chromosome: anchors every Poisson(gap_mean) (>=1) beads held fixed
+    at random-walk positions; free beads start on the straight line between
+    anchors plus noise."""
+    rng = np.random.default_rng(seed)
+    walk = random_walk(n, rng, step=bond)
+    fixed = np.zeros(n, np.uint8)
+    k = 0
+    while k < n:
+        fixed[k] = 1
+        k += max(1, int(rng.poisson(gap_mean)))
+    fixed[n - 1] = 1
+    pos = walk.copy()
+    anchors = np.nonzero(fixed)[0]
+    for a, b in zip(anchors[:-1], anchors[1:]):
+        if b - a > 1:
+            t = (np.arange(a + 1, b) - a) / (b - a)
+            pos[a + 1:b] = walk[a] + (walk[b] - walk[a]) * t[:, None]
+    pos += (rng.normal(size=pos.shape) * 0.25 * (1 - fixed[:, None])).astype(np.float32)
+    dtn = np.full(n, bond, np.float64)
+    return SmoothChain(pos.astype(np.float32), fixed, dtn, np.array([0, n], np.int64))
+
+
+def smooth_genome(total_beads: int = 300_000, seed: int = 3) -> list[SmoothChain]:
+    """23 chromosomes with lengths proportional to HUMAN_CHR_MB summing to
+    about total_beads."""
+    mb = np.array(HUMAN_CHR_MB, np.float64)
+    sizes = np.maximum(16, np.round(mb / mb.sum() * total_beads)).astype(int)
+    return [smooth_chain(int(s), seed=seed * 1000 + c) for c, s in enumerate(sizes)]
+
+
+def arcs_ensemble(n_structures: int = 64, n_blocks: int = 24, min_size: int = 32,
+                  max_size: int = 2048, arcs_per_bead: float = 1.5,
+                  seeds=None) -> list[list[ArcsRegion]]:
+    """structures x blocks arc regions; block sizes log-uniform in
+    [min_size, max_size]; structure s is generated from seed s."""
+    out = []
+    seeds = list(range(n_structures)) if seeds is None else list(seeds)
+    for s in seeds:
+        rng = np.random.default_rng(10_000 + s)
+        blocks = []
+        for b in range(n_blocks):
+            size = int(round(np.exp(rng.uniform(np.log(min_size), np.log(max_size)))))
+            blocks.append(arcs_region(size, seed=s * 1000 + b, arcs_per_bead=arcs_per_bead))
+        out.append(blocks)
+    return out
