@@ -1,0 +1,293 @@
+/*
+ * pmmc_gb300.h -- C ABI of the GB300-native pMMC annealing library.
+ *
+ * The reference (SFGLab/pMMC) exposes its GPU hot path as C++ member
+ * functions of LooperSolver / InteractionArcs that read the solver's state
+ * directly.  This library replaces them with plain-C entry points: pointers,
+ * sizes and status codes; no C++ or torch types.  Each declaration names the
+ * reference interface it replaces.  The C++ shim in pmmc_gb300/shim/ maps
+ * the reference's member functions onto these calls.
+ *
+ * Positions are float xyz triples (n*3 floats, the reference's
+ * clusters[active_region[i]].pos order).  Host pointers are copied in and
+ * out; the *_device / batch entry points take device pointers and a CUDA
+ * stream (passed as void*).  Every call returns a pmmc_status; nothing
+ * exits the process and there is no CPU fallback: without a usable GB300
+ * device the calls return PMMC_ERR_NO_DEVICE.
+ */
+#ifndef PMMC_GB300_H_
+#define PMMC_GB300_H_
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum pmmc_status {
+  PMMC_OK = 0,
+  PMMC_ERR_INVALID = 1,   /* bad argument or size                       */
+  PMMC_ERR_NO_DEVICE = 2, /* no CUDA device / library not usable         */
+  PMMC_ERR_CUDA = 3,      /* a CUDA runtime call failed                  */
+  PMMC_ERR_NOMEM = 4,     /* device allocation failed                    */
+  PMMC_ERR_TIMEOUT = 5,   /* a bounded device wait ran out               */
+  PMMC_ERR_BUDGET = 6,    /* request exceeds the device-memory budget    */
+  PMMC_ERR_FIXED = 7,     /* arc level: every bead is fixed              */
+  PMMC_ERR_BUSY = 8,      /* server: no free slot right now              */
+  PMMC_ERR_NOT_FOUND = 9  /* server: unknown request id                  */
+} pmmc_status;
+
+/* Stopping schedule of a chain. */
+enum {
+  /* The reference CUDA kernels (ParallelMonteCarloArcs.cu:520-658,
+   * ParallelMonteCarloSmooth.cu:267-337): milestones every 256 moves, stop
+   * after `milestone_fails` consecutive misses, at most `milestone_steps`
+   * moves (rounded up to 256). */
+  PMMC_SCHEDULE_GPU = 0,
+  /* The reference CPU loops (LooperSolver.hpp:4764-4783, 1529-1553,
+   * 5014-5034): a milestone every `milestone_steps` moves, stop at the first
+   * miss.  `max_moves` (or 200 milestones when 0) bounds the chain. */
+  PMMC_SCHEDULE_CPU = 1
+};
+
+/* Annealing parameters.  Each field is the reference Settings:: static of
+ * the same meaning (src/include/Settings.hpp:242-328, INI sections
+ * [simulation_arcs], [simulation_heatmap], [simulation_arcs_smooth],
+ * [springs], [simulation], [cuda]).  Use pmmc_default_params() for the
+ * reference defaults of a level. */
+typedef struct pmmc_anneal_params {
+  float max_temp;        /* max_temp*                              */
+  float dt_temp;         /* delta_temp*                            */
+  float jump_scale;      /* jump_temp_scale*                       */
+  float jump_coef;       /* jump_temp_coef*                        */
+  float improvement;     /* stop_condition_improvement_threshold*  */
+  int min_successes;     /* stop_condition_successes_threshold*    */
+  int milestone_steps;   /* stop_condition_steps*                  */
+  float k_stretch;       /* stretch_constant(_arcs)                */
+  float k_squeeze;       /* squeeze_constant(_arcs)                */
+  float k_angle;         /* angular_constant                       */
+  float w_dist;          /* dist_weight (smooth)                   */
+  float w_angle;         /* angle_weight (smooth)                  */
+  float sphere_radius;   /* [simulation] sphere_radius, 0 = off    */
+  int use2d;             /* 2D moves                               */
+  int milestone_fails;   /* [cuda] milestone_fails                 */
+  int schedule;          /* PMMC_SCHEDULE_GPU / PMMC_SCHEDULE_CPU  */
+  int resync_every;      /* FP64 energy recompute every L moves (0 = off) */
+  int64_t max_moves;     /* hard cap on moves per chain (0 = schedule's) */
+  /* Extended arc energy (off = the reference's arcs+loops+sphere): bond
+   * springs on consecutive beads with target `bond_target` and constants
+   * k_stretch_bond/k_squeeze_bond, and the smooth-level angle term
+   * k_angle_ext*((1-cos)/2)^3 at every interior bead. */
+  int arcs_extended;
+  float bond_target;
+  float k_stretch_bond;
+  float k_squeeze_bond;
+  float k_angle_ext;
+} pmmc_anneal_params;
+
+enum { PMMC_LEVEL_ARCS = 0, PMMC_LEVEL_HEATMAP = 1, PMMC_LEVEL_SMOOTH = 2 };
+
+/* Result of an annealing call (one chain, or the best of several). */
+typedef struct pmmc_result {
+  float score;           /* the FP32 score the reference returns             */
+  double energy;         /* running FP64 energy at the end of the chain       */
+  double energy_fp64;    /* FP64 recompute of the same energy definition      */
+  double rel_error;      /* |energy - energy_fp64| / max(|energy_fp64|,1e-30) */
+  int64_t moves;         /* counted moves of the reported chain               */
+  int64_t accepted;      /* accepted moves of the reported chain              */
+  int64_t total_moves;   /* moves over all chains of the call                 */
+  int best_chain;        /* index of the reported chain                       */
+  int status;            /* per-chain device status (0 = ok)                  */
+} pmmc_result;
+
+/* Anchor-level active region: positions, fixed flags and per-bead arc lists
+ * (CSR over both directions).  A pair listed in the CSR with target >= 1e-6
+ * is an arc spring; a pair listed with 0 <= target < 1e-6 contributes
+ * nothing; every pair not listed contributes the 1/d repulsion to the
+ * initial score only (the reference's dense -1 entries,
+ * LooperSolver.hpp:3226-3231 vs :3262-3266).  pmmc_arcs_dense_to_csr()
+ * converts the reference's dense n x n matrix. */
+typedef struct pmmc_arcs_problem {
+  int n;
+  const float *pos;            /* n*3                                    */
+  const unsigned char *fixed;  /* n, nullable                            */
+  const int *row_ptr;          /* n+1                                    */
+  const int *col;              /* row_ptr[n], sorted within each row     */
+  const float *target;         /* row_ptr[n]                             */
+  int n_loops;                 /* loop constraints (cluster indices are  */
+  const int *loop_i;           /* active-region indices here)            */
+  const int *loop_j;
+  const float *loop_k;
+  const float *loop_r0;
+} pmmc_arcs_problem;
+
+/* Heatmap-level active region: dense n x n expected-distance matrix
+ * (row-major, symmetric as createDistanceHeatmap builds it,
+ * LooperSolver.hpp:3042-3085), diagonal band width and optional chromosome
+ * boundaries. */
+typedef struct pmmc_heatmap_problem {
+  int n;
+  const float *pos;            /* n*3                        */
+  const unsigned char *fixed;  /* n, nullable                */
+  const float *heat;           /* n*n                        */
+  int diag;                    /* heatmap_dist.diagonal_size */
+  int n_bounds;                /* 0 = one block              */
+  const int *bounds;
+} pmmc_heatmap_problem;
+
+/* Subanchor smoothing region: positions, fixed flags, dist_to_next. */
+typedef struct pmmc_smooth_problem {
+  int n;
+  const float *pos;            /* n*3           */
+  const unsigned char *fixed;  /* n, nullable   */
+  const float *dist_to_next;   /* n             */
+} pmmc_smooth_problem;
+
+typedef struct pmmc_ctx pmmc_ctx;
+
+/* ---------------- context ---------------- */
+/* Replaces GpuResourceCache::init / cleanup (LooperSolver.hpp:54-106,
+ * ParallelMonteCarloArcs.cu:84-213): one context owns the device buffers. */
+pmmc_status pmmc_ctx_create(pmmc_ctx **out, int device);
+void pmmc_ctx_destroy(pmmc_ctx *ctx);
+const char *pmmc_status_string(pmmc_status s);
+/* Message of the last failing call on this context. */
+const char *pmmc_last_error(const pmmc_ctx *ctx);
+/* Replaces setGpuSeed (platform.h:106, ParallelMonteCarloHeatmap.cu:37-39)
+ * and LooperSolver_setArcsGpuSeed (ParallelMonteCarloArcs.cu:950-952): the
+ * Philox key of every later call.  Each call also advances a per-context
+ * call counter so that consecutive calls draw fresh streams. */
+void pmmc_set_seed(pmmc_ctx *ctx, uint64_t seed);
+/* Number of SMs of the context's device. */
+int pmmc_sm_count(const pmmc_ctx *ctx);
+/* Reference defaults of a level (Settings.hpp:397-505). */
+void pmmc_default_params(int level, pmmc_anneal_params *out);
+
+/* ---------------- conversions ---------------- */
+/* Reference dense matrix (heatmap_exp_dist_anchor.v, -1 = no arc) -> CSR
+ * over both directions, keeping every off-diagonal entry >= 0.  Entry
+ * (i, j) of the CSR holds dense[j*n + i] (the column the reference's local
+ * score reads, LooperSolver.hpp:3262).  With col/target NULL only counts. */
+pmmc_status pmmc_arcs_dense_to_csr(int n, const float *dense, int *row_ptr,
+                                   int *col, float *target, int64_t cap,
+                                   int64_t *nnz);
+
+/* ---------------- plain drop-in entry points (host buffers) ----------- */
+/* Replaces float LooperSolver::parallelMonteCarloArcs(float step_size)
+ * (LooperSolver.hpp:682, ParallelMonteCarloArcs.cu:680-944): n_chains
+ * independent chains (0 = 4 per SM, the reference's 128-thread x sm_count
+ * launch), the first converged chain stops the others, the best chain's
+ * positions are written to pos_out. */
+pmmc_status pmmc_arcs_anneal(pmmc_ctx *ctx, const pmmc_arcs_problem *pr,
+                             const pmmc_anneal_params *prm, float step_size,
+                             int n_chains, float *pos_out, pmmc_result *res);
+
+/* Replaces float LooperSolver::ParallelMonteCarloSmooth(float step_size,
+ * unsigned long long seed) (LooperSolver.hpp:482-483,
+ * ParallelMonteCarloSmooth.cu:357-506): n_chains chains (0 = one per SM),
+ * best chain's free beads written to pos_out (fixed beads are copied
+ * through unchanged). */
+pmmc_status pmmc_smooth_anneal(pmmc_ctx *ctx, const pmmc_smooth_problem *pr,
+                               const pmmc_anneal_params *prm, float step_size,
+                               int n_chains, float *pos_out, pmmc_result *res);
+
+/* Replaces float LooperSolver::ParallelMonteCarloHeatmap(float step_size)
+ * (LooperSolver.hpp:469, ParallelMonteCarloHeatmap.cu:365-511) with the
+ * semantics of the reference's CPU MonteCarloHeatmap (LooperSolver.hpp:
+ * 1424-1565): one chain, step_size*0.5, full-score Metropolis with the
+ * score updated incrementally as 2*(local_after - local_before). */
+pmmc_status pmmc_heatmap_anneal(pmmc_ctx *ctx, const pmmc_heatmap_problem *pr,
+                                const pmmc_anneal_params *prm, float step_size,
+                                float *pos_out, pmmc_result *res);
+
+/* Replaces void InteractionArcs::parallelMarkArcs(bool ignore_missing)
+ * (InteractionArcs.hpp, ParallelMarkArcs.cu:69-244) for one chromosome:
+ * anchors sorted by start; raw arcs in genomic coordinates.  Writes up to
+ * cap arcs of 7 ints (start end genomic_start genomic_end score eff_score
+ * factor) in the order of the reference's CPU markArcs
+ * (InteractionArcs.hpp:207-336). */
+pmmc_status pmmc_mark_arcs(pmmc_ctx *ctx, int n_anchors, const int *a_start,
+                           const int *a_end, int n_raw, const int *r_start,
+                           const int *r_end, const int *r_score,
+                           const int *r_factor, int *out, int cap, int *n_out,
+                           int *n_non_matching);
+
+/* ---------------- batched arc annealing (device resident) -------------- */
+/* Many independent active regions (ensemble members x interaction blocks,
+ * the reference's serial loops at LooperSolver.hpp:4026-4138 and
+ * main_reconstruct.cpp:405-477) annealed in one graph launch of persistent
+ * work-stealing kernels.  Units are staged once; run() anneals every unit
+ * from its staged start positions. */
+typedef struct pmmc_arcs_batch pmmc_arcs_batch;
+typedef struct pmmc_batch_opts {
+  int chains_per_unit;   /* independent chains per unit (>= 1)           */
+  int use_graph;         /* capture the launches in a CUDA graph          */
+  int lanes_per_chain;   /* 0 = autotune; else 8, 16 or 32                */
+} pmmc_batch_opts;
+pmmc_status pmmc_arcs_batch_create(pmmc_ctx *ctx, int n_units,
+                                   const pmmc_arcs_problem *units,
+                                   const pmmc_anneal_params *prm,
+                                   const float *step_sizes,
+                                   const pmmc_batch_opts *opts,
+                                   pmmc_arcs_batch **out);
+/* Enqueue one annealing pass of every unit on `stream` (NULL = the
+ * context's stream).  Asynchronous. */
+pmmc_status pmmc_arcs_batch_run(pmmc_arcs_batch *b, void *stream);
+/* Copy results to host (synchronises the batch's stream).  pos_out holds
+ * sum(n_u)*3 floats in unit order; res holds n_units results. */
+pmmc_status pmmc_arcs_batch_results(pmmc_arcs_batch *b, float *pos_out,
+                                    pmmc_result *res);
+/* Per-launch figures of the last run: device time of the annealing kernels
+ * (ms, CUDA events on the batch stream), total moves, lanes per chain. */
+pmmc_status pmmc_arcs_batch_stats(pmmc_arcs_batch *b, double *kernel_ms,
+                                  int64_t *total_moves, int *lanes_per_chain);
+void pmmc_arcs_batch_destroy(pmmc_arcs_batch *b);
+
+/* Host-buffer form of the above: stage, run, fetch, free. */
+pmmc_status pmmc_arcs_batch_anneal(pmmc_ctx *ctx, int n_units,
+                                   const pmmc_arcs_problem *units,
+                                   const pmmc_anneal_params *prm,
+                                   const float *step_sizes,
+                                   const pmmc_batch_opts *opts, float *pos_out,
+                                   pmmc_result *res);
+
+/* pmmc_arcs_batch_create with two more knobs: stop_all != 0 lets the first
+ * converged chain of a unit stop its other chains (the reference's shared
+ * d_isDone flag, ParallelMonteCarloArcs.cu:522,650); trace_cap > 0 records
+ * the first trace_cap moves of chain 0 (bead, local scores before/after,
+ * decision, displacement; 32 bytes each) for per-move parity checks. */
+pmmc_status pmmc_arcs_batch_create_ex(pmmc_ctx *ctx, int n_units,
+                                      const pmmc_arcs_problem *units,
+                                      const pmmc_anneal_params *prm,
+                                      const float *step_sizes,
+                                      const pmmc_batch_opts *opts,
+                                      int stop_all, int trace_cap,
+                                      pmmc_arcs_batch **out);
+/* Copy `count` (<= trace_cap) trace records of the last run to host. */
+pmmc_status pmmc_arcs_batch_trace(pmmc_arcs_batch *b, void *out, int count);
+
+/* ---------------- batched smoothing and heatmap annealing -------------- */
+/* Many smoothing regions (genome-scale smoothing splits chromosomes at their
+ * fixed anchors) with `chains` chains each, one pass; kernel_ms (nullable)
+ * receives the device time of the annealing kernel.  pos_out holds
+ * sum(n_u)*3 floats (best chain of each region). */
+pmmc_status pmmc_smooth_batch_anneal(pmmc_ctx *ctx, int n_units,
+                                     const pmmc_smooth_problem *units,
+                                     const pmmc_anneal_params *prm,
+                                     const float *step_sizes, int chains,
+                                     float *pos_out, pmmc_result *res,
+                                     double *kernel_ms);
+/* Many independent heatmap chains (distinct matrices), one CTA each.
+ * trace_out (nullable) receives trace_cap records of unit 0's first moves. */
+pmmc_status pmmc_heatmap_batch_anneal(pmmc_ctx *ctx, int n_units,
+                                      const pmmc_heatmap_problem *units,
+                                      const pmmc_anneal_params *prm,
+                                      const float *step_sizes, float *pos_out,
+                                      pmmc_result *res, double *kernel_ms,
+                                      void *trace_out, int trace_cap);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* PMMC_GB300_H_ */

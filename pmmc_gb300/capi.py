@@ -1,0 +1,405 @@
+"""ctypes binding of the C ABI (include/pmmc_gb300.h).
+
+The library is the in-tree ``libpmmc_gb300.so`` built by pmmc_gb300.build.
+Importing this module never falls back to anything: if the library is
+missing, :func:`lib` raises; if no GB300 device is present, creating a
+context raises :class:`PmmcError` with PMMC_ERR_NO_DEVICE.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libpmmc_gb300.so")
+
+PMMC_OK = 0
+PMMC_ERR_INVALID = 1
+PMMC_ERR_NO_DEVICE = 2
+PMMC_ERR_CUDA = 3
+PMMC_ERR_NOMEM = 4
+PMMC_ERR_TIMEOUT = 5
+PMMC_ERR_BUDGET = 6
+PMMC_ERR_FIXED = 7
+PMMC_ERR_BUSY = 8
+PMMC_ERR_NOT_FOUND = 9
+
+SCHEDULE_GPU = 0
+SCHEDULE_CPU = 1
+LEVEL_ARCS, LEVEL_HEATMAP, LEVEL_SMOOTH = 0, 1, 2
+
+# Symbols the header declares (checked by the CPU tests without calling them).
+HEADER_SYMBOLS = [
+    "pmmc_ctx_create", "pmmc_ctx_destroy", "pmmc_status_string", "pmmc_last_error",
+    "pmmc_set_seed", "pmmc_sm_count", "pmmc_default_params", "pmmc_arcs_dense_to_csr",
+    "pmmc_arcs_anneal", "pmmc_smooth_anneal", "pmmc_heatmap_anneal", "pmmc_mark_arcs",
+    "pmmc_arcs_batch_create", "pmmc_arcs_batch_run", "pmmc_arcs_batch_results",
+    "pmmc_arcs_batch_stats", "pmmc_arcs_batch_destroy", "pmmc_arcs_batch_anneal",
+    "pmmc_arcs_batch_create_ex", "pmmc_arcs_batch_trace", "pmmc_smooth_batch_anneal",
+    "pmmc_heatmap_batch_anneal",
+]
+
+
+class PmmcError(RuntimeError):
+    def __init__(self, status: int, message: str = ""):
+        self.status = status
+        super().__init__(f"pmmc status {status}: {message}")
+
+
+class AnnealParams(C.Structure):
+    _fields_ = [
+        ("max_temp", C.c_float), ("dt_temp", C.c_float), ("jump_scale", C.c_float),
+        ("jump_coef", C.c_float), ("improvement", C.c_float), ("min_successes", C.c_int),
+        ("milestone_steps", C.c_int), ("k_stretch", C.c_float), ("k_squeeze", C.c_float),
+        ("k_angle", C.c_float), ("w_dist", C.c_float), ("w_angle", C.c_float),
+        ("sphere_radius", C.c_float), ("use2d", C.c_int), ("milestone_fails", C.c_int),
+        ("schedule", C.c_int), ("resync_every", C.c_int), ("max_moves", C.c_int64),
+        ("arcs_extended", C.c_int), ("bond_target", C.c_float),
+        ("k_stretch_bond", C.c_float), ("k_squeeze_bond", C.c_float),
+        ("k_angle_ext", C.c_float),
+    ]
+
+
+class Result(C.Structure):
+    _fields_ = [
+        ("score", C.c_float), ("energy", C.c_double), ("energy_fp64", C.c_double),
+        ("rel_error", C.c_double), ("moves", C.c_int64), ("accepted", C.c_int64),
+        ("total_moves", C.c_int64), ("best_chain", C.c_int), ("status", C.c_int),
+    ]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+class ArcsProblem(C.Structure):
+    _fields_ = [
+        ("n", C.c_int), ("pos", C.c_void_p), ("fixed", C.c_void_p), ("row_ptr", C.c_void_p),
+        ("col", C.c_void_p), ("target", C.c_void_p), ("n_loops", C.c_int),
+        ("loop_i", C.c_void_p), ("loop_j", C.c_void_p), ("loop_k", C.c_void_p),
+        ("loop_r0", C.c_void_p),
+    ]
+
+
+class HeatmapProblem(C.Structure):
+    _fields_ = [
+        ("n", C.c_int), ("pos", C.c_void_p), ("fixed", C.c_void_p), ("heat", C.c_void_p),
+        ("diag", C.c_int), ("n_bounds", C.c_int), ("bounds", C.c_void_p),
+    ]
+
+
+class SmoothProblem(C.Structure):
+    _fields_ = [
+        ("n", C.c_int), ("pos", C.c_void_p), ("fixed", C.c_void_p),
+        ("dist_to_next", C.c_void_p),
+    ]
+
+
+class BatchOpts(C.Structure):
+    _fields_ = [("chains_per_unit", C.c_int), ("use_graph", C.c_int),
+                ("lanes_per_chain", C.c_int)]
+
+
+class MoveTrace(C.Structure):
+    _fields_ = [("bead", C.c_int), ("accepted", C.c_int), ("before", C.c_float),
+                ("after", C.c_float), ("dx", C.c_float), ("dy", C.c_float),
+                ("dz", C.c_float), ("pad", C.c_float)]
+
+
+TRACE_DTYPE = np.dtype([("bead", np.int32), ("accepted", np.int32), ("before", np.float32),
+                        ("after", np.float32), ("dx", np.float32), ("dy", np.float32),
+                        ("dz", np.float32), ("pad", np.float32)])
+
+_lib = None
+
+
+def lib():
+    """Load libpmmc_gb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(
+                f"{LIB_PATH} is missing: build it with "
+                "python -c 'import __graft_entry__ as g; g.build()'")
+        L = C.CDLL(LIB_PATH)
+        L.pmmc_status_string.restype = C.c_char_p
+        L.pmmc_last_error.restype = C.c_char_p
+        L.pmmc_ctx_create.argtypes = [C.POINTER(C.c_void_p), C.c_int]
+        L.pmmc_ctx_destroy.argtypes = [C.c_void_p]
+        L.pmmc_last_error.argtypes = [C.c_void_p]
+        L.pmmc_set_seed.argtypes = [C.c_void_p, C.c_uint64]
+        L.pmmc_sm_count.argtypes = [C.c_void_p]
+        L.pmmc_arcs_batch_destroy.argtypes = [C.c_void_p]
+        _lib = L
+    return _lib
+
+
+def _p(a):
+    return None if a is None else a.ctypes.data_as(C.c_void_p)
+
+
+def _f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def _i32(a):
+    return np.ascontiguousarray(a, dtype=np.int32)
+
+
+def default_params(level: int = LEVEL_ARCS, **kw) -> AnnealParams:
+    p = AnnealParams()
+    lib().pmmc_default_params(int(level), C.byref(p))
+    for k, v in kw.items():
+        if not hasattr(p, k):
+            raise AttributeError(k)
+        setattr(p, k, v)
+    return p
+
+
+def dense_to_csr(dense: np.ndarray):
+    """Reference dense matrix -> (row_ptr, col, target) over both directions
+    (pmmc_arcs_dense_to_csr)."""
+    d = _f32(dense)
+    n = d.shape[0]
+    rp = np.zeros(n + 1, np.int32)
+    nnz = C.c_int64()
+    _check(None, lib().pmmc_arcs_dense_to_csr(n, _p(d), _p(rp), None, None, C.c_int64(0),
+                                              C.byref(nnz)))
+    col = np.zeros(max(nnz.value, 1), np.int32)
+    tgt = np.zeros(max(nnz.value, 1), np.float32)
+    _check(None, lib().pmmc_arcs_dense_to_csr(n, _p(d), _p(rp), _p(col), _p(tgt),
+                                              C.c_int64(nnz.value), C.byref(nnz)))
+    return rp, col[:nnz.value], tgt[:nnz.value]
+
+
+def _check(ctx, status):
+    if status != PMMC_OK:
+        msg = lib().pmmc_status_string(status).decode()
+        if ctx is not None:
+            le = lib().pmmc_last_error(ctx)
+            if le:
+                msg += ": " + le.decode()
+        raise PmmcError(status, msg)
+
+
+class Context:
+    """Owns a pmmc_ctx (replaces the reference's GpuResourceCache)."""
+
+    def __init__(self, device: int = 0):
+        h = C.c_void_p()
+        _check(None, lib().pmmc_ctx_create(C.byref(h), int(device)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            lib().pmmc_ctx_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def check(self, status):
+        _check(self.h, status)
+
+    def set_seed(self, seed: int):
+        lib().pmmc_set_seed(self.h, C.c_uint64(int(seed) & (2**64 - 1)))
+
+    @property
+    def sm_count(self) -> int:
+        return lib().pmmc_sm_count(self.h)
+
+
+class ArcsInput:
+    """Keeps the numpy arrays of one arc problem alive behind the C struct."""
+
+    def __init__(self, pos, row_ptr, col, target, fixed=None, loops=None):
+        self.pos = _f32(pos).reshape(-1, 3)
+        self.row_ptr = _i32(row_ptr)
+        self.col = _i32(col) if len(col) else np.zeros(1, np.int32)
+        self.target = _f32(target) if len(target) else np.zeros(1, np.float32)
+        self.fixed = None if fixed is None else np.ascontiguousarray(fixed, dtype=np.uint8)
+        if loops is None:
+            loops = (np.zeros(0, np.int32),) * 2 + (np.zeros(0, np.float32),) * 2
+        self.li, self.lj = _i32(loops[0]), _i32(loops[1])
+        self.lk, self.lr = _f32(loops[2]), _f32(loops[3])
+        self.n = self.pos.shape[0]
+
+    @classmethod
+    def from_dense(cls, pos, dense, fixed=None, loops=None):
+        rp, col, tgt = dense_to_csr(dense)
+        return cls(pos, rp, col, tgt, fixed, loops)
+
+    def struct(self) -> ArcsProblem:
+        n_l = len(self.li)
+        return ArcsProblem(self.n, _p(self.pos), _p(self.fixed), _p(self.row_ptr), _p(self.col),
+                           _p(self.target), n_l, _p(self.li) if n_l else None,
+                           _p(self.lj) if n_l else None, _p(self.lk) if n_l else None,
+                           _p(self.lr) if n_l else None)
+
+
+class ArcsBatch:
+    """Device-resident batch of arc regions (pmmc_arcs_batch_*)."""
+
+    def __init__(self, ctx: Context, inputs, params: AnnealParams, steps, chains=1,
+                 use_graph=True, stop_all=False, trace_cap=0):
+        self.ctx = ctx
+        self.inputs = list(inputs)
+        arr = (ArcsProblem * len(self.inputs))(*[x.struct() for x in self.inputs])
+        self._arr = arr
+        self.steps = _f32(steps)
+        opts = BatchOpts(int(chains), int(bool(use_graph)), 32)
+        h = C.c_void_p()
+        ctx.check(lib().pmmc_arcs_batch_create_ex(
+            ctx.h, len(self.inputs), arr, C.byref(params), _p(self.steps), C.byref(opts),
+            int(bool(stop_all)), int(trace_cap), C.byref(h)))
+        self.h = h
+        self.trace_cap = trace_cap
+
+    def run(self, stream=None):
+        self.ctx.check(lib().pmmc_arcs_batch_run(self.h, C.c_void_p(stream) if stream else None))
+
+    def results(self):
+        tot = sum(x.n for x in self.inputs)
+        pos = np.zeros((tot, 3), np.float32)
+        res = (Result * len(self.inputs))()
+        self.ctx.check(lib().pmmc_arcs_batch_results(self.h, _p(pos), res))
+        out, off = [], 0
+        for x in self.inputs:
+            out.append(pos[off:off + x.n])
+            off += x.n
+        return out, [r for r in res]
+
+    def stats(self):
+        ms = C.c_double()
+        mv = C.c_int64()
+        lanes = C.c_int()
+        self.ctx.check(lib().pmmc_arcs_batch_stats(self.h, C.byref(ms), C.byref(mv),
+                                                   C.byref(lanes)))
+        return ms.value, mv.value, lanes.value
+
+    def trace(self, count=None):
+        count = self.trace_cap if count is None else count
+        out = np.zeros(count, TRACE_DTYPE)
+        self.ctx.check(lib().pmmc_arcs_batch_trace(self.h, _p(out), int(count)))
+        return out
+
+    def close(self):
+        if self.h:
+            lib().pmmc_arcs_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+def arcs_anneal(ctx: Context, inp: ArcsInput, params: AnnealParams, step: float,
+                n_chains: int = 0):
+    pos = np.zeros((inp.n, 3), np.float32)
+    res = Result()
+    s = inp.struct()
+    ctx.check(lib().pmmc_arcs_anneal(ctx.h, C.byref(s), C.byref(params), C.c_float(step),
+                                     int(n_chains), _p(pos), C.byref(res)))
+    return pos, res
+
+
+class SmoothInput:
+    def __init__(self, pos, dist_to_next, fixed=None):
+        self.pos = _f32(pos).reshape(-1, 3)
+        self.dtn = _f32(dist_to_next)
+        self.fixed = None if fixed is None else np.ascontiguousarray(fixed, dtype=np.uint8)
+        self.n = self.pos.shape[0]
+
+    def struct(self) -> SmoothProblem:
+        return SmoothProblem(self.n, _p(self.pos), _p(self.fixed), _p(self.dtn))
+
+
+def smooth_batch_anneal(ctx: Context, inputs, params: AnnealParams, steps, chains=1):
+    inputs = list(inputs)
+    arr = (SmoothProblem * len(inputs))(*[x.struct() for x in inputs])
+    st = _f32(steps)
+    tot = sum(x.n for x in inputs)
+    pos = np.zeros((tot, 3), np.float32)
+    res = (Result * len(inputs))()
+    ms = C.c_double()
+    ctx.check(lib().pmmc_smooth_batch_anneal(ctx.h, len(inputs), arr, C.byref(params), _p(st),
+                                             int(chains), _p(pos), res, C.byref(ms)))
+    out, off = [], 0
+    for x in inputs:
+        out.append(pos[off:off + x.n])
+        off += x.n
+    return out, [r for r in res], ms.value
+
+
+def smooth_anneal(ctx: Context, inp: SmoothInput, params: AnnealParams, step: float,
+                  n_chains: int = 0):
+    pos = np.zeros((inp.n, 3), np.float32)
+    res = Result()
+    s = inp.struct()
+    ctx.check(lib().pmmc_smooth_anneal(ctx.h, C.byref(s), C.byref(params), C.c_float(step),
+                                       int(n_chains), _p(pos), C.byref(res)))
+    return pos, res
+
+
+class HeatmapInput:
+    def __init__(self, pos, heat, diag=1, bounds=None, fixed=None):
+        self.pos = _f32(pos).reshape(-1, 3)
+        self.heat = _f32(heat)
+        self.diag = int(diag)
+        self.bounds = _i32(bounds if bounds is not None else np.zeros(0, np.int32))
+        self.fixed = None if fixed is None else np.ascontiguousarray(fixed, dtype=np.uint8)
+        self.n = self.pos.shape[0]
+
+    def struct(self) -> HeatmapProblem:
+        nb = len(self.bounds)
+        return HeatmapProblem(self.n, _p(self.pos), _p(self.fixed), _p(self.heat), self.diag,
+                              nb, _p(self.bounds) if nb else None)
+
+
+def heatmap_batch_anneal(ctx: Context, inputs, params: AnnealParams, steps, trace_cap=0):
+    inputs = list(inputs)
+    arr = (HeatmapProblem * len(inputs))(*[x.struct() for x in inputs])
+    st = _f32(steps)
+    tot = sum(x.n for x in inputs)
+    pos = np.zeros((tot, 3), np.float32)
+    res = (Result * len(inputs))()
+    ms = C.c_double()
+    tr = np.zeros(max(trace_cap, 1), TRACE_DTYPE)
+    ctx.check(lib().pmmc_heatmap_batch_anneal(ctx.h, len(inputs), arr, C.byref(params), _p(st),
+                                              _p(pos), res, C.byref(ms),
+                                              _p(tr) if trace_cap else None, int(trace_cap)))
+    out, off = [], 0
+    for x in inputs:
+        out.append(pos[off:off + x.n])
+        off += x.n
+    return out, [r for r in res], ms.value, (tr if trace_cap else None)
+
+
+def heatmap_anneal(ctx: Context, inp: HeatmapInput, params: AnnealParams, step: float):
+    pos = np.zeros((inp.n, 3), np.float32)
+    res = Result()
+    s = inp.struct()
+    ctx.check(lib().pmmc_heatmap_anneal(ctx.h, C.byref(s), C.byref(params), C.c_float(step),
+                                        _p(pos), C.byref(res)))
+    return pos, res
+
+
+def mark_arcs(ctx: Context, anchors, raw):
+    a = _i32(anchors).reshape(-1, 2)
+    r = _i32(raw).reshape(-1, 4)
+    cols = [np.ascontiguousarray(a[:, k]) for k in range(2)]
+    rc = [np.ascontiguousarray(r[:, k]) for k in range(4)]
+    cap = 2 * len(r) + 8
+    out = np.zeros((cap, 7), np.int32)
+    n_out = C.c_int()
+    nm = C.c_int()
+    ctx.check(lib().pmmc_mark_arcs(ctx.h, len(a), _p(cols[0]), _p(cols[1]), len(r), _p(rc[0]),
+                                   _p(rc[1]), _p(rc[2]), _p(rc[3]), _p(out), cap,
+                                   C.byref(n_out), C.byref(nm)))
+    return out[:n_out.value].copy(), nm.value

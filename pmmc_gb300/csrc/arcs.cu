@@ -1,0 +1,909 @@
+// arcs.cu -- arc-level (anchor) simulated annealing on GB300.
+//
+// Energy of an active region (LooperSolver.hpp:3215-3281, 3339-3371,
+// 4700-4730; ParallelMonteCarloArcs.cu:294-351):
+//   springs  sum over arcs (i,j), e_ij >= 1e-6:  k(d)*((d - e)/e)^2,
+//            k = stretch if d >= e else squeeze
+//   loops    sum over loop constraints: k_l (d - r0)^2
+//   sphere   sum over beads: max(0, |p| - R)^2
+//   and, in the initial score only, 1/d for every pair without an arc (the
+//   reference's -1 entries).  Moves are scored incrementally on the moved
+//   bead's arcs, so the running total is  R0 + springs + loops + sphere  with
+//   R0 the repulsion of the starting structure; the FP64 recompute uses the
+//   same definition.
+//
+// Layout in device memory: beads as float4 (16 B, one vector load), per-bead
+// arc lists as CSR with {col, target} packed in one int2 (8 B).  A chain is
+// one warp: the region's positions and arc lists are staged in the warp's
+// slice of shared memory (arc lists fall back to L1-cached global loads when
+// the region is too large), the Philox draws of 32 moves are made at once
+// (lane l draws move m+l: bead, displacement and the precomputed Metropolis
+// ratio threshold), and each move evaluates the moved bead's arcs with one
+// lane per arc and an xor-butterfly as wide as the bead's degree.  Lane 0
+// takes the decision and owns the chain state; the running energy is kept in
+// FP64, the per-move delta in FP32.
+//
+// Work distribution: persistent warps pull (unit, chain) items from an atomic
+// queue (largest regions first), one launch per shared-memory size class, the
+// classes on forked streams and the whole pass captured in a CUDA graph.
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <map>
+#include <numeric>
+#include <vector>
+
+#include "common.cuh"
+#include "internal.h"
+
+namespace pmmc {
+
+struct ArcsUnit {
+  int n;          // beads
+  int n_mov;      // movable beads
+  int pos_off;    // float4 index into pos0
+  int rp_off;     // index into row_ptr (n+1 entries, unit-relative values)
+  int nbr_off;    // index into nbr
+  int nnz;
+  int mov_off;    // index into movable, -1 = all beads movable
+  int lrp_off;    // index into loop row_ptr (n+1), -1 = no loops
+  int lent_off;   // index into loop entries
+  int n_lent;
+  int lst_off;    // index into the loop list (one entry per constraint)
+  int n_loops;
+  int chains;
+  int chain_base; // global chain id of the unit's chain 0
+  long long out_off;  // float index of chain 0's xyz output
+  float step;
+  int pad;
+};
+
+struct ArcsDevParams {
+  float max_temp;
+  float inv_scale;
+  float inv_coef;
+  float improvement;
+  float k_stretch;
+  float k_squeeze;
+  float sphere_r;
+  int min_successes;
+  int window;      // milestone window (moves)
+  int fails;       // consecutive misses that stop a chain
+  int resync;      // FP64 recompute interval (0 = off)
+  int use2d;
+  int stop_all;    // the first converged chain stops the unit's others
+  int trace_cap;
+  long long cap;   // hard move cap
+  int cap_is_error;
+  int pad;
+  uint64_t seed;
+  double dtpow[33];  // dt^l, l = 0..32
+};
+
+constexpr int kMoveBufBytes = 32 * 16 + 32 * 4;  // int4 moves + float thresholds
+
+__device__ __forceinline__ float spring(float len, float t, float ks, float kq) {
+  const float f = (len - t) / t;
+  return f * f * (f >= 0.0f ? ks : kq);
+}
+
+__device__ __forceinline__ float dist3(float ax, float ay, float az, float4 b) {
+  const float x = ax - b.x, y = ay - b.y, z = az - b.z;
+  return sqrtf(x * x + y * y + z * z);
+}
+
+// FP64 energy without repulsion: springs (pairs counted once, col < row so
+// that the target is the reference's upper-triangle entry v[col][row]),
+// loops and sphere.  Whole warp; result on every lane.
+__device__ double arcs_spring_energy(int n, const float4 *spos, const int *srp,
+                                     const int2 *nb, const int4 *loops,
+                                     int n_loops, const ArcsDevParams &P,
+                                     int lane) {
+  double acc = 0.0;
+  for (int i = lane; i < n; i += 32) {
+    const float4 pi = spos[i];
+    const int e1 = srp[i + 1];
+    for (int e = srp[i]; e < e1; ++e) {
+      const int2 ent = nb[e];
+      if (ent.x >= i) continue;
+      const float t = __int_as_float(ent.y);
+      if (t < 1e-6f) continue;
+      const float f = (dist3(pi.x, pi.y, pi.z, spos[ent.x]) - t) / t;
+      const double df = f;
+      acc += df * df * (double)(df >= 0.0 ? P.k_stretch : P.k_squeeze);
+    }
+    acc += sphere_penalty(pi.x, pi.y, pi.z, P.sphere_r);
+  }
+  for (int c = lane; c < n_loops; c += 32) {
+    const int4 L = loops[c];
+    const double d = dist3(spos[L.x].x, spos[L.x].y, spos[L.x].z, spos[L.y]);
+    const double delta = d - (double)__int_as_float(L.w);
+    acc += (double)__int_as_float(L.z) * delta * delta;
+  }
+  return warp_sum_d(acc);
+}
+
+// FP64 sum of 1/d over every pair (i<j) that the arc lists do not name.
+__device__ double arcs_repulsion(int n, const float4 *spos, const int *srp,
+                                 const int2 *nb, int lane) {
+  double acc = 0.0;
+  for (int i = lane; i < n; i += 32) {
+    const float4 pi = spos[i];
+    float part = 0.0f;
+    int cnt = 0;
+    for (int j = i + 1; j < n; ++j) {
+      part += 1.0f / dist3(pi.x, pi.y, pi.z, spos[j]);
+      if (++cnt == 64) {
+        acc += part;
+        part = 0.0f;
+        cnt = 0;
+      }
+    }
+    acc += part;
+    const int e1 = srp[i + 1];
+    for (int e = srp[i]; e < e1; ++e) {
+      const int j = nb[e].x;
+      if (j > i) acc -= (double)(1.0f / dist3(pi.x, pi.y, pi.z, spos[j]));
+    }
+  }
+  return warp_sum_d(acc);
+}
+
+__global__ void __launch_bounds__(128)
+arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
+                   const int2 *__restrict__ items, int n_items,
+                   int *__restrict__ head, const float4 *__restrict__ pos0,
+                   const int *__restrict__ row_ptr,
+                   const int2 *__restrict__ nbr, const int *__restrict__ movable,
+                   const int *__restrict__ lrp, const float4 *__restrict__ lent,
+                   const int4 *__restrict__ lst, ArcsDevParams P,
+                   int smem_per_warp, float *__restrict__ pos_out,
+                   ChainOut *__restrict__ outs, int *__restrict__ done,
+                   MoveTrace *__restrict__ trace) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const int lane = threadIdx.x & 31;
+  unsigned char *wbase = smem + (size_t)(threadIdx.x >> 5) * smem_per_warp;
+  int4 *s_mv = reinterpret_cast<int4 *>(wbase);
+  float *s_thr = reinterpret_cast<float *>(wbase + 32 * 16);
+  float4 *spos = reinterpret_cast<float4 *>(wbase + kMoveBufBytes);
+
+  for (;;) {
+    int item = 0;
+    if (lane == 0) item = atomicAdd(head, 1);
+    item = __shfl_sync(0xffffffffu, item, 0);
+    if (item >= n_items) break;
+    const int2 it = items[item];
+    const ArcsUnit U = units[it.x];
+    const int chain = it.y;
+    const int n = U.n;
+    const uint32_t chain_id = (uint32_t)(U.chain_base + chain);
+    int *done_flag = done + it.x;
+
+    // ---- stage the region in this warp's shared-memory slice ----
+    int *srp = reinterpret_cast<int *>(spos + n);
+    size_t off = (size_t)kMoveBufBytes + (size_t)n * 16 + (size_t)(n + 1) * 4;
+    off = (off + 7) & ~(size_t)7;
+    const bool nb_smem = off + (size_t)U.nnz * 8 <= (size_t)smem_per_warp;
+    int2 *snb = reinterpret_cast<int2 *>(wbase + off);
+    if (nb_smem) off += (size_t)U.nnz * 8;
+    const bool has_mov = U.mov_off >= 0;
+    const bool mov_smem = has_mov && off + (size_t)U.n_mov * 4 <= (size_t)smem_per_warp;
+    int *smov = reinterpret_cast<int *>(wbase + off);
+
+    for (int i = lane; i < n; i += 32) spos[i] = pos0[U.pos_off + i];
+    for (int i = lane; i <= n; i += 32) srp[i] = row_ptr[U.rp_off + i];
+    if (nb_smem)
+      for (int e = lane; e < U.nnz; e += 32) snb[e] = nbr[U.nbr_off + e];
+    if (mov_smem)
+      for (int k = lane; k < U.n_mov; k += 32) smov[k] = movable[U.mov_off + k];
+    __syncwarp();
+    const int2 *NB = nb_smem ? snb : nbr + U.nbr_off;
+    const int *MOV = has_mov ? (mov_smem ? smov : movable + U.mov_off) : nullptr;
+    const bool has_loops = U.lrp_off >= 0;
+    const int *LRP = has_loops ? lrp + U.lrp_off : nullptr;
+    const float4 *LENT = has_loops ? lent + U.lent_off : nullptr;
+    const int4 *LST = lst + U.lst_off;
+
+    // ---- initial FP64 energy: repulsion (frozen) + springs/loops/sphere ----
+    const double base = arcs_repulsion(n, spos, srp, NB, lane);
+    double E = base + arcs_spring_energy(n, spos, srp, NB, LST, U.n_loops, P, lane);
+    float Ef = (float)E;
+    double E_ms = E;
+    double T = P.max_temp;
+    long long moves = 0, accepted = 0;
+    int succ_ms = 0, misses = 0, status = kDevOk;
+    bool stop = U.n_mov == 0;
+    if (stop) status = kDevNoMovable;
+    const float step = U.step;
+    const float ks = P.k_stretch, kq = P.k_squeeze, R = P.sphere_r;
+    const bool tracing = trace != nullptr && chain_id == 0;
+    int batch_no = 0;
+
+    while (!stop) {
+      // ---- Philox draws of the next 32 moves: lane l draws move m+l ----
+      {
+        const uint64_t m = (uint64_t)moves + lane;
+        const uint4 r = philox_move(P.seed, chain_id, m, 0u);
+        const uint4 a = philox_move(P.seed, chain_id, m, 1u);
+        const int k = uniform_index(r.x, U.n_mov);
+        const int b = MOV ? MOV[k] : k;
+        const float dx = (2.0f * u01(r.y) - 1.0f) * step;
+        const float dy = (2.0f * u01(r.z) - 1.0f) * step;
+        const float dz = P.use2d ? 0.0f : (2.0f * u01(r.w) - 1.0f) * step;
+        const float Tl = (float)(T * P.dtpow[lane]);
+        s_mv[lane] = make_int4(b, __float_as_int(dx), __float_as_int(dy),
+                               __float_as_int(dz));
+        s_thr[lane] = ratio_threshold(u01(a.x), Tl, P.inv_scale, P.inv_coef);
+      }
+      long long kmax = 32;
+      kmax = min(kmax, (long long)(P.window - (int)(moves % P.window)));
+      if (P.resync > 0) kmax = min(kmax, (long long)(P.resync - (int)(moves % P.resync)));
+      kmax = min(kmax, P.cap - moves);
+      __syncwarp();
+
+      for (int k = 0; k < (int)kmax; ++k) {
+        const int4 mv = s_mv[k];
+        const int b = mv.x;
+        const float dx = __int_as_float(mv.y), dy = __int_as_float(mv.z),
+                    dz = __int_as_float(mv.w);
+        const float4 pb = spos[b];
+        const float nx = pb.x + dx, ny = pb.y + dy, nz = pb.z + dz;
+        const int beg = srp[b], end = srp[b + 1];
+        float so = 0.0f, sn = 0.0f;
+        for (int e = beg + lane; e < end; e += 32) {
+          const int2 ent = NB[e];
+          const float t = __int_as_float(ent.y);
+          if (t >= 1e-6f) {
+            const float4 pj = spos[ent.x];
+            so += spring(dist3(pb.x, pb.y, pb.z, pj), t, ks, kq);
+            sn += spring(dist3(nx, ny, nz, pj), t, ks, kq);
+          }
+        }
+        int width = end - beg;
+        if (has_loops) {
+          const int l0 = LRP[b], l1 = LRP[b + 1];
+          for (int e = l0 + lane; e < l1; e += 32) {
+            const float4 le = LENT[e];
+            const float4 pj = spos[__float_as_int(le.x)];
+            const float d0 = dist3(pb.x, pb.y, pb.z, pj) - le.z;
+            const float d1 = dist3(nx, ny, nz, pj) - le.z;
+            so += le.y * d0 * d0;
+            sn += le.y * d1 * d1;
+          }
+          width = max(width, l1 - l0);
+        }
+        if (lane == 0 && R > 0.0f) {
+          so += sphere_penalty(pb.x, pb.y, pb.z, R);
+          sn += sphere_penalty(nx, ny, nz, R);
+        }
+        if (width > 1) {
+          const int w = width >= 32 ? 32 : (1 << (32 - __clz(width - 1)));
+          for (int o = w >> 1; o > 0; o >>= 1) {
+            so += __shfl_xor_sync(0xffffffffu, so, o);
+            sn += __shfl_xor_sync(0xffffffffu, sn, o);
+          }
+        }
+        if (lane == 0) {
+          const float d = sn - so;
+          const bool acc = (d <= 0.0f) || (d < Ef * (s_thr[k] - 1.0f));
+          if (acc) {
+            spos[b] = make_float4(nx, ny, nz, 0.0f);
+            E += (double)d;
+            Ef = (float)E;
+            ++accepted;
+            ++succ_ms;
+          }
+          if (tracing && moves + k < P.trace_cap) {
+            MoveTrace tr;
+            tr.bead = b;
+            tr.accepted = acc ? 1 : 0;
+            tr.before = so;
+            tr.after = sn;
+            tr.dx = dx;
+            tr.dy = dy;
+            tr.dz = dz;
+            tr.pad = 0.0f;
+            trace[moves + k] = tr;
+          }
+        }
+        __syncwarp();
+      }
+      moves += kmax;
+      T *= P.dtpow[kmax];
+      ++batch_no;
+
+      // ---- milestone (the reference CPU predicate, FP64, lane 0) ----
+      int flag = 0;
+      if (moves % P.window == 0) {
+        if (lane == 0) {
+          const bool miss =
+              (E > (double)P.improvement * E_ms && succ_ms < P.min_successes) ||
+              E < 1e-5 || E / E_ms > 0.9999;
+          misses = miss ? misses + 1 : 0;
+          if (misses >= P.fails || E < 1e-5) flag = 1;
+          E_ms = E;
+          succ_ms = 0;
+        }
+      }
+      if (P.resync > 0 && moves % P.resync == 0 && !__shfl_sync(0xffffffffu, flag, 0)) {
+        const double es = arcs_spring_energy(n, spos, srp, NB, LST, U.n_loops, P, lane);
+        if (lane == 0) {
+          E = base + es;
+          Ef = (float)E;
+        }
+      }
+      if (lane == 0) {
+        if (!flag && moves >= P.cap) {
+          flag = 1;
+          if (P.cap_is_error) status = kDevMoveCap;
+        }
+        if (flag && P.stop_all) atomicExch(done_flag, 1);
+        if (!flag && P.stop_all && (batch_no & 7) == 0 &&
+            *((volatile int *)done_flag) != 0)
+          flag = 1;
+      }
+      stop = __shfl_sync(0xffffffffu, flag, 0) != 0;
+    }
+
+    // ---- final FP64 recompute and outputs ----
+    const double es = arcs_spring_energy(n, spos, srp, NB, LST, U.n_loops, P, lane);
+    if (lane == 0) {
+      ChainOut o;
+      o.energy = E;
+      o.energy_fp64 = base + es;
+      o.base = base;
+      o.score = (float)E;
+      o.status = status;
+      o.moves = moves;
+      o.accepted = accepted;
+      outs[U.chain_base + chain] = o;
+    }
+    float *po = pos_out + U.out_off + (long long)chain * n * 3;
+    for (int i = lane; i < n; i += 32) {
+      const float4 p = spos[i];
+      po[3 * i] = p.x;
+      po[3 * i + 1] = p.y;
+      po[3 * i + 2] = p.z;
+    }
+    __syncwarp();
+  }
+}
+
+// Best chain of each unit (lowest running energy, ties to the lower index,
+// as the reference's host argmin, ParallelMonteCarloArcs.cu:899-910).
+__global__ void arcs_pick_best_kernel(const ArcsUnit *__restrict__ units,
+                                      int n_units, const ChainOut *outs,
+                                      int *best) {
+  const int u = blockIdx.x * blockDim.x + threadIdx.x;
+  if (u >= n_units) return;
+  const ArcsUnit U = units[u];
+  int b = 0;
+  double be = outs[U.chain_base].energy;
+  for (int c = 1; c < U.chains; ++c) {
+    const double e = outs[U.chain_base + c].energy;
+    if (e < be) {
+      be = e;
+      b = c;
+    }
+  }
+  best[u] = b;
+}
+
+}  // namespace pmmc
+
+// ===========================================================================
+// Host side
+// ===========================================================================
+using namespace pmmc;
+
+struct ArcsClass {
+  int item_begin = 0, item_end = 0;
+  int smem_per_warp = 0;
+  int warps_per_cta = 1;
+  int grid = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t join = nullptr;
+};
+
+struct pmmc_arcs_batch {
+  pmmc_ctx *ctx = nullptr;
+  int n_units = 0;
+  std::vector<ArcsUnit> h_units;
+  std::vector<int> h_n;
+  long long total_pos_out = 0;  // floats over all chains
+  int total_chains = 0;
+  ArcsDevParams P{};
+  DevBuf<ArcsUnit> units;
+  DevBuf<int2> items;
+  DevBuf<int> heads;
+  DevBuf<float4> pos0;
+  DevBuf<int> row_ptr;
+  DevBuf<int2> nbr;
+  DevBuf<int> movable;
+  DevBuf<int> lrp;
+  DevBuf<float4> lent;
+  DevBuf<int4> lst;
+  DevBuf<float> pos_out;
+  DevBuf<ChainOut> outs;
+  DevBuf<int> done;
+  DevBuf<int> best;
+  MoveTrace *trace = nullptr;  // tests only (owned)
+  std::vector<ArcsClass> classes;
+  cudaEvent_t ev_fork = nullptr, ev_start = nullptr, ev_stop = nullptr;
+  cudaGraphExec_t graph = nullptr;
+  bool use_graph = true;
+  bool ran = false;
+  int lanes = 32;
+
+  ~pmmc_arcs_batch() {
+    for (auto &c : classes) {
+      if (c.stream) cudaStreamDestroy(c.stream);
+      if (c.join) cudaEventDestroy(c.join);
+    }
+    if (ev_fork) cudaEventDestroy(ev_fork);
+    if (ev_start) cudaEventDestroy(ev_start);
+    if (ev_stop) cudaEventDestroy(ev_stop);
+    if (graph) cudaGraphExecDestroy(graph);
+    if (trace) cudaFree(trace);
+  }
+};
+
+namespace {
+
+size_t unit_smem(int n, int nnz, int n_mov, bool has_mov) {
+  size_t s = (size_t)kMoveBufBytes + (size_t)n * 16 + (size_t)(n + 1) * 4;
+  s = (s + 7) & ~(size_t)7;
+  s += (size_t)nnz * 8;
+  if (has_mov) s += (size_t)n_mov * 4;
+  return s;
+}
+
+size_t unit_smem_min(int n) {
+  size_t s = (size_t)kMoveBufBytes + (size_t)n * 16 + (size_t)(n + 1) * 4;
+  return (s + 7) & ~(size_t)7;
+}
+
+pmmc_status validate_arcs(pmmc_ctx *ctx, const pmmc_arcs_problem *pr) {
+  if (!pr || pr->n < 1 || !pr->pos || !pr->row_ptr)
+    return fail(ctx, PMMC_ERR_INVALID, "arcs problem: n, pos and row_ptr are required");
+  if (pr->row_ptr[0] != 0)
+    return fail(ctx, PMMC_ERR_INVALID, "arcs problem: row_ptr[0] must be 0");
+  for (int i = 0; i < pr->n; ++i)
+    if (pr->row_ptr[i + 1] < pr->row_ptr[i])
+      return fail(ctx, PMMC_ERR_INVALID, "arcs problem: row_ptr not monotone");
+  const int nnz = pr->row_ptr[pr->n];
+  if (nnz > 0 && (!pr->col || !pr->target))
+    return fail(ctx, PMMC_ERR_INVALID, "arcs problem: col/target missing");
+  for (int e = 0; e < nnz; ++e)
+    if (pr->col[e] < 0 || pr->col[e] >= pr->n)
+      return fail(ctx, PMMC_ERR_INVALID, "arcs problem: column %d out of range", pr->col[e]);
+  if (pr->n_loops < 0 || (pr->n_loops > 0 && (!pr->loop_i || !pr->loop_j ||
+                                               !pr->loop_k || !pr->loop_r0)))
+    return fail(ctx, PMMC_ERR_INVALID, "arcs problem: loop arrays missing");
+  return PMMC_OK;
+}
+
+ArcsDevParams make_params(const pmmc_anneal_params *prm, uint64_t seed,
+                          bool stop_all) {
+  ArcsDevParams P{};
+  P.max_temp = prm->max_temp;
+  P.inv_scale = prm->jump_scale != 0.0f ? 1.0f / prm->jump_scale : 0.0f;
+  P.inv_coef = prm->jump_coef != 0.0f ? 1.0f / prm->jump_coef : 0.0f;
+  P.improvement = prm->improvement;
+  P.k_stretch = prm->k_stretch;
+  P.k_squeeze = prm->k_squeeze;
+  P.sphere_r = prm->sphere_radius;
+  P.min_successes = prm->min_successes;
+  P.use2d = prm->use2d;
+  P.resync = prm->resync_every > 0 ? prm->resync_every : 0;
+  P.stop_all = stop_all ? 1 : 0;
+  P.seed = seed;
+  if (prm->schedule == PMMC_SCHEDULE_CPU) {
+    P.window = std::max(1, prm->milestone_steps);
+    P.fails = 1;
+    P.cap = prm->max_moves > 0 ? prm->max_moves : 200ll * P.window;
+    P.cap_is_error = 0;
+  } else {
+    P.window = 256;
+    P.fails = std::max(1, prm->milestone_fails);
+    long long cap = std::max(1, prm->milestone_steps);
+    cap = (cap + 255) / 256 * 256;
+    if (prm->max_moves > 0) cap = std::min(cap, (long long)prm->max_moves);
+    P.cap = cap;
+    P.cap_is_error = 0;
+  }
+  double d = 1.0;
+  for (int l = 0; l <= 32; ++l) {
+    P.dtpow[l] = d;
+    d *= (double)prm->dt_temp;
+  }
+  return P;
+}
+
+}  // namespace
+
+extern "C" pmmc_status pmmc_arcs_batch_create_ex(
+    pmmc_ctx *ctx, int n_units, const pmmc_arcs_problem *units,
+    const pmmc_anneal_params *prm, const float *steps,
+    const pmmc_batch_opts *opts, int stop_all, int trace_cap,
+    pmmc_arcs_batch **out) {
+  if (!ctx || !out || n_units < 1 || !units || !prm || !steps)
+    return fail(ctx, PMMC_ERR_INVALID, "arcs batch: bad arguments");
+  *out = nullptr;
+  const int chains = opts && opts->chains_per_unit > 0 ? opts->chains_per_unit : 1;
+  for (int u = 0; u < n_units; ++u) {
+    pmmc_status s = validate_arcs(ctx, &units[u]);
+    if (s != PMMC_OK) return s;
+  }
+  auto *b = new pmmc_arcs_batch();
+  b->ctx = ctx;
+  b->n_units = n_units;
+  b->use_graph = !opts || opts->use_graph != 0;
+  b->P = make_params(prm, next_key(ctx), stop_all != 0);
+  b->P.trace_cap = trace_cap;
+
+  // ---- pack host arrays ----
+  std::vector<float4> h_pos;
+  std::vector<int> h_rp, h_mov, h_lrp;
+  std::vector<int2> h_nbr;
+  std::vector<float4> h_lent;
+  std::vector<int4> h_lst;
+  b->h_units.resize(n_units);
+  b->h_n.resize(n_units);
+  long long out_off = 0;
+  int chain_base = 0;
+  for (int u = 0; u < n_units; ++u) {
+    const pmmc_arcs_problem &pr = units[u];
+    ArcsUnit U{};
+    U.n = pr.n;
+    U.pos_off = (int)h_pos.size();
+    for (int i = 0; i < pr.n; ++i)
+      h_pos.push_back(make_float4(pr.pos[3 * i], pr.pos[3 * i + 1], pr.pos[3 * i + 2], 0.0f));
+    U.rp_off = (int)h_rp.size();
+    for (int i = 0; i <= pr.n; ++i) h_rp.push_back(pr.row_ptr[i]);
+    U.nbr_off = (int)h_nbr.size();
+    U.nnz = pr.row_ptr[pr.n];
+    for (int e = 0; e < U.nnz; ++e) {
+      int2 v;
+      v.x = pr.col[e];
+      v.y = __float_as_int_host(pr.target[e]);
+      h_nbr.push_back(v);
+    }
+    int nm = 0;
+    std::vector<int> mv;
+    for (int i = 0; i < pr.n; ++i)
+      if (!pr.fixed || !pr.fixed[i]) mv.push_back(i);
+    nm = (int)mv.size();
+    U.n_mov = nm;
+    if (nm < pr.n) {
+      U.mov_off = (int)h_mov.size();
+      h_mov.insert(h_mov.end(), mv.begin(), mv.end());
+    } else {
+      U.mov_off = -1;
+    }
+    // loop constraints: rebuildActiveLoopMap (LooperSolver.hpp:3318-3337):
+    // key (min,max), the last constraint of a key wins, std::map order.
+    std::map<std::pair<int, int>, int> lm;
+    for (int c = 0; c < pr.n_loops; ++c) {
+      int i = pr.loop_i[c], j = pr.loop_j[c];
+      if (i < 0 || j < 0 || i >= pr.n || j >= pr.n) continue;
+      lm[i < j ? std::make_pair(i, j) : std::make_pair(j, i)] = c;
+    }
+    U.lst_off = (int)h_lst.size();
+    U.n_loops = (int)lm.size();
+    if (!lm.empty()) {
+      std::vector<std::vector<float4>> per(pr.n);
+      for (auto &kv : lm) {
+        const int c = kv.second, i = kv.first.first, j = kv.first.second;
+        int4 L;
+        L.x = i;
+        L.y = j;
+        L.z = __float_as_int_host(pr.loop_k[c]);
+        L.w = __float_as_int_host(pr.loop_r0[c]);
+        h_lst.push_back(L);
+        per[i].push_back(make_float4(__int_as_float_host(j), pr.loop_k[c], pr.loop_r0[c], 0.0f));
+        if (j != i)
+          per[j].push_back(make_float4(__int_as_float_host(i), pr.loop_k[c], pr.loop_r0[c], 0.0f));
+      }
+      U.lrp_off = (int)h_lrp.size();
+      U.lent_off = (int)h_lent.size();
+      int acc = 0;
+      for (int i = 0; i < pr.n; ++i) {
+        h_lrp.push_back(acc);
+        for (auto &e : per[i]) h_lent.push_back(e);
+        acc += (int)per[i].size();
+      }
+      h_lrp.push_back(acc);
+      U.n_lent = acc;
+    } else {
+      U.lrp_off = -1;
+      U.lent_off = 0;
+      U.n_lent = 0;
+    }
+    U.chains = chains;
+    U.chain_base = chain_base;
+    U.out_off = out_off;
+    U.step = steps[u];
+    chain_base += chains;
+    out_off += (long long)chains * pr.n * 3;
+    b->h_units[u] = U;
+    b->h_n[u] = pr.n;
+  }
+  b->total_pos_out = out_off;
+  b->total_chains = chain_base;
+  if (h_lst.empty()) h_lst.push_back(make_int4(0, 0, 0, 0));
+
+  // ---- shared-memory classes: items sorted by need, largest first ----
+  const size_t cap_smem = ctx->smem_optin;
+  struct Need { int unit; size_t bytes; };
+  std::vector<Need> needs(n_units);
+  for (int u = 0; u < n_units; ++u) {
+    const ArcsUnit &U = b->h_units[u];
+    size_t full = unit_smem(U.n, U.nnz, U.n_mov, U.mov_off >= 0);
+    size_t minimal = unit_smem_min(U.n);
+    if (minimal > cap_smem) {
+      delete b;
+      return fail(ctx, PMMC_ERR_INVALID,
+                  "arcs batch: region of %d beads exceeds the %zu B shared-memory "
+                  "slice a chain can hold", U.n, cap_smem);
+    }
+    needs[u] = {u, std::min(full, cap_smem)};
+  }
+  std::stable_sort(needs.begin(), needs.end(),
+                   [](const Need &a, const Need &c) { return a.bytes > c.bytes; });
+  // classes: a class holds units whose need is within 2x of its largest
+  std::vector<int2> h_items;
+  cudaFuncSetAttribute(arcs_anneal_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)cap_smem);
+  size_t i0 = 0;
+  while (i0 < needs.size()) {
+    size_t top = needs[i0].bytes;
+    size_t i1 = i0;
+    while (i1 < needs.size() && needs[i1].bytes * 2 > top) ++i1;
+    ArcsClass c;
+    c.item_begin = (int)h_items.size();
+    for (size_t k = i0; k < i1; ++k)
+      for (int ch = 0; ch < chains; ++ch) h_items.push_back(make_int2(needs[k].unit, ch));
+    c.item_end = (int)h_items.size();
+    c.smem_per_warp = (int)((top + 15) & ~(size_t)15);
+    // warps per CTA: keep a CTA's footprint within the opt-in limit
+    int w = 4;
+    while (w > 1 && (size_t)w * c.smem_per_warp > cap_smem) w >>= 1;
+    c.warps_per_cta = w;
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, arcs_anneal_kernel, 32 * w,
+                                                  (size_t)w * c.smem_per_warp);
+    if (per_sm < 1) per_sm = 1;
+    const int items_n = c.item_end - c.item_begin;
+    c.grid = std::max(1, std::min(per_sm * ctx->sm_count, (items_n + w - 1) / w));
+    b->classes.push_back(c);
+    i0 = i1;
+  }
+
+  // ---- upload ----
+  cudaStream_t s = ctx->stream;
+  cudaError_t e = cudaSuccess;
+#define UP(buf, vec)                                                           \
+  if (e == cudaSuccess) e = b->buf.upload(vec, s);
+  std::vector<ArcsUnit> hu = b->h_units;
+  UP(units, hu);
+  UP(items, h_items);
+  UP(pos0, h_pos);
+  UP(row_ptr, h_rp);
+  UP(nbr, h_nbr);
+  UP(movable, h_mov);
+  UP(lrp, h_lrp);
+  UP(lent, h_lent);
+  UP(lst, h_lst);
+#undef UP
+  if (e == cudaSuccess) e = b->heads.alloc(b->classes.size());
+  if (e == cudaSuccess) e = b->pos_out.alloc((size_t)out_off);
+  if (e == cudaSuccess) e = b->outs.alloc((size_t)chain_base);
+  if (e == cudaSuccess) e = b->done.alloc((size_t)n_units);
+  if (e == cudaSuccess) e = b->best.alloc((size_t)n_units);
+  if (e == cudaSuccess && trace_cap > 0)
+    e = cudaMalloc(&b->trace, sizeof(MoveTrace) * (size_t)trace_cap);
+  if (e == cudaSuccess) e = cudaEventCreate(&b->ev_fork);
+  if (e == cudaSuccess) e = cudaEventCreate(&b->ev_start);
+  if (e == cudaSuccess) e = cudaEventCreate(&b->ev_stop);
+  for (auto &c : b->classes) {
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c.join, cudaEventDisableTiming);
+  }
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) {
+    delete b;
+    return fail(ctx, e == cudaErrorMemoryAllocation ? PMMC_ERR_NOMEM : PMMC_ERR_CUDA,
+                "arcs batch upload: %s", cudaGetErrorString(e));
+  }
+  *out = b;
+  return PMMC_OK;
+}
+
+namespace {
+
+cudaError_t enqueue_pass(pmmc_arcs_batch *b, cudaStream_t s) {
+  cudaError_t e = cudaMemsetAsync(b->heads.p, 0, sizeof(int) * b->classes.size(), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(b->done.p, 0, sizeof(int) * b->n_units, s);
+  if (e != cudaSuccess) return e;
+  e = cudaEventRecord(b->ev_fork, s);
+  for (size_t k = 0; k < b->classes.size() && e == cudaSuccess; ++k) {
+    ArcsClass &c = b->classes[k];
+    e = cudaStreamWaitEvent(c.stream, b->ev_fork, 0);
+    if (e != cudaSuccess) break;
+    arcs_anneal_kernel<<<c.grid, 32 * c.warps_per_cta,
+                         (size_t)c.warps_per_cta * c.smem_per_warp, c.stream>>>(
+        b->units.p, b->items.p + c.item_begin, c.item_end - c.item_begin,
+        b->heads.p + k, b->pos0.p, b->row_ptr.p, b->nbr.p, b->movable.p, b->lrp.p,
+        b->lent.p, b->lst.p, b->P, c.smem_per_warp, b->pos_out.p, b->outs.p,
+        b->done.p, b->trace);
+    e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaEventRecord(c.join, c.stream);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(s, c.join, 0);
+  }
+  if (e == cudaSuccess && b->classes.size() > 0 &&
+      b->h_units.size() > 0) {
+    int need_best = 0;
+    for (auto &U : b->h_units) need_best |= U.chains > 1;
+    if (need_best) {
+      arcs_pick_best_kernel<<<(b->n_units + 127) / 128, 128, 0, s>>>(
+          b->units.p, b->n_units, b->outs.p, b->best.p);
+      e = cudaGetLastError();
+    }
+  }
+  return e;
+}
+
+}  // namespace
+
+extern "C" pmmc_status pmmc_arcs_batch_create(pmmc_ctx *ctx, int n_units,
+                                              const pmmc_arcs_problem *units,
+                                              const pmmc_anneal_params *prm,
+                                              const float *step_sizes,
+                                              const pmmc_batch_opts *opts,
+                                              pmmc_arcs_batch **out) {
+  return pmmc_arcs_batch_create_ex(ctx, n_units, units, prm, step_sizes, opts, 0, 0, out);
+}
+
+extern "C" pmmc_status pmmc_arcs_batch_run(pmmc_arcs_batch *b, void *stream) {
+  if (!b) return PMMC_ERR_INVALID;
+  pmmc_ctx *ctx = b->ctx;
+  cudaStream_t s = stream ? (cudaStream_t)stream : ctx->stream;
+  PMMC_CUDA(ctx, cudaEventRecord(b->ev_start, s));
+  if (b->use_graph) {
+    if (!b->graph) {
+      cudaStream_t cap;
+      PMMC_CUDA(ctx, cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+      cudaGraph_t g = nullptr;
+      cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+      if (e == cudaSuccess) {
+        cudaError_t e2 = enqueue_pass(b, cap);
+        e = cudaStreamEndCapture(cap, &g);
+        if (e2 != cudaSuccess) e = e2;
+      }
+      if (e == cudaSuccess) e = cudaGraphInstantiate(&b->graph, g, 0);
+      if (g) cudaGraphDestroy(g);
+      cudaStreamDestroy(cap);
+      if (e != cudaSuccess)
+        return fail(ctx, PMMC_ERR_CUDA, "arcs batch graph capture: %s", cudaGetErrorString(e));
+    }
+    PMMC_CUDA(ctx, cudaGraphLaunch(b->graph, s));
+  } else {
+    PMMC_CUDA(ctx, enqueue_pass(b, s));
+  }
+  PMMC_CUDA(ctx, cudaEventRecord(b->ev_stop, s));
+  b->ran = true;
+  return PMMC_OK;
+}
+
+extern "C" pmmc_status pmmc_arcs_batch_results(pmmc_arcs_batch *b, float *pos_out,
+                                               pmmc_result *res) {
+  if (!b || !b->ran) return PMMC_ERR_INVALID;
+  pmmc_ctx *ctx = b->ctx;
+  PMMC_CUDA(ctx, cudaEventSynchronize(b->ev_stop));
+  std::vector<ChainOut> outs(b->total_chains);
+  PMMC_CUDA(ctx, cudaMemcpy(outs.data(), b->outs.p, sizeof(ChainOut) * outs.size(),
+                            cudaMemcpyDeviceToHost));
+  std::vector<int> best(b->n_units, 0);
+  bool multi = false;
+  for (auto &U : b->h_units) multi |= U.chains > 1;
+  if (multi)
+    PMMC_CUDA(ctx, cudaMemcpy(best.data(), b->best.p, sizeof(int) * b->n_units,
+                              cudaMemcpyDeviceToHost));
+  long long dst = 0;
+  for (int u = 0; u < b->n_units; ++u) {
+    const ArcsUnit &U = b->h_units[u];
+    const int c = best[u];
+    if (pos_out) {
+      PMMC_CUDA(ctx, cudaMemcpy(pos_out + dst, b->pos_out.p + U.out_off + (long long)c * U.n * 3,
+                                sizeof(float) * U.n * 3, cudaMemcpyDeviceToHost));
+    }
+    dst += (long long)U.n * 3;
+    if (res) {
+      const ChainOut &o = outs[U.chain_base + c];
+      pmmc_result r{};
+      r.score = o.score;
+      r.energy = o.energy;
+      r.energy_fp64 = o.energy_fp64;
+      r.rel_error = std::fabs(o.energy - o.energy_fp64) /
+                    std::max(std::fabs(o.energy_fp64), 1e-30);
+      r.moves = o.moves;
+      r.accepted = o.accepted;
+      long long tot = 0;
+      for (int k = 0; k < U.chains; ++k) tot += outs[U.chain_base + k].moves;
+      r.total_moves = tot;
+      r.best_chain = c;
+      r.status = o.status;
+      res[u] = r;
+    }
+  }
+  return PMMC_OK;
+}
+
+extern "C" pmmc_status pmmc_arcs_batch_stats(pmmc_arcs_batch *b, double *kernel_ms,
+                                             int64_t *total_moves,
+                                             int *lanes_per_chain) {
+  if (!b || !b->ran) return PMMC_ERR_INVALID;
+  pmmc_ctx *ctx = b->ctx;
+  PMMC_CUDA(ctx, cudaEventSynchronize(b->ev_stop));
+  if (kernel_ms) {
+    float ms = 0.0f;
+    PMMC_CUDA(ctx, cudaEventElapsedTime(&ms, b->ev_start, b->ev_stop));
+    *kernel_ms = ms;
+  }
+  if (total_moves) {
+    std::vector<ChainOut> outs(b->total_chains);
+    PMMC_CUDA(ctx, cudaMemcpy(outs.data(), b->outs.p, sizeof(ChainOut) * outs.size(),
+                              cudaMemcpyDeviceToHost));
+    long long t = 0;
+    for (auto &o : outs) t += o.moves;
+    *total_moves = t;
+  }
+  if (lanes_per_chain) *lanes_per_chain = b->lanes;
+  return PMMC_OK;
+}
+
+// Tests only: copy the per-move trace of chain 0 of the batch.
+extern "C" pmmc_status pmmc_arcs_batch_trace(pmmc_arcs_batch *b, void *out, int count) {
+  if (!b || !b->trace || count < 0 || count > b->P.trace_cap) return PMMC_ERR_INVALID;
+  pmmc_ctx *ctx = b->ctx;
+  PMMC_CUDA(ctx, cudaEventSynchronize(b->ev_stop));
+  PMMC_CUDA(ctx, cudaMemcpy(out, b->trace, sizeof(MoveTrace) * (size_t)count,
+                            cudaMemcpyDeviceToHost));
+  return PMMC_OK;
+}
+
+extern "C" void pmmc_arcs_batch_destroy(pmmc_arcs_batch *b) { delete b; }
+
+extern "C" pmmc_status pmmc_arcs_batch_anneal(pmmc_ctx *ctx, int n_units,
+                                              const pmmc_arcs_problem *units,
+                                              const pmmc_anneal_params *prm,
+                                              const float *step_sizes,
+                                              const pmmc_batch_opts *opts,
+                                              float *pos_out, pmmc_result *res) {
+  pmmc_arcs_batch *b = nullptr;
+  pmmc_batch_opts o = opts ? *opts : pmmc_batch_opts{1, 0, 0};
+  o.use_graph = 0;  // one pass: nothing to replay
+  pmmc_status s = pmmc_arcs_batch_create(ctx, n_units, units, prm, step_sizes, &o, &b);
+  if (s != PMMC_OK) return s;
+  s = pmmc_arcs_batch_run(b, nullptr);
+  if (s == PMMC_OK) s = pmmc_arcs_batch_results(b, pos_out, res);
+  pmmc_arcs_batch_destroy(b);
+  return s;
+}
+
+extern "C" pmmc_status pmmc_arcs_anneal(pmmc_ctx *ctx, const pmmc_arcs_problem *pr,
+                                        const pmmc_anneal_params *prm, float step_size,
+                                        int n_chains, float *pos_out, pmmc_result *res) {
+  if (!ctx || !pr || !prm) return fail(ctx, PMMC_ERR_INVALID, "arcs anneal: bad arguments");
+  if (n_chains <= 0) n_chains = 4 * ctx->sm_count;
+  pmmc_batch_opts o{n_chains, 0, 32};
+  pmmc_arcs_batch *b = nullptr;
+  pmmc_status s =
+      pmmc_arcs_batch_create_ex(ctx, 1, pr, prm, &step_size, &o, 1, 0, &b);
+  if (s != PMMC_OK) return s;
+  s = pmmc_arcs_batch_run(b, nullptr);
+  if (s == PMMC_OK) s = pmmc_arcs_batch_results(b, pos_out, res);
+  pmmc_arcs_batch_destroy(b);
+  return s;
+}

@@ -1,0 +1,125 @@
+// capi.cu -- context, parameters and format conversions of the C ABI.
+#include <cstring>
+
+#include "internal.h"
+
+using namespace pmmc;
+
+extern "C" const char *pmmc_status_string(pmmc_status s) {
+  switch (s) {
+    case PMMC_OK: return "ok";
+    case PMMC_ERR_INVALID: return "invalid argument";
+    case PMMC_ERR_NO_DEVICE: return "no usable CUDA device";
+    case PMMC_ERR_CUDA: return "CUDA error";
+    case PMMC_ERR_NOMEM: return "device out of memory";
+    case PMMC_ERR_TIMEOUT: return "device wait timed out";
+    case PMMC_ERR_BUDGET: return "device-memory budget exceeded";
+    case PMMC_ERR_FIXED: return "every bead is fixed";
+    case PMMC_ERR_BUSY: return "no free slot";
+    case PMMC_ERR_NOT_FOUND: return "unknown request";
+  }
+  return "unknown status";
+}
+
+extern "C" pmmc_status pmmc_ctx_create(pmmc_ctx **out, int device) {
+  if (!out) return PMMC_ERR_INVALID;
+  *out = nullptr;
+  int count = 0;
+  if (cudaGetDeviceCount(&count) != cudaSuccess || count <= 0) {
+    cudaGetLastError();
+    return PMMC_ERR_NO_DEVICE;
+  }
+  if (device < 0 || device >= count) return PMMC_ERR_INVALID;
+  if (cudaSetDevice(device) != cudaSuccess) return PMMC_ERR_NO_DEVICE;
+  cudaDeviceProp prop;
+  if (cudaGetDeviceProperties(&prop, device) != cudaSuccess) return PMMC_ERR_NO_DEVICE;
+  auto *c = new pmmc_ctx();
+  c->device = device;
+  c->sm_count = prop.multiProcessorCount;
+  c->smem_optin = prop.sharedMemPerBlockOptin;
+  c->smem_per_sm = prop.sharedMemPerMultiprocessor;
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    delete c;
+    return PMMC_ERR_CUDA;
+  }
+  *out = c;
+  return PMMC_OK;
+}
+
+extern "C" void pmmc_ctx_destroy(pmmc_ctx *ctx) {
+  if (!ctx) return;
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+}
+
+extern "C" const char *pmmc_last_error(const pmmc_ctx *ctx) {
+  return ctx ? ctx->last_error.c_str() : "";
+}
+
+extern "C" void pmmc_set_seed(pmmc_ctx *ctx, uint64_t seed) {
+  if (!ctx) return;
+  ctx->seed = seed;
+  ctx->calls = 0;
+}
+
+extern "C" int pmmc_sm_count(const pmmc_ctx *ctx) { return ctx ? ctx->sm_count : 0; }
+
+// Settings::init defaults (src/include/Settings.hpp:397-505).
+extern "C" void pmmc_default_params(int level, pmmc_anneal_params *o) {
+  if (!o) return;
+  memset(o, 0, sizeof(*o));
+  o->max_temp = 20.0f;
+  o->dt_temp = 0.99995f;
+  o->jump_scale = 50.0f;
+  o->jump_coef = 20.0f;
+  o->improvement = 0.995f;
+  o->min_successes = 5;
+  o->milestone_steps = 10000;
+  o->k_angle = 0.1f;
+  o->w_dist = 1.0f;
+  o->w_angle = 1.0f;
+  o->sphere_radius = 0.0f;
+  o->use2d = 0;
+  o->milestone_fails = 3;
+  o->schedule = PMMC_SCHEDULE_GPU;
+  o->resync_every = 0;
+  o->max_moves = 0;
+  o->bond_target = 1.0f;
+  o->k_stretch_bond = 0.1f;
+  o->k_squeeze_bond = 0.1f;
+  o->k_angle_ext = 0.1f;
+  if (level == PMMC_LEVEL_ARCS) {
+    o->k_stretch = 1.0f;  // springConstantStretchArcs
+    o->k_squeeze = 1.0f;  // springConstantSqueezeArcs
+  } else {
+    o->k_stretch = 0.1f;  // springConstantStretch
+    o->k_squeeze = 0.1f;  // springConstantSqueeze
+  }
+}
+
+extern "C" pmmc_status pmmc_arcs_dense_to_csr(int n, const float *dense, int *row_ptr,
+                                              int *col, float *target, int64_t cap,
+                                              int64_t *nnz) {
+  if (n < 0 || !dense || !row_ptr) return PMMC_ERR_INVALID;
+  int64_t k = 0;
+  row_ptr[0] = 0;
+  for (int i = 0; i < n; ++i) {
+    for (int j = 0; j < n; ++j) {
+      if (j == i) continue;
+      // the local score reads the column of the moved bead: v[j][i]
+      const float v = dense[(size_t)j * n + i];
+      if (v >= 0.0f) {
+        if (col && target) {
+          if (k >= cap) return PMMC_ERR_INVALID;
+          col[k] = j;
+          target[k] = v;
+        }
+        ++k;
+      }
+    }
+    if (k > 0x7fffffff) return PMMC_ERR_INVALID;
+    row_ptr[i + 1] = (int)k;
+  }
+  if (nnz) *nnz = k;
+  return PMMC_OK;
+}

@@ -1,0 +1,97 @@
+// internal.h -- host-side internals shared by the library's translation units.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "pmmc_gb300.h"
+
+struct pmmc_ctx {
+  int device = 0;
+  int sm_count = 0;
+  size_t smem_optin = 0;       // max dynamic shared memory per block (opt-in)
+  size_t smem_per_sm = 0;
+  uint64_t seed = 0;
+  uint64_t calls = 0;          // advanced by every annealing call
+  cudaStream_t stream = nullptr;
+  std::string last_error;
+};
+
+namespace pmmc {
+
+inline int __float_as_int_host(float f) {
+  int i;
+  memcpy(&i, &f, 4);
+  return i;
+}
+inline float __int_as_float_host(int i) {
+  float f;
+  memcpy(&f, &i, 4);
+  return f;
+}
+
+// Records a message on the context and returns the status.
+inline pmmc_status fail(pmmc_ctx *ctx, pmmc_status s, const char *fmt, ...) {
+  if (ctx) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    ctx->last_error = buf;
+  }
+  return s;
+}
+
+#define PMMC_CUDA(ctx, call)                                                   \
+  do {                                                                         \
+    cudaError_t e_ = (call);                                                   \
+    if (e_ != cudaSuccess)                                                     \
+      return ::pmmc::fail((ctx), e_ == cudaErrorMemoryAllocation               \
+                                     ? PMMC_ERR_NOMEM                          \
+                                     : PMMC_ERR_CUDA,                          \
+                          "%s: %s (%s:%d)", #call, cudaGetErrorString(e_),     \
+                          __FILE__, __LINE__);                                 \
+  } while (0)
+
+// The Philox key of the next annealing call: the context seed for the first
+// call after pmmc_set_seed, then a fresh key per call.
+inline uint64_t next_key(pmmc_ctx *ctx) {
+  uint64_t k = ctx->seed + ctx->calls * 0x9E3779B97F4A7C15ull;
+  ctx->calls++;
+  return k;
+}
+
+// RAII device buffer.
+template <typename T> struct DevBuf {
+  T *p = nullptr;
+  size_t n = 0;
+  DevBuf() = default;
+  DevBuf(const DevBuf &) = delete;
+  DevBuf &operator=(const DevBuf &) = delete;
+  ~DevBuf() { release(); }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    n = 0;
+  }
+  cudaError_t alloc(size_t count) {
+    release();
+    n = count;
+    if (count == 0) return cudaSuccess;
+    return cudaMalloc(&p, count * sizeof(T));
+  }
+  cudaError_t upload(const std::vector<T> &v, cudaStream_t s) {
+    cudaError_t e = alloc(v.size());
+    if (e != cudaSuccess || v.empty()) return e;
+    return cudaMemcpyAsync(p, v.data(), v.size() * sizeof(T),
+                           cudaMemcpyHostToDevice, s);
+  }
+};
+
+}  // namespace pmmc
