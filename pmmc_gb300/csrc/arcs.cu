@@ -43,7 +43,7 @@ struct ArcsUnit {
   int n_mov;      // movable beads
   int pos_off;    // float4 index into pos0
   int rp_off;     // index into row_ptr (n+1 entries, unit-relative values)
-  int nbr_off;    // index into nbr
+  int nbr_off;    // index into nbr / inv_t (spring entries, target >= 1e-6)
   int nnz;
   int mov_off;    // index into movable, -1 = all beads movable
   int lrp_off;    // index into loop row_ptr (n+1), -1 = no loops
@@ -51,6 +51,8 @@ struct ArcsUnit {
   int n_lent;
   int lst_off;    // index into the loop list (one entry per constraint)
   int n_loops;
+  int null_off;   // index into the listed-but-inert pairs (0 <= target < 1e-6)
+  int n_null;
   int chains;
   int chain_base; // global chain id of the unit's chain 0
   long long out_off;  // float index of chain 0's xyz output
@@ -77,19 +79,39 @@ struct ArcsDevParams {
   int cap_is_error;
   int pad;
   uint64_t seed;
-  double dtpow[33];  // dt^l, l = 0..32
+  float dtpow[33];  // dt^l, l = 0..32
 };
 
 constexpr int kMoveBufBytes = 32 * 16 + 32 * 4;  // int4 moves + float thresholds
-
-__device__ __forceinline__ float spring(float len, float t, float ks, float kq) {
-  const float f = (len - t) / t;
-  return f * f * (f >= 0.0f ? ks : kq);
-}
+constexpr int kCtaHeader = 256;                    // dt^l table shared by the CTA
 
 __device__ __forceinline__ float dist3(float ax, float ay, float az, float4 b) {
   const float x = ax - b.x, y = ay - b.y, z = az - b.z;
   return sqrtf(x * x + y * y + z * z);
+}
+
+// |a - b| from the hardware reciprocal square root (2 ulp); 0 stays 0.
+__device__ __forceinline__ float fast_len(float ax, float ay, float az, float4 b) {
+  const float x = ax - b.x, y = ay - b.y, z = az - b.z;
+  const float s = fmaf(x, x, fmaf(y, y, z * z));
+  return s * rsqrtf(fmaxf(s, 1e-30f));
+}
+
+// Spring term of one arc: ((len - t) / t)^2 * k, with 1/t precomputed.
+__device__ __forceinline__ float spring_fast(float len, float t, float it, float ks,
+                                             float kq) {
+  const float f = (len - t) * it;
+  return f * f * (f >= 0.0f ? ks : kq);
+}
+
+// float-float accumulation (Knuth two-sum) of a float increment
+__device__ __forceinline__ void ff_add(float &hi, float &lo, float d) {
+  const float s = hi + d;
+  const float bb = s - hi;
+  const float err = (hi - (s - bb)) + (d - bb);
+  const float l = lo + err;
+  hi = s + l;
+  lo = l - (hi - s);
 }
 
 // FP64 energy without repulsion: springs (pairs counted once, col < row so
@@ -107,7 +129,6 @@ __device__ double arcs_spring_energy(int n, const float4 *spos, const int *srp,
       const int2 ent = nb[e];
       if (ent.x >= i) continue;
       const float t = __int_as_float(ent.y);
-      if (t < 1e-6f) continue;
       const float f = (dist3(pi.x, pi.y, pi.z, spos[ent.x]) - t) / t;
       const double df = f;
       acc += df * df * (double)(df >= 0.0 ? P.k_stretch : P.k_squeeze);
@@ -125,14 +146,17 @@ __device__ double arcs_spring_energy(int n, const float4 *spos, const int *srp,
 
 // FP64 sum of 1/d over every pair (i<j) that the arc lists do not name.
 __device__ double arcs_repulsion(int n, const float4 *spos, const int *srp,
-                                 const int2 *nb, int lane) {
+                                 const int2 *nb, const int2 *nulls, int n_null,
+                                 int lane) {
   double acc = 0.0;
   for (int i = lane; i < n; i += 32) {
     const float4 pi = spos[i];
     float part = 0.0f;
     int cnt = 0;
     for (int j = i + 1; j < n; ++j) {
-      part += 1.0f / dist3(pi.x, pi.y, pi.z, spos[j]);
+      const float4 pj = spos[j];
+      const float x = pi.x - pj.x, y = pi.y - pj.y, z = pi.z - pj.z;
+      part += rsqrtf(fmaf(x, x, fmaf(y, y, z * z)));
       if (++cnt == 64) {
         acc += part;
         part = 0.0f;
@@ -143,26 +167,35 @@ __device__ double arcs_repulsion(int n, const float4 *spos, const int *srp,
     const int e1 = srp[i + 1];
     for (int e = srp[i]; e < e1; ++e) {
       const int j = nb[e].x;
-      if (j > i) acc -= (double)(1.0f / dist3(pi.x, pi.y, pi.z, spos[j]));
+      if (j < i) acc -= (double)(1.0f / dist3(spos[j].x, spos[j].y, spos[j].z, pi));
     }
+  }
+  for (int c = lane; c < n_null; c += 32) {
+    const int2 q = nulls[c];
+    acc -= (double)(1.0f / dist3(spos[q.x].x, spos[q.x].y, spos[q.x].z, spos[q.y]));
   }
   return warp_sum_d(acc);
 }
 
+template <bool NB_SMEM>
 __global__ void __launch_bounds__(128)
 arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
                    const int2 *__restrict__ items, int n_items,
                    int *__restrict__ head, const float4 *__restrict__ pos0,
                    const int *__restrict__ row_ptr,
-                   const int2 *__restrict__ nbr, const int *__restrict__ movable,
+                   const int2 *__restrict__ nbr, const float *__restrict__ inv_t,
+                   const int *__restrict__ movable,
                    const int *__restrict__ lrp, const float4 *__restrict__ lent,
-                   const int4 *__restrict__ lst, ArcsDevParams P,
-                   int smem_per_warp, float *__restrict__ pos_out,
+                   const int4 *__restrict__ lst, const int2 *__restrict__ nulls,
+                   ArcsDevParams P, int smem_per_warp, float *__restrict__ pos_out,
                    ChainOut *__restrict__ outs, int *__restrict__ done,
                    MoveTrace *__restrict__ trace) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31;
-  unsigned char *wbase = smem + (size_t)(threadIdx.x >> 5) * smem_per_warp;
+  float *s_dtpow = reinterpret_cast<float *>(smem);
+  if (threadIdx.x < 33) s_dtpow[threadIdx.x] = P.dtpow[threadIdx.x];
+  __syncthreads();
+  unsigned char *wbase = smem + kCtaHeader + (size_t)(threadIdx.x >> 5) * smem_per_warp;
   int4 *s_mv = reinterpret_cast<int4 *>(wbase);
   float *s_thr = reinterpret_cast<float *>(wbase + 32 * 16);
   float4 *spos = reinterpret_cast<float4 *>(wbase + kMoveBufBytes);
@@ -183,21 +216,26 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
     int *srp = reinterpret_cast<int *>(spos + n);
     size_t off = (size_t)kMoveBufBytes + (size_t)n * 16 + (size_t)(n + 1) * 4;
     off = (off + 7) & ~(size_t)7;
-    const bool nb_smem = off + (size_t)U.nnz * 8 <= (size_t)smem_per_warp;
     int2 *snb = reinterpret_cast<int2 *>(wbase + off);
-    if (nb_smem) off += (size_t)U.nnz * 8;
+    float *sinv = reinterpret_cast<float *>(wbase + off + (size_t)U.nnz * 8);
+    if (NB_SMEM) off += (size_t)U.nnz * 12;
     const bool has_mov = U.mov_off >= 0;
     const bool mov_smem = has_mov && off + (size_t)U.n_mov * 4 <= (size_t)smem_per_warp;
     int *smov = reinterpret_cast<int *>(wbase + off);
 
     for (int i = lane; i < n; i += 32) spos[i] = pos0[U.pos_off + i];
     for (int i = lane; i <= n; i += 32) srp[i] = row_ptr[U.rp_off + i];
-    if (nb_smem)
-      for (int e = lane; e < U.nnz; e += 32) snb[e] = nbr[U.nbr_off + e];
+    if (NB_SMEM) {
+      for (int e = lane; e < U.nnz; e += 32) {
+        snb[e] = nbr[U.nbr_off + e];
+        sinv[e] = inv_t[U.nbr_off + e];
+      }
+    }
     if (mov_smem)
       for (int k = lane; k < U.n_mov; k += 32) smov[k] = movable[U.mov_off + k];
     __syncwarp();
-    const int2 *NB = nb_smem ? snb : nbr + U.nbr_off;
+    const int2 *NB = NB_SMEM ? snb : nbr + U.nbr_off;
+    const float *INV = NB_SMEM ? sinv : inv_t + U.nbr_off;
     const int *MOV = has_mov ? (mov_smem ? smov : movable + U.mov_off) : nullptr;
     const bool has_loops = U.lrp_off >= 0;
     const int *LRP = has_loops ? lrp + U.lrp_off : nullptr;
@@ -205,9 +243,11 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
     const int4 *LST = lst + U.lst_off;
 
     // ---- initial FP64 energy: repulsion (frozen) + springs/loops/sphere ----
-    const double base = arcs_repulsion(n, spos, srp, NB, lane);
+    const double base = arcs_repulsion(n, spos, srp, NB, nulls + U.null_off, U.n_null, lane);
     double E = base + arcs_spring_energy(n, spos, srp, NB, LST, U.n_loops, P, lane);
-    float Ef = (float)E;
+    // running energy of the chain (lane 0): float-float pair on the move
+    // path, widened to FP64 at milestones, resyncs and the end
+    float e_hi = (float)E, e_lo = (float)(E - (double)(float)E);
     double E_ms = E;
     double T = P.max_temp;
     long long moves = 0, accepted = 0;
@@ -230,43 +270,69 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
         const float dx = (2.0f * u01(r.y) - 1.0f) * step;
         const float dy = (2.0f * u01(r.z) - 1.0f) * step;
         const float dz = P.use2d ? 0.0f : (2.0f * u01(r.w) - 1.0f) * step;
-        const float Tl = (float)(T * P.dtpow[lane]);
+        const float Tl = (float)T * s_dtpow[lane];
         s_mv[lane] = make_int4(b, __float_as_int(dx), __float_as_int(dy),
                                __float_as_int(dz));
         s_thr[lane] = ratio_threshold(u01(a.x), Tl, P.inv_scale, P.inv_coef);
       }
-      long long kmax = 32;
-      kmax = min(kmax, (long long)(P.window - (int)(moves % P.window)));
-      if (P.resync > 0) kmax = min(kmax, (long long)(P.resync - (int)(moves % P.resync)));
-      kmax = min(kmax, P.cap - moves);
+      int kmax = 32;
+      kmax = min(kmax, P.window - (int)(moves % P.window));
+      if (P.resync > 0) kmax = min(kmax, P.resync - (int)(moves % P.resync));
+      if (P.cap - moves < (long long)kmax) kmax = (int)(P.cap - moves);
       __syncwarp();
 
-      for (int k = 0; k < (int)kmax; ++k) {
-        const int4 mv = s_mv[k];
+      // static data of the batch's first move; each iteration prefetches
+      // the next move's (none of it depends on positions)
+      int4 mv = s_mv[0];
+      float thr = s_thr[0];
+      int beg = srp[mv.x];
+      int deg = srp[mv.x + 1] - beg;
+      int2 ent = lane < deg ? NB[beg + lane] : make_int2(mv.x, 0);
+      float itv = lane < deg ? INV[beg + lane] : 0.0f;
+
+      for (int k = 0; k < kmax; ++k) {
         const int b = mv.x;
+        const float4 pb = spos[b];
+        const float4 pj = spos[ent.x];
+        int4 mv1 = mv;
+        float thr1 = 0.0f;
+        int beg1 = 0, deg1 = 0;
+        int2 ent1 = ent;
+        float it1 = 0.0f;
+        if (k + 1 < kmax) {
+          mv1 = s_mv[k + 1];
+          thr1 = s_thr[k + 1];
+          beg1 = srp[mv1.x];
+          deg1 = srp[mv1.x + 1] - beg1;
+          ent1 = lane < deg1 ? NB[beg1 + lane] : make_int2(mv1.x, 0);
+          it1 = lane < deg1 ? INV[beg1 + lane] : 0.0f;
+        }
         const float dx = __int_as_float(mv.y), dy = __int_as_float(mv.z),
                     dz = __int_as_float(mv.w);
-        const float4 pb = spos[b];
         const float nx = pb.x + dx, ny = pb.y + dy, nz = pb.z + dz;
-        const int beg = srp[b], end = srp[b + 1];
         float so = 0.0f, sn = 0.0f;
-        for (int e = beg + lane; e < end; e += 32) {
-          const int2 ent = NB[e];
+        if (lane < deg) {
           const float t = __int_as_float(ent.y);
-          if (t >= 1e-6f) {
-            const float4 pj = spos[ent.x];
-            so += spring(dist3(pb.x, pb.y, pb.z, pj), t, ks, kq);
-            sn += spring(dist3(nx, ny, nz, pj), t, ks, kq);
+          so = spring_fast(fast_len(pb.x, pb.y, pb.z, pj), t, itv, ks, kq);
+          sn = spring_fast(fast_len(nx, ny, nz, pj), t, itv, ks, kq);
+        }
+        int width = deg;
+        if (deg > 32) {  // rare hub beads: the rest of the list
+          for (int e = beg + 32 + lane; e < beg + deg; e += 32) {
+            const int2 en = NB[e];
+            const float t = __int_as_float(en.y), iv = INV[e];
+            const float4 q = spos[en.x];
+            so += spring_fast(fast_len(pb.x, pb.y, pb.z, q), t, iv, ks, kq);
+            sn += spring_fast(fast_len(nx, ny, nz, q), t, iv, ks, kq);
           }
         }
-        int width = end - beg;
         if (has_loops) {
           const int l0 = LRP[b], l1 = LRP[b + 1];
           for (int e = l0 + lane; e < l1; e += 32) {
             const float4 le = LENT[e];
-            const float4 pj = spos[__float_as_int(le.x)];
-            const float d0 = dist3(pb.x, pb.y, pb.z, pj) - le.z;
-            const float d1 = dist3(nx, ny, nz, pj) - le.z;
+            const float4 q = spos[__float_as_int(le.x)];
+            const float d0 = dist3(pb.x, pb.y, pb.z, q) - le.z;
+            const float d1 = dist3(nx, ny, nz, q) - le.z;
             so += le.y * d0 * d0;
             sn += le.y * d1 * d1;
           }
@@ -276,20 +342,22 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
           so += sphere_penalty(pb.x, pb.y, pb.z, R);
           sn += sphere_penalty(nx, ny, nz, R);
         }
-        if (width > 1) {
-          const int w = width >= 32 ? 32 : (1 << (32 - __clz(width - 1)));
+        float d = sn - so;
+        const int w = width >= 32 ? 32 : (width <= 1 ? 1 : (1 << (32 - __clz(width - 1))));
+        if (tracing) {
           for (int o = w >> 1; o > 0; o >>= 1) {
             so += __shfl_xor_sync(0xffffffffu, so, o);
             sn += __shfl_xor_sync(0xffffffffu, sn, o);
           }
+          d = sn - so;
+        } else {
+          for (int o = w >> 1; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
         }
         if (lane == 0) {
-          const float d = sn - so;
-          const bool acc = (d <= 0.0f) || (d < Ef * (s_thr[k] - 1.0f));
+          const bool acc = (d <= 0.0f) || (d < e_hi * (thr - 1.0f));
           if (acc) {
             spos[b] = make_float4(nx, ny, nz, 0.0f);
-            E += (double)d;
-            Ef = (float)E;
+            ff_add(e_hi, e_lo, d);
             ++accepted;
             ++succ_ms;
           }
@@ -302,20 +370,27 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
             tr.dx = dx;
             tr.dy = dy;
             tr.dz = dz;
-            tr.pad = 0.0f;
+            tr.pad = d;
             trace[moves + k] = tr;
           }
         }
         __syncwarp();
+        mv = mv1;
+        thr = thr1;
+        beg = beg1;
+        deg = deg1;
+        ent = ent1;
+        itv = it1;
       }
       moves += kmax;
-      T *= P.dtpow[kmax];
+      T *= (double)s_dtpow[kmax];
       ++batch_no;
 
       // ---- milestone (the reference CPU predicate, FP64, lane 0) ----
       int flag = 0;
       if (moves % P.window == 0) {
         if (lane == 0) {
+          const double E = (double)e_hi + (double)e_lo;
           const bool miss =
               (E > (double)P.improvement * E_ms && succ_ms < P.min_successes) ||
               E < 1e-5 || E / E_ms > 0.9999;
@@ -328,8 +403,9 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
       if (P.resync > 0 && moves % P.resync == 0 && !__shfl_sync(0xffffffffu, flag, 0)) {
         const double es = arcs_spring_energy(n, spos, srp, NB, LST, U.n_loops, P, lane);
         if (lane == 0) {
-          E = base + es;
-          Ef = (float)E;
+          const double Er = base + es;
+          e_hi = (float)Er;
+          e_lo = (float)(Er - (double)e_hi);
         }
       }
       if (lane == 0) {
@@ -349,10 +425,10 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
     const double es = arcs_spring_energy(n, spos, srp, NB, LST, U.n_loops, P, lane);
     if (lane == 0) {
       ChainOut o;
-      o.energy = E;
+      o.energy = (double)e_hi + (double)e_lo;
       o.energy_fp64 = base + es;
       o.base = base;
-      o.score = (float)E;
+      o.score = e_hi;
       o.status = status;
       o.moves = moves;
       o.accepted = accepted;
@@ -398,6 +474,7 @@ using namespace pmmc;
 
 struct ArcsClass {
   int item_begin = 0, item_end = 0;
+  bool nb_smem = true;
   int smem_per_warp = 0;
   int warps_per_cta = 1;
   int grid = 0;
@@ -419,6 +496,8 @@ struct pmmc_arcs_batch {
   DevBuf<float4> pos0;
   DevBuf<int> row_ptr;
   DevBuf<int2> nbr;
+  DevBuf<float> inv_t;
+  DevBuf<int2> nulls;
   DevBuf<int> movable;
   DevBuf<int> lrp;
   DevBuf<float4> lent;
@@ -453,7 +532,7 @@ namespace {
 size_t unit_smem(int n, int nnz, int n_mov, bool has_mov) {
   size_t s = (size_t)kMoveBufBytes + (size_t)n * 16 + (size_t)(n + 1) * 4;
   s = (s + 7) & ~(size_t)7;
-  s += (size_t)nnz * 8;
+  s += (size_t)nnz * 12;
   if (has_mov) s += (size_t)n_mov * 4;
   return s;
 }
@@ -514,7 +593,7 @@ ArcsDevParams make_params(const pmmc_anneal_params *prm, uint64_t seed,
   }
   double d = 1.0;
   for (int l = 0; l <= 32; ++l) {
-    P.dtpow[l] = d;
+    P.dtpow[l] = (float)d;
     d *= (double)prm->dt_temp;
   }
   return P;
@@ -545,7 +624,8 @@ extern "C" pmmc_status pmmc_arcs_batch_create_ex(
   // ---- pack host arrays ----
   std::vector<float4> h_pos;
   std::vector<int> h_rp, h_mov, h_lrp;
-  std::vector<int2> h_nbr;
+  std::vector<int2> h_nbr, h_null;
+  std::vector<float> h_inv;
   std::vector<float4> h_lent;
   std::vector<int4> h_lst;
   b->h_units.resize(n_units);
@@ -559,16 +639,31 @@ extern "C" pmmc_status pmmc_arcs_batch_create_ex(
     U.pos_off = (int)h_pos.size();
     for (int i = 0; i < pr.n; ++i)
       h_pos.push_back(make_float4(pr.pos[3 * i], pr.pos[3 * i + 1], pr.pos[3 * i + 2], 0.0f));
+    // spring entries (target >= 1e-6) with 1/target; listed pairs with
+    // 0 <= target < 1e-6 are inert and only leave the repulsion sum
     U.rp_off = (int)h_rp.size();
-    for (int i = 0; i <= pr.n; ++i) h_rp.push_back(pr.row_ptr[i]);
     U.nbr_off = (int)h_nbr.size();
-    U.nnz = pr.row_ptr[pr.n];
-    for (int e = 0; e < U.nnz; ++e) {
-      int2 v;
-      v.x = pr.col[e];
-      v.y = __float_as_int_host(pr.target[e]);
-      h_nbr.push_back(v);
+    U.null_off = (int)h_null.size();
+    int cnt = 0;
+    h_rp.push_back(0);
+    for (int i = 0; i < pr.n; ++i) {
+      for (int e = pr.row_ptr[i]; e < pr.row_ptr[i + 1]; ++e) {
+        const float t = pr.target[e];
+        if (t >= 1e-6f) {
+          int2 v;
+          v.x = pr.col[e];
+          v.y = __float_as_int_host(t);
+          h_nbr.push_back(v);
+          h_inv.push_back(1.0f / t);
+          ++cnt;
+        } else if (t >= 0.0f && pr.col[e] < i) {
+          h_null.push_back(make_int2(pr.col[e], i));
+        }
+      }
+      h_rp.push_back(cnt);
     }
+    U.nnz = cnt;
+    U.n_null = (int)h_null.size() - U.null_off;
     int nm = 0;
     std::vector<int> mv;
     for (int i = 0; i < pr.n; ++i)
@@ -632,35 +727,43 @@ extern "C" pmmc_status pmmc_arcs_batch_create_ex(
   b->total_pos_out = out_off;
   b->total_chains = chain_base;
   if (h_lst.empty()) h_lst.push_back(make_int4(0, 0, 0, 0));
+  if (h_null.empty()) h_null.push_back(make_int2(0, 0));
 
   // ---- shared-memory classes: items sorted by need, largest first ----
-  const size_t cap_smem = ctx->smem_optin;
-  struct Need { int unit; size_t bytes; };
+  // A unit whose arc lists fit next to its positions is staged whole
+  // (NB_SMEM); otherwise only positions go to shared memory.
+  const size_t cap_smem = ctx->smem_optin - kCtaHeader;
+  struct Need { int unit; size_t bytes; bool nb_smem; };
   std::vector<Need> needs(n_units);
   for (int u = 0; u < n_units; ++u) {
     const ArcsUnit &U = b->h_units[u];
-    size_t full = unit_smem(U.n, U.nnz, U.n_mov, U.mov_off >= 0);
-    size_t minimal = unit_smem_min(U.n);
+    const size_t full = unit_smem(U.n, U.nnz, U.n_mov, U.mov_off >= 0);
+    const size_t minimal = unit_smem_min(U.n);
     if (minimal > cap_smem) {
       delete b;
       return fail(ctx, PMMC_ERR_INVALID,
                   "arcs batch: region of %d beads exceeds the %zu B shared-memory "
                   "slice a chain can hold", U.n, cap_smem);
     }
-    needs[u] = {u, std::min(full, cap_smem)};
+    needs[u] = full <= cap_smem ? Need{u, full, true} : Need{u, minimal, false};
   }
-  std::stable_sort(needs.begin(), needs.end(),
-                   [](const Need &a, const Need &c) { return a.bytes > c.bytes; });
-  // classes: a class holds units whose need is within 2x of its largest
+  std::stable_sort(needs.begin(), needs.end(), [](const Need &a, const Need &c) {
+    if (a.nb_smem != c.nb_smem) return !a.nb_smem;
+    return a.bytes > c.bytes;
+  });
   std::vector<int2> h_items;
-  cudaFuncSetAttribute(arcs_anneal_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)cap_smem);
+  cudaFuncSetAttribute(arcs_anneal_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)ctx->smem_optin);
+  cudaFuncSetAttribute(arcs_anneal_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                       (int)ctx->smem_optin);
   size_t i0 = 0;
   while (i0 < needs.size()) {
-    size_t top = needs[i0].bytes;
+    const size_t top = needs[i0].bytes;
+    const bool nbs = needs[i0].nb_smem;
     size_t i1 = i0;
-    while (i1 < needs.size() && needs[i1].bytes * 2 > top) ++i1;
+    while (i1 < needs.size() && needs[i1].nb_smem == nbs && needs[i1].bytes * 2 > top) ++i1;
     ArcsClass c;
+    c.nb_smem = nbs;
     c.item_begin = (int)h_items.size();
     for (size_t k = i0; k < i1; ++k)
       for (int ch = 0; ch < chains; ++ch) h_items.push_back(make_int2(needs[k].unit, ch));
@@ -671,8 +774,11 @@ extern "C" pmmc_status pmmc_arcs_batch_create_ex(
     while (w > 1 && (size_t)w * c.smem_per_warp > cap_smem) w >>= 1;
     c.warps_per_cta = w;
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, arcs_anneal_kernel, 32 * w,
-                                                  (size_t)w * c.smem_per_warp);
+    const size_t dyn = kCtaHeader + (size_t)w * c.smem_per_warp;
+    if (nbs)
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, arcs_anneal_kernel<true>, 32 * w, dyn);
+    else
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, arcs_anneal_kernel<false>, 32 * w, dyn);
     if (per_sm < 1) per_sm = 1;
     const int items_n = c.item_end - c.item_begin;
     c.grid = std::max(1, std::min(per_sm * ctx->sm_count, (items_n + w - 1) / w));
@@ -691,6 +797,8 @@ extern "C" pmmc_status pmmc_arcs_batch_create_ex(
   UP(pos0, h_pos);
   UP(row_ptr, h_rp);
   UP(nbr, h_nbr);
+  UP(inv_t, h_inv);
+  UP(nulls, h_null);
   UP(movable, h_mov);
   UP(lrp, h_lrp);
   UP(lent, h_lent);
@@ -731,12 +839,19 @@ cudaError_t enqueue_pass(pmmc_arcs_batch *b, cudaStream_t s) {
     ArcsClass &c = b->classes[k];
     e = cudaStreamWaitEvent(c.stream, b->ev_fork, 0);
     if (e != cudaSuccess) break;
-    arcs_anneal_kernel<<<c.grid, 32 * c.warps_per_cta,
-                         (size_t)c.warps_per_cta * c.smem_per_warp, c.stream>>>(
-        b->units.p, b->items.p + c.item_begin, c.item_end - c.item_begin,
-        b->heads.p + k, b->pos0.p, b->row_ptr.p, b->nbr.p, b->movable.p, b->lrp.p,
-        b->lent.p, b->lst.p, b->P, c.smem_per_warp, b->pos_out.p, b->outs.p,
-        b->done.p, b->trace);
+    const size_t dyn = kCtaHeader + (size_t)c.warps_per_cta * c.smem_per_warp;
+    if (c.nb_smem)
+      arcs_anneal_kernel<true><<<c.grid, 32 * c.warps_per_cta, dyn, c.stream>>>(
+          b->units.p, b->items.p + c.item_begin, c.item_end - c.item_begin, b->heads.p + k,
+          b->pos0.p, b->row_ptr.p, b->nbr.p, b->inv_t.p, b->movable.p, b->lrp.p, b->lent.p,
+          b->lst.p, b->nulls.p, b->P, c.smem_per_warp, b->pos_out.p, b->outs.p, b->done.p,
+          b->trace);
+    else
+      arcs_anneal_kernel<false><<<c.grid, 32 * c.warps_per_cta, dyn, c.stream>>>(
+          b->units.p, b->items.p + c.item_begin, c.item_end - c.item_begin, b->heads.p + k,
+          b->pos0.p, b->row_ptr.p, b->nbr.p, b->inv_t.p, b->movable.p, b->lrp.p, b->lent.p,
+          b->lst.p, b->nulls.p, b->P, c.smem_per_warp, b->pos_out.p, b->outs.p, b->done.p,
+          b->trace);
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaEventRecord(c.join, c.stream);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(s, c.join, 0);

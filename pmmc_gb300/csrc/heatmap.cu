@@ -59,8 +59,7 @@ struct HeatDevParams {
   double dtpow[33];
 };
 
-constexpr int kHeatThreads = 512;
-constexpr int kHeatWarps = kHeatThreads / 32;
+constexpr int kHeatMaxThreads = 512;
 constexpr long long kSpinLimit = 1ll << 26;
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
@@ -126,6 +125,21 @@ __device__ __forceinline__ float hm_term(float4 a, float4 b, float h) {
   return c * c;
 }
 
+// Change of one pair term when bead b moves from pb to nb: the hardware
+// reciprocal square root and one reciprocal of h shared by both terms.
+__device__ __forceinline__ float hm_delta(float4 pi, float4 pb, float4 nb, float h) {
+  const float rh = __fdividef(1.0f, h);
+  float x = pi.x - pb.x, y = pi.y - pb.y, z = pi.z - pb.z;
+  float s = fmaf(x, x, fmaf(y, y, z * z));
+  const float co = (s * rsqrtf(fmaxf(s, 1e-30f)) - h) * rh;
+  x = pi.x - nb.x;
+  y = pi.y - nb.y;
+  z = pi.z - nb.z;
+  s = fmaf(x, x, fmaf(y, y, z * z));
+  const float cn = (s * rsqrtf(fmaxf(s, 1e-30f)) - h) * rh;
+  return fmaf(cn, cn, -co * co);
+}
+
 // FP64 full score, the whole block; every thread returns the total.
 __device__ double heat_full(const HeatUnit &U, const float4 *spos, const float *heat,
                             const int2 *blk, double *red) {
@@ -153,7 +167,7 @@ __device__ double heat_full(const HeatUnit &U, const float4 *spos, const float *
   return t;
 }
 
-__global__ void __launch_bounds__(kHeatThreads, 1)
+__global__ void __launch_bounds__(kHeatMaxThreads, 1)
 heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restrict__ pos0,
                       const float *__restrict__ heat, const int *__restrict__ movable,
                       const int2 *__restrict__ blk_all, HeatDevParams P,
@@ -163,6 +177,7 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
   const HeatUnit U = units[blockIdx.x];
   const int n = U.n;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int nthr = blockDim.x, nwarps = nthr >> 5;
   const int D = P.depth;
   // ---- shared-memory carve ----
   unsigned char *p = smem;
@@ -266,12 +281,12 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
     const int2 r = blk[b];
     const float *row = slots + (size_t)slot * U.pitch - st;
     float part = 0.0f;
-    for (int i = r.x + tid; i <= r.y; i += kHeatThreads) {
+    for (int i = r.x + tid; i <= r.y; i += nthr) {
       if (abs(i - b) < U.diag || i == b) continue;
       const float h = row[i];
       if (h < 1e-6f) continue;
       const float4 pi = (i == prev_b && prev_acc) ? prev_new : spos[i];
-      part += hm_term(pi, nb, h) - hm_term(pi, pb, h);
+      part += hm_delta(pi, pb, nb, h);
     }
     part = warp_sum_f(part);
     const int any_to = __any_sync(0xffffffffu, timed_out) ? 1 : 0;
@@ -282,7 +297,7 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
     __syncthreads();
     // every thread sees the same timeout flags (double-buffered by parity)
     const bool block_to =
-        __any_sync(0xffffffffu, lane < kHeatWarps && tflag[(k & 1) * 32 + lane] != 0);
+        __any_sync(0xffffffffu, lane < nwarps && tflag[(k & 1) * 32 + lane] != 0);
     // refill the draws of moves k+32..k+63 (their ring slots held moves
     // k-32..k-1) and issue the copy for move k + D (slot k % D is free)
     if (warp == 0) {
@@ -298,7 +313,7 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
       }
     }
     // every warp reduces the partials in the same order: identical decisions
-    float tot = lane < kHeatWarps ? partial[(k & 1) * 32 + lane] : 0.0f;
+    float tot = lane < nwarps ? partial[(k & 1) * 32 + lane] : 0.0f;
     tot = warp_sum_f(tot);
     const float d = 2.0f * tot + (sphere_penalty(nb.x, nb.y, nb.z, P.R) -
                                   sphere_penalty(pb.x, pb.y, pb.z, P.R));
@@ -507,7 +522,10 @@ extern "C" pmmc_status pmmc_heatmap_batch_anneal(pmmc_ctx *ctx, int n_units,
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   cudaEventRecord(e0, s);
-  heatmap_anneal_kernel<<<n_units, kHeatThreads, smem, s>>>(
+  // threads per chain: about four row entries per thread, 128..512
+  int threads = 128;
+  while (threads < kHeatMaxThreads && threads * 4 < max_n) threads *= 2;
+  heatmap_anneal_kernel<<<n_units, threads, smem, s>>>(
       d_units.p, d_pos.p, d_heat.p, d_mov.p, d_blk.p, P, d_out.p, d_outs.p,
       trace_cap > 0 ? d_trace.p : nullptr);
   e = cudaGetLastError();

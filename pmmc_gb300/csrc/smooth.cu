@@ -58,32 +58,34 @@ struct SmoothDevParams {
   uint64_t seed;
 };
 
-__device__ __forceinline__ float bond_e(float4 a, float4 b, float d0, float ks,
+// Bond term with the clamped target d0 and its reciprocal precomputed:
+// ((|a - b| - d0) / d0)^2 * (stretch | squeeze).
+__device__ __forceinline__ float bond_e(float4 a, float4 b, float2 d, float ks,
                                         float kq) {
-  if (d0 < 1e-6f) d0 = 1e-6f;
   const float x = a.x - b.x, y = a.y - b.y, z = a.z - b.z;
-  const float f = (sqrtf(x * x + y * y + z * z) - d0) / d0;
+  const float s = fmaf(x, x, fmaf(y, y, z * z));
+  const float f = (s * rsqrtf(fmaxf(s, 1e-30f)) - d.x) * d.y;
   return f * f * (f >= 0.0f ? ks : kq);
 }
 
 // angle() of the reference (common.cpp:39-46) for v1 = a - b, v2 = b - c
-// (the bonds before and after bead b), cubed and scaled.
+// (the bonds before and after bead b): (1 - cos) / 2, cubed and scaled; a
+// zero-length bond normalises to the zero vector (cos = 0).
 __device__ __forceinline__ float angle_e(float4 a, float4 b, float4 c,
                                          float kang) {
-  float x1 = a.x - b.x, y1 = a.y - b.y, z1 = a.z - b.z;
-  float x2 = b.x - c.x, y2 = b.y - c.y, z2 = b.z - c.z;
-  float m1 = sqrtf(x1 * x1 + y1 * y1 + z1 * z1);
-  float m2 = sqrtf(x2 * x2 + y2 * y2 + z2 * z2);
-  m1 = m1 > 0.0f ? 1.0f / m1 : 0.0f;
-  m2 = m2 > 0.0f ? 1.0f / m2 : 0.0f;
-  const float dot = (x1 * m1) * (x2 * m2) + (y1 * m1) * (y2 * m2) + (z1 * m1) * (z2 * m2);
-  const float ang = 1.0f - (dot + 1.0f) * 0.5f;
+  const float x1 = a.x - b.x, y1 = a.y - b.y, z1 = a.z - b.z;
+  const float x2 = b.x - c.x, y2 = b.y - c.y, z2 = b.z - c.z;
+  const float s1 = fmaf(x1, x1, fmaf(y1, y1, z1 * z1));
+  const float s2 = fmaf(x2, x2, fmaf(y2, y2, z2 * z2));
+  const float m = (s1 > 0.0f && s2 > 0.0f) ? rsqrtf(s1) * rsqrtf(s2) : 0.0f;
+  const float dot = fmaf(x1, x2, fmaf(y1, y2, z1 * z2)) * m;
+  const float ang = 0.5f - 0.5f * dot;
   return ang * ang * ang * kang;
 }
 
 // Local score of bead p at position q (calcScoreStructureSmooth(p,true,true)
 // plus the bead's sphere term).
-__device__ __forceinline__ float smooth_local(const float4 *P, const float *dtn,
+__device__ __forceinline__ float smooth_local(const float4 *P, const float2 *dtn,
                                               int n, int p, float4 q,
                                               const SmoothDevParams &S) {
   float s = 0.0f;
@@ -98,23 +100,52 @@ __device__ __forceinline__ float smooth_local(const float4 *P, const float *dtn,
   return s;
 }
 
+// Exact (IEEE sqrt / division) forms for the FP64 recompute.
+__device__ __forceinline__ double bond_exact(float4 a, float4 b, float d0, float ks, float kq) {
+  const float x = a.x - b.x, y = a.y - b.y, z = a.z - b.z;
+  const double f = ((double)sqrtf(x * x + y * y + z * z) - (double)d0) / (double)d0;
+  return f * f * (double)(f >= 0.0 ? ks : kq);
+}
+
+__device__ __forceinline__ double angle_exact(float4 a, float4 b, float4 c, float kang) {
+  float x1 = a.x - b.x, y1 = a.y - b.y, z1 = a.z - b.z;
+  float x2 = b.x - c.x, y2 = b.y - c.y, z2 = b.z - c.z;
+  float m1 = sqrtf(x1 * x1 + y1 * y1 + z1 * z1);
+  float m2 = sqrtf(x2 * x2 + y2 * y2 + z2 * z2);
+  m1 = m1 > 0.0f ? 1.0f / m1 : 0.0f;
+  m2 = m2 > 0.0f ? 1.0f / m2 : 0.0f;
+  const float dot = (x1 * m1) * (x2 * m2) + (y1 * m1) * (y2 * m2) + (z1 * m1) * (z2 * m2);
+  const double ang = 1.0f - (dot + 1.0f) / 2.0f;
+  return ang * ang * ang * (double)kang;
+}
+
 // FP64 full score (calcScoreStructureSmooth(true,true) + sphere).
-__device__ double smooth_full(const float4 *P, const float *dtn, int n,
+__device__ double smooth_full(const float4 *P, const float2 *dtn, int n,
                               const SmoothDevParams &S) {
   double sa = 0.0, sb = 0.0, sp = 0.0;
   for (int i = 0; i + 1 < n; ++i) {
-    sa += (double)bond_e(P[i], P[i + 1], dtn[i], S.ks, S.kq);
-    if (i > 0) sb += (double)angle_e(P[i - 1], P[i], P[i + 1], S.kang);
+    sa += bond_exact(P[i], P[i + 1], dtn[i].x, S.ks, S.kq);
+    if (i > 0) sb += angle_exact(P[i - 1], P[i], P[i + 1], S.kang);
   }
   for (int i = 0; i < n; ++i) sp += sphere_penalty(P[i].x, P[i].y, P[i].z, S.R);
   return sa * (double)S.wd + sb * (double)S.wa + sp;
+}
+
+// float-float accumulation (Knuth two-sum) of a float increment
+__device__ __forceinline__ void ff_add(float &hi, float &lo, float d) {
+  const float s = hi + d;
+  const float bb = s - hi;
+  const float err = (hi - (s - bb)) + (d - bb);
+  const float l = lo + err;
+  hi = s + l;
+  lo = l - (hi - s);
 }
 
 template <bool SMEM>
 __global__ void __launch_bounds__(128)
 smooth_anneal_kernel(const SmoothUnit *__restrict__ units,
                      const int2 *__restrict__ items, int n_items,
-                     const float4 *__restrict__ pos0, const float *__restrict__ dtn_all,
+                     const float4 *__restrict__ pos0, const float2 *__restrict__ dtn_all,
                      const int *__restrict__ movable, SmoothDevParams S,
                      float4 *__restrict__ work, float *__restrict__ pos_out,
                      ChainOut *__restrict__ outs) {
@@ -128,13 +159,14 @@ smooth_anneal_kernel(const SmoothUnit *__restrict__ units,
   const uint32_t chain_id = (uint32_t)(U.chain_base + chain);
   float4 *P = SMEM ? reinterpret_cast<float4 *>(smem) + (size_t)threadIdx.x * S.slice
                    : work + U.work_off + (long long)chain * n;
-  const float *dtn = dtn_all + U.dtn_off;
+  const float2 *dtn = dtn_all + U.dtn_off;
   const int *MOV = U.mov_off >= 0 ? movable + U.mov_off : nullptr;
   for (int i = 0; i < n; ++i) P[i] = pos0[U.pos_off + i];
 
-  double E = smooth_full(P, dtn, n, S);
-  float Ef = (float)E;
-  double E_ms = E;
+  const double E0 = smooth_full(P, dtn, n, S);
+  // running score: float-float pair per move, widened to FP64 at milestones
+  float e_hi = (float)E0, e_lo = (float)(E0 - (double)(float)E0);
+  double E_ms = E0;
   float T = S.max_temp;
   long long moves = 0, accepted = 0;
   int succ = 0, misses = 0, status = kDevOk;
@@ -157,17 +189,17 @@ smooth_anneal_kernel(const SmoothUnit *__restrict__ units,
     if (!acc && T > 0.0f) {
       const uint4 a = philox_move(S.seed, chain_id, (uint64_t)moves, 1u);
       const float thr = ratio_threshold(u01(a.x), T, S.inv_scale, S.inv_coef);
-      acc = d < Ef * (thr - 1.0f);
+      acc = d < e_hi * (thr - 1.0f);
     }
     if (acc) {
       P[b] = nb;
-      E += (double)d;
-      Ef = (float)E;
+      ff_add(e_hi, e_lo, d);
       ++accepted;
       ++succ;
     }
     ++moves;
     if (moves % S.window == 0) {
+      const double E = (double)e_hi + (double)e_lo;
       const bool miss = (E > (double)S.improvement * E_ms && succ < S.min_succ) || E < 1e-6;
       misses = miss ? misses + 1 : 0;
       if (misses >= S.fails || E < 1e-6) stop = true;
@@ -178,10 +210,10 @@ smooth_anneal_kernel(const SmoothUnit *__restrict__ units,
     if (!stop && moves >= S.cap) stop = true;
   }
   ChainOut o;
-  o.energy = E;
+  o.energy = (double)e_hi + (double)e_lo;
   o.energy_fp64 = smooth_full(P, dtn, n, S);
   o.base = 0.0;
-  o.score = (float)E;
+  o.score = e_hi;
   o.status = status;
   o.moves = moves;
   o.accepted = accepted;
@@ -247,7 +279,7 @@ extern "C" pmmc_status pmmc_smooth_batch_anneal(pmmc_ctx *ctx, int n_units,
   if (chains < 1) chains = 1;
   std::vector<SmoothUnit> hu(n_units);
   std::vector<float4> hpos;
-  std::vector<float> hdtn;
+  std::vector<float2> hdtn;
   std::vector<int> hmov;
   long long out_off = 0, work_off = 0;
   int chain_base = 0, max_n = 0;
@@ -261,7 +293,9 @@ extern "C" pmmc_status pmmc_smooth_batch_anneal(pmmc_ctx *ctx, int n_units,
     U.dtn_off = (int)hdtn.size();
     for (int i = 0; i < pr.n; ++i) {
       hpos.push_back(make_float4(pr.pos[3 * i], pr.pos[3 * i + 1], pr.pos[3 * i + 2], 0.0f));
-      hdtn.push_back(pr.dist_to_next[i]);
+      // clamp as calcScoreStructureSmooth does (LooperSolver.hpp:3470-3471)
+      const float d0 = pr.dist_to_next[i] < 1e-6f ? 1e-6f : pr.dist_to_next[i];
+      hdtn.push_back(make_float2(d0, 1.0f / d0));
     }
     std::vector<int> mv;
     for (int i = 0; i < pr.n; ++i)
@@ -308,7 +342,8 @@ extern "C" pmmc_status pmmc_smooth_batch_anneal(pmmc_ctx *ctx, int n_units,
   DevBuf<SmoothUnit> d_units;
   DevBuf<int2> d_items;
   DevBuf<float4> d_pos, d_work;
-  DevBuf<float> d_dtn, d_out;
+  DevBuf<float2> d_dtn;
+  DevBuf<float> d_out;
   DevBuf<int> d_mov;
   DevBuf<ChainOut> d_outs;
   cudaError_t e = d_units.upload(hu, s);
