@@ -271,13 +271,15 @@ pmmc_status pmmc_arcs_batch_trace(pmmc_arcs_batch *b, void *out, int count);
 /* Many smoothing regions (genome-scale smoothing splits chromosomes at their
  * fixed anchors) with `chains` chains each, one pass; kernel_ms (nullable)
  * receives the device time of the annealing kernel.  pos_out holds
- * sum(n_u)*3 floats (best chain of each region). */
+ * sum(n_u)*3 floats (best chain of each region).  trace_out (nullable)
+ * receives trace_cap move records of chain 0 of region 0. */
 pmmc_status pmmc_smooth_batch_anneal(pmmc_ctx *ctx, int n_units,
                                      const pmmc_smooth_problem *units,
                                      const pmmc_anneal_params *prm,
                                      const float *step_sizes, int chains,
                                      float *pos_out, pmmc_result *res,
-                                     double *kernel_ms);
+                                     double *kernel_ms, void *trace_out,
+                                     int trace_cap);
 /* Many independent heatmap chains (distinct matrices), one CTA each.
  * trace_out (nullable) receives trace_cap records of unit 0's first moves. */
 pmmc_status pmmc_heatmap_batch_anneal(pmmc_ctx *ctx, int n_units,

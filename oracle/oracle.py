@@ -398,3 +398,68 @@ def philox(ctr, key):
     o = (C.c_uint32 * 4)()
     lib().orc_philox4x32_10(c, k, o)
     return [o[i] for i in range(4)]
+
+
+# ---------------------------------------------------------------------------
+# Replay of a kernel trace
+# ---------------------------------------------------------------------------
+class ReplayOut(C.Structure):
+    _fields_ = [("before", C.c_void_p), ("after", C.c_void_p), ("orc_acc", C.c_void_p),
+                ("margin", C.c_void_p), ("proposal_mismatch", C.c_int),
+                ("final_energy", C.c_double)]
+
+
+def _replay_prep(trace):
+    m = len(trace)
+    bead = np.ascontiguousarray(trace["bead"], dtype=np.int32)
+    disp = np.ascontiguousarray(np.stack([trace["dx"], trace["dy"], trace["dz"]], 1),
+                                dtype=np.float32)
+    acc = np.ascontiguousarray(trace["accepted"], dtype=np.int32)
+    before = np.zeros(m, np.float64)
+    after = np.zeros(m, np.float64)
+    oacc = np.zeros(m, np.int32)
+    margin = np.zeros(m, np.float64)
+    out = ReplayOut(_p(before), _p(after), _p(oacc), _p(margin), 0, 0.0)
+    keep = (bead, disp, acc, before, after, oacc, margin)
+    return m, bead, disp, acc, out, keep
+
+
+def _replay_result(out, keep):
+    return {"before": keep[3], "after": keep[4], "orc_acc": keep[5], "margin": keep[6],
+            "proposal_mismatch": out.proposal_mismatch, "final_energy": out.final_energy}
+
+
+def arcs_replay(pr: ArcsProblem, prm: Params, step: float, seed: int, chain: int, trace):
+    m, bead, disp, acc, out, keep = _replay_prep(trace)
+    la, lkeep = _loops(pr)
+    fx = _u8(pr.fixed)
+    lib().orc_arcs_replay(pr.n, _p(_f32(pr.pos)), _p(fx), _p(_f32(pr.exp_dist)), *la,
+                          C.byref(prm.c()), C.c_float(step), C.c_uint64(seed),
+                          C.c_uint32(chain), m, _p(bead), _p(disp), _p(acc), C.byref(out))
+    return _replay_result(out, keep)
+
+
+def smooth_replay(pr: SmoothProblem, prm: Params, step: float, seed: int, chain: int, trace):
+    m, bead, disp, acc, out, keep = _replay_prep(trace)
+    fx = _u8(pr.fixed)
+    lib().orc_smooth_replay(pr.n, _p(_f32(pr.pos)), _p(fx), _p(_f64(pr.dist_to_next)),
+                            C.byref(prm.c()), C.c_float(step), C.c_uint64(seed),
+                            C.c_uint32(chain), m, _p(bead), _p(disp), _p(acc), C.byref(out))
+    return _replay_result(out, keep)
+
+
+def heatmap_replay(pr: HeatmapProblem, prm: Params, step: float, seed: int, chain: int, trace):
+    m, bead, disp, acc, out, keep = _replay_prep(trace)
+    fx = _u8(pr.fixed)
+    b = _i32(pr.bounds)
+    lib().orc_heatmap_replay(pr.n, _p(_f32(pr.pos)), _p(fx), _p(_f32(pr.heat)), int(pr.diag),
+                             len(b), _p(b), C.byref(prm.c()), C.c_float(step),
+                             C.c_uint64(seed), C.c_uint32(chain), m, _p(bead), _p(disp),
+                             _p(acc), C.byref(out))
+    return _replay_result(out, keep)
+
+
+def ref_random_vectors(seed: int, count: int, max_size: float = 1.0, in2d: bool = False):
+    out = np.zeros((count, 3), np.float32)
+    ref().ref_random_vectors(C.c_uint(seed), count, C.c_float(max_size), int(in2d), _p(out))
+    return out

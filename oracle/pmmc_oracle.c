@@ -906,3 +906,157 @@ int orc_hcm_arc_line(char *buf, int cap, const int a[7]) {
   return snprintf(buf, cap, "%d %d %d %d %d %d %d\n", a[0], a[1], a[2], a[3],
                   a[4], a[5], a[6]);
 }
+
+/* ------------------------------------------------------------------ */
+/* Replay of a kernel trace (test infrastructure)                      */
+/* ------------------------------------------------------------------ */
+typedef double (*local_fn)(void *ctx, const float *pos, int moved);
+
+typedef struct {
+  int n;
+  const float *exp_dist;
+  const loop_ent *loops;
+  int m;
+  const orc_params *p;
+  const double *dtn;
+  const float *heat;
+  int diag, n_bounds;
+  const int *bounds;
+} replay_ctx;
+
+static double arcs_local_cb(void *vc, const float *pos, int moved) {
+  replay_ctx *c = (replay_ctx *)vc;
+  double sc = arcs_dist_local(c->n, pos, c->exp_dist, c->p, moved) +
+              loop_energy(pos, c->loops, c->m, moved);
+  if (c->p->sphere_radius > 0.0f)
+    sc += sphere_pen(pos + 3 * moved, c->p->sphere_radius);
+  return sc;
+}
+
+static double smooth_local_cb(void *vc, const float *pos, int moved) {
+  replay_ctx *c = (replay_ctx *)vc;
+  return orc_smooth_local_score(c->n, pos, c->dtn, c->p, moved);
+}
+
+static double heat_local_cb(void *vc, const float *pos, int moved) {
+  replay_ctx *c = (replay_ctx *)vc;
+  return hm_local(c->n, pos, c->heat, c->diag, c->n_bounds, c->bounds, moved);
+}
+
+/* kind: 0 arcs (<=, no T check), 1 heatmap (<=, T>0, delta counted twice),
+ * 2 smoothing (strict <, T>0). */
+static void replay_core(int kind, void *ctx, local_fn fn, int n, float *pos,
+                        const unsigned char *fixed, const orc_params *p,
+                        float step, double E, uint64_t seed, uint32_t chain,
+                        int n_moves, const int *bead, const float *disp,
+                        const int *gpu_acc, orc_replay_out *out) {
+  orc_rng r;
+  r.kind = ORC_RNG_PHILOX;
+  r.seed = seed;
+  r.chain = chain;
+  r.move = 0;
+  rng_ctx c;
+  rng_begin(&c, &r, n, fixed);
+  double T = p->max_temp;
+  out->proposal_mismatch = 0;
+  for (int k = 0; k < n_moves; ++k) {
+    int b = draw_bead(&c, n);
+    float d[3];
+    draw_disp(&c, step, p->use2d, d);
+    if (b != bead[k] || d[0] != disp[3 * k] || d[1] != disp[3 * k + 1] ||
+        d[2] != disp[3 * k + 2])
+      out->proposal_mismatch++;
+    b = bead[k];
+    float *q = pos + 3 * b;
+    float old[3] = {q[0], q[1], q[2]};
+    double before = fn(ctx, pos, b);
+    q[0] += disp[3 * k];
+    q[1] += disp[3 * k + 1];
+    q[2] += disp[3 * k + 2];
+    double after = fn(ctx, pos, b);
+    double dE = (kind == 1 ? 2.0 : 1.0) * (after - before);
+    if (kind == 1 && p->sphere_radius > 0.0f)
+      dE += sphere_pen(q, p->sphere_radius) - sphere_pen(old, p->sphere_radius);
+    double En = E + dE;
+    int ok = kind == 2 ? En < E : En <= E;
+    uint32_t o[4];
+    philox_block(&r, 1u, o);
+    float u = orc_u01(o[0]);
+    if (!ok && (kind == 0 || T > 0.0)) {
+      double tp = p->jump_scale * exp(-p->jump_coef * (En / E) / T);
+      ok = u < (float)tp;
+    }
+    /* distance of the decision from its threshold, in log-ratio units */
+    double thr = (T > 0.0 && u > 0.0f) ? -T * log((double)u / p->jump_scale) / p->jump_coef : 0.0;
+    double margin = (E > 0.0 && En > 0.0 && thr > 0.0) ? fabs(log(En / E) - log(thr)) : 1e300;
+    if (dE <= 0.0 && kind != 2) margin = fabs(dE) / (fabs(E) > 0 ? fabs(E) : 1.0);
+    if (kind == 2 && dE < 0.0) margin = fabs(dE) / (fabs(E) > 0 ? fabs(E) : 1.0);
+    out->before[k] = before;
+    out->after[k] = after;
+    out->orc_acc[k] = ok;
+    out->margin[k] = margin;
+    if (gpu_acc[k]) {
+      E = En;
+    } else {
+      q[0] = old[0];
+      q[1] = old[1];
+      q[2] = old[2];
+    }
+    r.move++;
+    T *= p->dt_temp;
+  }
+  out->final_energy = E;
+  rng_end(&c);
+}
+
+void orc_arcs_replay(int n, const float *pos0, const unsigned char *fixed,
+                     const float *exp_dist, int n_loops, const int *loop_i,
+                     const int *loop_j, const float *loop_k,
+                     const float *loop_r0, const orc_params *p,
+                     float step_size, uint64_t seed, uint32_t chain,
+                     int n_moves, const int *bead, const float *disp,
+                     const int *gpu_acc, orc_replay_out *out) {
+  int m;
+  loop_ent *e = build_loops(n, n_loops, loop_i, loop_j, loop_k, loop_r0, &m);
+  float *pos = (float *)malloc(sizeof(float) * 3 * (n > 0 ? n : 1));
+  memcpy(pos, pos0, sizeof(float) * 3 * n);
+  replay_ctx c = {n, exp_dist, e, m, p, NULL, NULL, 0, 0, NULL};
+  double E = arcs_dist_full(n, pos, exp_dist, p, 1, 1) + loop_energy(pos, e, m, -1);
+  if (p->sphere_radius > 0.0f)
+    for (int k = 0; k < n; ++k) E += sphere_pen(pos + 3 * k, p->sphere_radius);
+  replay_core(0, &c, arcs_local_cb, n, pos, fixed, p, step_size, E, seed, chain,
+              n_moves, bead, disp, gpu_acc, out);
+  free(pos);
+  free(e);
+}
+
+void orc_smooth_replay(int n, const float *pos0, const unsigned char *fixed,
+                       const double *dist_to_next, const orc_params *p,
+                       float step_size, uint64_t seed, uint32_t chain,
+                       int n_moves, const int *bead, const float *disp,
+                       const int *gpu_acc, orc_replay_out *out) {
+  float *pos = (float *)malloc(sizeof(float) * 3 * (n > 0 ? n : 1));
+  memcpy(pos, pos0, sizeof(float) * 3 * n);
+  replay_ctx c = {n, NULL, NULL, 0, p, dist_to_next, NULL, 0, 0, NULL};
+  double E = orc_smooth_full_score(n, pos, dist_to_next, p);
+  replay_core(2, &c, smooth_local_cb, n, pos, fixed, p, step_size, E, seed, chain,
+              n_moves, bead, disp, gpu_acc, out);
+  free(pos);
+}
+
+void orc_heatmap_replay(int n, const float *pos0, const unsigned char *fixed,
+                        const float *heat, int diag, int n_bounds,
+                        const int *bounds, const orc_params *p,
+                        float step_size, uint64_t seed, uint32_t chain,
+                        int n_moves, const int *bead, const float *disp,
+                        const int *gpu_acc, orc_replay_out *out) {
+  float *pos = (float *)malloc(sizeof(float) * 3 * (n > 0 ? n : 1));
+  memcpy(pos, pos0, sizeof(float) * 3 * n);
+  replay_ctx c = {n, NULL, NULL, 0, p, NULL, heat, diag, n_bounds, bounds};
+  double E = orc_heatmap_score(n, pos, heat, diag, n_bounds, bounds, -1);
+  if (p->sphere_radius > 0.0f)
+    for (int k = 0; k < n; ++k) E += sphere_pen(pos + 3 * k, p->sphere_radius);
+  replay_core(1, &c, heat_local_cb, n, pos, fixed, p, step_size * 0.5f, E, seed, chain,
+              n_moves, bead, disp, gpu_acc, out);
+  free(pos);
+}

@@ -144,6 +144,46 @@ int orc_mark_arcs(int n_anchors, const int *a_start, const int *a_end,
                   const int *r_score, const int *r_factor, int *out, int cap,
                   int *non_matching);
 
+/* ---------------- replay of a kernel's move trace ---------------- */
+/* Follows a CUDA chain move by move: for move k the trace gives the bead,
+ * the displacement and the kernel's decision.  The oracle re-derives the
+ * Philox draw of move k (proposal_mismatch counts draws that differ from the
+ * trace), scores the move in FP64 on its own copy of the structure
+ * (before[k], after[k] = local scores of the reference's local scoring
+ * functions), takes its own Metropolis decision from its FP64 running score,
+ * temperature T0*dt^k and the move's Philox uniform (orc_acc[k]), records
+ * margin[k] = |ln(E_new/E_prev) - ln(threshold ratio)| (how close the
+ * decision was), and then applies the KERNEL's decision so that both stay on
+ * the same trajectory.  kind: 0 arc level, 1 heatmap (before/after are the
+ * local scores of the moved bead), 2 smoothing. */
+typedef struct orc_replay_out {
+  double *before;
+  double *after;
+  int *orc_acc;
+  double *margin;
+  int proposal_mismatch;
+  double final_energy; /* oracle running energy after the last move */
+} orc_replay_out;
+
+void orc_arcs_replay(int n, const float *pos0, const unsigned char *fixed,
+                     const float *exp_dist, int n_loops, const int *loop_i,
+                     const int *loop_j, const float *loop_k,
+                     const float *loop_r0, const orc_params *p,
+                     float step_size, uint64_t seed, uint32_t chain,
+                     int n_moves, const int *bead, const float *disp,
+                     const int *gpu_acc, orc_replay_out *out);
+void orc_smooth_replay(int n, const float *pos0, const unsigned char *fixed,
+                       const double *dist_to_next, const orc_params *p,
+                       float step_size, uint64_t seed, uint32_t chain,
+                       int n_moves, const int *bead, const float *disp,
+                       const int *gpu_acc, orc_replay_out *out);
+void orc_heatmap_replay(int n, const float *pos0, const unsigned char *fixed,
+                        const float *heat, int diag, int n_bounds,
+                        const int *bounds, const orc_params *p,
+                        float step_size, uint64_t seed, uint32_t chain,
+                        int n_moves, const int *bead, const float *disp,
+                        const int *gpu_acc, orc_replay_out *out);
+
 /* ---------------- HCM text lines ---------------- */
 /* Cluster::toFile (src/include/Cluster.hpp:175-181). Returns bytes written. */
 int orc_hcm_cluster_line(char *buf, int cap, int start, int end, char orient,

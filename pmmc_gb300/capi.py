@@ -320,7 +320,8 @@ class SmoothInput:
         return SmoothProblem(self.n, _p(self.pos), _p(self.fixed), _p(self.dtn))
 
 
-def smooth_batch_anneal(ctx: Context, inputs, params: AnnealParams, steps, chains=1):
+def smooth_batch_anneal(ctx: Context, inputs, params: AnnealParams, steps, chains=1,
+                        trace_cap=0):
     inputs = list(inputs)
     arr = (SmoothProblem * len(inputs))(*[x.struct() for x in inputs])
     st = _f32(steps)
@@ -328,12 +329,16 @@ def smooth_batch_anneal(ctx: Context, inputs, params: AnnealParams, steps, chain
     pos = np.zeros((tot, 3), np.float32)
     res = (Result * len(inputs))()
     ms = C.c_double()
+    tr = np.zeros(max(trace_cap, 1), TRACE_DTYPE)
     ctx.check(lib().pmmc_smooth_batch_anneal(ctx.h, len(inputs), arr, C.byref(params), _p(st),
-                                             int(chains), _p(pos), res, C.byref(ms)))
+                                             int(chains), _p(pos), res, C.byref(ms),
+                                             _p(tr) if trace_cap else None, int(trace_cap)))
     out, off = [], 0
     for x in inputs:
         out.append(pos[off:off + x.n])
         off += x.n
+    if trace_cap:
+        return out, [r for r in res], ms.value, tr
     return out, [r for r in res], ms.value
 
 

@@ -148,7 +148,8 @@ smooth_anneal_kernel(const SmoothUnit *__restrict__ units,
                      const float4 *__restrict__ pos0, const float2 *__restrict__ dtn_all,
                      const int *__restrict__ movable, SmoothDevParams S,
                      float4 *__restrict__ work, float *__restrict__ pos_out,
-                     ChainOut *__restrict__ outs) {
+                     ChainOut *__restrict__ outs, MoveTrace *__restrict__ trace,
+                     int trace_cap) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int item = blockIdx.x * blockDim.x + threadIdx.x;
   if (item >= n_items) return;
@@ -177,10 +178,13 @@ smooth_anneal_kernel(const SmoothUnit *__restrict__ units,
     const int k = uniform_index(r.x, U.n_mov);
     const int b = MOV ? MOV[k] : k;
     const float4 ob = P[b];
+    const float ddx = (2.0f * u01(r.y) - 1.0f) * U.step;
+    const float ddy = (2.0f * u01(r.z) - 1.0f) * U.step;
+    const float ddz = S.use2d ? 0.0f : (2.0f * u01(r.w) - 1.0f) * U.step;
     float4 nb = ob;
-    nb.x += (2.0f * u01(r.y) - 1.0f) * U.step;
-    nb.y += (2.0f * u01(r.z) - 1.0f) * U.step;
-    if (!S.use2d) nb.z += (2.0f * u01(r.w) - 1.0f) * U.step;
+    nb.x += ddx;
+    nb.y += ddy;
+    nb.z += ddz;
     const float so = smooth_local(P, dtn, n, b, ob, S);
     const float sn = smooth_local(P, dtn, n, b, nb, S);
     const float d = sn - so;
@@ -196,6 +200,18 @@ smooth_anneal_kernel(const SmoothUnit *__restrict__ units,
       ff_add(e_hi, e_lo, d);
       ++accepted;
       ++succ;
+    }
+    if (trace != nullptr && chain_id == 0 && moves < trace_cap) {
+      MoveTrace tr;
+      tr.bead = b;
+      tr.accepted = acc ? 1 : 0;
+      tr.before = so;
+      tr.after = sn;
+      tr.dx = ddx;
+      tr.dy = ddy;
+      tr.dz = ddz;
+      tr.pad = d;
+      trace[moves] = tr;
     }
     ++moves;
     if (moves % S.window == 0) {
@@ -273,7 +289,8 @@ extern "C" pmmc_status pmmc_smooth_batch_anneal(pmmc_ctx *ctx, int n_units,
                                                const pmmc_anneal_params *prm,
                                                const float *steps, int chains,
                                                float *pos_out, pmmc_result *res,
-                                               double *kernel_ms) {
+                                               double *kernel_ms, void *trace_out,
+                                               int trace_cap) {
   if (!ctx || n_units < 1 || !units || !prm || !steps)
     return fail(ctx, PMMC_ERR_INVALID, "smooth batch: bad arguments");
   if (chains < 1) chains = 1;
@@ -346,7 +363,9 @@ extern "C" pmmc_status pmmc_smooth_batch_anneal(pmmc_ctx *ctx, int n_units,
   DevBuf<float> d_out;
   DevBuf<int> d_mov;
   DevBuf<ChainOut> d_outs;
+  DevBuf<MoveTrace> d_trace;
   cudaError_t e = d_units.upload(hu, s);
+  if (e == cudaSuccess && trace_cap > 0) e = d_trace.alloc((size_t)trace_cap);
   if (e == cudaSuccess) e = d_items.upload(items, s);
   if (e == cudaSuccess) e = d_pos.upload(hpos, s);
   if (e == cudaSuccess) e = d_dtn.upload(hdtn, s);
@@ -368,11 +387,11 @@ extern "C" pmmc_status pmmc_smooth_batch_anneal(pmmc_ctx *ctx, int n_units,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     smooth_anneal_kernel<true><<<grid, threads, smem, s>>>(
         d_units.p, d_items.p, n_items, d_pos.p, d_dtn.p, d_mov.p, S, nullptr, d_out.p,
-        d_outs.p);
+        d_outs.p, trace_cap > 0 ? d_trace.p : nullptr, trace_cap);
   } else {
     smooth_anneal_kernel<false><<<grid, threads, 0, s>>>(
         d_units.p, d_items.p, n_items, d_pos.p, d_dtn.p, d_mov.p, S, d_work.p, d_out.p,
-        d_outs.p);
+        d_outs.p, trace_cap > 0 ? d_trace.p : nullptr, trace_cap);
   }
   e = cudaGetLastError();
   cudaEventRecord(e1, s);
@@ -390,6 +409,9 @@ extern "C" pmmc_status pmmc_smooth_batch_anneal(pmmc_ctx *ctx, int n_units,
   std::vector<ChainOut> outs(chain_base);
   PMMC_CUDA(ctx, cudaMemcpy(outs.data(), d_outs.p, sizeof(ChainOut) * outs.size(),
                             cudaMemcpyDeviceToHost));
+  if (trace_out && trace_cap > 0)
+    PMMC_CUDA(ctx, cudaMemcpy(trace_out, d_trace.p, sizeof(MoveTrace) * trace_cap,
+                              cudaMemcpyDeviceToHost));
   long long dst = 0;
   for (int u = 0; u < n_units; ++u) {
     const SmoothUnit &U = hu[u];
@@ -432,5 +454,6 @@ extern "C" pmmc_status pmmc_smooth_anneal(pmmc_ctx *ctx, const pmmc_smooth_probl
                                           int n_chains, float *pos_out, pmmc_result *res) {
   if (!ctx || !pr || !prm) return fail(ctx, PMMC_ERR_INVALID, "smooth anneal: bad arguments");
   if (n_chains <= 0) n_chains = ctx->sm_count;
-  return pmmc_smooth_batch_anneal(ctx, 1, pr, prm, &step_size, n_chains, pos_out, res, nullptr);
+  return pmmc_smooth_batch_anneal(ctx, 1, pr, prm, &step_size, n_chains, pos_out, res, nullptr,
+                                  nullptr, 0);
 }

@@ -1,0 +1,158 @@
+"""Writes the golden fixtures of the parity tests from the REFERENCE itself.
+
+Runs where the reference sources exist: oracle/Makefile builds
+oracle/_ref/libpmmc_ref.so from them (the reference's own LooperSolver /
+InteractionArcs CPU code behind a C harness) and this script records its
+outputs on small seeded inputs into tests/golden/*.npz.  The tests then pin
+the plain-C oracle against these files on any machine, including ones without
+the reference tree.
+
+    python tests/golden/gen_golden.py
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from oracle import oracle as O  # noqa: E402
+from pmmc_gb300 import synth  # noqa: E402
+
+
+def params_array(p: O.Params) -> np.ndarray:
+    return np.array([getattr(p, f) for f, _ in O.OrcParams._fields_], np.float64)
+
+
+def arcs_cases():
+    out = {}
+    # 1: config-0 shape scaled down; 2: loops + sphere + a fixed-free region;
+    # 3: 2D moves
+    specs = [
+        dict(n=64, arcs=100, seed=1, loops=0, sphere=0.0, use2d=0, steps=2000),
+        dict(n=48, arcs=60, seed=2, loops=6, sphere=6.0, use2d=0, steps=1500),
+        dict(n=40, arcs=50, seed=3, loops=0, sphere=0.0, use2d=1, steps=1000),
+    ]
+    for k, sp in enumerate(specs):
+        r = synth.arcs_region(sp["n"], sp["arcs"], seed=sp["seed"])
+        dense = r.dense()
+        rng = np.random.default_rng(100 + k)
+        li = rng.integers(0, sp["n"], sp["loops"]).astype(np.int32)
+        lj = rng.integers(0, sp["n"], sp["loops"]).astype(np.int32)
+        lk = rng.uniform(0.5, 2.0, sp["loops"]).astype(np.float32)
+        lr = rng.uniform(1.0, 3.0, sp["loops"]).astype(np.float32)
+        pr = O.ArcsProblem(r.pos, dense, None, li, lj, lk, lr)
+        prm = O.Params(max_temp=5.0, dt_temp=0.9999, milestone_steps=sp["steps"],
+                       improvement=0.99, sphere_radius=sp["sphere"], use2d=sp["use2d"])
+        beads = np.array([0, 1, sp["n"] // 2, sp["n"] - 1], np.int32)
+        local = np.array([O.ref_arcs_score(pr, prm, int(b)) for b in beads])
+        full = O.ref_arcs_score(pr, prm, -1)
+        pos, score, moves = O.ref_arcs_anneal(pr, prm, 0.5, 1000 + k)
+        out[f"arcs{k}"] = dict(pos=r.pos, dense=dense, li=li, lj=lj, lk=lk, lr=lr,
+                               params=params_array(prm), beads=beads, local=local,
+                               full=np.array([full]), step=np.array([0.5]),
+                               seed=np.array([1000 + k]), out_pos=pos,
+                               out_score=np.array([score]), out_moves=np.array([moves]))
+    return out
+
+
+def heatmap_cases():
+    out = {}
+    specs = [dict(n=64, diag=1, bounds=[], sphere=0.0, seed=4),
+             dict(n=72, diag=2, bounds=[0, 30, 72], sphere=5.0, seed=5)]
+    for k, sp in enumerate(specs):
+        h = synth.heatmap_region(sp["n"], seed=sp["seed"], n_tads=3, tad_min=8, tad_max=16)
+        fixed = np.zeros(sp["n"], np.uint8)
+        fixed[0] = 1
+        pr = O.HeatmapProblem(h.pos, h.heat, sp["diag"], np.array(sp["bounds"], np.int32), fixed)
+        prm = O.Params(max_temp=5.0, dt_temp=0.9999, milestone_steps=400, improvement=0.99,
+                       sphere_radius=sp["sphere"])
+        beads = np.array([0, 5, sp["n"] - 1], np.int32)
+        local = np.array([O.ref_heatmap_score(pr, int(b)) for b in beads])
+        full = O.ref_heatmap_score(pr, -1)
+        pos, score, moves = O.ref_heatmap_anneal(pr, prm, 1.0, 2000 + k)
+        out[f"heatmap{k}"] = dict(pos=h.pos, heat=h.heat, diag=np.array([sp["diag"]]),
+                                  bounds=np.array(sp["bounds"], np.int32), fixed=fixed,
+                                  params=params_array(prm), beads=beads, local=local,
+                                  full=np.array([full]), step=np.array([1.0]),
+                                  seed=np.array([2000 + k]), out_pos=pos,
+                                  out_score=np.array([score]), out_moves=np.array([moves]))
+    return out
+
+
+def smooth_cases():
+    out = {}
+    specs = [dict(n=60, seed=6, w=(1.0, 1.0), sphere=0.0),
+             dict(n=50, seed=7, w=(0.7, 1.3), sphere=8.0)]
+    for k, sp in enumerate(specs):
+        c = synth.smooth_chain(sp["n"], seed=sp["seed"])
+        dtn = c.dist_to_next.copy()
+        dtn[3] = 0.0  # exercises the 1e-6 clamp
+        pr = O.SmoothProblem(c.pos, dtn, c.fixed)
+        prm = O.Params(max_temp=5.0, dt_temp=0.9999, milestone_steps=800, improvement=0.99,
+                       k_stretch=0.1, k_squeeze=0.1, k_angle=0.1, w_dist=sp["w"][0],
+                       w_angle=sp["w"][1], sphere_radius=sp["sphere"])
+        beads = np.array([0, 1, 2, sp["n"] // 2, sp["n"] - 2, sp["n"] - 1], np.int32)
+        local = np.array([O.ref_smooth_score(pr, prm, int(b)) for b in beads])
+        full = O.ref_smooth_score(pr, prm, -1)
+        pos, score, moves = O.ref_smooth_anneal(pr, prm, 0.5, 3000 + k)
+        out[f"smooth{k}"] = dict(pos=c.pos, dtn=dtn, fixed=c.fixed, params=params_array(prm),
+                                 beads=beads, local=local, full=np.array([full]),
+                                 step=np.array([0.5]), seed=np.array([3000 + k]),
+                                 out_pos=pos, out_score=np.array([score]),
+                                 out_moves=np.array([moves]))
+    return out
+
+
+def mark_cases():
+    out = {}
+    rng = np.random.default_rng(8)
+    starts = np.sort(rng.choice(50_000, 30, replace=False)) * 20
+    anchors = np.stack([starts, starts + rng.integers(0, 4000, 30)], 1).astype(np.int32)
+    anchors[3] = [anchors[3, 0], anchors[3, 0]]       # length 1: never matches
+    anchors[5, 1] = anchors[6, 1] + 10               # overlaps the next anchor
+    raw = []
+    for _ in range(250):  # arcs between anchors (duplicates, factors, self loops)
+        i, j = rng.integers(0, 30, 2)
+        raw.append([int(rng.integers(anchors[i, 0], anchors[i, 1] + 1)),
+                    int(rng.integers(anchors[j, 0], anchors[j, 1] + 1)),
+                    int(rng.integers(1, 12)), int(rng.integers(0, 3))])
+    for _ in range(40):   # arcs outside every anchor
+        a, b = sorted(rng.integers(0, 1_000_000, 2))
+        raw.append([int(a), int(b), int(rng.integers(1, 5)), 0])
+    raw += raw[:10]       # exact duplicates
+    raw = np.array(raw, np.int32)
+    ref = O.ref_mark_arcs(anchors, raw)
+    out["mark0"] = dict(anchors=anchors, raw=raw, arcs=ref)
+    return out
+
+
+def hcm_cases():
+    lines = [O.hcm_cluster_line(10, 20, "N", (1.5, -2.25, 3.125), [4, 5], use_ref=True),
+             O.hcm_cluster_line(0, 0, "L", (1e-7, 123456.789, -0.5), [], use_ref=True),
+             O.hcm_arc_line([1, 2, 300, 400, 5, 6, -1], use_ref=True),
+             O.hcm_arc_line([7, 9, -1, -1, 0, 12, 2], use_ref=True)]
+    return {"hcm": dict(lines=np.array(lines))}
+
+
+def main():
+    if not O.ref_available():
+        O.build()
+    if not O.ref_available():
+        raise SystemExit("the reference harness could not be built (no reference tree)")
+    fixtures = {}
+    for fn in (arcs_cases, heatmap_cases, smooth_cases, mark_cases, hcm_cases):
+        fixtures.update(fn())
+    fixtures["rng"] = dict(random_vectors=O.ref_random_vectors(5, 4, 1.0, False),
+                           random_vectors_2d=O.ref_random_vectors(6, 4, 1.0, True))
+    for name, d in fixtures.items():
+        np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **d)
+    print("wrote", len(fixtures), "fixtures")
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,54 @@
+"""Host-side checks of the C ABI that need no GPU: the library loads, exports
+every symbol the header declares, converts the reference's dense layout, and
+fails loudly (no CPU fallback) when no device is present."""
+import os
+import re
+
+import numpy as np
+import pytest
+
+from pmmc_gb300 import capi
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_header_symbols_exported(built_lib):
+    h = open(os.path.join(ROOT, "include", "pmmc_gb300.h")).read()
+    declared = set(re.findall(r"\b(pmmc_[a-z0-9_]+)\s*\(", h))
+    assert declared == set(capi.HEADER_SYMBOLS)
+    for name in declared:
+        assert hasattr(built_lib, name), name
+
+
+def test_default_params_match_reference_settings(built_lib):
+    p = capi.default_params(capi.LEVEL_ARCS)
+    # Settings::init, src/include/Settings.hpp:479-505
+    assert (p.max_temp, p.jump_scale, p.jump_coef, p.min_successes, p.milestone_steps) == \
+        (20.0, 50.0, 20.0, 5, 10000)
+    assert abs(p.dt_temp - 0.99995) < 1e-7 and abs(p.improvement - 0.995) < 1e-7
+    assert (p.k_stretch, p.k_squeeze, p.milestone_fails) == (1.0, 1.0, 3)
+    s = capi.default_params(capi.LEVEL_SMOOTH)
+    assert abs(s.k_stretch - 0.1) < 1e-7 and abs(s.k_angle - 0.1) < 1e-7
+
+
+def test_dense_to_csr_reads_columns(built_lib):
+    d = np.full((4, 4), -1.0, np.float32)
+    np.fill_diagonal(d, 0.0)
+    d[0, 2], d[2, 0] = 1.5, 2.5     # asymmetric on purpose: row i gets column i
+    d[1, 3] = d[3, 1] = 0.0         # listed but inert
+    rp, col, tgt = capi.dense_to_csr(d)
+    assert list(rp) == [0, 1, 2, 3, 4]
+    assert list(col) == [2, 3, 0, 1]
+    np.testing.assert_array_equal(tgt, np.array([2.5, 0.0, 1.5, 0.0], np.float32))
+
+
+def test_no_device_is_an_error(built_lib):
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a device is present")
+    except ImportError:
+        pass
+    with pytest.raises(capi.PmmcError) as e:
+        capi.Context(0)
+    assert e.value.status == capi.PMMC_ERR_NO_DEVICE

@@ -1,0 +1,146 @@
+"""Arc-level annealing on the GPU against the oracle, through the C ABI."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from pmmc_gb300 import capi, synth
+from parity import check_replay, distmap_pearson, kabsch_rmsd, ks_2samp_p
+
+pytestmark = pytest.mark.gpu
+
+
+def problem(variant, n=96, arcs=160, seed=3):
+    r = synth.arcs_region(n, arcs, seed=seed)
+    dense = r.dense()
+    fixed = None
+    loops = None
+    kw = {}
+    if variant == "loops_sphere":
+        rng = np.random.default_rng(seed)
+        li = rng.integers(0, n, 12).astype(np.int32)
+        lj = rng.integers(0, n, 12).astype(np.int32)
+        lk = rng.uniform(0.5, 2.0, 12).astype(np.float32)
+        lr = rng.uniform(1.0, 3.0, 12).astype(np.float32)
+        loops = (li, lj, lk, lr)
+        kw["sphere_radius"] = 7.0
+    if variant == "fixed":
+        fixed = np.zeros(n, np.uint8)
+        fixed[::7] = 1
+    if variant == "2d":
+        kw["use2d"] = 1
+    if variant == "inert_pairs":   # listed pairs with 0 <= target < 1e-6
+        dense[1, 5] = dense[5, 1] = 0.0
+        dense[10, 40] = dense[40, 10] = 0.0
+    if variant == "hub":           # a bead with more than 32 arcs
+        for j in range(2, n, 2):
+            dense[0, j] = dense[j, 0] = 1.0 + 0.01 * j
+    pr = O.ArcsProblem(r.pos, dense, fixed, *(loops or ()))
+    inp = capi.ArcsInput.from_dense(r.pos, dense, fixed, loops)
+    return pr, inp, kw
+
+
+@pytest.mark.parametrize("variant", ["plain", "loops_sphere", "fixed", "2d", "inert_pairs", "hub"])
+def test_arcs_trace_parity(ctx, variant):
+    pr, inp, kw = problem(variant)
+    base = dict(max_temp=5.0, dt_temp=0.9999, milestone_steps=4000, improvement=0.99, **kw)
+    prm = capi.default_params(capi.LEVEL_ARCS, schedule=capi.SCHEDULE_CPU, max_moves=12000, **base)
+    ctx.set_seed(777)
+    b = capi.ArcsBatch(ctx, [inp], prm, [0.5], use_graph=False, trace_cap=12000)
+    b.run()
+    pos, res = b.results()
+    m = int(res[0].moves)
+    tr = b.trace(m)
+    rep = O.arcs_replay(pr, O.Params(**base), 0.5, 777, 0, tr)
+    check_replay(tr, rep)
+    # the oracle, following the kernel's decisions, lands on the same structure
+    # and the same running energy
+    assert abs(rep["final_energy"] - res[0].energy) <= 1e-5 * abs(rep["final_energy"])
+
+
+def test_arcs_fp64_energy_and_resync(ctx):
+    pr, inp, _ = problem("plain", n=256, arcs=400, seed=42)
+    oprm = O.Params(max_temp=5.0, dt_temp=0.9999, milestone_steps=50000, improvement=0.99)
+    r0 = O.arcs_repulsion(pr)
+    for resync in (0, 1000):
+        prm = capi.default_params(capi.LEVEL_ARCS, max_temp=5.0, dt_temp=0.9999,
+                                  milestone_steps=50000, improvement=0.99,
+                                  schedule=capi.SCHEDULE_CPU, resync_every=resync)
+        pos, res = capi.arcs_anneal(ctx, inp, prm, 0.5, 1)
+        e64 = r0 + O.arcs_full(pr, oprm, pos=pos, repulsion=False)
+        assert abs(res.energy_fp64 - e64) <= 1e-6 * e64
+        assert res.rel_error < (1e-6 if resync else 1e-4)
+        assert abs(res.energy - e64) <= 0.01 * e64   # the 1% final-energy bar
+
+
+def test_arcs_dropin_multichain(ctx):
+    pr, inp, _ = problem("plain", n=256, arcs=400, seed=42)
+    prm = capi.default_params(capi.LEVEL_ARCS, max_temp=5.0, dt_temp=0.9999,
+                              milestone_steps=50000, improvement=0.99)
+    pos, res = capi.arcs_anneal(ctx, inp, prm, 0.5, 64)
+    assert np.isfinite(pos).all()
+    assert 0 <= res.best_chain < 64 and res.total_moves >= res.moves > 0
+    oprm = O.Params(max_temp=5.0, dt_temp=0.9999, milestone_steps=50000, improvement=0.99)
+    e64 = O.arcs_repulsion(pr) + O.arcs_full(pr, oprm, pos=pos, repulsion=False)
+    assert abs(res.energy_fp64 - e64) <= 1e-6 * e64
+
+
+def test_arcs_batch_units_match_oracle(ctx):
+    """Every unit of a batch follows the oracle's Philox-mode annealer."""
+    regs = [synth.arcs_region(n, int(1.5 * n), seed=s) for s, n in enumerate([32, 57, 130, 300, 80, 41])]
+    inputs = [capi.ArcsInput.from_dense(r.pos, r.dense()) for r in regs]
+    base = dict(max_temp=5.0, dt_temp=0.9999, milestone_steps=1000, improvement=0.99)
+    prm = capi.default_params(capi.LEVEL_ARCS, schedule=capi.SCHEDULE_CPU, max_moves=3000, **base)
+    ctx.set_seed(99)
+    b = capi.ArcsBatch(ctx, inputs, prm, [0.5] * len(inputs))
+    b.run()
+    pos, res = b.results()
+    same = 0
+    for u, r in enumerate(regs):
+        pr = O.ArcsProblem(r.pos, r.dense())
+        opos, ores = O.arcs_anneal(pr, O.Params(max_moves=3000, **base), 0.5, 99,
+                                   rng=O.RNG_PHILOX, chain=u)
+        assert abs(ores.score - res[u].energy) <= 1e-3 * abs(ores.score)
+        same += int(ores.moves == res[u].moves and np.allclose(opos, pos[u], atol=1e-3))
+    assert same >= len(regs) - 1
+
+
+def test_arcs_batch_graph_replay_is_deterministic(ctx):
+    regs = [synth.arcs_region(n, int(1.5 * n), seed=s) for s, n in enumerate([64, 200, 700])]
+    inputs = [capi.ArcsInput.from_dense(r.pos, r.dense()) for r in regs]
+    prm = capi.default_params(capi.LEVEL_ARCS, max_temp=5.0, dt_temp=0.9999,
+                              milestone_steps=5000, improvement=0.99, resync_every=1000)
+    b = capi.ArcsBatch(ctx, inputs, prm, [0.5] * 3, use_graph=True)
+    b.run()
+    p1, r1 = b.results()
+    b.run()
+    p2, r2 = b.results()
+    for a, c in zip(p1, p2):
+        np.testing.assert_array_equal(a, c)
+    assert [x.moves for x in r1] == [x.moves for x in r2]
+
+
+def test_arcs_statistics_match_reference(ctx):
+    """16 seeds: final energy, RMSD to the start and distance-map Pearson of
+    the GPU annealer vs the reference's CPU MonteCarloArcs (the oracle in
+    libc mode is bit-identical to it)."""
+    r = synth.arcs_region(64, 100, seed=8)
+    dense = r.dense()
+    pr = O.ArcsProblem(r.pos, dense)
+    base = dict(max_temp=5.0, dt_temp=0.9999, milestone_steps=2000, improvement=0.99)
+    ref_e, ref_rmsd, ref_p = [], [], []
+    for s in range(16):
+        p, res = O.arcs_anneal(pr, O.Params(**base), 0.5, 500 + s)
+        ref_e.append(res.score)
+        ref_rmsd.append(kabsch_rmsd(p, r.pos))
+        ref_p.append(distmap_pearson(p, r.pos))
+    inputs = [capi.ArcsInput.from_dense(r.pos, dense) for _ in range(16)]
+    prm = capi.default_params(capi.LEVEL_ARCS, schedule=capi.SCHEDULE_CPU, **base)
+    ctx.set_seed(4242)
+    b = capi.ArcsBatch(ctx, inputs, prm, [0.5] * 16)
+    b.run()
+    pos, res = b.results()
+    gpu_e = [x.energy for x in res]
+    gpu_rmsd = [kabsch_rmsd(p, r.pos) for p in pos]
+    gpu_p = [distmap_pearson(p, r.pos) for p in pos]
+    for a, c in ((ref_e, gpu_e), (ref_rmsd, gpu_rmsd), (ref_p, gpu_p)):
+        assert ks_2samp_p(a, c) > 0.05

@@ -1,0 +1,60 @@
+"""Heatmap-level annealing on the GPU against the oracle, through the C ABI."""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from pmmc_gb300 import capi, synth
+from parity import check_replay, ks_2samp_p
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("n,diag,bounds,sphere", [(128, 1, [], 0.0), (200, 2, [0, 90, 200], 0.0),
+                                                  (96, 1, [], 6.0)])
+def test_heatmap_trace_parity(ctx, n, diag, bounds, sphere):
+    h = synth.heatmap_region(n, seed=n, n_tads=4, tad_min=10, tad_max=30)
+    fixed = np.zeros(n, np.uint8)
+    fixed[[0, n // 2]] = 1
+    base = dict(max_temp=5.0, dt_temp=0.9999, milestone_steps=3000, improvement=0.99,
+                sphere_radius=sphere)
+    prm = capi.default_params(capi.LEVEL_HEATMAP, schedule=capi.SCHEDULE_CPU, max_moves=6000, **base)
+    ctx.set_seed(17)
+    inp = capi.HeatmapInput(h.pos, h.heat, diag, np.array(bounds, np.int32), fixed)
+    out, res, ms, tr = capi.heatmap_batch_anneal(ctx, [inp], prm, [1.0], trace_cap=6000)
+    m = int(res[0].moves)
+    pr = O.HeatmapProblem(h.pos, h.heat, diag, np.array(bounds, np.int32), fixed)
+    rep = O.heatmap_replay(pr, O.Params(**base), 1.0, 17, 0, tr[:m])
+    check_replay(tr[:m], rep, scale_factor=2.0, delta_only=True)
+    e64 = O.heatmap_score(pr, -1, pos=out[0])
+    if sphere > 0:
+        e64 += float(np.sum(np.maximum(np.linalg.norm(out[0], axis=1) - sphere, 0) ** 2))
+    assert abs(res[0].energy - e64) <= 1e-4 * e64
+    if sphere == 0:
+        assert abs(res[0].energy_fp64 - e64) <= 1e-6 * e64
+    np.testing.assert_array_equal(out[0][fixed == 1], h.pos[fixed == 1])
+
+
+def test_heatmap_batch_distinct_maps(ctx):
+    hs = [synth.heatmap_region(256, seed=s, n_tads=5, tad_min=10, tad_max=40) for s in range(4)]
+    base = dict(max_temp=5.0, dt_temp=0.9999, milestone_steps=2000, improvement=0.99)
+    prm = capi.default_params(capi.LEVEL_HEATMAP, schedule=capi.SCHEDULE_CPU, max_moves=4000, **base)
+    ctx.set_seed(3)
+    out, res, ms, _ = capi.heatmap_batch_anneal(ctx, [capi.HeatmapInput(h.pos, h.heat) for h in hs],
+                                                prm, [1.0] * 4)
+    for u, h in enumerate(hs):
+        pr = O.HeatmapProblem(h.pos, h.heat)
+        opos, ores = O.heatmap_anneal(pr, O.Params(max_moves=4000, **base), 1.0, 3,
+                                      rng=O.RNG_PHILOX, incremental=True, chain=u)
+        assert abs(ores.score - res[u].energy) <= 1e-3 * ores.score
+
+
+def test_heatmap_statistics_match_reference(ctx):
+    h = synth.heatmap_region(48, seed=5, n_tads=2, tad_min=6, tad_max=10)
+    pr = O.HeatmapProblem(h.pos, h.heat)
+    base = dict(max_temp=5.0, dt_temp=0.9999, milestone_steps=600, improvement=0.99)
+    ref_e = [O.heatmap_anneal(pr, O.Params(**base), 1.0, 900 + s)[1].score for s in range(16)]
+    prm = capi.default_params(capi.LEVEL_HEATMAP, schedule=capi.SCHEDULE_CPU, **base)
+    ctx.set_seed(55)
+    out, res, ms, _ = capi.heatmap_batch_anneal(ctx, [capi.HeatmapInput(h.pos, h.heat)] * 16,
+                                                prm, [1.0] * 16)
+    assert ks_2samp_p(ref_e, [r.energy for r in res]) > 0.05

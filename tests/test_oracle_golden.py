@@ -1,0 +1,110 @@
+"""The CPU oracle against golden vectors recorded from the reference itself
+(tests/golden/gen_golden.py runs the reference's LooperSolver/InteractionArcs
+CPU code).  Bit-exact: the oracle restates the reference's float/double
+expression types and draws the same libc rand() stream."""
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+
+GOLD = os.path.join(os.path.dirname(__file__), "golden")
+
+
+def load(name):
+    return dict(np.load(os.path.join(GOLD, name + ".npz")))
+
+
+def params(arr):
+    f = [n for n, _ in O.OrcParams._fields_]
+    kw = {}
+    for n, v in zip(f, arr):
+        kw[n] = int(v) if n in ("min_successes", "milestone_steps", "use2d", "max_moves") else float(v)
+    return O.Params(**kw)
+
+
+def test_philox_known_answers():
+    # Random123 known-answer vectors for philox4x32-10
+    assert O.philox([0, 0, 0, 0], [0, 0]) == [0x6627E8D5, 0xE169C58D, 0xBC57AC4C, 0x9B00DBD8]
+    assert O.philox([0xFFFFFFFF] * 4, [0xFFFFFFFF] * 2) == [0x408F276D, 0x41C83B0E,
+                                                            0xA20BC7C6, 0x6D5451FD]
+    assert O.philox([0x243F6A88, 0x85A308D3, 0x13198A2E, 0x03707344],
+                    [0xA4093822, 0x299F31D0]) == [0xD16CFE09, 0x94FDCCEB, 0x5001E420, 0x24126EA1]
+
+
+def test_random_vector_draw_order():
+    import ctypes
+    g = load("rng")
+    libc = ctypes.CDLL(None)
+    for key, seed, in2d in (("random_vectors", 5, False), ("random_vectors_2d", 6, True)):
+        libc.srand(seed)
+        vals = []
+        for _ in range(4):
+            k = 2 if in2d else 3
+            u = [np.float32(libc.rand()) / np.float32(2147483647.0) for _ in range(k)]
+            d = [np.float32((np.float32(2.0) * x - np.float32(1.0)) * np.float32(1.0)) for x in u]
+            vals.append([d[2], d[1], d[0]] if not in2d else [d[1], d[0], 0.0])
+        np.testing.assert_array_equal(np.array(vals, np.float32), g[key])
+
+
+@pytest.mark.parametrize("case", ["arcs0", "arcs1", "arcs2"])
+def test_arcs_scores_and_anneal(case):
+    g = load(case)
+    pr = O.ArcsProblem(g["pos"], g["dense"], None, g["li"], g["lj"], g["lk"], g["lr"])
+    prm = params(g["params"])
+    for b, want in zip(g["beads"], g["local"]):
+        assert O.arcs_local(pr, prm, int(b)) == want
+    assert O.arcs_full(pr, prm) == g["full"][0]
+    pos, res = O.arcs_anneal(pr, prm, float(g["step"][0]), int(g["seed"][0]))
+    assert res.moves == g["out_moves"][0]
+    assert res.score == g["out_score"][0]
+    np.testing.assert_array_equal(pos, g["out_pos"])
+
+
+@pytest.mark.parametrize("case", ["heatmap0", "heatmap1"])
+def test_heatmap_scores_and_anneal(case):
+    g = load(case)
+    pr = O.HeatmapProblem(g["pos"], g["heat"], int(g["diag"][0]), g["bounds"], g["fixed"])
+    prm = params(g["params"])
+    for b, want in zip(g["beads"], g["local"]):
+        assert O.heatmap_score(pr, int(b)) == want
+    assert O.heatmap_score(pr, -1) == g["full"][0]
+    pos, res = O.heatmap_anneal(pr, prm, float(g["step"][0]), int(g["seed"][0]))
+    assert res.moves == g["out_moves"][0]
+    assert res.score == g["out_score"][0]
+    np.testing.assert_array_equal(pos, g["out_pos"])
+
+
+@pytest.mark.parametrize("case", ["smooth0", "smooth1"])
+def test_smooth_scores_and_anneal(case):
+    g = load(case)
+    pr = O.SmoothProblem(g["pos"], g["dtn"], g["fixed"])
+    prm = params(g["params"])
+    for b, want in zip(g["beads"], g["local"]):
+        assert O.smooth_local(pr, prm, int(b)) == want
+    assert O.smooth_full(pr, prm) == g["full"][0]
+    pos, res = O.smooth_anneal(pr, prm, float(g["step"][0]), int(g["seed"][0]))
+    assert res.moves == g["out_moves"][0]
+    assert res.score == g["out_score"][0]
+    np.testing.assert_array_equal(pos, g["out_pos"])
+
+
+def test_mark_arcs():
+    g = load("mark0")
+    np.testing.assert_array_equal(O.mark_arcs(g["anchors"], g["raw"]), g["arcs"])
+
+
+def test_mark_arcs_empty_inputs():
+    assert O.mark_arcs(np.zeros((0, 2), np.int32), np.zeros((0, 4), np.int32)).shape == (0, 7)
+    a = np.array([[100, 200], [300, 400]], np.int32)
+    assert O.mark_arcs(a, np.zeros((0, 4), np.int32)).shape == (0, 7)
+
+
+def test_hcm_lines():
+    g = load("hcm")
+    got = [O.hcm_cluster_line(10, 20, "N", (1.5, -2.25, 3.125), [4, 5]),
+           O.hcm_cluster_line(0, 0, "L", (1e-7, 123456.789, -0.5), []),
+           O.hcm_arc_line([1, 2, 300, 400, 5, 6, -1]),
+           O.hcm_arc_line([7, 9, -1, -1, 0, 12, 2])]
+    assert got == list(g["lines"])
