@@ -90,11 +90,9 @@ __device__ __forceinline__ float dist3(float ax, float ay, float az, float4 b) {
   return sqrtf(x * x + y * y + z * z);
 }
 
-// |a - b| from the hardware reciprocal square root (2 ulp); 0 stays 0.
+// |a - b| as the reference rounds it (see ref_len).
 __device__ __forceinline__ float fast_len(float ax, float ay, float az, float4 b) {
-  const float x = ax - b.x, y = ay - b.y, z = az - b.z;
-  const float s = fmaf(x, x, fmaf(y, y, z * z));
-  return s * rsqrtf(fmaxf(s, 1e-30f));
+  return ref_len(__fsub_rn(ax, b.x), __fsub_rn(ay, b.y), __fsub_rn(az, b.z));
 }
 
 // Spring term of one arc: ((len - t) / t)^2 * k, with 1/t precomputed.
@@ -330,9 +328,11 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
           const int l0 = LRP[b], l1 = LRP[b + 1];
           for (int e = l0 + lane; e < l1; e += 32) {
             const float4 le = LENT[e];
-            const float4 q = spos[__float_as_int(le.x)];
-            const float d0 = dist3(pb.x, pb.y, pb.z, q) - le.z;
-            const float d1 = dist3(nx, ny, nz, q) - le.z;
+            const int j = __float_as_int(le.x);
+            const float4 q = spos[j];
+            // a constraint of a bead with itself stays at distance 0
+            const float d0 = (j == b ? 0.0f : fast_len(pb.x, pb.y, pb.z, q)) - le.z;
+            const float d1 = (j == b ? 0.0f : fast_len(nx, ny, nz, q)) - le.z;
             so += le.y * d0 * d0;
             sn += le.y * d1 * d1;
           }
@@ -649,6 +649,7 @@ extern "C" pmmc_status pmmc_arcs_batch_create_ex(
     for (int i = 0; i < pr.n; ++i) {
       for (int e = pr.row_ptr[i]; e < pr.row_ptr[i + 1]; ++e) {
         const float t = pr.target[e];
+        if (pr.col[e] == i) continue;  // the reference never pairs a bead with itself
         if (t >= 1e-6f) {
           int2 v;
           v.x = pr.col[e];

@@ -128,16 +128,12 @@ __device__ __forceinline__ float hm_term(float4 a, float4 b, float h) {
 // Change of one pair term when bead b moves from pb to nb: the hardware
 // reciprocal square root and one reciprocal of h shared by both terms.
 __device__ __forceinline__ float hm_delta(float4 pi, float4 pb, float4 nb, float h) {
-  const float rh = __fdividef(1.0f, h);
-  float x = pi.x - pb.x, y = pi.y - pb.y, z = pi.z - pb.z;
-  float s = fmaf(x, x, fmaf(y, y, z * z));
-  const float co = (s * rsqrtf(fmaxf(s, 1e-30f)) - h) * rh;
-  x = pi.x - nb.x;
-  y = pi.y - nb.y;
-  z = pi.z - nb.z;
-  s = fmaf(x, x, fmaf(y, y, z * z));
-  const float cn = (s * rsqrtf(fmaxf(s, 1e-30f)) - h) * rh;
-  return fmaf(cn, cn, -co * co);
+  const float rh = __frcp_rn(h);
+  const float co =
+      (ref_len(__fsub_rn(pi.x, pb.x), __fsub_rn(pi.y, pb.y), __fsub_rn(pi.z, pb.z)) - h) * rh;
+  const float cn =
+      (ref_len(__fsub_rn(pi.x, nb.x), __fsub_rn(pi.y, nb.y), __fsub_rn(pi.z, nb.z)) - h) * rh;
+  return cn * cn - co * co;
 }
 
 // FP64 full score, the whole block; every thread returns the total.

@@ -62,9 +62,8 @@ struct SmoothDevParams {
 // ((|a - b| - d0) / d0)^2 * (stretch | squeeze).
 __device__ __forceinline__ float bond_e(float4 a, float4 b, float2 d, float ks,
                                         float kq) {
-  const float x = a.x - b.x, y = a.y - b.y, z = a.z - b.z;
-  const float s = fmaf(x, x, fmaf(y, y, z * z));
-  const float f = (s * rsqrtf(fmaxf(s, 1e-30f)) - d.x) * d.y;
+  const float len = ref_len(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z));
+  const float f = (len - d.x) * d.y;
   return f * f * (f >= 0.0f ? ks : kq);
 }
 
