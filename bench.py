@@ -1,0 +1,401 @@
+"""Benchmark: batched arc-level annealing of an ensemble (64 structures x 24
+anchor blocks, block sizes log-uniform 32..2048 beads, 1.5 arcs per bead),
+the configuration the batched-vs-plain metric is quoted on.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+A step anneals every block of the ensemble once (T0 5, cooling 0.9999,
+milestones every 50k moves with improvement threshold 0.99 -- the reference
+CPU schedule of MonteCarloArcs -- and an FP64 energy resync every 1000 moves)
+in one CUDA-graph launch of the persistent work-stealing kernels.  Inputs are
+seeded synthetic regions (no datasets ship with the reference).  Rank r of N
+anneals its own ensemble (seeds 64r..64r+63): weak scaling, no collective.
+
+One JSON line on rank 0: value = MC moves/s over all ranks (device time,
+CUDA events on the launching stream); structures/s beside it; e2e = the same
+metric through the host-buffer C-ABI call (staging, copies and result reads
+inside the timed region); roofline of the annealing kernel against the
+measured HBM peak; cpu_baseline = the reference's CPU annealer (the oracle's
+bit-identical restatement) on a bounded sample on all host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_STRUCT, N_BLOCKS = 64, 24
+ANNEAL = dict(max_temp=5.0, dt_temp=0.9999, milestone_steps=50000, improvement=0.99)
+RESYNC = 1000
+STEP = 0.5
+WORKLOAD = (f"arcs_ensemble_{N_STRUCT}x{N_BLOCKS}_blocks32-2048_1.5arcs_per_bead_"
+            f"T0=5_cool0.9999_milestone50k_thr0.99")
+
+
+def log(*a):
+    print(*a, file=sys.stderr, flush=True)
+
+
+# --------------------------------------------------------------------------
+# CPU leg (the oracle restates MonteCarloArcs bit for bit; see oracle/)
+# --------------------------------------------------------------------------
+def _cpu_block(args):
+    n, seed = args
+    from oracle import oracle as O
+    from pmmc_gb300 import synth
+    r = synth.arcs_region(n, arcs_per_bead=1.5, seed=seed)
+    pr = O.ArcsProblem(r.pos, r.dense())
+    t = time.perf_counter()
+    _, res = O.arcs_anneal(pr, O.Params(**ANNEAL), STEP, seed)
+    return res.moves, time.perf_counter() - t, n
+
+
+def cpu_sample(budget_s: float = 20.0):
+    """Anneal a bounded sample of the ensemble's blocks on every host core.
+    Block sizes follow the workload's distribution; the sample grows until it
+    holds about budget_s of CPU work."""
+    from oracle import oracle as O
+    O.build()
+    cores = os.cpu_count() or 1
+    rng = np.random.default_rng(123)
+    sizes = [int(round(math.exp(rng.uniform(math.log(32), math.log(2048)))))
+             for _ in range(4 * cores)]
+    jobs = [(n, 9000 + k) for k, n in enumerate(sizes)]
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    moves = cpu_s = 0.0
+    done = 0
+    with ctx.Pool(cores) as pool:
+        for mv, dt, n in pool.imap_unordered(_cpu_block, jobs):
+            moves += mv
+            cpu_s += dt
+            done += 1
+            if cpu_s > budget_s * cores or time.perf_counter() - t0 > budget_s:
+                pool.terminate()
+                break
+    wall = time.perf_counter() - t0
+    return {"moves": moves, "cpu_s": cpu_s, "wall_s": wall, "blocks": done,
+            "cores": cores, "moves_per_s": moves / wall}
+
+
+# --------------------------------------------------------------------------
+# GPU helpers
+# --------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except FileNotFoundError:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if f[5 + k].lower() == "active":
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_per_launch():
+    """DRAM bytes of one annealing launch from the committed ncu summary
+    (profiles/traffic_per_launch.txt: '<kernel> <workload> <bytes>')."""
+    p = os.path.join(ROOT, "profiles", "traffic_per_launch.txt")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        f = line.split()
+        if len(f) >= 3 and f[0] == "arcs_anneal_kernel" and f[1] == "config2":
+            return float(f[2])
+    return None
+
+
+def make_inputs(rank: int):
+    from pmmc_gb300 import capi, synth
+    ens = synth.arcs_ensemble(N_STRUCT, N_BLOCKS, seeds=range(N_STRUCT * rank,
+                                                               N_STRUCT * (rank + 1)))
+    regs = [r for s in ens for r in s]
+    inputs = [capi.ArcsInput(r.pos, *r.csr()) for r in regs]
+    return regs, inputs
+
+
+def staged_bytes(inputs):
+    """Host->device bytes of one staging of the batch (positions as float4,
+    row pointers, arc entries {col,target} + reciprocal) and device->host
+    bytes of the results (xyz positions + one result record per block)."""
+    h2d = d2h = 0
+    for x in inputs:
+        nnz = int(x.row_ptr[-1])
+        h2d += 16 * x.n + 4 * (x.n + 1) + 12 * nnz + 80
+        d2h += 12 * x.n + 56
+    return h2d, d2h
+
+
+def flush_l2(buf):
+    buf.fill_(1)
+
+
+def run_gpu(args, rank, world):
+    import torch
+
+    from pmmc_gb300 import build, capi
+    build.build()
+    torch.cuda.set_device(0 if world == 1 else int(os.environ.get("LOCAL_RANK", rank)))
+    dev = torch.cuda.current_device()
+    ctx = capi.Context(dev)
+    ctx.set_seed(2024 + rank)
+    regs, inputs = make_inputs(rank)
+    prm = capi.default_params(capi.LEVEL_ARCS, schedule=capi.SCHEDULE_CPU,
+                              resync_every=RESYNC, **ANNEAL)
+    steps = [STEP] * len(inputs)
+    batch = capi.ArcsBatch(ctx, inputs, prm, steps, chains=1, use_graph=True)
+    stream = torch.cuda.Stream()
+    l2 = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")  # > 129 MB L2
+    # warm-up (graph capture happens on the first run)
+    for _ in range(args.warmup):
+        batch.run(stream.cuda_stream)
+        batch.results()
+    _, moves_per_step, n_launch = batch.stats()
+    # ---- timed region ----
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize()
+    clocks = ClockSampler(dev)
+    clocks.start()
+    kernel_ms = []
+    t_wall = time.perf_counter()
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush_l2(l2)
+        batch.run(stream.cuda_stream)
+        ms, mv, _ = batch.stats()
+        assert mv == moves_per_step
+        kernel_ms.append(ms)
+    torch.cuda.synchronize()
+    t_wall = time.perf_counter() - t_wall
+    clk = clocks.stop()
+    if world > 1:
+        torch.distributed.barrier()
+    pos, res = batch.results()
+    step_ms = sum(kernel_ms) / len(kernel_ms)
+    rel_err = max(r.rel_error for r in res)
+    status_bad = sum(1 for r in res if r.status not in (0,))
+    # ---- e2e through the host-buffer call ----
+    e2e_ms = []
+    for k in range(args.e2e_steps):
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        p2, r2 = _batch_anneal_host(ctx, inputs, prm, steps)
+        e2e_ms.append((time.perf_counter() - t) * 1e3)
+    e2e_moves = sum(r.moves for r in r2)
+    h2d, d2h = staged_bytes(inputs)
+    # ---- plain drop-in form: one structure, blocks annealed one call each ----
+    plain_s = None
+    if rank == 0 and args.plain:
+        t = time.perf_counter()
+        for x in inputs[:N_BLOCKS]:
+            capi.arcs_anneal(ctx, x, prm, STEP, 1)
+        plain_s = time.perf_counter() - t
+    batch.close()
+    from pmmc_gb300.capi import lib  # noqa: F401
+    return dict(step_ms=step_ms, moves=moves_per_step, kernel_ms=kernel_ms, wall=t_wall,
+                clocks=clk, rel_err=rel_err, bad=status_bad, e2e_ms=e2e_ms,
+                e2e_moves=e2e_moves, h2d=h2d, d2h=d2h, plain_s=plain_s, n_launch=n_launch,
+                n_units=len(inputs))
+
+
+def _batch_anneal_host(ctx, inputs, prm, steps):
+    import ctypes as C
+
+    from pmmc_gb300 import capi
+    arr = (capi.ArcsProblem * len(inputs))(*[x.struct() for x in inputs])
+    st = np.ascontiguousarray(steps, dtype=np.float32)
+    tot = sum(x.n for x in inputs)
+    pos = np.zeros((tot, 3), np.float32)
+    res = (capi.Result * len(inputs))()
+    opts = capi.BatchOpts(1, 0, 32)
+    ctx.check(capi.lib().pmmc_arcs_batch_anneal(ctx.h, len(inputs), arr, C.byref(prm),
+                                                st.ctypes.data_as(C.c_void_p), C.byref(opts),
+                                                pos.ctypes.data_as(C.c_void_p), res))
+    return pos, list(res)
+
+
+def algorithmic_bytes(inputs, moves):
+    """HBM bytes one launch must move: each region's positions (float4),
+    row pointers and arc entries (12 B) read once, positions (12 B/bead) and
+    one result record written once."""
+    b = 0
+    for x in inputs:
+        nnz = int(x.row_ptr[-1])
+        b += 16 * x.n + 4 * (x.n + 1) + 12 * nnz + 12 * x.n + 56
+    return b
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--no-plain", dest="plain", action="store_false")
+    ap.add_argument("--cpu-budget", type=float, default=20.0)
+    args = ap.parse_args()
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+
+    if args.impl == "reference":
+        # the reference's own CPU annealer (bit-identical oracle restatement;
+        # the reference sources do not travel to the GPU host) on all cores
+        if rank != 0:
+            return
+        vals = []
+        per = max(5.0, min(args.cpu_budget, 150.0 / max(1, args.steps + args.warmup)))
+        for k in range(args.warmup + args.steps):
+            s = cpu_sample(per)
+            if k >= args.warmup:
+                vals.append(s)
+        v = sum(s["moves"] for s in vals) / sum(s["wall_s"] for s in vals)
+        line = {
+            "impl": "reference", "metric": "MC moves/s", "value": v, "unit": "moves/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "sample": "blocks with the ensemble's size "
+                       "distribution, about %.0f s per step" % per},
+            "cpu_baseline": {"value": v, "unit": "moves/s", "cores": vals[0]["cores"],
+                             "kind": "port",
+                             "sample": f"{sum(s['blocks'] for s in vals)} blocks in "
+                                       f"{len(vals)} steps"},
+            "e2e": {"value": v, "unit": "moves/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0},
+        }
+        print(json.dumps(line))
+        return
+
+    # CPU baseline first (spawn pool, before any CUDA call in this process)
+    cpu = cpu_sample(args.cpu_budget) if rank == 0 else None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", rank)))
+        dist.init_process_group("nccl")
+    r = run_gpu(args, rank, world)
+    # max over ranks
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        t = torch.tensor([r["step_ms"], float(r["moves"])], dtype=torch.float64, device="cuda")
+        gathered = [torch.zeros_like(t) for _ in range(world)]
+        dist.all_gather(gathered, t)
+        step_ms = max(float(g[0]) for g in gathered)
+        total_moves = sum(float(g[1]) for g in gathered)
+        dist.destroy_process_group()
+    else:
+        step_ms = r["step_ms"]
+        total_moves = float(r["moves"])
+    if rank != 0:
+        return
+    value = total_moves / (step_ms * 1e-3)
+    structs = world * N_STRUCT / (step_ms * 1e-3)
+    e2e_ms = min(r["e2e_ms"]) if r["e2e_ms"] else None
+    e2e_val = world * r["e2e_moves"] / (e2e_ms * 1e-3) if e2e_ms else None
+    peak, peak_kind = measured_peaks()
+    _, inputs = make_inputs(0)
+    alg = algorithmic_bytes(inputs, r["moves"])
+    achieved = alg / (r["step_ms"] * 1e-3) / 1e9
+    traffic = traffic_per_launch()
+    line = {
+        "metric": "MC moves/s", "value": value, "unit": "moves/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": WORKLOAD, "structures": N_STRUCT * world,
+                   "blocks_per_structure": N_BLOCKS, "regions": r["n_units"] * world,
+                   "moves_per_step": total_moves, "fp64_resync_every": RESYNC,
+                   "l2": "256 MB buffer written between timed steps",
+                   "parallelism": f"replicas x{world}"},
+        "structures_per_s": structs,
+        "final_energy_rel_error_max": r["rel_err"],
+        "chains_not_ok": r["bad"],
+        "e2e": {"value": e2e_val, "unit": "moves/s", "h2d_bytes_per_step": r["h2d"],
+                "d2h_bytes_per_step": r["d2h"], "ms_per_step": e2e_ms},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic,
+                     "peak_source": peak_kind,
+                     "note": "serial Metropolis chains: one warp per chain, latency-bound; "
+                             "HBM carries only the one-time staging"},
+        "clocks": r["clocks"],
+        "gpu_launches": r["n_launch"] * args.steps,
+    }
+    if r["plain_s"] is not None:
+        line["plain_structures_per_s"] = 1.0 / r["plain_s"]
+        line["batched_over_plain"] = structs / world / (1.0 / r["plain_s"])
+    if cpu:
+        line["cpu_baseline"] = {"value": cpu["moves_per_s"], "unit": "moves/s",
+                                "cores": cpu["cores"], "kind": "port",
+                                "sample": f"{cpu['blocks']} blocks of the ensemble's size "
+                                          f"distribution, {cpu['wall_s']:.1f} s wall"}
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

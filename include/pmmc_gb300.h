@@ -238,10 +238,13 @@ pmmc_status pmmc_arcs_batch_run(pmmc_arcs_batch *b, void *stream);
  * sum(n_u)*3 floats in unit order; res holds n_units results. */
 pmmc_status pmmc_arcs_batch_results(pmmc_arcs_batch *b, float *pos_out,
                                     pmmc_result *res);
-/* Per-launch figures of the last run: device time of the annealing kernels
- * (ms, CUDA events on the batch stream), total moves, lanes per chain. */
+/* Figures of the last run: device time of the pass (ms, CUDA events on the
+ * launching stream around the graph), total moves over all chains, and the
+ * number of kernels one pass launches (one persistent annealing kernel per
+ * shared-memory size class, plus the best-chain pick when units have several
+ * chains). */
 pmmc_status pmmc_arcs_batch_stats(pmmc_arcs_batch *b, double *kernel_ms,
-                                  int64_t *total_moves, int *lanes_per_chain);
+                                  int64_t *total_moves, int *launches_per_run);
 void pmmc_arcs_batch_destroy(pmmc_arcs_batch *b);
 
 /* Host-buffer form of the above: stage, run, fetch, free. */

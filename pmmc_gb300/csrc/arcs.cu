@@ -958,7 +958,7 @@ extern "C" pmmc_status pmmc_arcs_batch_results(pmmc_arcs_batch *b, float *pos_ou
 
 extern "C" pmmc_status pmmc_arcs_batch_stats(pmmc_arcs_batch *b, double *kernel_ms,
                                              int64_t *total_moves,
-                                             int *lanes_per_chain) {
+                                             int *launches_per_run) {
   if (!b || !b->ran) return PMMC_ERR_INVALID;
   pmmc_ctx *ctx = b->ctx;
   PMMC_CUDA(ctx, cudaEventSynchronize(b->ev_stop));
@@ -975,7 +975,11 @@ extern "C" pmmc_status pmmc_arcs_batch_stats(pmmc_arcs_batch *b, double *kernel_
     for (auto &o : outs) t += o.moves;
     *total_moves = t;
   }
-  if (lanes_per_chain) *lanes_per_chain = b->lanes;
+  if (launches_per_run) {
+    int multi = 0;
+    for (auto &U : b->h_units) multi |= U.chains > 1;
+    *launches_per_run = (int)b->classes.size() + multi;
+  }
   return PMMC_OK;
 }
 

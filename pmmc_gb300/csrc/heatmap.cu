@@ -136,10 +136,14 @@ __device__ __forceinline__ float hm_delta(float4 pi, float4 pb, float4 nb, float
   return cn * cn - co * co;
 }
 
-// FP64 full score, the whole block; every thread returns the total.
+// FP64 full score plus the sphere penalties of all beads (the reference adds
+// the boundary sum to the initial score, LooperSolver.hpp:1451-1457); the
+// whole block, every thread returns the total.
 __device__ double heat_full(const HeatUnit &U, const float4 *spos, const float *heat,
-                            const int2 *blk, double *red) {
+                            const int2 *blk, double *red, float R) {
   double acc = 0.0;
+  for (int i = threadIdx.x; i < U.n; i += blockDim.x)
+    acc += sphere_penalty(spos[i].x, spos[i].y, spos[i].z, R);
   for (int m = 0; m < U.n; ++m) {
     const int2 r = blk[m];
     const float *row = heat + U.heat_off + (long long)m * U.pitch;
@@ -205,7 +209,7 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
   for (int i = tid; i < n; i += blockDim.x) spos[i] = pos0[U.pos_off + i];
   __syncthreads();
 
-  const double E0 = heat_full(U, spos, heat, blk_all + U.blk_off, red);
+  const double E0 = heat_full(U, spos, heat, blk_all + U.blk_off, red, P.R);
   double T = P.max_temp;  // temperature of the next batch's first move (warp 0)
 
   // draws of one batch of 32 moves (warp 0)
@@ -358,7 +362,7 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
       if (!mbar_wait(&bars[k % D], (uint32_t)((k / D) & 1))) status = PMMC_ERR_TIMEOUT;
   }
   __syncthreads();
-  const double Efin = heat_full(U, spos, heat, blk_all + U.blk_off, red);
+  const double Efin = heat_full(U, spos, heat, blk_all + U.blk_off, red, P.R);
   if (tid == 0) {
     ChainOut o;
     const double E = run ? (double)e_hi + (double)e_lo : 0.0;

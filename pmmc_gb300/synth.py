@@ -48,6 +48,20 @@ class ArcsRegion:
     def n(self) -> int:
         return int(self.pos.shape[0])
 
+    def csr(self):
+        """Per-bead arc lists over both directions, columns sorted: the layout
+        pmmc_arcs_dense_to_csr produces from dense(), built directly."""
+        n = self.n
+        i = np.concatenate([self.arcs[:, 0], self.arcs[:, 1]])
+        j = np.concatenate([self.arcs[:, 1], self.arcs[:, 0]])
+        t = np.concatenate([self.target, self.target])
+        order = np.lexsort((j, i))
+        i, j, t = i[order], j[order], t[order]
+        row_ptr = np.zeros(n + 1, np.int32)
+        np.add.at(row_ptr, i + 1, 1)
+        row_ptr = np.cumsum(row_ptr).astype(np.int32)
+        return row_ptr, j.astype(np.int32), t.astype(np.float32)
+
     def dense(self) -> np.ndarray:
         """The reference layout: -1 everywhere, 0 on the diagonal, targets on
         arc pairs (both triangles)."""
@@ -61,33 +75,39 @@ class ArcsRegion:
 
 def arcs_region(n: int = 256, n_arcs: int = 400, seed: int = 42,
                 mean_count: float = 8.0, arcs_per_bead: float | None = None) -> ArcsRegion:
+    """Arcs i<j with |i-j| = round(exp U[ln 3, ln(n-1)]), i uniform, PET
+    counts geometric with the given mean; distinct pairs in draw order."""
     rng = np.random.default_rng(seed)
     pos = random_walk(n, rng)
     if arcs_per_bead is not None:
         n_arcs = int(round(arcs_per_bead * n))
     max_sep = n - 1
-    n_arcs = min(n_arcs, n * (n - 1) // 2 - (n - 1) * 2)
-    seen = {}
-    p_geo = 1.0 / mean_count
-    tries = 0
-    while len(seen) < n_arcs and tries < 50 * n_arcs + 1000:
-        tries += 1
-        if max_sep < 3:
-            sep = max(1, max_sep)
-        else:
-            sep = int(round(np.exp(rng.uniform(np.log(3), np.log(max_sep)))))
-            sep = min(max(sep, 3), max_sep)
-        i = int(rng.integers(0, n - sep))
-        j = i + sep
-        if (i, j) in seen:
-            continue
-        cnt = int(rng.geometric(p_geo))
-        seen[(i, j)] = cnt
-    keys = sorted(seen)
-    arcs = np.array(keys, np.int32).reshape(-1, 2)
-    count = np.array([seen[k] for k in keys], np.int32)
-    sep = (arcs[:, 1] - arcs[:, 0]).astype(np.float64)
-    target = (count.astype(np.float64) ** -0.5 * sep ** 0.25).astype(np.float32)
+    n_arcs = max(0, min(n_arcs, n * (n - 1) // 2 - (n - 1) * 2))
+    keys = np.zeros(0, np.int64)
+    counts = np.zeros(0, np.int64)
+    lo = np.log(3.0)
+    hi = np.log(max(max_sep, 3))
+    for _ in range(64):
+        need = n_arcs - len(keys)
+        if need <= 0:
+            break
+        m = 2 * need + 16
+        sep = np.rint(np.exp(rng.uniform(lo, hi, m))).astype(np.int64)
+        sep = np.clip(sep, min(3, max_sep), max_sep)
+        i = (rng.random(m) * (n - sep)).astype(np.int64)
+        cnt = rng.geometric(1.0 / mean_count, m)
+        keys = np.concatenate([keys, i * n + i + sep])
+        counts = np.concatenate([counts, cnt])
+        _, first = np.unique(keys, return_index=True)
+        first = np.sort(first)
+        keys, counts = keys[first], counts[first]
+    keys, counts = keys[:n_arcs], counts[:n_arcs]
+    order = np.argsort(keys)
+    keys, counts = keys[order], counts[order]
+    arcs = np.stack([keys // n, keys % n], 1).astype(np.int32).reshape(-1, 2)
+    count = counts.astype(np.int32)
+    sepf = (arcs[:, 1] - arcs[:, 0]).astype(np.float64)
+    target = (count.astype(np.float64) ** -0.5 * sepf ** 0.25).astype(np.float32)
     return ArcsRegion(pos, arcs, target, count)
 
 
