@@ -44,6 +44,14 @@ WORKLOAD = (f"arcs_ensemble_{N_STRUCT}x{N_BLOCKS}_blocks32-2048_1.5arcs_per_bead
             f"T0=5_cool0.9999_milestone50k_thr0.99")
 
 
+def set_workload(structures: int, milestone: int) -> None:
+    global N_STRUCT, WORKLOAD
+    N_STRUCT = structures
+    ANNEAL["milestone_steps"] = milestone
+    WORKLOAD = (f"arcs_ensemble_{N_STRUCT}x{N_BLOCKS}_blocks32-2048_1.5arcs_per_bead_"
+                f"T0=5_cool0.9999_milestone{milestone // 1000}k_thr0.99")
+
+
 def log(*a):
     print(*a, file=sys.stderr, flush=True)
 
@@ -240,6 +248,7 @@ def run_gpu(args, rank, world):
     status_bad = sum(1 for r in res if r.status not in (0,))
     # ---- e2e through the host-buffer call ----
     e2e_ms = []
+    r2 = []
     for k in range(args.e2e_steps):
         torch.cuda.synchronize()
         t = time.perf_counter()
@@ -298,7 +307,12 @@ def main():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--no-plain", dest="plain", action="store_false")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--structures", type=int, default=N_STRUCT,
+                    help="ensemble size (smaller for profiling runs)")
+    ap.add_argument("--milestone", type=int, default=ANNEAL["milestone_steps"],
+                    help="milestone interval (smaller for profiling runs)")
     args = ap.parse_args()
+    set_workload(args.structures, args.milestone)
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
 
@@ -332,7 +346,7 @@ def main():
         return
 
     # CPU baseline first (spawn pool, before any CUDA call in this process)
-    cpu = cpu_sample(args.cpu_budget) if rank == 0 else None
+    cpu = cpu_sample(args.cpu_budget) if rank == 0 and args.cpu_budget > 0 else None
     if world > 1:
         import torch
         import torch.distributed as dist

@@ -223,7 +223,9 @@ typedef struct pmmc_arcs_batch pmmc_arcs_batch;
 typedef struct pmmc_batch_opts {
   int chains_per_unit;   /* independent chains per unit (>= 1)           */
   int use_graph;         /* capture the launches in a CUDA graph          */
-  int lanes_per_chain;   /* 0 = autotune; else 8, 16 or 32                */
+  int lanes_per_chain;   /* lanes that score one proposal: 2, 4, 8 or 32;
+                          * a chain's warp scores 32/lanes proposals at
+                          * once (0 = the default, 4)                      */
 } pmmc_batch_opts;
 pmmc_status pmmc_arcs_batch_create(pmmc_ctx *ctx, int n_units,
                                    const pmmc_arcs_problem *units,

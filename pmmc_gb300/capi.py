@@ -245,13 +245,13 @@ class ArcsBatch:
     """Device-resident batch of arc regions (pmmc_arcs_batch_*)."""
 
     def __init__(self, ctx: Context, inputs, params: AnnealParams, steps, chains=1,
-                 use_graph=True, stop_all=False, trace_cap=0):
+                 use_graph=True, stop_all=False, trace_cap=0, lanes=0):
         self.ctx = ctx
         self.inputs = list(inputs)
         arr = (ArcsProblem * len(self.inputs))(*[x.struct() for x in self.inputs])
         self._arr = arr
         self.steps = _f32(steps)
-        opts = BatchOpts(int(chains), int(bool(use_graph)), 32)
+        opts = BatchOpts(int(chains), int(bool(use_graph)), int(lanes))
         h = C.c_void_p()
         ctx.check(lib().pmmc_arcs_batch_create_ex(
             ctx.h, len(self.inputs), arr, C.byref(params), _p(self.steps), C.byref(opts),

@@ -82,7 +82,9 @@ struct ArcsDevParams {
   float dtpow[33];  // dt^l, l = 0..32
 };
 
-constexpr int kMoveBufBytes = 32 * 16 + 32 * 4;  // int4 moves + float thresholds
+// per-warp scratch: 32 drawn moves (int4) + their ratio thresholds, and the
+// window's per-slot delta, conflict mask and (tracing) local scores
+constexpr int kMoveBufBytes = 32 * 16 + 32 * 4 + 4 * 32 * 4;
 constexpr int kCtaHeader = 256;                    // dt^l table shared by the CTA
 
 __device__ __forceinline__ float dist3(float ax, float ay, float az, float4 b) {
@@ -175,7 +177,7 @@ __device__ double arcs_repulsion(int n, const float4 *spos, const int *srp,
   return warp_sum_d(acc);
 }
 
-template <bool NB_SMEM>
+template <bool NB_SMEM, int G>
 __global__ void __launch_bounds__(128)
 arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
                    const int2 *__restrict__ items, int n_items,
@@ -196,6 +198,10 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
   unsigned char *wbase = smem + kCtaHeader + (size_t)(threadIdx.x >> 5) * smem_per_warp;
   int4 *s_mv = reinterpret_cast<int4 *>(wbase);
   float *s_thr = reinterpret_cast<float *>(wbase + 32 * 16);
+  float *s_d = reinterpret_cast<float *>(wbase + 32 * 20);
+  unsigned *s_c = reinterpret_cast<unsigned *>(wbase + 32 * 24);
+  float *s_so = reinterpret_cast<float *>(wbase + 32 * 28);
+  float *s_sn = reinterpret_cast<float *>(wbase + 32 * 32);
   float4 *spos = reinterpret_cast<float4 *>(wbase + kMoveBufBytes);
 
   for (;;) {
@@ -243,8 +249,8 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
     // ---- initial FP64 energy: repulsion (frozen) + springs/loops/sphere ----
     const double base = arcs_repulsion(n, spos, srp, NB, nulls + U.null_off, U.n_null, lane);
     double E = base + arcs_spring_energy(n, spos, srp, NB, LST, U.n_loops, P, lane);
-    // running energy of the chain (lane 0): float-float pair on the move
-    // path, widened to FP64 at milestones, resyncs and the end
+    // running energy of the chain (identical on every lane): float-float
+    // pair on the move path, widened to FP64 at milestones, resyncs, the end
     float e_hi = (float)E, e_lo = (float)(E - (double)(float)E);
     double E_ms = E;
     double T = P.max_temp;
@@ -257,168 +263,190 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
     const bool tracing = trace != nullptr && chain_id == 0;
     int batch_no = 0;
 
+    // ---- windows of W = 32/G proposals, G lanes each ----
+    // Every proposal of a window is scored against the positions at the
+    // window's start; the proposals are then resolved in order.  A proposal
+    // whose bead, or one of whose arc / loop partners, was moved by an earlier
+    // accepted proposal of the same window closes the window there: it is
+    // re-scored from the updated positions as the first proposal of the next
+    // window.  The accepted sequence is therefore the one the one-move-at-a-
+    // time algorithm produces.
+    constexpr int W = 32 / G;
+    const int g = lane / G;    // proposal slot of this lane
+    const int sub = lane % G;  // lane within the slot
+    long long bm = 0;          // first move held by the draw buffer
+    auto refill = [&](long long first) {
+      const uint64_t m = (uint64_t)first + lane;
+      const uint4 r = philox_move(P.seed, chain_id, m, 0u);
+      const uint4 a = philox_move(P.seed, chain_id, m, 1u);
+      const int k = uniform_index(r.x, U.n_mov);
+      const int b = MOV ? MOV[k] : k;
+      const float dx = (2.0f * u01(r.y) - 1.0f) * step;
+      const float dy = (2.0f * u01(r.z) - 1.0f) * step;
+      const float dz = P.use2d ? 0.0f : (2.0f * u01(r.w) - 1.0f) * step;
+      const float Tl = (float)T * s_dtpow[lane];
+      s_mv[lane] = make_int4(b, __float_as_int(dx), __float_as_int(dy), __float_as_int(dz));
+      s_thr[lane] = ratio_threshold(u01(a.x), Tl, P.inv_scale, P.inv_coef);
+    };
+    if (!stop) refill(0);
+    __syncwarp();
+
     while (!stop) {
-      // ---- Philox draws of the next 32 moves: lane l draws move m+l ----
-      {
-        const uint64_t m = (uint64_t)moves + lane;
-        const uint4 r = philox_move(P.seed, chain_id, m, 0u);
-        const uint4 a = philox_move(P.seed, chain_id, m, 1u);
-        const int k = uniform_index(r.x, U.n_mov);
-        const int b = MOV ? MOV[k] : k;
-        const float dx = (2.0f * u01(r.y) - 1.0f) * step;
-        const float dy = (2.0f * u01(r.z) - 1.0f) * step;
-        const float dz = P.use2d ? 0.0f : (2.0f * u01(r.w) - 1.0f) * step;
-        const float Tl = (float)T * s_dtpow[lane];
-        s_mv[lane] = make_int4(b, __float_as_int(dx), __float_as_int(dy),
-                               __float_as_int(dz));
-        s_thr[lane] = ratio_threshold(u01(a.x), Tl, P.inv_scale, P.inv_coef);
+      long long lim = (moves / P.window + 1) * (long long)P.window;
+      if (P.resync > 0) lim = min(lim, (moves / P.resync + 1) * (long long)P.resync);
+      lim = min(lim, P.cap);
+      if (moves + W > bm + 32 && bm + 32 < lim) {  // draw the next 32 moves
+        T *= (double)s_dtpow[moves - bm];
+        bm = moves;
+        __syncwarp();
+        refill(bm);
+        __syncwarp();
       }
-      int kmax = 32;
-      kmax = min(kmax, P.window - (int)(moves % P.window));
-      if (P.resync > 0) kmax = min(kmax, P.resync - (int)(moves % P.resync));
-      if (P.cap - moves < (long long)kmax) kmax = (int)(P.cap - moves);
-      __syncwarp();
-
-      // static data of the batch's first move; each iteration prefetches
-      // the next move's (none of it depends on positions)
-      int4 mv = s_mv[0];
-      float thr = s_thr[0];
-      int beg = srp[mv.x];
-      int deg = srp[mv.x + 1] - beg;
-      int2 ent = lane < deg ? NB[beg + lane] : make_int2(mv.x, 0);
-      float itv = lane < deg ? INV[beg + lane] : 0.0f;
-
-      for (int k = 0; k < kmax; ++k) {
-        const int b = mv.x;
-        const float4 pb = spos[b];
-        const float4 pj = spos[ent.x];
-        int4 mv1 = mv;
-        float thr1 = 0.0f;
-        int beg1 = 0, deg1 = 0;
-        int2 ent1 = ent;
-        float it1 = 0.0f;
-        if (k + 1 < kmax) {
-          mv1 = s_mv[k + 1];
-          thr1 = s_thr[k + 1];
-          beg1 = srp[mv1.x];
-          deg1 = srp[mv1.x + 1] - beg1;
-          ent1 = lane < deg1 ? NB[beg1 + lane] : make_int2(mv1.x, 0);
-          it1 = lane < deg1 ? INV[beg1 + lane] : 0.0f;
-        }
-        const float dx = __int_as_float(mv.y), dy = __int_as_float(mv.z),
-                    dz = __int_as_float(mv.w);
-        const float nx = pb.x + dx, ny = pb.y + dy, nz = pb.z + dz;
-        float so = 0.0f, sn = 0.0f;
-        if (lane < deg) {
-          const float t = __int_as_float(ent.y);
-          so = spring_fast(fast_len(pb.x, pb.y, pb.z, pj), t, itv, ks, kq);
-          sn = spring_fast(fast_len(nx, ny, nz, pj), t, itv, ks, kq);
-        }
-        int width = deg;
-        if (deg > 32) {  // rare hub beads: the rest of the list
-          for (int e = beg + 32 + lane; e < beg + deg; e += 32) {
-            const int2 en = NB[e];
-            const float t = __int_as_float(en.y), iv = INV[e];
-            const float4 q = spos[en.x];
-            so += spring_fast(fast_len(pb.x, pb.y, pb.z, q), t, iv, ks, kq);
-            sn += spring_fast(fast_len(nx, ny, nz, q), t, iv, ks, kq);
-          }
+      const int L = (int)min((long long)W, min(lim, bm + 32) - moves);
+      const int k0 = (int)(moves - bm);
+      const bool active = g < L;
+      const int4 mv = active ? s_mv[k0 + g] : make_int4(0, 0, 0, 0);
+      const int b = mv.x;
+      int bj[W];
+#pragma unroll
+      for (int j = 0; j < W; ++j) bj[j] = __shfl_sync(0xffffffffu, b, j * G);
+      float so = 0.0f, sn = 0.0f;
+      unsigned cm = 0u;
+      float4 pb = make_float4(0.f, 0.f, 0.f, 0.f);
+      float nx = 0.f, ny = 0.f, nz = 0.f;
+      if (active) {
+        pb = spos[b];
+        nx = pb.x + __int_as_float(mv.y);
+        ny = pb.y + __int_as_float(mv.z);
+        nz = pb.z + __int_as_float(mv.w);
+        const int beg = srp[b], end = srp[b + 1];
+        for (int e = beg + sub; e < end; e += G) {
+          const int2 ent = NB[e];
+          const float t = __int_as_float(ent.y), iv = INV[e];
+          const float4 q = spos[ent.x];
+          so += spring_fast(fast_len(pb.x, pb.y, pb.z, q), t, iv, ks, kq);
+          sn += spring_fast(fast_len(nx, ny, nz, q), t, iv, ks, kq);
+#pragma unroll
+          for (int j = 0; j < W; ++j)
+            if (j < g && ent.x == bj[j]) cm |= 1u << j;
         }
         if (has_loops) {
-          const int l0 = LRP[b], l1 = LRP[b + 1];
-          for (int e = l0 + lane; e < l1; e += 32) {
+          const int l1 = LRP[b + 1];
+          for (int e = LRP[b] + sub; e < l1; e += G) {
             const float4 le = LENT[e];
-            const int j = __float_as_int(le.x);
-            const float4 q = spos[j];
+            const int pj = __float_as_int(le.x);
+            const float4 q = spos[pj];
             // a constraint of a bead with itself stays at distance 0
-            const float d0 = (j == b ? 0.0f : fast_len(pb.x, pb.y, pb.z, q)) - le.z;
-            const float d1 = (j == b ? 0.0f : fast_len(nx, ny, nz, q)) - le.z;
+            const float d0 = (pj == b ? 0.0f : fast_len(pb.x, pb.y, pb.z, q)) - le.z;
+            const float d1 = (pj == b ? 0.0f : fast_len(nx, ny, nz, q)) - le.z;
             so += le.y * d0 * d0;
             sn += le.y * d1 * d1;
-          }
-          width = max(width, l1 - l0);
-        }
-        if (lane == 0 && R > 0.0f) {
-          so += sphere_penalty(pb.x, pb.y, pb.z, R);
-          sn += sphere_penalty(nx, ny, nz, R);
-        }
-        float d = sn - so;
-        const int w = width >= 32 ? 32 : (width <= 1 ? 1 : (1 << (32 - __clz(width - 1))));
-        if (tracing) {
-          for (int o = w >> 1; o > 0; o >>= 1) {
-            so += __shfl_xor_sync(0xffffffffu, so, o);
-            sn += __shfl_xor_sync(0xffffffffu, sn, o);
-          }
-          d = sn - so;
-        } else {
-          for (int o = w >> 1; o > 0; o >>= 1) d += __shfl_xor_sync(0xffffffffu, d, o);
-        }
-        if (lane == 0) {
-          const bool acc = (d <= 0.0f) || (d < e_hi * (thr - 1.0f));
-          if (acc) {
-            spos[b] = make_float4(nx, ny, nz, 0.0f);
-            ff_add(e_hi, e_lo, d);
-            ++accepted;
-            ++succ_ms;
-          }
-          if (tracing && moves + k < P.trace_cap) {
-            MoveTrace tr;
-            tr.bead = b;
-            tr.accepted = acc ? 1 : 0;
-            tr.before = so;
-            tr.after = sn;
-            tr.dx = dx;
-            tr.dy = dy;
-            tr.dz = dz;
-            tr.pad = d;
-            trace[moves + k] = tr;
+#pragma unroll
+            for (int j = 0; j < W; ++j)
+              if (j < g && pj == bj[j]) cm |= 1u << j;
           }
         }
-        __syncwarp();
-        mv = mv1;
-        thr = thr1;
-        beg = beg1;
-        deg = deg1;
-        ent = ent1;
-        itv = it1;
+        if (sub == 0) {
+          if (R > 0.0f) {
+            so += sphere_penalty(pb.x, pb.y, pb.z, R);
+            sn += sphere_penalty(nx, ny, nz, R);
+          }
+#pragma unroll
+          for (int j = 0; j < W; ++j)
+            if (j < g && b == bj[j]) cm |= 1u << j;
+        }
       }
-      moves += kmax;
-      T *= (double)s_dtpow[kmax];
+      float d = sn - so;
+#pragma unroll
+      for (int o = G >> 1; o > 0; o >>= 1) {
+        cm |= __shfl_xor_sync(0xffffffffu, cm, o);
+        if (tracing) {
+          so += __shfl_xor_sync(0xffffffffu, so, o);
+          sn += __shfl_xor_sync(0xffffffffu, sn, o);
+        } else {
+          d += __shfl_xor_sync(0xffffffffu, d, o);
+        }
+      }
+      if (tracing) d = sn - so;
+      if (active && sub == 0) {
+        s_d[g] = d;
+        s_c[g] = cm;
+        if (tracing) {
+          s_so[g] = so;
+          s_sn[g] = sn;
+        }
+      }
+      __syncwarp();
+      // in-order resolution, identical on every lane
+      unsigned accm = 0u;
+      float pacc = 0.0f;
+      int lend = L;
+      for (int j = 0; j < L; ++j) {
+        if (s_c[j] & accm) {
+          lend = j;
+          break;
+        }
+        const float dj = s_d[j];
+        const float ef = e_hi + pacc;
+        if (dj <= 0.0f || dj < ef * (s_thr[k0 + j] - 1.0f)) {
+          accm |= 1u << j;
+          pacc += dj;
+        }
+      }
+      if (active && sub == 0 && g < lend && ((accm >> g) & 1u))
+        spos[b] = make_float4(nx, ny, nz, 0.0f);
+      if (tracing && lane == 0) {
+        for (int j = 0; j < lend && moves + j < P.trace_cap; ++j) {
+          const int4 m = s_mv[k0 + j];
+          MoveTrace tr;
+          tr.bead = m.x;
+          tr.accepted = (accm >> j) & 1u;
+          tr.before = s_so[j];
+          tr.after = s_sn[j];
+          tr.dx = __int_as_float(m.y);
+          tr.dy = __int_as_float(m.z);
+          tr.dz = __int_as_float(m.w);
+          tr.pad = s_d[j];
+          trace[moves + j] = tr;
+        }
+      }
+      __syncwarp();
+      if (accm) ff_add(e_hi, e_lo, pacc);
+      const int na = __popc(accm);
+      accepted += na;
+      succ_ms += na;
+      moves += lend;
       ++batch_no;
 
-      // ---- milestone (the reference CPU predicate, FP64, lane 0) ----
-      int flag = 0;
+      // ---- milestone (the reference CPU predicate, FP64, every lane) ----
+      bool flag = false;
       if (moves % P.window == 0) {
-        if (lane == 0) {
-          const double E = (double)e_hi + (double)e_lo;
-          const bool miss =
-              (E > (double)P.improvement * E_ms && succ_ms < P.min_successes) ||
-              E < 1e-5 || E / E_ms > 0.9999;
-          misses = miss ? misses + 1 : 0;
-          if (misses >= P.fails || E < 1e-5) flag = 1;
-          E_ms = E;
-          succ_ms = 0;
-        }
+        const double E = (double)e_hi + (double)e_lo;
+        const bool miss =
+            (E > (double)P.improvement * E_ms && succ_ms < P.min_successes) ||
+            E < 1e-5 || E / E_ms > 0.9999;
+        misses = miss ? misses + 1 : 0;
+        if (misses >= P.fails || E < 1e-5) flag = true;
+        E_ms = E;
+        succ_ms = 0;
       }
-      if (P.resync > 0 && moves % P.resync == 0 && !__shfl_sync(0xffffffffu, flag, 0)) {
+      if (P.resync > 0 && moves % P.resync == 0 && !flag) {
         const double es = arcs_spring_energy(n, spos, srp, NB, LST, U.n_loops, P, lane);
-        if (lane == 0) {
-          const double Er = base + es;
-          e_hi = (float)Er;
-          e_lo = (float)(Er - (double)e_hi);
-        }
+        const double Er = base + es;
+        e_hi = (float)Er;
+        e_lo = (float)(Er - (double)e_hi);
       }
+      if (!flag && moves >= P.cap) {
+        flag = true;
+        if (P.cap_is_error) status = kDevMoveCap;
+      }
+      int f = flag ? 1 : 0;
       if (lane == 0) {
-        if (!flag && moves >= P.cap) {
-          flag = 1;
-          if (P.cap_is_error) status = kDevMoveCap;
-        }
-        if (flag && P.stop_all) atomicExch(done_flag, 1);
-        if (!flag && P.stop_all && (batch_no & 7) == 0 &&
-            *((volatile int *)done_flag) != 0)
-          flag = 1;
+        if (f && P.stop_all) atomicExch(done_flag, 1);
+        if (!f && P.stop_all && (batch_no & 31) == 0 && *((volatile int *)done_flag) != 0)
+          f = 1;
       }
-      stop = __shfl_sync(0xffffffffu, flag, 0) != 0;
+      stop = __shfl_sync(0xffffffffu, f, 0) != 0;
     }
 
     // ---- final FP64 recompute and outputs ----
@@ -463,6 +491,21 @@ __global__ void arcs_pick_best_kernel(const ArcsUnit *__restrict__ units,
     }
   }
   best[u] = b;
+}
+
+using ArcsKernelFn = void (*)(const ArcsUnit *, const int2 *, int, int *, const float4 *,
+                              const int *, const int2 *, const float *, const int *,
+                              const int *, const float4 *, const int4 *, const int2 *,
+                              ArcsDevParams, int, float *, ChainOut *, int *, MoveTrace *);
+
+// The instantiation for a launch: arc lists staged or not, G lanes per move.
+inline ArcsKernelFn arcs_kernel_for(bool nb_smem, int lanes) {
+  switch (lanes) {
+    case 2: return nb_smem ? arcs_anneal_kernel<true, 2> : arcs_anneal_kernel<false, 2>;
+    case 8: return nb_smem ? arcs_anneal_kernel<true, 8> : arcs_anneal_kernel<false, 8>;
+    case 32: return nb_smem ? arcs_anneal_kernel<true, 32> : arcs_anneal_kernel<false, 32>;
+    default: return nb_smem ? arcs_anneal_kernel<true, 4> : arcs_anneal_kernel<false, 4>;
+  }
 }
 
 }  // namespace pmmc
@@ -753,9 +796,12 @@ extern "C" pmmc_status pmmc_arcs_batch_create_ex(
     return a.bytes > c.bytes;
   });
   std::vector<int2> h_items;
-  cudaFuncSetAttribute(arcs_anneal_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  int lanes = opts && opts->lanes_per_chain > 0 ? opts->lanes_per_chain : 4;
+  if (lanes != 2 && lanes != 4 && lanes != 8 && lanes != 32) lanes = 4;
+  b->lanes = lanes;
+  cudaFuncSetAttribute(arcs_kernel_for(true, lanes), cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)ctx->smem_optin);
-  cudaFuncSetAttribute(arcs_anneal_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  cudaFuncSetAttribute(arcs_kernel_for(false, lanes), cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)ctx->smem_optin);
   size_t i0 = 0;
   while (i0 < needs.size()) {
@@ -776,10 +822,8 @@ extern "C" pmmc_status pmmc_arcs_batch_create_ex(
     c.warps_per_cta = w;
     int per_sm = 0;
     const size_t dyn = kCtaHeader + (size_t)w * c.smem_per_warp;
-    if (nbs)
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, arcs_anneal_kernel<true>, 32 * w, dyn);
-    else
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, arcs_anneal_kernel<false>, 32 * w, dyn);
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, arcs_kernel_for(nbs, lanes), 32 * w,
+                                                  dyn);
     if (per_sm < 1) per_sm = 1;
     const int items_n = c.item_end - c.item_begin;
     c.grid = std::max(1, std::min(per_sm * ctx->sm_count, (items_n + w - 1) / w));
@@ -841,18 +885,11 @@ cudaError_t enqueue_pass(pmmc_arcs_batch *b, cudaStream_t s) {
     e = cudaStreamWaitEvent(c.stream, b->ev_fork, 0);
     if (e != cudaSuccess) break;
     const size_t dyn = kCtaHeader + (size_t)c.warps_per_cta * c.smem_per_warp;
-    if (c.nb_smem)
-      arcs_anneal_kernel<true><<<c.grid, 32 * c.warps_per_cta, dyn, c.stream>>>(
-          b->units.p, b->items.p + c.item_begin, c.item_end - c.item_begin, b->heads.p + k,
-          b->pos0.p, b->row_ptr.p, b->nbr.p, b->inv_t.p, b->movable.p, b->lrp.p, b->lent.p,
-          b->lst.p, b->nulls.p, b->P, c.smem_per_warp, b->pos_out.p, b->outs.p, b->done.p,
-          b->trace);
-    else
-      arcs_anneal_kernel<false><<<c.grid, 32 * c.warps_per_cta, dyn, c.stream>>>(
-          b->units.p, b->items.p + c.item_begin, c.item_end - c.item_begin, b->heads.p + k,
-          b->pos0.p, b->row_ptr.p, b->nbr.p, b->inv_t.p, b->movable.p, b->lrp.p, b->lent.p,
-          b->lst.p, b->nulls.p, b->P, c.smem_per_warp, b->pos_out.p, b->outs.p, b->done.p,
-          b->trace);
+    arcs_kernel_for(c.nb_smem, b->lanes)<<<c.grid, 32 * c.warps_per_cta, dyn, c.stream>>>(
+        b->units.p, b->items.p + c.item_begin, c.item_end - c.item_begin, b->heads.p + k,
+        b->pos0.p, b->row_ptr.p, b->nbr.p, b->inv_t.p, b->movable.p, b->lrp.p, b->lent.p,
+        b->lst.p, b->nulls.p, b->P, c.smem_per_warp, b->pos_out.p, b->outs.p, b->done.p,
+        b->trace);
     e = cudaGetLastError();
     if (e == cudaSuccess) e = cudaEventRecord(c.join, c.stream);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(s, c.join, 0);
@@ -1017,7 +1054,7 @@ extern "C" pmmc_status pmmc_arcs_anneal(pmmc_ctx *ctx, const pmmc_arcs_problem *
                                         int n_chains, float *pos_out, pmmc_result *res) {
   if (!ctx || !pr || !prm) return fail(ctx, PMMC_ERR_INVALID, "arcs anneal: bad arguments");
   if (n_chains <= 0) n_chains = 4 * ctx->sm_count;
-  pmmc_batch_opts o{n_chains, 0, 32};
+  pmmc_batch_opts o{n_chains, 0, 0};
   pmmc_arcs_batch *b = nullptr;
   pmmc_status s =
       pmmc_arcs_batch_create_ex(ctx, 1, pr, prm, &step_size, &o, 1, 0, &b);

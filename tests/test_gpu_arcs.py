@@ -39,13 +39,17 @@ def problem(variant, n=96, arcs=160, seed=3):
     return pr, inp, kw
 
 
-@pytest.mark.parametrize("variant", ["plain", "loops_sphere", "fixed", "2d", "inert_pairs", "hub"])
-def test_arcs_trace_parity(ctx, variant):
+@pytest.mark.parametrize("variant,lanes", [("plain", 4), ("loops_sphere", 4), ("fixed", 4),
+                                           ("2d", 4), ("inert_pairs", 4), ("hub", 4),
+                                           ("plain", 2), ("plain", 8), ("plain", 32),
+                                           ("hub", 2), ("loops_sphere", 8)])
+def test_arcs_trace_parity(ctx, variant, lanes):
+    """Windows of 32/lanes proposals resolve to the one-move-at-a-time chain."""
     pr, inp, kw = problem(variant)
     base = dict(max_temp=5.0, dt_temp=0.9999, milestone_steps=4000, improvement=0.99, **kw)
     prm = capi.default_params(capi.LEVEL_ARCS, schedule=capi.SCHEDULE_CPU, max_moves=12000, **base)
     ctx.set_seed(777)
-    b = capi.ArcsBatch(ctx, [inp], prm, [0.5], use_graph=False, trace_cap=12000)
+    b = capi.ArcsBatch(ctx, [inp], prm, [0.5], use_graph=False, trace_cap=12000, lanes=lanes)
     b.run()
     pos, res = b.results()
     m = int(res[0].moves)
@@ -84,14 +88,15 @@ def test_arcs_dropin_multichain(ctx):
     assert abs(res.energy_fp64 - e64) <= 1e-6 * e64
 
 
-def test_arcs_batch_units_match_oracle(ctx):
+@pytest.mark.parametrize("lanes", [2, 4, 8])
+def test_arcs_batch_units_match_oracle(ctx, lanes):
     """Every unit of a batch follows the oracle's Philox-mode annealer."""
     regs = [synth.arcs_region(n, int(1.5 * n), seed=s) for s, n in enumerate([32, 57, 130, 300, 80, 41])]
     inputs = [capi.ArcsInput.from_dense(r.pos, r.dense()) for r in regs]
     base = dict(max_temp=5.0, dt_temp=0.9999, milestone_steps=1000, improvement=0.99)
     prm = capi.default_params(capi.LEVEL_ARCS, schedule=capi.SCHEDULE_CPU, max_moves=3000, **base)
     ctx.set_seed(99)
-    b = capi.ArcsBatch(ctx, inputs, prm, [0.5] * len(inputs))
+    b = capi.ArcsBatch(ctx, inputs, prm, [0.5] * len(inputs), lanes=lanes)
     b.run()
     pos, res = b.results()
     same = 0
