@@ -280,7 +280,7 @@ def _batch_anneal_host(ctx, inputs, prm, steps):
     tot = sum(x.n for x in inputs)
     pos = np.zeros((tot, 3), np.float32)
     res = (capi.Result * len(inputs))()
-    opts = capi.BatchOpts(1, 0, 32)
+    opts = capi.BatchOpts(1, 0, 0)
     ctx.check(capi.lib().pmmc_arcs_batch_anneal(ctx.h, len(inputs), arr, C.byref(prm),
                                                 st.ctypes.data_as(C.c_void_p), C.byref(opts),
                                                 pos.ctypes.data_as(C.c_void_p), res))

@@ -27,6 +27,7 @@
 // queue (largest regions first), one launch per shared-memory size class, the
 // classes on forked streams and the whole pass captured in a CUDA graph.
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <map>
@@ -178,7 +179,7 @@ __device__ double arcs_repulsion(int n, const float4 *spos, const int *srp,
 }
 
 template <bool NB_SMEM, int G>
-__global__ void __launch_bounds__(128)
+__global__ void __launch_bounds__(128, 4)
 arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
                    const int2 *__restrict__ items, int n_items,
                    int *__restrict__ head, const float4 *__restrict__ pos0,
@@ -291,10 +292,10 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
     if (!stop) refill(0);
     __syncwarp();
 
+    long long next_ms = P.window;
+    long long next_rs = P.resync > 0 ? (long long)P.resync : LLONG_MAX;
     while (!stop) {
-      long long lim = (moves / P.window + 1) * (long long)P.window;
-      if (P.resync > 0) lim = min(lim, (moves / P.resync + 1) * (long long)P.resync);
-      lim = min(lim, P.cap);
+      const long long lim = min(min(next_ms, next_rs), P.cap);
       if (moves + W > bm + 32 && bm + 32 < lim) {  // draw the next 32 moves
         T *= (double)s_dtpow[moves - bm];
         bm = moves;
@@ -306,6 +307,7 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
       const int k0 = (int)(moves - bm);
       const bool active = g < L;
       const int4 mv = active ? s_mv[k0 + g] : make_int4(0, 0, 0, 0);
+      const float thr = active ? s_thr[k0 + g] : 0.0f;
       const int b = mv.x;
       int bj[W];
 #pragma unroll
@@ -367,47 +369,55 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
           d += __shfl_xor_sync(0xffffffffu, d, o);
         }
       }
-      if (tracing) d = sn - so;
-      if (active && sub == 0) {
-        s_d[g] = d;
-        s_c[g] = cm;
-        if (tracing) {
+      if (tracing) {
+        d = sn - so;
+        if (active && sub == 0) {
           s_so[g] = so;
           s_sn[g] = sn;
+          s_d[g] = d;
         }
       }
-      __syncwarp();
-      // in-order resolution, identical on every lane
+      // ---- resolution, exactly the in-order loop: every unresolved slot
+      // tests acceptance against the running partial sum at once, a ballot
+      // finds the first acceptance, and the window ends at the first later
+      // slot that depends on an accepted bead ----
+      const bool leader = active && sub == 0;
       unsigned accm = 0u;
       float pacc = 0.0f;
       int lend = L;
-      for (int j = 0; j < L; ++j) {
-        if (s_c[j] & accm) {
-          lend = j;
-          break;
-        }
-        const float dj = s_d[j];
+      int first = 0;
+      for (;;) {
         const float ef = e_hi + pacc;
-        if (dj <= 0.0f || dj < ef * (s_thr[k0 + j] - 1.0f)) {
-          accm |= 1u << j;
-          pacc += dj;
-        }
+        const bool t = leader && g >= first && g < lend &&
+                       (d <= 0.0f || d < ef * (thr - 1.0f));
+        const unsigned am = __ballot_sync(0xffffffffu, t);
+        if (am == 0u) break;
+        const int j = (__ffs(am) - 1) / G;
+        accm |= 1u << j;
+        pacc += __shfl_sync(0xffffffffu, d, j * G);
+        const unsigned km = __ballot_sync(0xffffffffu, leader && g > j && g < lend &&
+                                                            ((cm >> j) & 1u));
+        if (km) lend = (__ffs(km) - 1) / G;
+        first = j + 1;
+        if (first >= lend) break;
       }
-      if (active && sub == 0 && g < lend && ((accm >> g) & 1u))
-        spos[b] = make_float4(nx, ny, nz, 0.0f);
-      if (tracing && lane == 0) {
-        for (int j = 0; j < lend && moves + j < P.trace_cap; ++j) {
-          const int4 m = s_mv[k0 + j];
-          MoveTrace tr;
-          tr.bead = m.x;
-          tr.accepted = (accm >> j) & 1u;
-          tr.before = s_so[j];
-          tr.after = s_sn[j];
-          tr.dx = __int_as_float(m.y);
-          tr.dy = __int_as_float(m.z);
-          tr.dz = __int_as_float(m.w);
-          tr.pad = s_d[j];
-          trace[moves + j] = tr;
+      if (leader && g < lend && ((accm >> g) & 1u)) spos[b] = make_float4(nx, ny, nz, 0.0f);
+      if (tracing) {
+        __syncwarp();
+        if (lane == 0) {
+          for (int j = 0; j < lend && moves + j < P.trace_cap; ++j) {
+            const int4 m = s_mv[k0 + j];
+            MoveTrace tr;
+            tr.bead = m.x;
+            tr.accepted = (accm >> j) & 1u;
+            tr.before = s_so[j];
+            tr.after = s_sn[j];
+            tr.dx = __int_as_float(m.y);
+            tr.dy = __int_as_float(m.z);
+            tr.dz = __int_as_float(m.w);
+            tr.pad = s_d[j];
+            trace[moves + j] = tr;
+          }
         }
       }
       __syncwarp();
@@ -420,7 +430,8 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
 
       // ---- milestone (the reference CPU predicate, FP64, every lane) ----
       bool flag = false;
-      if (moves % P.window == 0) {
+      if (moves == next_ms) {
+        next_ms += P.window;
         const double E = (double)e_hi + (double)e_lo;
         const bool miss =
             (E > (double)P.improvement * E_ms && succ_ms < P.min_successes) ||
@@ -430,11 +441,14 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
         E_ms = E;
         succ_ms = 0;
       }
-      if (P.resync > 0 && moves % P.resync == 0 && !flag) {
-        const double es = arcs_spring_energy(n, spos, srp, NB, LST, U.n_loops, P, lane);
-        const double Er = base + es;
-        e_hi = (float)Er;
-        e_lo = (float)(Er - (double)e_hi);
+      if (moves == next_rs) {
+        next_rs += P.resync;
+        if (!flag) {
+          const double es = arcs_spring_energy(n, spos, srp, NB, LST, U.n_loops, P, lane);
+          const double Er = base + es;
+          e_hi = (float)Er;
+          e_lo = (float)(Er - (double)e_hi);
+        }
       }
       if (!flag && moves >= P.cap) {
         flag = true;
