@@ -225,7 +225,7 @@ typedef struct pmmc_batch_opts {
   int use_graph;         /* capture the launches in a CUDA graph          */
   int lanes_per_chain;   /* lanes that score one proposal: 2, 4, 8 or 32;
                           * a chain's warp scores 32/lanes proposals at
-                          * once (0 = the default, 4)                      */
+                          * once (0 = the default, 2)                      */
 } pmmc_batch_opts;
 pmmc_status pmmc_arcs_batch_create(pmmc_ctx *ctx, int n_units,
                                    const pmmc_arcs_problem *units,

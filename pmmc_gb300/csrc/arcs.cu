@@ -145,6 +145,62 @@ __device__ double arcs_spring_energy(int n, const float4 *spos, const int *srp,
   return warp_sum_d(acc);
 }
 
+// The same energy for the periodic resync, which only has to remove the
+// drift of the running total: each term in FP32 (hardware reciprocal square
+// root for the length), summed per lane in float-float (error-free two-sum)
+// and across lanes in FP64.  A lane walks four bead rows at once with four
+// independent accumulators so that the loads and arithmetic of different rows
+// overlap; the per-term work stays off the narrow FP64 pipe.
+__device__ __forceinline__ float resync_len(float4 a, float4 b) {
+  const float x = a.x - b.x, y = a.y - b.y, z = a.z - b.z;
+  const float s = fmaf(x, x, fmaf(y, y, z * z));
+  return s * rsqrtf(fmaxf(s, 1e-30f));
+}
+
+__device__ double arcs_spring_energy_ff(int n, const float4 *spos, const int *srp,
+                                        const int2 *nb, const float *inv, const int4 *loops,
+                                        int n_loops, const ArcsDevParams &P, int lane) {
+  const float ks = P.k_stretch, kq = P.k_squeeze, R = P.sphere_r;
+  float hi[4] = {0.f, 0.f, 0.f, 0.f}, lo[4] = {0.f, 0.f, 0.f, 0.f};
+  for (int i0 = lane; i0 < n; i0 += 128) {
+    float4 pi[4];
+    int e[4], e1[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int i = min(i0 + 32 * r, n - 1);
+      const bool ok = i0 + 32 * r < n;
+      pi[r] = spos[i];
+      e[r] = srp[i];
+      e1[r] = ok ? srp[i + 1] : e[r];
+      ff_add(hi[r], lo[r], ok ? sphere_penalty(pi[r].x, pi[r].y, pi[r].z, R) : 0.0f);
+    }
+    // branch-free: the four rows' chains interleave
+    for (;;) {
+      bool any = false;
+#pragma unroll
+      for (int r = 0; r < 4; ++r) {
+        const bool ok = e[r] < e1[r];
+        any |= ok;
+        const int ee = ok ? e[r] : 0;
+        const int2 ent = nb[ee];
+        const float4 q = spos[ent.x];
+        const float v = spring_fast(resync_len(pi[r], q), __int_as_float(ent.y), inv[ee], ks, kq);
+        ff_add(hi[r], lo[r], (ok && ent.x < i0 + 32 * r) ? v : 0.0f);
+        e[r] += ok ? 1 : 0;
+      }
+      if (!any) break;
+    }
+  }
+  for (int c = lane; c < n_loops; c += 32) {
+    const int4 L = loops[c];
+    const float d = (L.x == L.y ? 0.0f : resync_len(spos[L.x], spos[L.y])) - __int_as_float(L.w);
+    ff_add(hi[0], lo[0], __int_as_float(L.z) * d * d);
+  }
+  const double t = ((double)hi[0] + (double)lo[0]) + ((double)hi[1] + (double)lo[1]) +
+                   ((double)hi[2] + (double)lo[2]) + ((double)hi[3] + (double)lo[3]);
+  return warp_sum_d(t);
+}
+
 // FP64 sum of 1/d over every pair (i<j) that the arc lists do not name.
 __device__ double arcs_repulsion(int n, const float4 *spos, const int *srp,
                                  const int2 *nb, const int2 *nulls, int n_null,
@@ -322,15 +378,29 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
         ny = pb.y + __int_as_float(mv.z);
         nz = pb.z + __int_as_float(mv.w);
         const int beg = srp[b], end = srp[b + 1];
-        for (int e = beg + sub; e < end; e += G) {
+        const unsigned earlier = (1u << g) - 1u;  // slots before this one
+        // two arcs per lane per iteration: independent loads in flight
+        for (int e = beg + sub; e < end; e += 2 * G) {
+          const int e2 = e + G;
+          const bool two = e2 < end;
           const int2 ent = NB[e];
-          const float t = __int_as_float(ent.y), iv = INV[e];
+          const float iv = INV[e];
+          const int2 ent2 = two ? NB[e2] : ent;
+          const float iv2 = two ? INV[e2] : 0.0f;
           const float4 q = spos[ent.x];
-          so += spring_fast(fast_len(pb.x, pb.y, pb.z, q), t, iv, ks, kq);
-          sn += spring_fast(fast_len(nx, ny, nz, q), t, iv, ks, kq);
+          const float4 q2 = spos[ent2.x];
+          const float t = __int_as_float(ent.y), t2 = __int_as_float(ent2.y);
+          const float o1 = spring_fast(fast_len(pb.x, pb.y, pb.z, q), t, iv, ks, kq);
+          const float n1 = spring_fast(fast_len(nx, ny, nz, q), t, iv, ks, kq);
+          const float o2 = spring_fast(fast_len(pb.x, pb.y, pb.z, q2), t2, iv2, ks, kq);
+          const float n2 = spring_fast(fast_len(nx, ny, nz, q2), t2, iv2, ks, kq);
+          so += o1 + (two ? o2 : 0.0f);
+          sn += n1 + (two ? n2 : 0.0f);
+          unsigned hit = 0u;
 #pragma unroll
           for (int j = 0; j < W; ++j)
-            if (j < g && ent.x == bj[j]) cm |= 1u << j;
+            hit |= (unsigned)(ent.x == bj[j] || ent2.x == bj[j]) << j;
+          cm |= hit & earlier;
         }
         if (has_loops) {
           const int l1 = LRP[b + 1];
@@ -343,9 +413,10 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
             const float d1 = (pj == b ? 0.0f : fast_len(nx, ny, nz, q)) - le.z;
             so += le.y * d0 * d0;
             sn += le.y * d1 * d1;
+            unsigned hit = 0u;
 #pragma unroll
-            for (int j = 0; j < W; ++j)
-              if (j < g && pj == bj[j]) cm |= 1u << j;
+            for (int j = 0; j < W; ++j) hit |= (unsigned)(pj == bj[j]) << j;
+            cm |= hit & ((1u << g) - 1u);
           }
         }
         if (sub == 0) {
@@ -353,9 +424,10 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
             so += sphere_penalty(pb.x, pb.y, pb.z, R);
             sn += sphere_penalty(nx, ny, nz, R);
           }
+          unsigned hit = 0u;
 #pragma unroll
-          for (int j = 0; j < W; ++j)
-            if (j < g && b == bj[j]) cm |= 1u << j;
+          for (int j = 0; j < W; ++j) hit |= (unsigned)(b == bj[j]) << j;
+          cm |= hit & ((1u << g) - 1u);
         }
       }
       float d = sn - so;
@@ -444,7 +516,8 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
       if (moves == next_rs) {
         next_rs += P.resync;
         if (!flag) {
-          const double es = arcs_spring_energy(n, spos, srp, NB, LST, U.n_loops, P, lane);
+          const double es =
+              arcs_spring_energy_ff(n, spos, srp, NB, INV, LST, U.n_loops, P, lane);
           const double Er = base + es;
           e_hi = (float)Er;
           e_lo = (float)(Er - (double)e_hi);
@@ -518,7 +591,8 @@ inline ArcsKernelFn arcs_kernel_for(bool nb_smem, int lanes) {
     case 2: return nb_smem ? arcs_anneal_kernel<true, 2> : arcs_anneal_kernel<false, 2>;
     case 8: return nb_smem ? arcs_anneal_kernel<true, 8> : arcs_anneal_kernel<false, 8>;
     case 32: return nb_smem ? arcs_anneal_kernel<true, 32> : arcs_anneal_kernel<false, 32>;
-    default: return nb_smem ? arcs_anneal_kernel<true, 4> : arcs_anneal_kernel<false, 4>;
+    case 4: return nb_smem ? arcs_anneal_kernel<true, 4> : arcs_anneal_kernel<false, 4>;
+    default: return nb_smem ? arcs_anneal_kernel<true, 2> : arcs_anneal_kernel<false, 2>;
   }
 }
 
@@ -810,8 +884,8 @@ extern "C" pmmc_status pmmc_arcs_batch_create_ex(
     return a.bytes > c.bytes;
   });
   std::vector<int2> h_items;
-  int lanes = opts && opts->lanes_per_chain > 0 ? opts->lanes_per_chain : 4;
-  if (lanes != 2 && lanes != 4 && lanes != 8 && lanes != 32) lanes = 4;
+  int lanes = opts && opts->lanes_per_chain > 0 ? opts->lanes_per_chain : 2;
+  if (lanes != 2 && lanes != 4 && lanes != 8 && lanes != 32) lanes = 2;
   b->lanes = lanes;
   cudaFuncSetAttribute(arcs_kernel_for(true, lanes), cudaFuncAttributeMaxDynamicSharedMemorySize,
                        (int)ctx->smem_optin);
