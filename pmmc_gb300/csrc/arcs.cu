@@ -250,7 +250,7 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31;
   float *s_dtpow = reinterpret_cast<float *>(smem);
-  if (threadIdx.x < 33) s_dtpow[threadIdx.x] = P.dtpow[threadIdx.x];
+  for (int i = threadIdx.x; i < 33; i += blockDim.x) s_dtpow[i] = P.dtpow[i];
   __syncthreads();
   unsigned char *wbase = smem + kCtaHeader + (size_t)(threadIdx.x >> 5) * smem_per_warp;
   int4 *s_mv = reinterpret_cast<int4 *>(wbase);
