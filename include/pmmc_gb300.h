@@ -294,6 +294,30 @@ pmmc_status pmmc_heatmap_batch_anneal(pmmc_ctx *ctx, int n_units,
                                       pmmc_result *res, double *kernel_ms,
                                       void *trace_out, int trace_cap);
 
+/* ---------------- arc-level anneal that allocates nothing ------------- */
+/* No counterpart in the reference.  For callers that cannot allocate device
+ * memory -- code that must not call cudaMalloc because a host framework owns
+ * the device pool and lends out only its own buffers, or a plugin running
+ * under a fixed memory budget.  Every pointer in *pr is a DEVICE pointer (the
+ * caller's inputs: positions, optional fixed flags, row_ptr/col/target);
+ * pos_out is a device buffer of n*3 floats; res is a host struct.  One chain
+ * is annealed with the same kernel and Philox stream as pmmc_arcs_batch_*
+ * with one chain (key = seed, chain 0), on `stream` (NULL = legacy default).
+ * All intermediates live in one fixed device array of the library (about
+ * 0.4 MB, held by every GPU that loads it until the process exits): regions
+ * of at most 4096 beads and 16384 arc-list entries, no loop constraints;
+ * larger regions return PMMC_ERR_BUDGET, loop constraints PMMC_ERR_INVALID.
+ * Nothing is allocated: no cudaMalloc/cudaFree and no allocating library
+ * call.  The first call on a device looks up the array's device address
+ * (with that device current) and should come before any stream capture.
+ * Calls share the array and each starts by re-initialising it; calls whose
+ * work overlaps on the GPU (two streams, two host threads) race on it. */
+pmmc_status pmmc_arcs_anneal_noalloc(const pmmc_arcs_problem *pr,
+                                     const pmmc_anneal_params *prm,
+                                     float step_size, uint64_t seed,
+                                     float *pos_out, pmmc_result *res,
+                                     void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -38,7 +38,7 @@ HEADER_SYMBOLS = [
     "pmmc_arcs_batch_create", "pmmc_arcs_batch_run", "pmmc_arcs_batch_results",
     "pmmc_arcs_batch_stats", "pmmc_arcs_batch_destroy", "pmmc_arcs_batch_anneal",
     "pmmc_arcs_batch_create_ex", "pmmc_arcs_batch_trace", "pmmc_smooth_batch_anneal",
-    "pmmc_heatmap_batch_anneal",
+    "pmmc_heatmap_batch_anneal", "pmmc_arcs_anneal_noalloc",
 ]
 
 
@@ -408,3 +408,16 @@ def mark_arcs(ctx: Context, anchors, raw):
                                    _p(rc[1]), _p(rc[2]), _p(rc[3]), _p(out), cap,
                                    C.byref(n_out), C.byref(nm)))
     return out[:n_out.value].copy(), nm.value
+
+
+def arcs_anneal_noalloc(prob_dev: ArcsProblem, params: AnnealParams, step: float, seed: int,
+                        pos_out_dev: int, stream: int = 0) -> Result:
+    """pmmc_arcs_anneal_noalloc: every pointer of prob_dev and pos_out_dev is
+    a device address owned by the caller; nothing is allocated."""
+    res = Result()
+    st = lib().pmmc_arcs_anneal_noalloc(C.byref(prob_dev), C.byref(params), C.c_float(step),
+                                        C.c_uint64(int(seed) & (2**64 - 1)),
+                                        C.c_void_p(pos_out_dev), C.byref(res),
+                                        C.c_void_p(stream) if stream else None)
+    _check(None, st)
+    return res

@@ -31,6 +31,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <numeric>
 #include <vector>
 
@@ -256,7 +257,6 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
   int4 *s_mv = reinterpret_cast<int4 *>(wbase);
   float *s_thr = reinterpret_cast<float *>(wbase + 32 * 16);
   float *s_d = reinterpret_cast<float *>(wbase + 32 * 20);
-  unsigned *s_c = reinterpret_cast<unsigned *>(wbase + 32 * 24);
   float *s_so = reinterpret_cast<float *>(wbase + 32 * 28);
   float *s_sn = reinterpret_cast<float *>(wbase + 32 * 32);
   float4 *spos = reinterpret_cast<float4 *>(wbase + kMoveBufBytes);
@@ -1151,4 +1151,218 @@ extern "C" pmmc_status pmmc_arcs_anneal(pmmc_ctx *ctx, const pmmc_arcs_problem *
   if (s == PMMC_OK) s = pmmc_arcs_batch_results(b, pos_out, res);
   pmmc_arcs_batch_destroy(b);
   return s;
+}
+
+// ===========================================================================
+// Arc-level anneal that allocates nothing
+// ===========================================================================
+// For callers that cannot allocate device memory themselves or through us:
+// code running where cudaMalloc is unavailable or forbidden (a host
+// framework that owns the whole device pool and hands out only its own
+// buffers, a plugin loaded into a process with a fixed memory budget, code
+// between stream-capture phases that must not trigger allocations).  The
+// caller passes device-resident inputs and an output buffer; every
+// intermediate the anneal needs lives in one file-scope device array of
+// fixed size, which every GPU that loads this library holds until exit.
+namespace {
+
+constexpr int kNoAllocMaxBeads = 4096;      // beads of the region
+constexpr int kNoAllocMaxEntries = 16384;   // arc-list entries, both directions
+
+struct NoAllocScratch {
+  ArcsUnit unit;
+  int2 item;
+  int head;
+  int done;
+  int best;
+  int n_null;
+  int status;
+  int pad[3];
+  ChainOut out;
+  float4 pos0[kNoAllocMaxBeads];
+  int row_ptr[kNoAllocMaxBeads + 1];
+  int movable[kNoAllocMaxBeads];
+  int2 nbr[kNoAllocMaxEntries];
+  float inv_t[kNoAllocMaxEntries];
+  int2 nulls[kNoAllocMaxEntries];
+  int4 lst[1];
+};
+
+static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoAllocScratch)];
+
+// One block packs the caller's region into the scratch array: float4
+// positions, spring-only arc lists with reciprocals, inert pairs, movable
+// list, work item and counters (the counters must start at zero).
+__global__ void noalloc_stage_kernel(NoAllocScratch *S, int n, int nnz, const float *pos,
+                                     const unsigned char *fixed, const int *row_ptr,
+                                     const int *col, const float *target, float step) {
+  __shared__ int s_cnt[kNoAllocMaxBeads + 1];
+  __shared__ int s_mov[kNoAllocMaxBeads + 1];
+  __shared__ int s_bad;
+  const int t = threadIdx.x;
+  if (t == 0) s_bad = 0;
+  __syncthreads();
+  // the caller's arc lists are checked before anything reads through them
+  for (int i = t; i < n; i += blockDim.x) {
+    const int a = row_ptr[i], z = row_ptr[i + 1];
+    if (a < 0 || z < a || z > nnz) atomicOr(&s_bad, 1);
+  }
+  if (t == 0 && row_ptr[0] != 0) atomicOr(&s_bad, 1);
+  __syncthreads();
+  if (!s_bad)
+    for (int e = t; e < nnz; e += blockDim.x)
+      if (col[e] < 0 || col[e] >= n) atomicOr(&s_bad, 1);
+  __syncthreads();
+  const bool bad = s_bad != 0;
+  for (int i = t; i < n; i += blockDim.x) {
+    S->pos0[i] = make_float4(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], 0.0f);
+    int c = 0;
+    if (!bad)
+      for (int e = row_ptr[i]; e < row_ptr[i + 1]; ++e)
+        c += (target[e] >= 1e-6f && col[e] != i) ? 1 : 0;
+    s_cnt[i] = c;
+    s_mov[i] = (bad || (fixed && fixed[i])) ? 0 : 1;
+  }
+  __syncthreads();
+  if (t == 0) {  // prefix sums (n <= 4096: one thread is fast enough here)
+    int acc = 0, m = 0, nn = 0;
+    for (int i = 0; i < n; ++i) {
+      const int c = s_cnt[i];
+      s_cnt[i] = acc;
+      acc += c;
+      const int mv = s_mov[i];
+      s_mov[i] = m;
+      m += mv;
+      if (!bad)
+        for (int e = row_ptr[i]; e < row_ptr[i + 1]; ++e)
+          if (target[e] >= 0.0f && target[e] < 1e-6f && col[e] < i)
+            S->nulls[nn++] = make_int2(col[e], i);
+    }
+    s_cnt[n] = acc;
+    s_mov[n] = m;
+    S->n_null = nn;
+    ArcsUnit U{};
+    U.n = n;
+    U.n_mov = m;  // 0 for a malformed region: the kernel then makes no move
+    U.pos_off = 0;
+    U.rp_off = 0;
+    U.nbr_off = 0;
+    U.nnz = acc;
+    U.mov_off = m < n ? 0 : -1;
+    U.lrp_off = -1;
+    U.lent_off = 0;
+    U.n_lent = 0;
+    U.lst_off = 0;
+    U.n_loops = 0;
+    U.null_off = 0;
+    U.n_null = nn;
+    U.chains = 1;
+    U.chain_base = 0;
+    U.out_off = 0;
+    U.step = step;
+    S->unit = U;
+    S->item = make_int2(0, 0);
+    S->head = 0;
+    S->done = 0;
+    S->best = 0;
+    S->status = bad ? 1 : 0;
+    S->lst[0] = make_int4(0, 0, 0, 0);
+  }
+  __syncthreads();
+  for (int i = t; i <= n; i += blockDim.x) S->row_ptr[i] = s_cnt[i];
+  for (int i = t; i < n; i += blockDim.x) {
+    if (!bad && !(fixed && fixed[i])) S->movable[s_mov[i]] = i;
+    if (bad) continue;
+    int k = s_cnt[i];
+    for (int e = row_ptr[i]; e < row_ptr[i + 1]; ++e) {
+      const float tg = target[e];
+      if (tg >= 1e-6f && col[e] != i) {
+        S->nbr[k] = make_int2(col[e], __float_as_int(tg));
+        S->inv_t[k] = 1.0f / tg;
+        ++k;
+      }
+    }
+  }
+}
+
+std::mutex g_noalloc_mutex;
+NoAllocScratch *g_noalloc_ptr[64] = {};
+
+}  // namespace
+
+extern "C" pmmc_status pmmc_arcs_anneal_noalloc(const pmmc_arcs_problem *pr,
+                                                const pmmc_anneal_params *prm,
+                                                float step_size, uint64_t seed,
+                                                float *pos_out, pmmc_result *res,
+                                                void *stream) {
+  if (!pr || !prm || !pos_out || !res || !pr->pos || !pr->row_ptr || pr->n < 1)
+    return PMMC_ERR_INVALID;
+  if (pr->n_loops != 0) return PMMC_ERR_INVALID;       // loop constraints need packing
+  if (pr->n > kNoAllocMaxBeads) return PMMC_ERR_BUDGET; // beyond the fixed scratch
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return PMMC_ERR_NO_DEVICE;
+  NoAllocScratch *S = nullptr;
+  {
+    // once per device, with that device current: the host-side name of a
+    // __device__ array is not a device address, so look the address up
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_ptr[dev]) {
+      void *p = nullptr;
+      if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
+        cudaGetLastError();
+        return PMMC_ERR_CUDA;
+      }
+      g_noalloc_ptr[dev] = reinterpret_cast<NoAllocScratch *>(p);
+    }
+    S = g_noalloc_ptr[dev];
+  }
+  cudaStream_t s = (cudaStream_t)stream;
+  int nnz = 0;
+  if (cudaMemcpyAsync(&nnz, pr->row_ptr + pr->n, sizeof(int), cudaMemcpyDeviceToHost, s) !=
+          cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return PMMC_ERR_CUDA;
+  if (nnz > kNoAllocMaxEntries) return PMMC_ERR_BUDGET;
+  if (nnz < 0 || (nnz > 0 && (!pr->col || !pr->target))) return PMMC_ERR_INVALID;
+  int dev_smem = 0;
+  cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  const int n = pr->n;
+  const size_t minimal = unit_smem_min(n);
+  const size_t full = unit_smem(n, nnz, n, true);
+  const bool nbs = kCtaHeader + full <= (size_t)dev_smem;
+  const size_t per_warp = ((nbs ? full : minimal) + 15) & ~(size_t)15;
+  if (kCtaHeader + per_warp > (size_t)dev_smem) return PMMC_ERR_INVALID;
+  ArcsDevParams P = make_params(prm, seed, false);
+  ArcsKernelFn fn = arcs_kernel_for(nbs, 2);
+  // the device's opt-in maximum, as the batched path sets it: never lower
+  // the limit under a batch created earlier
+  if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, dev_smem) !=
+      cudaSuccess)
+    return PMMC_ERR_CUDA;
+  noalloc_stage_kernel<<<1, 256, 0, s>>>(S, n, nnz, pr->pos, pr->fixed, pr->row_ptr, pr->col,
+                                         pr->target, step_size);
+  fn<<<1, 32, kCtaHeader + per_warp, s>>>(&S->unit, &S->item, 1, &S->head, S->pos0,
+                                          S->row_ptr, S->nbr, S->inv_t, S->movable, nullptr,
+                                          nullptr, S->lst, S->nulls, P, (int)per_warp, pos_out,
+                                          &S->out, &S->done, nullptr);
+  if (cudaGetLastError() != cudaSuccess) return PMMC_ERR_CUDA;
+  ChainOut o;
+  int bad = 0;
+  if (cudaMemcpyAsync(&o, &S->out, sizeof(o), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaMemcpyAsync(&bad, &S->status, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return PMMC_ERR_CUDA;
+  if (bad) return PMMC_ERR_INVALID;  // malformed arc lists: nothing was annealed
+  pmmc_result r{};
+  r.score = o.score;
+  r.energy = o.energy;
+  r.energy_fp64 = o.energy_fp64;
+  r.rel_error = std::fabs(o.energy - o.energy_fp64) / std::max(std::fabs(o.energy_fp64), 1e-30);
+  r.moves = o.moves;
+  r.accepted = o.accepted;
+  r.total_moves = o.moves;
+  r.best_chain = 0;
+  r.status = o.status;
+  *res = r;
+  return PMMC_OK;
 }
