@@ -311,8 +311,20 @@ def main():
                     help="ensemble size (smaller for profiling runs)")
     ap.add_argument("--milestone", type=int, default=ANNEAL["milestone_steps"],
                     help="milestone interval (smaller for profiling runs)")
+    ap.add_argument("--workload", default="ensemble",
+                    choices=["ensemble", "heatmap", "heatmap-batch", "smooth"],
+                    help="ensemble: the batched arc-level ensemble (default line); "
+                         "heatmap: one 2048-bead heatmap chain; heatmap-batch: one chain "
+                         "per distinct 2048-bead map, one per SM; smooth: genome-scale "
+                         "subanchor smoothing")
+    ap.add_argument("--maps", type=int, default=0, help="heatmap-batch: number of maps")
+    ap.add_argument("--moves", type=int, default=0, help="moves per chain (heatmap/smooth)")
     args = ap.parse_args()
     set_workload(args.structures, args.milestone)
+    if args.workload != "ensemble":
+        from pmmc_gb300 import workloads
+        workloads.main(args)
+        return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
 
