@@ -197,19 +197,29 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
   float *slots = reinterpret_cast<float *>(p);    // D * pitch floats
   p += (size_t)D * U.pitch * 4;
   float4 *spos = reinterpret_cast<float4 *>(p);
+  p += (size_t)n * 16;
+  // per-bead chromosome block and the movable list, read on every move's
+  // critical path: staged next to the positions
+  int2 *blk = reinterpret_cast<int2 *>(p);
+  p += (size_t)n * 8;
+  int *smov = reinterpret_cast<int *>(p);
 
-  const int2 *blk = blk_all + U.blk_off;
-  const int *MOV = U.mov_off >= 0 ? movable + U.mov_off : nullptr;
+  const int *MOV = U.mov_off >= 0 ? smov : nullptr;
   const float *hrow0 = heat + U.heat_off;
 
   if (tid == 0) {
     for (int s = 0; s < D; ++s) mbar_init(&bars[s], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  for (int i = tid; i < n; i += blockDim.x) spos[i] = pos0[U.pos_off + i];
+  for (int i = tid; i < n; i += blockDim.x) {
+    spos[i] = pos0[U.pos_off + i];
+    blk[i] = blk_all[U.blk_off + i];
+  }
+  if (U.mov_off >= 0)
+    for (int k = tid; k < U.n_mov; k += blockDim.x) smov[k] = movable[U.mov_off + k];
   __syncthreads();
 
-  const double E0 = heat_full(U, spos, heat, blk_all + U.blk_off, red, P.R);
+  const double E0 = heat_full(U, spos, heat, blk, red, P.R);
   double T = P.max_temp;  // temperature of the next batch's first move (warp 0)
 
   // draws of one batch of 32 moves (warp 0)
@@ -362,7 +372,7 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
       if (!mbar_wait(&bars[k % D], (uint32_t)((k / D) & 1))) status = PMMC_ERR_TIMEOUT;
   }
   __syncthreads();
-  const double Efin = heat_full(U, spos, heat, blk_all + U.blk_off, red, P.R);
+  const double Efin = heat_full(U, spos, heat, blk, red, P.R);
   if (tid == 0) {
     ChainOut o;
     const double E = run ? (double)e_hi + (double)e_lo : 0.0;
@@ -478,7 +488,7 @@ extern "C" pmmc_status pmmc_heatmap_batch_anneal(pmmc_ctx *ctx, int n_units,
   }
   // shared memory: header + D row slots + positions
   const size_t head = 4096;
-  const size_t pos_bytes = (size_t)max_n * 16;
+  const size_t pos_bytes = (size_t)max_n * (16 + 8 + 4);  // positions, blocks, movable
   const size_t row_bytes = (size_t)max_pitch * 4;
   const size_t avail = ctx->smem_optin;
   if (head + pos_bytes + 2 * row_bytes > avail)

@@ -53,6 +53,7 @@ struct SmoothDevParams {
   int window;
   int fails;
   int use2d;
+  int resync;     // full recompute every `resync` moves (0 = off)
   int slice;      // beads per thread slice (shared-memory path)
   long long cap;
   uint64_t seed;
@@ -213,6 +214,13 @@ smooth_anneal_kernel(const SmoothUnit *__restrict__ units,
       trace[moves] = tr;
     }
     ++moves;
+    if (S.resync > 0 && moves % S.resync == 0) {
+      // remove the drift of the running score (a region is small: the
+      // recompute is a few dozen terms)
+      const double Er = smooth_full(P, dtn, n, S);
+      e_hi = (float)Er;
+      e_lo = (float)(Er - (double)e_hi);
+    }
     if (moves % S.window == 0) {
       const double E = (double)e_hi + (double)e_lo;
       const bool miss = (E > (double)S.improvement * E_ms && succ < S.min_succ) || E < 1e-6;
@@ -262,6 +270,10 @@ SmoothDevParams smooth_params(const pmmc_anneal_params *prm, uint64_t seed) {
   S.R = prm->sphere_radius;
   S.min_succ = prm->min_successes;
   S.use2d = prm->use2d;
+  // the weighted full score equals the running (unweighted-delta) score only
+  // at unit weights (the reference's convention): recompute only then
+  S.resync = (prm->resync_every > 0 && prm->w_dist == 1.0f && prm->w_angle == 1.0f)
+                 ? prm->resync_every : 0;
   S.seed = seed;
   if (prm->schedule == PMMC_SCHEDULE_CPU) {
     S.window = std::max(1, prm->milestone_steps);

@@ -86,7 +86,7 @@ def _smooth(args):
     sweeps = args.moves or 20_000
     prm = capi.default_params(capi.LEVEL_SMOOTH, max_temp=5.0, dt_temp=0.9999,
                               milestone_steps=10**9, improvement=0.99,
-                              schedule=capi.SCHEDULE_CPU)
+                              schedule=capi.SCHEDULE_CPU, resync_every=1000)
     steps = []
     for x in segs:
         steps.append(0.5)
