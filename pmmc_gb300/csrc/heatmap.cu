@@ -8,16 +8,27 @@
 // builds are symmetric, :3042-3085).  The reference CPU annealer re-scores all
 // N^2 pairs after every move (:1488); here a move reads one row.
 //
-// One CTA runs one chain.  Positions (float4) live in shared memory.  The row
-// of the bead a move displaces is streamed from HBM into a ring of D
-// shared-memory slots with cp.async.bulk (TMA bulk copy, completion counted
-// on an mbarrier per slot); because the Philox stream is counter-based the
-// beads of future moves are known, so the copy for move k+D is issued while
-// move k is scored.  Each thread scores a strided slice of the row, a warp
-// shuffle plus one barrier reduces the partial sums, and every warp takes the
-// (identical) Metropolis decision itself, so one __syncthreads per move
-// suffices; the running score is a float-float pair in every thread.
+// One CTA runs one chain.  Positions (float4) live in shared memory.  The
+// device matrix holds r = 1/h, zero wherever the reference skips the pair
+// (h < 1e-6, the diagonal band, another chromosome block), so a pair term is
+// branch-free and needs no division.  The row of the bead a move displaces is
+// streamed from HBM into a ring of D shared-memory slots with cp.async.bulk
+// (TMA bulk copy, completion counted on an mbarrier per slot); because the
+// Philox stream is counter-based the beads of future moves are known, so rows
+// are requested a window or more before they are scored.
+//
+// Moves are scored in windows of up to 8: every thread takes a slice of the
+// beads and accumulates the change of all 8 moves at once against the
+// window-start positions; the 8 sums are reduced with warp shuffles and one
+// barrier, warp 0 takes the Metropolis decisions in move order (adding, for a
+// move after an accepted one, the exact change of the pair between the two
+// moved beads), and warp 1 meanwhile draws future moves and requests their
+// rows.  A window never holds the same bead twice and ends at milestones, so
+// the accepted sequence is the one-move-at-a-time sequence.  The running score
+// is a float-float pair; the start and end scores are FP64 recomputes.
 #include <algorithm>
+#include <atomic>
+#include <thread>
 #include <cmath>
 #include <vector>
 
@@ -60,7 +71,8 @@ struct HeatDevParams {
 };
 
 constexpr int kHeatMaxThreads = 512;
-constexpr long long kSpinLimit = 1ll << 26;
+// A row copy that has not landed after this long is reported as a timeout.
+constexpr unsigned long long kWaitLimitNs = 2000000000ull;
 
 __device__ __forceinline__ uint32_t smem_u32(const void *p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -76,10 +88,17 @@ __device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
                : "memory");
 }
 
-// Bounded wait on an mbarrier phase; returns false when the limit ran out.
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+// Bounded wait on an mbarrier phase; returns false when the time limit ran out.
 __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
   const uint32_t a = smem_u32(bar);
-  for (long long it = 0; it < kSpinLimit; ++it) {
+  unsigned long long t0 = 0;
+  for (unsigned it = 0;; ++it) {
     uint32_t ok;
     asm volatile(
         "{\n .reg .pred p;\n"
@@ -89,8 +108,12 @@ __device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
         : "r"(a), "r"(parity)
         : "memory");
     if (ok) return true;
+    if ((it & 255u) == 0u) {
+      const unsigned long long t = globaltimer_ns();
+      if (it == 0u) t0 = t;
+      else if (t - t0 > kWaitLimitNs) return false;
+    }
   }
-  return false;
 }
 
 __device__ __forceinline__ void tma_row(void *dst, const void *src, uint32_t bytes,
@@ -119,57 +142,126 @@ struct MoveRec {
   float dx, dy, dz;
 };
 
-__device__ __forceinline__ float hm_term(float4 a, float4 b, float h) {
-  const float x = a.x - b.x, y = a.y - b.y, z = a.z - b.z;
-  const float c = (sqrtf(x * x + y * y + z * z) - h) / h;
-  return c * c;
+// Approximate reciprocal square root and reciprocal (one special-function
+// operation each, flush-to-zero; callers keep the arguments normal).
+__device__ __forceinline__ float rsqrt_approx(float s) {
+  float r;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(s));
+  return r;
+}
+__device__ __forceinline__ float rcp_approx(float s) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(s));
+  return r;
 }
 
-// Change of one pair term when bead b moves from pb to nb: the hardware
-// reciprocal square root and one reciprocal of h shared by both terms.
-__device__ __forceinline__ float hm_delta(float4 pi, float4 pb, float4 nb, float h) {
-  const float rh = __frcp_rn(h);
-  const float co =
-      (ref_len(__fsub_rn(pi.x, pb.x), __fsub_rn(pi.y, pb.y), __fsub_rn(pi.z, pb.z)) - h) * rh;
-  const float cn =
-      (ref_len(__fsub_rn(pi.x, nb.x), __fsub_rn(pi.y, nb.y), __fsub_rn(pi.z, nb.z)) - h) * rh;
-  return cn * cn - co * co;
+// |v| from |v|^2 with one reciprocal square root; |v|^2 is clamped to 1e-30
+// so coincident beads give ~1e-15 instead of 0 * inf.
+__device__ __forceinline__ float len_from_sq(float s) {
+  s = fmaxf(s, 1e-30f);
+  return s * rsqrt_approx(s);
 }
 
-// FP64 full score plus the sphere penalties of all beads (the reference adds
-// the boundary sum to the initial score, LooperSolver.hpp:1451-1457); the
-// whole block, every thread returns the total.
-__device__ double heat_full(const HeatUnit &U, const float4 *spos, const float *heat,
+// A proposed move: old position, -2 * displacement and |displacement|^2.
+struct MoveGeo {
+  float ox, oy, oz;
+  float mx, my, mz;
+  float dd;
+};
+
+// Change of the pair term (d r - 1)^2 (r = 1/h) between a bead at p and a
+// bead that moves from o to o + delta.  With v = p - o, s_o = |v|^2,
+// t = s_n - s_o = |delta|^2 - 2 v.delta (formed directly, no cancellation)
+// and d_n - d_o = t / (d_n + d_o):
+//   (d_n r - 1)^2 - (d_o r - 1)^2 = r t (r - 2 / (d_n + d_o)).
+// r = 0 (no target, inside the diagonal band, the bead itself, another
+// chromosome block) contributes exactly 0.
+__device__ __forceinline__ float pair_delta(float px, float py, float pz, const MoveGeo &g,
+                                            float r) {
+  const float vx = px - g.ox, vy = py - g.oy, vz = pz - g.oz;
+  const float so = fmaf(vx, vx, fmaf(vy, vy, vz * vz));
+  const float t = fmaf(vx, g.mx, fmaf(vy, g.my, fmaf(vz, g.mz, g.dd)));
+  const float dsum = len_from_sq(so) + len_from_sq(so + t);
+  const float q = fmaf(-2.0f, rcp_approx(dsum), r);
+  return (r * t) * q;
+}
+
+// Full score in FP64 (FP32 terms (d r - 1)^2 summed per row, rows summed in
+// FP64) plus the sphere penalties of all beads (the reference adds the
+// boundary sum to the initial score, LooperSolver.hpp:1451-1457).  One warp
+// per row of the reciprocal targets (zero outside the bead's block, in the
+// diagonal band and where h < 1e-6); lane l takes beads i = l mod 32, so the
+// row loads coalesce and the position reads hit 32 distinct banks; a lane
+// issues kB loads before it computes.  The whole block calls it and every
+// thread returns the total.
+__device__ double heat_full(const HeatUnit &U, const float4 *spos, const float *rheat,
                             const int2 *blk, double *red, float R) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  constexpr int kB = 32;
   double acc = 0.0;
   for (int i = threadIdx.x; i < U.n; i += blockDim.x)
     acc += sphere_penalty(spos[i].x, spos[i].y, spos[i].z, R);
-  for (int m = 0; m < U.n; ++m) {
+  for (int m = warp; m < U.n; m += nw) {
     const int2 r = blk[m];
-    const float *row = heat + U.heat_off + (long long)m * U.pitch;
+    const float *row = rheat + U.heat_off + (long long)m * U.pitch;
     const float4 pm = spos[m];
     float part = 0.0f;
-    for (int i = r.x + threadIdx.x; i <= r.y; i += blockDim.x) {
-      if (abs(i - m) < U.diag || i == m) continue;
-      const float h = row[i];
-      if (h < 1e-6f) continue;
-      part += hm_term(spos[i], pm, h);
+    for (int i0 = r.x; i0 <= r.y; i0 += 32 * kB) {
+      float rv[kB];
+#pragma unroll
+      for (int k = 0; k < kB; ++k) {
+        const int i = i0 + lane + 32 * k;
+        rv[k] = i <= r.y ? __ldg(row + i) : 0.0f;
+      }
+#pragma unroll
+      for (int k = 0; k < kB; ++k) {
+        if (rv[k] > 0.0f) {  // a nonzero entry lies inside the row's block
+          const float4 pi = spos[i0 + lane + 32 * k];
+          const float x = pi.x - pm.x, y = pi.y - pm.y, z = pi.z - pm.z;
+          const float f = fmaf(len_from_sq(fmaf(x, x, fmaf(y, y, z * z))), rv[k], -1.0f);
+          part = fmaf(f, f, part);
+        }
+      }
     }
-    acc += part;
+    acc += (double)part;
   }
   acc = warp_sum_d(acc);
   __syncthreads();
-  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = acc;
+  if (lane == 0) red[warp] = acc;
   __syncthreads();
   double t = 0.0;
-  for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += red[w];
+  for (int w = 0; w < nw; ++w) t += red[w];
   __syncthreads();
   return t;
 }
 
+constexpr int kWin = 8;  // moves scored per CTA step
+
+// What warp 0 publishes between windows.
+struct WinPlan {
+  float4 ga[kWin];  // old position, |delta|^2
+  float4 gb[kWin];  // -2 delta, row offset of the move's slot (int bits)
+  int bw[kWin];     // moved beads
+  unsigned accm;    // accepted moves of the window just resolved (bit w)
+  int lend;         // moves in the window just resolved
+  float pacc;       // sum of its accepted energy changes
+  int len;          // moves in the next window
+  int same;         // every move of the next window in one chromosome block
+  int timeout;      // a row copy of the next window never landed
+  int pad[2];
+};
+
+// Exact in-order windows: every thread scores its slice of the rows of up to
+// kWin moves against the window-start positions; pair corrections restore the
+// terms between two beads of the same window once the earlier one has been
+// accepted, and warp 0 takes the Metropolis decisions in move order.  The
+// window ends early before a bead that already moves earlier in it, at a
+// milestone and at the move cap, so the decisions are those of one move at a
+// time.  Two CTA barriers per window; warp 0 does the serial work between
+// them (decisions, draws, row copies, the next window's plan and row waits).
 __global__ void __launch_bounds__(kHeatMaxThreads, 1)
 heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restrict__ pos0,
-                      const float *__restrict__ heat, const int *__restrict__ movable,
+                      const float *__restrict__ rheat, const int *__restrict__ movable,
                       const int2 *__restrict__ blk_all, HeatDevParams P,
                       float *__restrict__ pos_out, ChainOut *__restrict__ outs,
                       MoveTrace *__restrict__ trace) {
@@ -178,51 +270,57 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
   const int n = U.n;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nthr = blockDim.x, nwarps = nthr >> 5;
-  const int D = P.depth;
+  const int D = P.depth;  // a power of two
+  const int dmask = D - 1, dshift = __ffs(D) - 1;
+  const int pitch = U.pitch;
   // ---- shared-memory carve ----
   unsigned char *p = smem;
   uint64_t *bars = reinterpret_cast<uint64_t *>(p);
   p += 16 * 8;
   double *red = reinterpret_cast<double *>(p);
   p += 32 * 8;
-  float *partial = reinterpret_cast<float *>(p);  // [2][kHeatWarps]
-  p += 2 * 32 * 4;
-  int *tflag = reinterpret_cast<int *>(p);        // [2][kHeatWarps] wait timed out
-  p += 2 * 32 * 4;
-  MoveRec *recs = reinterpret_cast<MoveRec *>(p); // ring of 64
-  p += 64 * sizeof(MoveRec);
-  float *thrs = reinterpret_cast<float *>(p);     // ring of 64
-  p += 64 * 4;
+  float *partial = reinterpret_cast<float *>(p);  // [warp][kWin]
+  p += 16 * kWin * 4;
+  float *corr = reinterpret_cast<float *>(p);     // [w][j], j < w
+  p += kWin * kWin * 4;
+  WinPlan *plan_s = reinterpret_cast<WinPlan *>(p);
+  p += sizeof(WinPlan);
+  p = smem + (((p - smem) + 15) & ~(size_t)15);
+  MoveRec *recs = reinterpret_cast<MoveRec *>(p); // ring of 128 draws
+  p += 128 * sizeof(MoveRec);
+  float *thrs = reinterpret_cast<float *>(p);     // ring of 128
+  p += 128 * 4;
   p = smem + (((p - smem) + 127) & ~(size_t)127);
-  float *slots = reinterpret_cast<float *>(p);    // D * pitch floats
-  p += (size_t)D * U.pitch * 4;
+  float *slots = reinterpret_cast<float *>(p);    // D rows of 1/h
+  p += (size_t)D * pitch * 4;
   float4 *spos = reinterpret_cast<float4 *>(p);
   p += (size_t)n * 16;
-  // per-bead chromosome block and the movable list, read on every move's
-  // critical path: staged next to the positions
+  // per-bead chromosome block and the movable list: staged next to the positions
   int2 *blk = reinterpret_cast<int2 *>(p);
   p += (size_t)n * 8;
   int *smov = reinterpret_cast<int *>(p);
 
   const int *MOV = U.mov_off >= 0 ? smov : nullptr;
-  const float *hrow0 = heat + U.heat_off;
+  const float *rrow0 = rheat + U.heat_off;
 
   if (tid == 0) {
     for (int s = 0; s < D; ++s) mbar_init(&bars[s], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  for (int i = tid; i < n; i += blockDim.x) {
+  for (int i = tid; i < n; i += nthr) {
     spos[i] = pos0[U.pos_off + i];
     blk[i] = blk_all[U.blk_off + i];
   }
   if (U.mov_off >= 0)
-    for (int k = tid; k < U.n_mov; k += blockDim.x) smov[k] = movable[U.mov_off + k];
+    for (int k = tid; k < U.n_mov; k += nthr) smov[k] = movable[U.mov_off + k];
   __syncthreads();
 
-  const double E0 = heat_full(U, spos, heat, blk, red, P.R);
-  double T = P.max_temp;  // temperature of the next batch's first move (warp 0)
+  const double E0 = heat_full(U, spos, rheat, blk, red, P.R);
+  double T = P.max_temp;  // temperature of the next filled move (warp 1)
+  long long filled = 0;   // records exist for moves [filled - 128, filled) (warp 1)
+  long long issued = 0;   // moves whose rows were requested (warp 1)
 
-  // draws of one batch of 32 moves (warp 0)
+  // draws of 32 moves [first, first + 32) into the ring (warp 1)
   auto fill = [&](long long first) {
     const uint64_t m = (uint64_t)(first + lane);
     const uint4 r = philox_move(P.seed, (uint32_t)U.chain_id, m, 0u);
@@ -234,123 +332,243 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
     rec.dy = (2.0f * u01(r.z) - 1.0f) * U.step;
     rec.dz = P.use2d ? 0.0f : (2.0f * u01(r.w) - 1.0f) * U.step;
     const float Tl = (float)(T * P.dtpow[lane]);
-    const int slot = (int)(m & 63);
+    const int slot = (int)(m & 127);
     recs[slot] = rec;
     thrs[slot] = ratio_threshold(u01(a.x), Tl, P.inv_scale, P.inv_coef);
     T *= P.dtpow[32];
   };
-  // row range [st_al, st_al + len) of bead b, 16-byte aligned
-  auto row_range = [&](int b, int &st_al, int &len) {
-    const int2 r = blk[b];
-    st_al = r.x & ~3;
-    int en = (r.y + 4) & ~3;
-    if (en > U.pitch) en = U.pitch;
-    len = en - st_al;
+  // row copies up to move `upto` (exclusive), one per lane (warp 1)
+  auto issue = [&](long long upto) {
+    while (issued < upto) {
+      const int cnt = (int)min(32ll, upto - issued);
+      if (lane < cnt) {
+        const long long k = issued + lane;
+        const int b = recs[k & 127].b;
+        const int2 r = blk[b];
+        const int st = r.x & ~3;
+        const int en = min((r.y + 4) & ~3, pitch);
+        tma_row(slots + (size_t)(k & dmask) * pitch, rrow0 + (long long)b * pitch + st,
+                (uint32_t)(en - st) * 4, &bars[k & dmask]);
+      }
+      issued += cnt;
+    }
+  };
+  const bool run = U.n_mov > 0 && E0 >= 1e-6 && E0 == E0;
+  const long long cap = run ? P.cap : 0;
+  // The window starting at m0 (warp 0; the draws of [m0, m0 + kWin) are in
+  // the ring and its rows were requested): its length, whether its beads share
+  // one block, each move's geometry at the current positions, and the wait
+  // for its rows.  Slots past the length repeat move 0 (scored, unused).
+  auto plan = [&](long long m0, long long nms) {
+    const int lim = (int)max(1ll, min((long long)min(kWin, D), min(nms, cap) - m0));
+    const int b = lane < lim ? recs[(m0 + lane) & 127].b : -1 - lane;
+    bool rep = false;
+#pragma unroll
+    for (int j = 0; j < kWin; ++j) {
+      const int bj = __shfl_sync(0xffffffffu, b, j);  // every lane takes part
+      rep |= j < lane && bj == b;
+    }
+    const unsigned rm = __ballot_sync(0xffffffffu, rep && lane < lim);
+    const int L = rm ? min(lim, __ffs(rm) - 1) : lim;
+    const int ww = lane < L ? lane : 0;
+    const long long k = m0 + ww;
+    const MoveRec rec = recs[k & 127];
+    const int2 bk = blk[rec.b];
+    const int bx0 = __shfl_sync(0xffffffffu, bk.x, 0), by0 = __shfl_sync(0xffffffffu, bk.y, 0);
+    const unsigned diff = __ballot_sync(0xffffffffu, bk.x != bx0 || bk.y != by0);
+    bool late = false;
+    if (lane < kWin) {
+      const float4 o = spos[rec.b];
+      plan_s->ga[lane] = make_float4(o.x, o.y, o.z,
+                                     fmaf(rec.dx, rec.dx, fmaf(rec.dy, rec.dy, rec.dz * rec.dz)));
+      const int roff = (int)(k & dmask) * pitch - (bk.x & ~3);
+      plan_s->gb[lane] =
+          make_float4(-2.0f * rec.dx, -2.0f * rec.dy, -2.0f * rec.dz, __int_as_float(roff));
+      plan_s->bw[lane] = rec.b;
+      if (lane < L) late = !mbar_wait(&bars[k & dmask], (uint32_t)((k >> dshift) & 1));
+    }
+    const unsigned lm = __ballot_sync(0xffffffffu, late);
+    if (lane == 0) {
+      plan_s->len = L;
+      plan_s->same = diff == 0u;
+      plan_s->timeout = lm != 0u;
+    }
   };
 
-  const bool run = U.n_mov > 0 && E0 >= 1e-6 && E0 == E0;
-  long long cap = run ? P.cap : 0;
-  long long issued = 0;  // moves whose rows were requested (thread 0)
-  if (warp == 0 && cap > 0) {
-    fill(0);
-    fill(32);
-    __syncwarp();
-    if (lane == 0) {
-      const long long first = std::min((long long)D, cap);
-      for (long long k = 0; k < first; ++k) {
-        int st, len;
-        row_range(recs[k & 63].b, st, len);
-        tma_row(slots + (size_t)(k % D) * U.pitch, hrow0 + (long long)recs[k & 63].b * U.pitch + st,
-                (uint32_t)len * 4, &bars[k % D]);
-      }
-      issued = first;
+  if (warp == 1 && cap > 0) {
+    for (int f = 0; f < 4; ++f) {
+      fill(filled);
+      filled += 32;
     }
+    __syncwarp();
+    issue(min((long long)D, cap));
   }
+  __syncthreads();
+  if (warp == 0 && cap > 0) plan(0, P.window);
   __syncthreads();
 
   float e_hi = (float)E0, e_lo = (float)(E0 - (double)(float)E0);
   double E_ms = E0;
   int succ = 0, misses = 0, status = kDevOk;
   long long moves = 0, accepted = 0;
-  int prev_b = -1;
-  bool prev_acc = false;
-  float4 prev_new = make_float4(0.f, 0.f, 0.f, 0.f);
+  long long next_ms = P.window;
   bool stop = cap == 0;
+  if (!stop && plan_s->timeout) {
+    status = PMMC_ERR_TIMEOUT;
+    stop = true;
+  }
+  // corrections (w, j) are spread over the warps: thread c * cstride
+  const int cstride = nthr / (kWin * kWin);
 
   while (!stop) {
-    const long long k = moves;
-    const MoveRec rec = recs[k & 63];
-    const float thr = thrs[k & 63];
-    const int b = rec.b;
-    const int slot = (int)(k % D);
-    const bool timed_out = !mbar_wait(&bars[slot], (uint32_t)((k / D) & 1));
-    const float4 pb = (b == prev_b && prev_acc) ? prev_new : spos[b];
-    const float4 nb = make_float4(pb.x + rec.dx, pb.y + rec.dy, pb.z + rec.dz, 0.0f);
-    int st, len;
-    row_range(b, st, len);
-    const int2 r = blk[b];
-    const float *row = slots + (size_t)slot * U.pitch - st;
-    float part = 0.0f;
-    for (int i = r.x + tid; i <= r.y; i += nthr) {
-      if (abs(i - b) < U.diag || i == b) continue;
-      const float h = row[i];
-      if (h < 1e-6f) continue;
-      const float4 pi = (i == prev_b && prev_acc) ? prev_new : spos[i];
-      part += hm_delta(pi, pb, nb, h);
+    const long long m = moves;
+    const int L = plan_s->len;
+    const bool same = plan_s->same != 0;
+    MoveGeo g[kWin];
+    int roff[kWin];
+#pragma unroll
+    for (int w = 0; w < kWin; ++w) {
+      const float4 a = plan_s->ga[w], b = plan_s->gb[w];
+      g[w].ox = a.x;
+      g[w].oy = a.y;
+      g[w].oz = a.z;
+      g[w].dd = a.w;
+      g[w].mx = b.x;
+      g[w].my = b.y;
+      g[w].mz = b.z;
+      roff[w] = __float_as_int(b.w);
     }
-    part = warp_sum_f(part);
-    const int any_to = __any_sync(0xffffffffu, timed_out) ? 1 : 0;
-    if (lane == 0) {
-      partial[(k & 1) * 32 + warp] = part;
-      tflag[(k & 1) * 32 + warp] = any_to;
-    }
-    __syncthreads();
-    // every thread sees the same timeout flags (double-buffered by parity)
-    const bool block_to =
-        __any_sync(0xffffffffu, lane < nwarps && tflag[(k & 1) * 32 + lane] != 0);
-    // refill the draws of moves k+32..k+63 (their ring slots held moves
-    // k-32..k-1) and issue the copy for move k + D (slot k % D is free)
-    if (warp == 0) {
-      if ((k & 31) == 0 && k > 0) fill(k + 32);
-      __syncwarp();
-      if (lane == 0 && issued < cap && issued == k + D) {
-        const MoveRec rn = recs[issued & 63];
-        int s2, l2;
-        row_range(rn.b, s2, l2);
-        tma_row(slots + (size_t)(issued % D) * U.pitch, hrow0 + (long long)rn.b * U.pitch + s2,
-                (uint32_t)l2 * 4, &bars[issued % D]);
-        ++issued;
+    float part[kWin];
+#pragma unroll
+    for (int w = 0; w < kWin; ++w) part[w] = 0.0f;
+    if (same) {
+      const int2 r = blk[plan_s->bw[0]];
+      for (int i = r.x + tid; i <= r.y; i += nthr) {
+        const float4 pi = spos[i];
+#pragma unroll
+        for (int w = 0; w < kWin; ++w)
+          part[w] += pair_delta(pi.x, pi.y, pi.z, g[w], slots[roff[w] + i]);
+      }
+    } else {
+#pragma unroll
+      for (int w = 0; w < kWin; ++w) {
+        if (w < L) {
+          const int2 r = blk[plan_s->bw[w]];
+          for (int i = r.x + tid; i <= r.y; i += nthr) {
+            const float4 pi = spos[i];
+            part[w] += pair_delta(pi.x, pi.y, pi.z, g[w], slots[roff[w] + i]);
+          }
+        }
       }
     }
-    // every warp reduces the partials in the same order: identical decisions
-    float tot = lane < nwarps ? partial[(k & 1) * 32 + lane] : 0.0f;
-    tot = warp_sum_f(tot);
-    const float d = 2.0f * tot + (sphere_penalty(nb.x, nb.y, nb.z, P.R) -
-                                  sphere_penalty(pb.x, pb.y, pb.z, P.R));
-    const bool acc = (d <= 0.0f) || (d < e_hi * (thr - 1.0f));
-    if (acc) {
-      ff_add(e_hi, e_lo, d);
-      ++accepted;
-      ++succ;
-      if (tid == 0) spos[b] = nb;  // visible to all after the next barrier
+    // pair corrections: the (b_w, b_j) term once move j (< w) has moved
+    if (tid % cstride == 0 && tid / cstride < kWin * kWin) {
+      const int c = tid / cstride, w = c >> 3, j = c & 7;
+      float v = 0.0f;
+      if (j < w && w < L) {
+        const int bw = plan_s->bw[w], bj = plan_s->bw[j];
+        const int2 r = blk[bw];
+        if (bj >= r.x && bj <= r.y) {
+          const float4 gb = plan_s->gb[w];
+          const float rv = slots[__float_as_int(gb.w) + bj];
+          const float4 oj = plan_s->ga[j], dj = plan_s->gb[j];
+          MoveGeo gw;
+          const float4 ow = plan_s->ga[w];
+          gw.ox = ow.x;
+          gw.oy = ow.y;
+          gw.oz = ow.z;
+          gw.dd = ow.w;
+          gw.mx = gb.x;
+          gw.my = gb.y;
+          gw.mz = gb.z;
+          v = pair_delta(fmaf(-0.5f, dj.x, oj.x), fmaf(-0.5f, dj.y, oj.y),
+                         fmaf(-0.5f, dj.z, oj.z), gw, rv) -
+              pair_delta(oj.x, oj.y, oj.z, gw, rv);
+        }
+      }
+      corr[c] = v;
     }
-    if (tid == 0 && trace != nullptr && U.chain_id == 0 && k < P.trace_cap) {
-      MoveTrace tr;
-      tr.bead = b;
-      tr.accepted = acc ? 1 : 0;
-      tr.before = 0.0f;
-      tr.after = 2.0f * tot;
-      tr.dx = rec.dx;
-      tr.dy = rec.dy;
-      tr.dz = rec.dz;
-      tr.pad = d;
-      trace[k] = tr;
+#pragma unroll
+    for (int w = 0; w < kWin; ++w) {
+      const float v = warp_sum_f(part[w]);
+      if (lane == 0) partial[warp * kWin + w] = v;
     }
-    prev_b = b;
-    prev_acc = acc;
-    prev_new = nb;
-    moves = k + 1;
-    if (moves % P.window == 0) {
+    __syncthreads();
+    // ---- warp 0: decisions, draws, row copies, the next window ----
+    if (warp == 0) {
+      const int wl = lane & (kWin - 1);
+      float t = 0.0f;
+      for (int k = lane >> 3; k < nwarps; k += 4) t += partial[k * kWin + wl];
+      t += __shfl_xor_sync(0xffffffffu, t, 8);
+      t += __shfl_xor_sync(0xffffffffu, t, 16);
+      float cr[kWin];
+#pragma unroll
+      for (int j = 0; j < kWin; ++j) cr[j] = corr[wl * kWin + j];
+      const int ll = lane < L ? lane : 0;
+      const MoveRec rec = recs[(m + ll) & 127];
+      const float4 ow = spos[rec.b];
+      const float4 nw = make_float4(ow.x + rec.dx, ow.y + rec.dy, ow.z + rec.dz, 0.f);
+      const float sph =
+          P.R > 0.0f ? sphere_penalty(nw.x, nw.y, nw.z, P.R) - sphere_penalty(ow.x, ow.y, ow.z, P.R)
+                     : 0.0f;
+      const float thr = thrs[(m + ll) & 127];
+      float dloc = t;  // local change of this move given the accepted earlier ones
+      unsigned accm = 0u;
+      float pacc = 0.0f;
+#pragma unroll
+      for (int j = 0; j < kWin; ++j) {
+        if (j < L) {
+          const float dj = __shfl_sync(0xffffffffu, 2.0f * dloc + sph, j);
+          const float tj = __shfl_sync(0xffffffffu, thr, j);
+          if (dj <= 0.0f || dj < (e_hi + pacc) * (tj - 1.0f)) {
+            accm |= 1u << j;
+            pacc += dj;
+            dloc += cr[j];
+          }
+        }
+      }
+      if (lane < L && ((accm >> lane) & 1u)) spos[rec.b] = nw;
+      if (trace != nullptr && U.chain_id == 0 && lane < L && m + lane < P.trace_cap) {
+        MoveTrace tr;
+        tr.bead = rec.b;
+        tr.accepted = (accm >> lane) & 1u;
+        tr.before = 0.0f;
+        tr.after = 2.0f * dloc;
+        tr.dx = rec.dx;
+        tr.dy = rec.dy;
+        tr.dz = rec.dz;
+        tr.pad = 2.0f * dloc + sph;
+        trace[m + lane] = tr;
+      }
+      __syncwarp();
+      const long long mn = m + L;
+      if (lane == 0) {
+        plan_s->accm = accm;
+        plan_s->lend = L;
+        plan_s->pacc = pacc;
+        plan_s->timeout = 0;
+      }
+      if (mn < cap) plan(mn, mn == next_ms ? next_ms + P.window : next_ms);
+    } else if (warp == 1) {
+      // meanwhile: draws (moves below m are done, so the records of
+      // [filled - 128, filled - 96) are free when filled <= m + 64) and the
+      // row copies that the slots freed by this window can take
+      if (filled <= m + 64) {
+        fill(filled);
+        filled += 32;
+        __syncwarp();
+      }
+      issue(min(cap, m + L + D));
+    }
+    __syncthreads();
+    const unsigned accm = plan_s->accm;
+    if (accm) ff_add(e_hi, e_lo, plan_s->pacc);
+    const int na = __popc(accm);
+    accepted += na;
+    succ += na;
+    moves = m + plan_s->lend;
+    if (moves == next_ms) {
+      next_ms += P.window;
       // LooperSolver.hpp:1543-1548 (FP64)
       const double E = (double)e_hi + (double)e_lo;
       const bool miss = (E > (double)P.improvement * E_ms && succ < P.min_succ) || E < 1e-6;
@@ -360,19 +578,24 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
       succ = 0;
     }
     if (moves >= cap) stop = true;
-    if (block_to) {  // a row copy never arrived: give up on this chain
-      stop = true;
+    if (!stop && plan_s->timeout) {  // a row copy never landed: give up on this chain
       status = PMMC_ERR_TIMEOUT;
+      stop = true;
     }
   }
   __syncthreads();
   // drain copies still in flight (rows prefetched past the last move)
-  if (tid == 0) {
-    for (long long k = moves; k < issued; ++k)
-      if (!mbar_wait(&bars[k % D], (uint32_t)((k / D) & 1))) status = PMMC_ERR_TIMEOUT;
+  if (warp == 1) {
+    bool late = false;
+    for (long long k = moves + lane; k < issued; k += 32)
+      late |= !mbar_wait(&bars[k & dmask], (uint32_t)((k >> dshift) & 1));
+    const bool any_late = __any_sync(0xffffffffu, late);
+    if (lane == 0) plan_s->pad[0] = any_late ? 1 : 0;
   }
   __syncthreads();
-  const double Efin = heat_full(U, spos, heat, blk, red, P.R);
+  if (plan_s->pad[0] != 0) status = PMMC_ERR_TIMEOUT;
+  __syncthreads();
+  const double Efin = heat_full(U, spos, rheat, blk, red, P.R);
   if (tid == 0) {
     ChainOut o;
     const double E = run ? (double)e_hi + (double)e_lo : 0.0;
@@ -386,7 +609,7 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
     outs[blockIdx.x] = o;
   }
   float *po = pos_out + U.out_off;
-  for (int i = tid; i < n; i += blockDim.x) {
+  for (int i = tid; i < n; i += nthr) {
     const float4 q = spos[i];
     po[3 * i] = q.x;
     po[3 * i + 1] = q.y;
@@ -487,37 +710,57 @@ extern "C" pmmc_status pmmc_heatmap_batch_anneal(pmmc_ctx *ctx, int n_units,
     dp *= (double)prm->dt_temp;
   }
   // shared memory: header + D row slots + positions
-  const size_t head = 4096;
+  const size_t head = 6144;
   const size_t pos_bytes = (size_t)max_n * (16 + 8 + 4);  // positions, blocks, movable
   const size_t row_bytes = (size_t)max_pitch * 4;
   const size_t avail = ctx->smem_optin;
   if (head + pos_bytes + 2 * row_bytes > avail)
     return fail(ctx, PMMC_ERR_INVALID, "heatmap region of %d beads does not fit shared memory", max_n);
-  int depth = (int)std::min<size_t>(16, (avail - head - pos_bytes) / row_bytes);
-  depth = std::max(2, depth);
+  // ring depth: a power of two up to 16 that fits
+  const size_t fit = (avail - head - pos_bytes) / row_bytes;
+  int depth = 2;
+  while (depth < 16 && (size_t)depth * 2 <= fit) depth *= 2;
   P.depth = depth;
   const size_t smem = head + (size_t)depth * row_bytes + pos_bytes;
 
   cudaStream_t s = ctx->stream;
-  // the heatmaps, rows padded to a 16-byte pitch
-  std::vector<float> hheat((size_t)heat_floats, 0.0f);
-  for (int u = 0; u < n_units; ++u) {
-    const HeatUnit &U = hu[u];
-    const pmmc_heatmap_problem &pr = units[u];
-    for (int i = 0; i < pr.n; ++i)
-      memcpy(&hheat[(size_t)U.heat_off + (size_t)i * U.pitch], pr.heat + (size_t)i * pr.n,
-             sizeof(float) * pr.n);
+  // The kernels read r = 1/h, rows padded to a 16-byte pitch, with r = 0
+  // wherever the reference skips the pair: h < 1e-6, |i - m| < diag, i == m,
+  // and i outside bead m's chromosome block (LooperSolver.hpp:3597-3611).
+  std::vector<float> hrheat((size_t)heat_floats, 0.0f);
+  {
+    auto pack = [&](int u) {
+      const HeatUnit &U = hu[u];
+      const pmmc_heatmap_problem &pr = units[u];
+      for (int m = 0; m < pr.n; ++m) {
+        const int2 b = hblk[(size_t)U.blk_off + m];
+        const float *src = pr.heat + (size_t)m * pr.n;
+        float *dst = &hrheat[(size_t)U.heat_off + (size_t)m * U.pitch];
+        for (int i = b.x; i <= b.y; ++i) {
+          const float h = src[i];
+          if (std::abs(i - m) >= U.diag && i != m && h >= 1e-6f) dst[i] = 1.0f / h;
+        }
+      }
+    };
+    const int nt = (int)std::max(1u, std::min<unsigned>(std::thread::hardware_concurrency(), 32u));
+    std::vector<std::thread> pool;
+    std::atomic<int> next{0};
+    for (int t = 0; t < std::min(nt, n_units); ++t)
+      pool.emplace_back([&] {
+        for (int u = next++; u < n_units; u = next++) pack(u);
+      });
+    for (auto &th : pool) th.join();
   }
   DevBuf<HeatUnit> d_units;
   DevBuf<float4> d_pos;
-  DevBuf<float> d_heat, d_out;
+  DevBuf<float> d_rheat, d_out;
   DevBuf<int> d_mov;
   DevBuf<int2> d_blk;
   DevBuf<ChainOut> d_outs;
   DevBuf<MoveTrace> d_trace;
   cudaError_t e = d_units.upload(hu, s);
   if (e == cudaSuccess) e = d_pos.upload(hpos, s);
-  if (e == cudaSuccess) e = d_heat.upload(hheat, s);
+  if (e == cudaSuccess) e = d_rheat.upload(hrheat, s);
   if (e == cudaSuccess) e = d_mov.upload(hmov, s);
   if (e == cudaSuccess) e = d_blk.upload(hblk, s);
   if (e == cudaSuccess) e = d_out.alloc((size_t)out_off);
@@ -536,7 +779,7 @@ extern "C" pmmc_status pmmc_heatmap_batch_anneal(pmmc_ctx *ctx, int n_units,
   int threads = 128;
   while (threads < kHeatMaxThreads && threads * 4 < max_n) threads *= 2;
   heatmap_anneal_kernel<<<n_units, threads, smem, s>>>(
-      d_units.p, d_pos.p, d_heat.p, d_mov.p, d_blk.p, P, d_out.p, d_outs.p,
+      d_units.p, d_pos.p, d_rheat.p, d_mov.p, d_blk.p, P, d_out.p, d_outs.p,
       trace_cap > 0 ? d_trace.p : nullptr);
   e = cudaGetLastError();
   cudaEventRecord(e1, s);
