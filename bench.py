@@ -98,6 +98,92 @@ def cpu_sample(budget_s: float = 20.0):
             "cores": cores, "moves_per_s": moves / wall}
 
 
+def _cpu_request(args):
+    k, n = args
+    from oracle import oracle as O
+    from pmmc_gb300 import workloads as W
+    r = W.serve_region(k, n)
+    pr = O.ArcsProblem(r.pos, r.dense())
+    t = time.perf_counter()
+    prm = {k_: v for k_, v in W.SERVE_ANNEAL.items() if k_ != "resync_every"}
+    _, res = O.arcs_anneal(pr, O.Params(**prm), W.SERVE_STEP, W.serve_seed(k))
+    return k, n, res.moves, time.perf_counter() - t
+
+
+def cpu_serve_baseline(n_req: int, budget_s: float = 20.0):
+    """The reference CPU annealer (oracle port) behind the same trace: a
+    bounded sample of the trace's requests is annealed on every host core,
+    service time is fitted as a + b*n over the sample, and a FIFO queue with
+    one server per core replays the whole trace (arrivals, sizes) with those
+    service times.  Returns latency percentiles and capacity."""
+    import heapq
+    from oracle import oracle as O
+    from pmmc_gb300 import workloads as W
+    O.build()
+    cores = os.cpu_count() or 1
+    sizes, arrivals = W.serve_trace(n_req)
+    rng = np.random.default_rng(5)
+    idx = rng.permutation(n_req)[:max(4 * cores, 32)]
+    jobs = [(int(k), int(sizes[k])) for k in idx]
+    ctx = mp.get_context("spawn")
+    t0 = time.perf_counter()
+    samp = []
+    with ctx.Pool(cores) as pool:
+        for out in pool.imap_unordered(_cpu_request, jobs):
+            samp.append(out)
+            if time.perf_counter() - t0 > budget_s and len(samp) >= 8:
+                pool.terminate()
+                break
+    ns = np.array([x[1] for x in samp], float)
+    ts = np.array([x[3] for x in samp], float)
+    mv = np.array([x[2] for x in samp], float)
+    b, a = np.polyfit(ns, ts, 1) if len(set(ns)) > 1 else (0.0, float(ts.mean()))
+    service = np.maximum(a + b * sizes, 1e-4)
+    free = [0.0] * cores
+    heapq.heapify(free)
+    lat = np.empty(n_req)
+    for k in range(n_req):
+        f = heapq.heappop(free)
+        start = max(f, arrivals[k])
+        done = start + service[k]
+        heapq.heappush(free, done)
+        lat[k] = (done - arrivals[k]) * 1e3
+    return {"value": cores / float(service.mean()), "unit": "structures/s", "cores": cores,
+            "kind": "port",
+            "sample": f"{len(samp)} of the trace's requests annealed by the oracle port on "
+                      f"{cores} cores ({float(ts.sum()):.1f} CPU s), service time fitted "
+                      f"a + b*n, FIFO queue of {cores} servers replayed over the trace",
+            "moves_per_s_per_core": float(mv.sum() / ts.sum()),
+            "latency_ms_p50_at_200rps": float(np.percentile(lat, 50)),
+            "latency_ms_p99_at_200rps": float(np.percentile(lat, 99))}
+
+
+def serve_main(args):
+    from pmmc_gb300 import workloads as W
+    n_req = args.requests or 5000
+    if args.impl == "reference":
+        if int(os.environ.get("RANK", "0")) != 0:
+            return
+        cb = cpu_serve_baseline(n_req, args.cpu_budget)
+        line = {"metric": "structures/s", "value": cb["value"], "unit": "structures/s",
+                "n_gpus": 0, "steps": 1, "warmup": 0, "ms_per_step": None,
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                "dtype": "f64", "data": "synthetic", "impl": "reference",
+                "config": {"workload": "serve", "requests": n_req},
+                "cpu_baseline": cb,
+                "e2e": {"value": cb["value"], "unit": "structures/s",
+                        "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line))
+        return
+    sampler = ClockSampler(0)
+    sampler.start()
+    line = W.serve(args)
+    line["clocks"] = sampler.stop()
+    line["gpu_launches"] = line["saturated"]["waves"]
+    line["cpu_baseline"] = cpu_serve_baseline(n_req, args.cpu_budget)
+    print(json.dumps(line))
+
+
 # --------------------------------------------------------------------------
 # GPU helpers
 # --------------------------------------------------------------------------
@@ -312,15 +398,19 @@ def main():
     ap.add_argument("--milestone", type=int, default=ANNEAL["milestone_steps"],
                     help="milestone interval (smaller for profiling runs)")
     ap.add_argument("--workload", default="ensemble",
-                    choices=["ensemble", "heatmap", "heatmap-batch", "smooth"],
+                    choices=["ensemble", "heatmap", "heatmap-batch", "smooth", "serve"],
                     help="ensemble: the batched arc-level ensemble (default line); "
                          "heatmap: one 2048-bead heatmap chain; heatmap-batch: one chain "
                          "per distinct 2048-bead map, one per SM; smooth: genome-scale "
-                         "subanchor smoothing")
+                         "subanchor smoothing; serve: the request loop on a Poisson trace")
     ap.add_argument("--maps", type=int, default=0, help="heatmap-batch: number of maps")
     ap.add_argument("--moves", type=int, default=0, help="moves per chain (heatmap/smooth)")
+    ap.add_argument("--requests", type=int, default=0, help="serve: requests in the trace")
     args = ap.parse_args()
     set_workload(args.structures, args.milestone)
+    if args.workload == "serve":
+        serve_main(args)
+        return
     if args.workload != "ensemble":
         from pmmc_gb300 import workloads
         workloads.main(args)

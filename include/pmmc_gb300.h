@@ -318,6 +318,53 @@ pmmc_status pmmc_arcs_anneal_noalloc(const pmmc_arcs_problem *pr,
                                      float *pos_out, pmmc_result *res,
                                      void *stream);
 
+/* ---------------- request loop (continuous batching) ------------------ */
+/* Replaces running region reconstructions one after another under the
+ * reference's memory budget (-M, Settings::maxMemoryMB, checked by
+ * checkMemoryBudget in the ensemble loop, apps/pMMC-reconstruct/
+ * main_reconstruct.cpp:423, src/main.cpp:2018-2019).  A server accepts
+ * arc-level regions from any host thread; a scheduler thread admits them in
+ * arrival order as launch slots and device memory (budget_bytes, counted on
+ * the device bytes of every resident region) free up, launches each admitted
+ * wave as one persistent kernel on its own stream, and overlaps up to
+ * max_waves waves on the device.  Every region anneals with the server's
+ * parameters, its own step size and its own Philox key (seed, chain 0): its
+ * result does not depend on the other regions in flight. */
+typedef struct pmmc_server pmmc_server;
+
+typedef struct {
+  size_t budget_bytes;    /* device bytes of resident regions; 0 = half the free memory */
+  int max_waves;          /* launches in flight at once; 0 = 8 */
+  int max_wave_requests;  /* regions per launch; 0 = 4 x SM count */
+  int lanes_per_chain;    /* 2, 4, 8 or 32 lanes per proposal; 0 = 2 */
+} pmmc_server_opts;
+
+typedef struct {
+  long long submitted, completed, rejected, failed, waves, queued;
+  long long bytes_in_use, bytes_peak, budget_bytes;
+  int running_peak;       /* most regions resident at once */
+  int waves_peak;         /* most launches in flight at once */
+} pmmc_server_stats;
+
+pmmc_status pmmc_server_create(pmmc_ctx *ctx, const pmmc_anneal_params *prm,
+                               const pmmc_server_opts *opts, pmmc_server **out);
+/* Queues one region (host arrays, copied before the call returns).
+ * PMMC_ERR_BUDGET if the region alone needs more device bytes than the
+ * budget. */
+pmmc_status pmmc_server_submit(pmmc_server *sv, const pmmc_arcs_problem *pr,
+                               float step_size, uint64_t seed, long long *ticket);
+/* done = 1 once the region's result is ready. */
+pmmc_status pmmc_server_poll(pmmc_server *sv, long long ticket, int *done);
+/* Blocks up to timeout_ms (< 0: no limit) for the result; on success the
+ * ticket is released.  pos_out receives n*3 floats; latency_ms the time from
+ * submit to the result landing in host memory.  PMMC_ERR_TIMEOUT leaves the
+ * request queued. */
+pmmc_status pmmc_server_wait(pmmc_server *sv, long long ticket, int timeout_ms,
+                             float *pos_out, pmmc_result *res, double *latency_ms);
+pmmc_status pmmc_server_get_stats(pmmc_server *sv, pmmc_server_stats *st);
+/* Finishes every queued and running region, then frees the server. */
+void pmmc_server_destroy(pmmc_server *sv);
+
 #ifdef __cplusplus
 }
 #endif

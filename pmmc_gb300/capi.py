@@ -39,6 +39,8 @@ HEADER_SYMBOLS = [
     "pmmc_arcs_batch_stats", "pmmc_arcs_batch_destroy", "pmmc_arcs_batch_anneal",
     "pmmc_arcs_batch_create_ex", "pmmc_arcs_batch_trace", "pmmc_smooth_batch_anneal",
     "pmmc_heatmap_batch_anneal", "pmmc_arcs_anneal_noalloc",
+    "pmmc_server_create", "pmmc_server_submit", "pmmc_server_poll", "pmmc_server_wait",
+    "pmmc_server_get_stats", "pmmc_server_destroy",
 ]
 
 
@@ -101,6 +103,23 @@ class BatchOpts(C.Structure):
                 ("lanes_per_chain", C.c_int)]
 
 
+class ServerOpts(C.Structure):
+    _fields_ = [("budget_bytes", C.c_size_t), ("max_waves", C.c_int),
+                ("max_wave_requests", C.c_int), ("lanes_per_chain", C.c_int)]
+
+
+class ServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_longlong), ("completed", C.c_longlong),
+                ("rejected", C.c_longlong), ("failed", C.c_longlong),
+                ("waves", C.c_longlong), ("queued", C.c_longlong),
+                ("bytes_in_use", C.c_longlong), ("bytes_peak", C.c_longlong),
+                ("budget_bytes", C.c_longlong), ("running_peak", C.c_int),
+                ("waves_peak", C.c_int)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
 class MoveTrace(C.Structure):
     _fields_ = [("bead", C.c_int), ("accepted", C.c_int), ("before", C.c_float),
                 ("after", C.c_float), ("dx", C.c_float), ("dy", C.c_float),
@@ -131,6 +150,16 @@ def lib():
         L.pmmc_set_seed.argtypes = [C.c_void_p, C.c_uint64]
         L.pmmc_sm_count.argtypes = [C.c_void_p]
         L.pmmc_arcs_batch_destroy.argtypes = [C.c_void_p]
+        L.pmmc_server_create.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p,
+                                         C.POINTER(C.c_void_p)]
+        L.pmmc_server_submit.argtypes = [C.c_void_p, C.c_void_p, C.c_float, C.c_uint64,
+                                         C.POINTER(C.c_longlong)]
+        L.pmmc_server_poll.argtypes = [C.c_void_p, C.c_longlong, C.POINTER(C.c_int)]
+        L.pmmc_server_wait.argtypes = [C.c_void_p, C.c_longlong, C.c_int, C.c_void_p,
+                                       C.c_void_p, C.POINTER(C.c_double)]
+        L.pmmc_server_get_stats.argtypes = [C.c_void_p, C.c_void_p]
+        L.pmmc_server_destroy.argtypes = [C.c_void_p]
+        L.pmmc_server_destroy.restype = None
         _lib = L
     return _lib
 
@@ -307,6 +336,61 @@ def arcs_anneal(ctx: Context, inp: ArcsInput, params: AnnealParams, step: float,
     ctx.check(lib().pmmc_arcs_anneal(ctx.h, C.byref(s), C.byref(params), C.c_float(step),
                                      int(n_chains), _p(pos), C.byref(res)))
     return pos, res
+
+
+class Server:
+    """Request loop over arc-level regions (pmmc_server_*): submit from any
+    thread, results come back per ticket with their latency."""
+
+    def __init__(self, ctx: Context, params: AnnealParams, budget_bytes: int = 0,
+                 max_waves: int = 0, max_wave_requests: int = 0, lanes: int = 0):
+        self.ctx = ctx
+        self.params = params
+        opts = ServerOpts(int(budget_bytes), int(max_waves), int(max_wave_requests), int(lanes))
+        h = C.c_void_p()
+        ctx.check(lib().pmmc_server_create(ctx.h, C.byref(params), C.byref(opts), C.byref(h)))
+        self.h = h
+        self._n = {}
+
+    def submit(self, inp: ArcsInput, step: float, seed: int) -> int:
+        s = inp.struct()
+        t = C.c_longlong()
+        self.ctx.check(lib().pmmc_server_submit(self.h, C.byref(s), C.c_float(step),
+                                                C.c_uint64(int(seed) & (2**64 - 1)),
+                                                C.byref(t)))
+        self._n[t.value] = inp.n
+        return t.value
+
+    def poll(self, ticket: int) -> bool:
+        d = C.c_int()
+        self.ctx.check(lib().pmmc_server_poll(self.h, C.c_longlong(ticket), C.byref(d)))
+        return bool(d.value)
+
+    def wait(self, ticket: int, timeout_ms: int = -1):
+        """(positions, Result, latency_ms) of a finished request."""
+        pos = np.zeros((self._n.get(ticket, 0), 3), np.float32)
+        res = Result()
+        lat = C.c_double()
+        self.ctx.check(lib().pmmc_server_wait(self.h, C.c_longlong(ticket), int(timeout_ms),
+                                              _p(pos), C.byref(res), C.byref(lat)))
+        self._n.pop(ticket, None)
+        return pos, res, lat.value
+
+    def stats(self) -> dict:
+        st = ServerStats()
+        self.ctx.check(lib().pmmc_server_get_stats(self.h, C.byref(st)))
+        return st.as_dict()
+
+    def close(self):
+        if self.h:
+            lib().pmmc_server_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
 
 
 class SmoothInput:

@@ -35,59 +35,10 @@
 #include <numeric>
 #include <vector>
 
-#include "common.cuh"
-#include "internal.h"
+#include "arcs_impl.h"
 
 namespace pmmc {
 
-struct ArcsUnit {
-  int n;          // beads
-  int n_mov;      // movable beads
-  int pos_off;    // float4 index into pos0
-  int rp_off;     // index into row_ptr (n+1 entries, unit-relative values)
-  int nbr_off;    // index into nbr / inv_t (spring entries, target >= 1e-6)
-  int nnz;
-  int mov_off;    // index into movable, -1 = all beads movable
-  int lrp_off;    // index into loop row_ptr (n+1), -1 = no loops
-  int lent_off;   // index into loop entries
-  int n_lent;
-  int lst_off;    // index into the loop list (one entry per constraint)
-  int n_loops;
-  int null_off;   // index into the listed-but-inert pairs (0 <= target < 1e-6)
-  int n_null;
-  int chains;
-  int chain_base; // global chain id of the unit's chain 0
-  long long out_off;  // float index of chain 0's xyz output
-  float step;
-  int pad;
-};
-
-struct ArcsDevParams {
-  float max_temp;
-  float inv_scale;
-  float inv_coef;
-  float improvement;
-  float k_stretch;
-  float k_squeeze;
-  float sphere_r;
-  int min_successes;
-  int window;      // milestone window (moves)
-  int fails;       // consecutive misses that stop a chain
-  int resync;      // FP64 recompute interval (0 = off)
-  int use2d;
-  int stop_all;    // the first converged chain stops the unit's others
-  int trace_cap;
-  long long cap;   // hard move cap
-  int cap_is_error;
-  int pad;
-  uint64_t seed;
-  float dtpow[33];  // dt^l, l = 0..32
-};
-
-// per-warp scratch: 32 drawn moves (int4) + their ratio thresholds, and the
-// window's per-slot delta, conflict mask and (tracing) local scores
-constexpr int kMoveBufBytes = 32 * 16 + 32 * 4 + 4 * 32 * 4;
-constexpr int kCtaHeader = 256;                    // dt^l table shared by the CTA
 
 __device__ __forceinline__ float dist3(float ax, float ay, float az, float4 b) {
   const float x = ax - b.x, y = ay - b.y, z = az - b.z;
@@ -270,7 +221,7 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
     const ArcsUnit U = units[it.x];
     const int chain = it.y;
     const int n = U.n;
-    const uint32_t chain_id = (uint32_t)(U.chain_base + chain);
+    const uint32_t chain_id = (uint32_t)(U.rng_chain + chain);
     int *done_flag = done + it.x;
 
     // ---- stage the region in this warp's shared-memory slice ----
@@ -334,8 +285,8 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
     long long bm = 0;          // first move held by the draw buffer
     auto refill = [&](long long first) {
       const uint64_t m = (uint64_t)first + lane;
-      const uint4 r = philox_move(P.seed, chain_id, m, 0u);
-      const uint4 a = philox_move(P.seed, chain_id, m, 1u);
+      const uint4 r = philox_move(U.seed, chain_id, m, 0u);
+      const uint4 a = philox_move(U.seed, chain_id, m, 1u);
       const int k = uniform_index(r.x, U.n_mov);
       const int b = MOV ? MOV[k] : k;
       const float dx = (2.0f * u01(r.y) - 1.0f) * step;
@@ -658,9 +609,9 @@ struct pmmc_arcs_batch {
   }
 };
 
-namespace {
+namespace pmmc {
 
-size_t unit_smem(int n, int nnz, int n_mov, bool has_mov) {
+size_t arcs_unit_smem(int n, int nnz, int n_mov, bool has_mov) {
   size_t s = (size_t)kMoveBufBytes + (size_t)n * 16 + (size_t)(n + 1) * 4;
   s = (s + 7) & ~(size_t)7;
   s += (size_t)nnz * 12;
@@ -668,12 +619,12 @@ size_t unit_smem(int n, int nnz, int n_mov, bool has_mov) {
   return s;
 }
 
-size_t unit_smem_min(int n) {
+size_t arcs_unit_smem_min(int n) {
   size_t s = (size_t)kMoveBufBytes + (size_t)n * 16 + (size_t)(n + 1) * 4;
   return (s + 7) & ~(size_t)7;
 }
 
-pmmc_status validate_arcs(pmmc_ctx *ctx, const pmmc_arcs_problem *pr) {
+pmmc_status arcs_validate(pmmc_ctx *ctx, const pmmc_arcs_problem *pr) {
   if (!pr || pr->n < 1 || !pr->pos || !pr->row_ptr)
     return fail(ctx, PMMC_ERR_INVALID, "arcs problem: n, pos and row_ptr are required");
   if (pr->row_ptr[0] != 0)
@@ -693,8 +644,7 @@ pmmc_status validate_arcs(pmmc_ctx *ctx, const pmmc_arcs_problem *pr) {
   return PMMC_OK;
 }
 
-ArcsDevParams make_params(const pmmc_anneal_params *prm, uint64_t seed,
-                          bool stop_all) {
+ArcsDevParams arcs_make_params(const pmmc_anneal_params *prm, uint64_t seed, bool stop_all) {
   ArcsDevParams P{};
   P.max_temp = prm->max_temp;
   P.inv_scale = prm->jump_scale != 0.0f ? 1.0f / prm->jump_scale : 0.0f;
@@ -730,7 +680,159 @@ ArcsDevParams make_params(const pmmc_anneal_params *prm, uint64_t seed,
   return P;
 }
 
-}  // namespace
+void ArcsPack::add(const pmmc_arcs_problem &pr, int n_chains, float step, uint64_t seed,
+                   int rng_chain) {
+  ArcsUnit U{};
+  U.n = pr.n;
+  U.pos_off = (int)pos.size();
+  for (int i = 0; i < pr.n; ++i)
+    pos.push_back(make_float4(pr.pos[3 * i], pr.pos[3 * i + 1], pr.pos[3 * i + 2], 0.0f));
+  // spring entries (target >= 1e-6) with 1/target; listed pairs with
+  // 0 <= target < 1e-6 are inert and only leave the repulsion sum
+  U.rp_off = (int)rp.size();
+  U.nbr_off = (int)nbr.size();
+  U.null_off = (int)nulls.size();
+  int cnt = 0;
+  rp.push_back(0);
+  for (int i = 0; i < pr.n; ++i) {
+    for (int e = pr.row_ptr[i]; e < pr.row_ptr[i + 1]; ++e) {
+      const float t = pr.target[e];
+      if (pr.col[e] == i) continue;  // the reference never pairs a bead with itself
+      if (t >= 1e-6f) {
+        int2 v;
+        v.x = pr.col[e];
+        v.y = __float_as_int_host(t);
+        nbr.push_back(v);
+        inv.push_back(1.0f / t);
+        ++cnt;
+      } else if (t >= 0.0f && pr.col[e] < i) {
+        nulls.push_back(make_int2(pr.col[e], i));
+      }
+    }
+    rp.push_back(cnt);
+  }
+  U.nnz = cnt;
+  U.n_null = (int)nulls.size() - U.null_off;
+  std::vector<int> mv;
+  for (int i = 0; i < pr.n; ++i)
+    if (!pr.fixed || !pr.fixed[i]) mv.push_back(i);
+  U.n_mov = (int)mv.size();
+  if (U.n_mov < pr.n) {
+    U.mov_off = (int)mov.size();
+    mov.insert(mov.end(), mv.begin(), mv.end());
+  } else {
+    U.mov_off = -1;
+  }
+  // loop constraints: rebuildActiveLoopMap (LooperSolver.hpp:3318-3337):
+  // key (min,max), the last constraint of a key wins, std::map order.
+  std::map<std::pair<int, int>, int> lm;
+  for (int c = 0; c < pr.n_loops; ++c) {
+    int i = pr.loop_i[c], j = pr.loop_j[c];
+    if (i < 0 || j < 0 || i >= pr.n || j >= pr.n) continue;
+    lm[i < j ? std::make_pair(i, j) : std::make_pair(j, i)] = c;
+  }
+  U.lst_off = (int)lst.size();
+  U.n_loops = (int)lm.size();
+  if (!lm.empty()) {
+    std::vector<std::vector<float4>> per(pr.n);
+    for (auto &kv : lm) {
+      const int c = kv.second, i = kv.first.first, j = kv.first.second;
+      int4 L;
+      L.x = i;
+      L.y = j;
+      L.z = __float_as_int_host(pr.loop_k[c]);
+      L.w = __float_as_int_host(pr.loop_r0[c]);
+      lst.push_back(L);
+      per[i].push_back(make_float4(__int_as_float_host(j), pr.loop_k[c], pr.loop_r0[c], 0.0f));
+      if (j != i)
+        per[j].push_back(make_float4(__int_as_float_host(i), pr.loop_k[c], pr.loop_r0[c], 0.0f));
+    }
+    U.lrp_off = (int)lrp.size();
+    U.lent_off = (int)lent.size();
+    int acc = 0;
+    for (int i = 0; i < pr.n; ++i) {
+      lrp.push_back(acc);
+      for (auto &e : per[i]) lent.push_back(e);
+      acc += (int)per[i].size();
+    }
+    lrp.push_back(acc);
+    U.n_lent = acc;
+  } else {
+    U.lrp_off = -1;
+    U.lent_off = 0;
+    U.n_lent = 0;
+  }
+  U.chains = n_chains;
+  U.chain_base = chains;
+  U.out_off = out_floats;
+  U.step = step;
+  U.rng_chain = rng_chain;
+  U.seed = seed;
+  chains += n_chains;
+  out_floats += (long long)n_chains * pr.n * 3;
+  units.push_back(U);
+}
+
+void ArcsPack::append(const ArcsPack &o) {
+  const int pos0 = (int)pos.size(), rp0 = (int)rp.size(), nbr0 = (int)nbr.size();
+  const int null0 = (int)nulls.size(), mov0 = (int)mov.size(), lrp0 = (int)lrp.size();
+  const int lent0 = (int)lent.size(), lst0 = (int)lst.size();
+  for (ArcsUnit U : o.units) {
+    U.pos_off += pos0;
+    U.rp_off += rp0;
+    U.nbr_off += nbr0;
+    U.null_off += null0;
+    if (U.mov_off >= 0) U.mov_off += mov0;
+    if (U.lrp_off >= 0) U.lrp_off += lrp0;
+    U.lent_off += lent0;
+    U.lst_off += lst0;
+    U.chain_base += chains;
+    U.out_off += out_floats;
+    units.push_back(U);
+  }
+  pos.insert(pos.end(), o.pos.begin(), o.pos.end());
+  rp.insert(rp.end(), o.rp.begin(), o.rp.end());
+  mov.insert(mov.end(), o.mov.begin(), o.mov.end());
+  lrp.insert(lrp.end(), o.lrp.begin(), o.lrp.end());
+  nbr.insert(nbr.end(), o.nbr.begin(), o.nbr.end());
+  nulls.insert(nulls.end(), o.nulls.begin(), o.nulls.end());
+  inv.insert(inv.end(), o.inv.begin(), o.inv.end());
+  lent.insert(lent.end(), o.lent.begin(), o.lent.end());
+  lst.insert(lst.end(), o.lst.begin(), o.lst.end());
+  chains += o.chains;
+  out_floats += o.out_floats;
+}
+
+void ArcsPack::finish() {
+  if (lst.empty()) lst.push_back(make_int4(0, 0, 0, 0));
+  if (nulls.empty()) nulls.push_back(make_int2(0, 0));
+}
+
+cudaError_t arcs_launch(const ArcsLaunch &a, const ArcsDevParams &P, bool nb_smem, int lanes,
+                        int grid, int warps, int smem_per_warp, cudaStream_t s) {
+  const size_t dyn = kCtaHeader + (size_t)warps * smem_per_warp;
+  arcs_kernel_for(nb_smem, lanes)<<<grid, 32 * warps, dyn, s>>>(
+      a.units, a.items, a.n_items, a.head, a.pos0, a.row_ptr, a.nbr, a.inv_t, a.movable, a.lrp,
+      a.lent, a.lst, a.nulls, P, smem_per_warp, a.pos_out, a.outs, a.done, a.trace);
+  return cudaGetLastError();
+}
+
+int arcs_ctas_per_sm(bool nb_smem, int lanes, int warps, int smem_per_warp) {
+  int per_sm = 0;
+  const size_t dyn = kCtaHeader + (size_t)warps * smem_per_warp;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, arcs_kernel_for(nb_smem, lanes),
+                                                32 * warps, dyn);
+  return per_sm < 1 ? 1 : per_sm;
+}
+
+void arcs_set_smem_limit(int bytes) {
+  for (int lanes : {2, 4, 8, 32})
+    for (bool nbs : {true, false})
+      cudaFuncSetAttribute(arcs_kernel_for(nbs, lanes),
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+}
+
+}  // namespace pmmc
 
 extern "C" pmmc_status pmmc_arcs_batch_create_ex(
     pmmc_ctx *ctx, int n_units, const pmmc_arcs_problem *units,
@@ -742,124 +844,28 @@ extern "C" pmmc_status pmmc_arcs_batch_create_ex(
   *out = nullptr;
   const int chains = opts && opts->chains_per_unit > 0 ? opts->chains_per_unit : 1;
   for (int u = 0; u < n_units; ++u) {
-    pmmc_status s = validate_arcs(ctx, &units[u]);
+    pmmc_status s = arcs_validate(ctx, &units[u]);
     if (s != PMMC_OK) return s;
   }
   auto *b = new pmmc_arcs_batch();
   b->ctx = ctx;
   b->n_units = n_units;
   b->use_graph = !opts || opts->use_graph != 0;
-  b->P = make_params(prm, next_key(ctx), stop_all != 0);
+  b->P = arcs_make_params(prm, next_key(ctx), stop_all != 0);
   b->P.trace_cap = trace_cap;
 
   // ---- pack host arrays ----
-  std::vector<float4> h_pos;
-  std::vector<int> h_rp, h_mov, h_lrp;
-  std::vector<int2> h_nbr, h_null;
-  std::vector<float> h_inv;
-  std::vector<float4> h_lent;
-  std::vector<int4> h_lst;
-  b->h_units.resize(n_units);
+  ArcsPack pk;
+  for (int u = 0; u < n_units; ++u)
+    pk.add(units[u], chains, steps[u], b->P.seed, pk.chains);
+  pk.finish();
+  b->h_units = pk.units;
   b->h_n.resize(n_units);
-  long long out_off = 0;
-  int chain_base = 0;
-  for (int u = 0; u < n_units; ++u) {
-    const pmmc_arcs_problem &pr = units[u];
-    ArcsUnit U{};
-    U.n = pr.n;
-    U.pos_off = (int)h_pos.size();
-    for (int i = 0; i < pr.n; ++i)
-      h_pos.push_back(make_float4(pr.pos[3 * i], pr.pos[3 * i + 1], pr.pos[3 * i + 2], 0.0f));
-    // spring entries (target >= 1e-6) with 1/target; listed pairs with
-    // 0 <= target < 1e-6 are inert and only leave the repulsion sum
-    U.rp_off = (int)h_rp.size();
-    U.nbr_off = (int)h_nbr.size();
-    U.null_off = (int)h_null.size();
-    int cnt = 0;
-    h_rp.push_back(0);
-    for (int i = 0; i < pr.n; ++i) {
-      for (int e = pr.row_ptr[i]; e < pr.row_ptr[i + 1]; ++e) {
-        const float t = pr.target[e];
-        if (pr.col[e] == i) continue;  // the reference never pairs a bead with itself
-        if (t >= 1e-6f) {
-          int2 v;
-          v.x = pr.col[e];
-          v.y = __float_as_int_host(t);
-          h_nbr.push_back(v);
-          h_inv.push_back(1.0f / t);
-          ++cnt;
-        } else if (t >= 0.0f && pr.col[e] < i) {
-          h_null.push_back(make_int2(pr.col[e], i));
-        }
-      }
-      h_rp.push_back(cnt);
-    }
-    U.nnz = cnt;
-    U.n_null = (int)h_null.size() - U.null_off;
-    int nm = 0;
-    std::vector<int> mv;
-    for (int i = 0; i < pr.n; ++i)
-      if (!pr.fixed || !pr.fixed[i]) mv.push_back(i);
-    nm = (int)mv.size();
-    U.n_mov = nm;
-    if (nm < pr.n) {
-      U.mov_off = (int)h_mov.size();
-      h_mov.insert(h_mov.end(), mv.begin(), mv.end());
-    } else {
-      U.mov_off = -1;
-    }
-    // loop constraints: rebuildActiveLoopMap (LooperSolver.hpp:3318-3337):
-    // key (min,max), the last constraint of a key wins, std::map order.
-    std::map<std::pair<int, int>, int> lm;
-    for (int c = 0; c < pr.n_loops; ++c) {
-      int i = pr.loop_i[c], j = pr.loop_j[c];
-      if (i < 0 || j < 0 || i >= pr.n || j >= pr.n) continue;
-      lm[i < j ? std::make_pair(i, j) : std::make_pair(j, i)] = c;
-    }
-    U.lst_off = (int)h_lst.size();
-    U.n_loops = (int)lm.size();
-    if (!lm.empty()) {
-      std::vector<std::vector<float4>> per(pr.n);
-      for (auto &kv : lm) {
-        const int c = kv.second, i = kv.first.first, j = kv.first.second;
-        int4 L;
-        L.x = i;
-        L.y = j;
-        L.z = __float_as_int_host(pr.loop_k[c]);
-        L.w = __float_as_int_host(pr.loop_r0[c]);
-        h_lst.push_back(L);
-        per[i].push_back(make_float4(__int_as_float_host(j), pr.loop_k[c], pr.loop_r0[c], 0.0f));
-        if (j != i)
-          per[j].push_back(make_float4(__int_as_float_host(i), pr.loop_k[c], pr.loop_r0[c], 0.0f));
-      }
-      U.lrp_off = (int)h_lrp.size();
-      U.lent_off = (int)h_lent.size();
-      int acc = 0;
-      for (int i = 0; i < pr.n; ++i) {
-        h_lrp.push_back(acc);
-        for (auto &e : per[i]) h_lent.push_back(e);
-        acc += (int)per[i].size();
-      }
-      h_lrp.push_back(acc);
-      U.n_lent = acc;
-    } else {
-      U.lrp_off = -1;
-      U.lent_off = 0;
-      U.n_lent = 0;
-    }
-    U.chains = chains;
-    U.chain_base = chain_base;
-    U.out_off = out_off;
-    U.step = steps[u];
-    chain_base += chains;
-    out_off += (long long)chains * pr.n * 3;
-    b->h_units[u] = U;
-    b->h_n[u] = pr.n;
-  }
+  for (int u = 0; u < n_units; ++u) b->h_n[u] = units[u].n;
+  const long long out_off = pk.out_floats;
+  const int chain_base = pk.chains;
   b->total_pos_out = out_off;
   b->total_chains = chain_base;
-  if (h_lst.empty()) h_lst.push_back(make_int4(0, 0, 0, 0));
-  if (h_null.empty()) h_null.push_back(make_int2(0, 0));
 
   // ---- shared-memory classes: items sorted by need, largest first ----
   // A unit whose arc lists fit next to its positions is staged whole
@@ -869,8 +875,8 @@ extern "C" pmmc_status pmmc_arcs_batch_create_ex(
   std::vector<Need> needs(n_units);
   for (int u = 0; u < n_units; ++u) {
     const ArcsUnit &U = b->h_units[u];
-    const size_t full = unit_smem(U.n, U.nnz, U.n_mov, U.mov_off >= 0);
-    const size_t minimal = unit_smem_min(U.n);
+    const size_t full = arcs_unit_smem(U.n, U.nnz, U.n_mov, U.mov_off >= 0);
+    const size_t minimal = arcs_unit_smem_min(U.n);
     if (minimal > cap_smem) {
       delete b;
       return fail(ctx, PMMC_ERR_INVALID,
@@ -887,10 +893,7 @@ extern "C" pmmc_status pmmc_arcs_batch_create_ex(
   int lanes = opts && opts->lanes_per_chain > 0 ? opts->lanes_per_chain : 2;
   if (lanes != 2 && lanes != 4 && lanes != 8 && lanes != 32) lanes = 2;
   b->lanes = lanes;
-  cudaFuncSetAttribute(arcs_kernel_for(true, lanes), cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)ctx->smem_optin);
-  cudaFuncSetAttribute(arcs_kernel_for(false, lanes), cudaFuncAttributeMaxDynamicSharedMemorySize,
-                       (int)ctx->smem_optin);
+  arcs_set_smem_limit((int)ctx->smem_optin);
   size_t i0 = 0;
   while (i0 < needs.size()) {
     const size_t top = needs[i0].bytes;
@@ -908,11 +911,7 @@ extern "C" pmmc_status pmmc_arcs_batch_create_ex(
     int w = 4;
     while (w > 1 && (size_t)w * c.smem_per_warp > cap_smem) w >>= 1;
     c.warps_per_cta = w;
-    int per_sm = 0;
-    const size_t dyn = kCtaHeader + (size_t)w * c.smem_per_warp;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, arcs_kernel_for(nbs, lanes), 32 * w,
-                                                  dyn);
-    if (per_sm < 1) per_sm = 1;
+    const int per_sm = arcs_ctas_per_sm(nbs, lanes, w, c.smem_per_warp);
     const int items_n = c.item_end - c.item_begin;
     c.grid = std::max(1, std::min(per_sm * ctx->sm_count, (items_n + w - 1) / w));
     b->classes.push_back(c);
@@ -924,18 +923,17 @@ extern "C" pmmc_status pmmc_arcs_batch_create_ex(
   cudaError_t e = cudaSuccess;
 #define UP(buf, vec)                                                           \
   if (e == cudaSuccess) e = b->buf.upload(vec, s);
-  std::vector<ArcsUnit> hu = b->h_units;
-  UP(units, hu);
+  UP(units, pk.units);
   UP(items, h_items);
-  UP(pos0, h_pos);
-  UP(row_ptr, h_rp);
-  UP(nbr, h_nbr);
-  UP(inv_t, h_inv);
-  UP(nulls, h_null);
-  UP(movable, h_mov);
-  UP(lrp, h_lrp);
-  UP(lent, h_lent);
-  UP(lst, h_lst);
+  UP(pos0, pk.pos);
+  UP(row_ptr, pk.rp);
+  UP(nbr, pk.nbr);
+  UP(inv_t, pk.inv);
+  UP(nulls, pk.nulls);
+  UP(movable, pk.mov);
+  UP(lrp, pk.lrp);
+  UP(lent, pk.lent);
+  UP(lst, pk.lst);
 #undef UP
   if (e == cudaSuccess) e = b->heads.alloc(b->classes.size());
   if (e == cudaSuccess) e = b->pos_out.alloc((size_t)out_off);
@@ -972,13 +970,12 @@ cudaError_t enqueue_pass(pmmc_arcs_batch *b, cudaStream_t s) {
     ArcsClass &c = b->classes[k];
     e = cudaStreamWaitEvent(c.stream, b->ev_fork, 0);
     if (e != cudaSuccess) break;
-    const size_t dyn = kCtaHeader + (size_t)c.warps_per_cta * c.smem_per_warp;
-    arcs_kernel_for(c.nb_smem, b->lanes)<<<c.grid, 32 * c.warps_per_cta, dyn, c.stream>>>(
-        b->units.p, b->items.p + c.item_begin, c.item_end - c.item_begin, b->heads.p + k,
-        b->pos0.p, b->row_ptr.p, b->nbr.p, b->inv_t.p, b->movable.p, b->lrp.p, b->lent.p,
-        b->lst.p, b->nulls.p, b->P, c.smem_per_warp, b->pos_out.p, b->outs.p, b->done.p,
-        b->trace);
-    e = cudaGetLastError();
+    ArcsLaunch a{b->units.p, b->items.p + c.item_begin, c.item_end - c.item_begin,
+                 b->heads.p + k, b->pos0.p, b->row_ptr.p, b->nbr.p, b->inv_t.p, b->movable.p,
+                 b->lrp.p, b->lent.p, b->lst.p, b->nulls.p, b->pos_out.p, b->outs.p,
+                 b->done.p, b->trace};
+    e = arcs_launch(a, b->P, c.nb_smem, b->lanes, c.grid, c.warps_per_cta, c.smem_per_warp,
+                    c.stream);
     if (e == cudaSuccess) e = cudaEventRecord(c.join, c.stream);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(s, c.join, 0);
   }
@@ -1195,7 +1192,8 @@ static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoAllocS
 // list, work item and counters (the counters must start at zero).
 __global__ void noalloc_stage_kernel(NoAllocScratch *S, int n, int nnz, const float *pos,
                                      const unsigned char *fixed, const int *row_ptr,
-                                     const int *col, const float *target, float step) {
+                                     const int *col, const float *target, float step,
+                                     uint64_t seed) {
   __shared__ int s_cnt[kNoAllocMaxBeads + 1];
   __shared__ int s_mov[kNoAllocMaxBeads + 1];
   __shared__ int s_bad;
@@ -1260,6 +1258,8 @@ __global__ void noalloc_stage_kernel(NoAllocScratch *S, int n, int nnz, const fl
     U.chain_base = 0;
     U.out_off = 0;
     U.step = step;
+    U.rng_chain = 0;
+    U.seed = seed;
     S->unit = U;
     S->item = make_int2(0, 0);
     S->head = 0;
@@ -1327,12 +1327,12 @@ extern "C" pmmc_status pmmc_arcs_anneal_noalloc(const pmmc_arcs_problem *pr,
   int dev_smem = 0;
   cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   const int n = pr->n;
-  const size_t minimal = unit_smem_min(n);
-  const size_t full = unit_smem(n, nnz, n, true);
+  const size_t minimal = arcs_unit_smem_min(n);
+  const size_t full = arcs_unit_smem(n, nnz, n, true);
   const bool nbs = kCtaHeader + full <= (size_t)dev_smem;
   const size_t per_warp = ((nbs ? full : minimal) + 15) & ~(size_t)15;
   if (kCtaHeader + per_warp > (size_t)dev_smem) return PMMC_ERR_INVALID;
-  ArcsDevParams P = make_params(prm, seed, false);
+  ArcsDevParams P = arcs_make_params(prm, seed, false);
   ArcsKernelFn fn = arcs_kernel_for(nbs, 2);
   // the device's opt-in maximum, as the batched path sets it: never lower
   // the limit under a batch created earlier
@@ -1340,7 +1340,7 @@ extern "C" pmmc_status pmmc_arcs_anneal_noalloc(const pmmc_arcs_problem *pr,
       cudaSuccess)
     return PMMC_ERR_CUDA;
   noalloc_stage_kernel<<<1, 256, 0, s>>>(S, n, nnz, pr->pos, pr->fixed, pr->row_ptr, pr->col,
-                                         pr->target, step_size);
+                                         pr->target, step_size, seed);
   fn<<<1, 32, kCtaHeader + per_warp, s>>>(&S->unit, &S->item, 1, &S->head, S->pos0,
                                           S->row_ptr, S->nbr, S->inv_t, S->movable, nullptr,
                                           nullptr, S->lst, S->nulls, P, (int)per_warp, pos_out,

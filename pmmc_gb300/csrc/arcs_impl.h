@@ -1,0 +1,122 @@
+// arcs_impl.h -- arc-level annealing internals shared by the batched,
+// allocation-free and serving paths (host and device layouts, packing,
+// launch).
+#pragma once
+#include <cstdint>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "common.cuh"
+#include "internal.h"
+
+namespace pmmc {
+
+struct ArcsUnit {
+  int n;          // beads
+  int n_mov;      // movable beads
+  int pos_off;    // float4 index into pos0
+  int rp_off;     // index into row_ptr (n+1 entries, unit-relative values)
+  int nbr_off;    // index into nbr / inv_t (spring entries, target >= 1e-6)
+  int nnz;
+  int mov_off;    // index into movable, -1 = all beads movable
+  int lrp_off;    // index into loop row_ptr (n+1), -1 = no loops
+  int lent_off;   // index into loop entries
+  int n_lent;
+  int lst_off;    // index into the loop list (one entry per constraint)
+  int n_loops;
+  int null_off;   // index into the listed-but-inert pairs (0 <= target < 1e-6)
+  int n_null;
+  int chains;
+  int chain_base; // global chain id of the unit's chain 0
+  long long out_off;  // float index of chain 0's xyz output
+  float step;
+  int rng_chain;  // Philox chain id of the unit's chain 0
+  uint64_t seed;  // Philox key of the unit's chains
+};
+
+struct ArcsDevParams {
+  float max_temp;
+  float inv_scale;
+  float inv_coef;
+  float improvement;
+  float k_stretch;
+  float k_squeeze;
+  float sphere_r;
+  int min_successes;
+  int window;      // milestone window (moves)
+  int fails;       // consecutive misses that stop a chain
+  int resync;      // FP64 recompute interval (0 = off)
+  int use2d;
+  int stop_all;    // the first converged chain stops the unit's others
+  int trace_cap;
+  long long cap;   // hard move cap
+  int cap_is_error;
+  int pad;
+  uint64_t seed;   // default Philox key (each unit carries its own)
+  float dtpow[33];  // dt^l, l = 0..32
+};
+
+// per-warp scratch: 32 drawn moves (int4) + their ratio thresholds, and the
+// window's per-slot delta, conflict mask and (tracing) local scores
+constexpr int kMoveBufBytes = 32 * 16 + 32 * 4 + 4 * 32 * 4;
+constexpr int kCtaHeader = 256;                    // dt^l table shared by the CTA
+
+// Host-side packing of regions into the flat arrays the kernel reads: float4
+// positions, spring-only CSR arc lists {col, target bits} with reciprocals,
+// listed-but-inert pairs, movable list, loop-constraint lists.
+struct ArcsPack {
+  std::vector<ArcsUnit> units;
+  std::vector<float4> pos;
+  std::vector<int> rp, mov, lrp;
+  std::vector<int2> nbr, nulls;
+  std::vector<float> inv;
+  std::vector<float4> lent;
+  std::vector<int4> lst;
+  long long out_floats = 0;  // xyz floats over all chains
+  int chains = 0;            // chains over all units
+  // Appends one region with `chains` chains; Philox key `seed`, chain ids
+  // rng_chain .. rng_chain + chains - 1.  The region must be valid.
+  void add(const pmmc_arcs_problem &pr, int n_chains, float step, uint64_t seed, int rng_chain);
+  // Appends every region of another pack (offsets rebased).
+  void append(const ArcsPack &o);
+  // Placeholder entries so that no device array is empty.
+  void finish();
+};
+
+// Shared-memory bytes of one chain's slice: everything staged / positions only.
+size_t arcs_unit_smem(int n, int nnz, int n_mov, bool has_mov);
+size_t arcs_unit_smem_min(int n);
+pmmc_status arcs_validate(pmmc_ctx *ctx, const pmmc_arcs_problem *pr);
+ArcsDevParams arcs_make_params(const pmmc_anneal_params *prm, uint64_t seed, bool stop_all);
+
+// Device pointers of one persistent pass.
+struct ArcsLaunch {
+  const ArcsUnit *units;
+  const int2 *items;
+  int n_items;
+  int *head;
+  const float4 *pos0;
+  const int *row_ptr;
+  const int2 *nbr;
+  const float *inv_t;
+  const int *movable;
+  const int *lrp;
+  const float4 *lent;
+  const int4 *lst;
+  const int2 *nulls;
+  float *pos_out;
+  ChainOut *outs;
+  int *done;
+  MoveTrace *trace;
+};
+
+// One persistent pass of `grid` CTAs x `warps` warps over the items on `s`.
+cudaError_t arcs_launch(const ArcsLaunch &a, const ArcsDevParams &P, bool nb_smem, int lanes,
+                        int grid, int warps, int smem_per_warp, cudaStream_t s);
+// Resident CTAs per SM of that configuration (at least 1).
+int arcs_ctas_per_sm(bool nb_smem, int lanes, int warps, int smem_per_warp);
+// Raise the dynamic shared-memory limit of every instantiation to `bytes`.
+void arcs_set_smem_limit(int bytes);
+
+}  // namespace pmmc

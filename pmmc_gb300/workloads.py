@@ -11,6 +11,12 @@ heatmap-batch  one chain per distinct 2048-bead map (16 MB each; the
 smooth         genome-scale smoothing: 23 chromosomes (~300k beads, anchors
                every Poisson(10) beads, fixed), split at the anchors into
                independent regions; 20k sweeps (moves = 20k x free beads).
+serve          request loop: 5000 arc-level regions, sizes round(exp U[ln 64,
+               ln 8192]), 1.5625 arcs per bead (400 per 256 beads), Poisson
+               arrivals at 200 requests/s (seed 11), 20k moves each, device
+               budget 40 GiB.  Replayed open-loop at the trace's arrival times
+               (latency p50/p99) and saturated (all requests at once:
+               structures/s and moves/s).
 """
 from __future__ import annotations
 
@@ -128,6 +134,112 @@ def _smooth_run(ctx, segs, prm, sweeps):
             res_all[i] = res[j]
             out_all[i] = out[j]
     return out_all, res_all, ms_total
+
+
+SERVE_ANNEAL = dict(max_temp=5.0, dt_temp=0.9999, milestone_steps=20_000, improvement=0.99,
+                    max_moves=20_000, resync_every=1000)
+SERVE_STEP = 0.5
+SERVE_BUDGET = 40 << 30
+
+
+def serve_trace(n_req: int = 5000, rate: float = 200.0, seed: int = 11,
+                lo: int = 64, hi: int = 8192):
+    """Region sizes and arrival times (s) of the serving trace."""
+    rng = np.random.default_rng(seed)
+    sizes = np.rint(np.exp(rng.uniform(np.log(lo), np.log(hi), n_req))).astype(int)
+    gaps = rng.exponential(1.0 / rate, n_req)
+    arrivals = np.cumsum(gaps) - gaps[0]
+    return sizes, arrivals
+
+
+def serve_region(k: int, n: int, seed: int = 11):
+    return synth.arcs_region(int(n), int(round(1.5625 * n)), seed=seed * 100_000 + k)
+
+
+def serve_seed(k: int) -> int:
+    return 11_000 + k
+
+
+def _serve_pass(ctx, prm, inputs, arrivals):
+    """One pass through a fresh server; arrivals None = all at once.
+    Returns (latencies ms, moves, wall s, stats, max rel error)."""
+    import queue
+    import threading
+    sv = capi.Server(ctx, prm, budget_bytes=SERVE_BUDGET)
+    q = queue.Queue()
+    t0 = time.perf_counter()
+
+    def produce():
+        for k, inp in enumerate(inputs):
+            if arrivals is not None:
+                dt = t0 + arrivals[k] - time.perf_counter()
+                if dt > 0:
+                    time.sleep(dt)
+            q.put(sv.submit(inp, SERVE_STEP, serve_seed(k)))
+        q.put(None)
+
+    th = threading.Thread(target=produce)
+    th.start()
+    lat, moves, err = [], 0, 0.0
+    while True:
+        t = q.get()
+        if t is None:
+            break
+        _, res, ms = sv.wait(t)
+        lat.append(ms)
+        moves += res.moves
+        err = max(err, res.rel_error)
+    th.join()
+    wall = time.perf_counter() - t0
+    st = sv.stats()
+    sv.close()
+    return np.array(lat), moves, wall, st, err
+
+
+def serve(args) -> dict:
+    """The serving line (without the CPU baseline, which the caller adds)."""
+    n_req = args.requests or 5000
+    sizes, arrivals = serve_trace(n_req)
+    t = time.perf_counter()
+    inputs = []
+    for k, n in enumerate(sizes):
+        r = serve_region(k, n)
+        rp, col, tgt = r.csr()
+        inputs.append(capi.ArcsInput(r.pos, rp, col, tgt))
+    gen_s = time.perf_counter() - t
+    ctx = capi.Context(0)
+    prm = capi.default_params(capi.LEVEL_ARCS, schedule=capi.SCHEDULE_CPU, **SERVE_ANNEAL)
+    # warm-up: module load, pinned staging, allocator pool
+    for _ in range(max(1, args.warmup)):
+        _serve_pass(ctx, prm, inputs[:64], None)
+    sat_lat, sat_moves, sat_wall, sat_st, sat_err = _serve_pass(ctx, prm, inputs, None)
+    ol_lat, ol_moves, ol_wall, ol_st, ol_err = _serve_pass(ctx, prm, inputs, arrivals)
+    line = {
+        "metric": "structures/s", "value": n_req / sat_wall, "unit": "structures/s",
+        "n_gpus": 1, "steps": 1, "warmup": max(1, args.warmup),
+        "ms_per_step": sat_wall * 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": f"serve_{n_req}req_poisson200_sizes64-8192_"
+                               f"1.5625arcs_per_bead_20k_moves_budget40GiB",
+                   "requests": n_req, "beads_total": int(sizes.sum()),
+                   "generation_s": gen_s},
+        "saturated": {"structures_per_s": n_req / sat_wall, "moves_per_s": sat_moves / sat_wall,
+                      "wall_s": sat_wall, "latency_ms_p50": float(np.percentile(sat_lat, 50)),
+                      "latency_ms_p99": float(np.percentile(sat_lat, 99)),
+                      "waves": sat_st["waves"], "running_peak": sat_st["running_peak"],
+                      "bytes_peak": sat_st["bytes_peak"]},
+        "open_loop_200rps": {"structures_per_s": n_req / ol_wall,
+                             "moves_per_s": ol_moves / ol_wall, "wall_s": ol_wall,
+                             "latency_ms_p50": float(np.percentile(ol_lat, 50)),
+                             "latency_ms_p99": float(np.percentile(ol_lat, 99)),
+                             "latency_ms_mean": float(ol_lat.mean()),
+                             "waves": ol_st["waves"], "running_peak": ol_st["running_peak"]},
+        "final_energy_rel_error_max": max(sat_err, ol_err),
+        "e2e": {"value": n_req / sat_wall, "unit": "structures/s",
+                "h2d_bytes_per_step": None, "d2h_bytes_per_step": None,
+                "note": "host arrays in, host results out, through pmmc_server_*"},
+    }
+    return line
 
 
 def main(args):

@@ -52,3 +52,18 @@ def test_no_device_is_an_error(built_lib):
     with pytest.raises(capi.PmmcError) as e:
         capi.Context(0)
     assert e.value.status == capi.PMMC_ERR_NO_DEVICE
+
+
+def test_serve_trace_shape():
+    """The serving trace: sizes log-uniform in [64, 8192], Poisson arrivals
+    at about 200 requests/s, reproducible from its seed."""
+    from pmmc_gb300 import workloads as W
+    s1, a1 = W.serve_trace(5000)
+    s2, a2 = W.serve_trace(5000)
+    np.testing.assert_array_equal(s1, s2)
+    np.testing.assert_array_equal(a1, a2)
+    assert s1.min() >= 64 and s1.max() <= 8192
+    assert abs(np.log(s1).mean() - 0.5 * (np.log(64) + np.log(8192))) < 0.1
+    rate = len(a1) / a1[-1]
+    assert 180 < rate < 220
+    assert np.all(np.diff(a1) >= 0) and a1[0] == 0.0
