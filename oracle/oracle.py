@@ -130,6 +130,7 @@ def lib():
         L.orc_smooth_full_score.restype = C.c_double
         L.orc_smooth_local_score.restype = C.c_double
         L.orc_u01.restype = C.c_float
+        L.orc_arcs_ext_score.restype = C.c_double
         L.orc_u01.argtypes = [C.c_uint32]
         for name in ("orc_arcs_full_score", "orc_arcs_spring_score",
                      "orc_arcs_local_score", "orc_arcs_anneal"):
@@ -152,6 +153,7 @@ def ref():
         R.ref_arcs_score.restype = C.c_double
         R.ref_heatmap_score.restype = C.c_double
         R.ref_smooth_score.restype = C.c_double
+        R.ref_lengths_score.restype = C.c_double
         _ref = R
     return _ref
 
@@ -208,16 +210,28 @@ def arcs_local(pr: ArcsProblem, prm: Params, moved: int, pos=None) -> float:
                                       int(moved))
 
 
+class Ext(C.Structure):
+    """Extended arc energy (orc_ext): one bond target, the bond constants
+    and the angle constant."""
+    _fields_ = [("bond_target", C.c_double), ("k_stretch", C.c_float),
+                ("k_squeeze", C.c_float), ("k_angle", C.c_float)]
+
+
+def arcs_ext_score(n: int, pos, ext: Ext, moved: int = -1) -> float:
+    return lib().orc_arcs_ext_score(int(n), _p(_f32(pos)), C.byref(ext), int(moved))
+
+
 def arcs_anneal(pr: ArcsProblem, prm: Params, step: float, seed: int,
-                rng=RNG_LIBC, chain=0):
+                rng=RNG_LIBC, chain=0, ext: Ext | None = None):
     pos = _f32(pr.pos).copy()
     ed = _f32(pr.exp_dist)
     fx = _u8(pr.fixed)
     la, keep = _loops(pr)
     r = OrcRng(rng, seed, chain, 0)
     res = OrcResult()
-    lib().orc_arcs_anneal(pr.n, _p(pos), _p(fx), _p(ed), *la, C.byref(prm.c()),
-                          C.c_float(step), C.byref(r), C.byref(res))
+    lib().orc_arcs_anneal_ext(pr.n, _p(pos), _p(fx), _p(ed), *la, C.byref(prm.c()),
+                              C.byref(ext) if ext is not None else None,
+                              C.c_float(step), C.byref(r), C.byref(res))
     return pos, res
 
 
@@ -347,6 +361,11 @@ def ref_smooth_score(pr: SmoothProblem, prm: Params, moved=-1, pos=None) -> floa
                                   C.byref(prm.c()), int(moved))
 
 
+def ref_lengths_score(n: int, pos, dist_to_next, prm: Params, moved=-1) -> float:
+    return ref().ref_lengths_score(int(n), _p(_f32(pos)), _p(_f64(dist_to_next)),
+                                   C.byref(prm.c()), int(moved))
+
+
 # ---------------------------------------------------------------------------
 # Arc marking, HCM lines, Philox
 # ---------------------------------------------------------------------------
@@ -429,13 +448,15 @@ def _replay_result(out, keep):
             "proposal_mismatch": out.proposal_mismatch, "final_energy": out.final_energy}
 
 
-def arcs_replay(pr: ArcsProblem, prm: Params, step: float, seed: int, chain: int, trace):
+def arcs_replay(pr: ArcsProblem, prm: Params, step: float, seed: int, chain: int, trace,
+                ext: Ext | None = None):
     m, bead, disp, acc, out, keep = _replay_prep(trace)
     la, lkeep = _loops(pr)
     fx = _u8(pr.fixed)
-    lib().orc_arcs_replay(pr.n, _p(_f32(pr.pos)), _p(fx), _p(_f32(pr.exp_dist)), *la,
-                          C.byref(prm.c()), C.c_float(step), C.c_uint64(seed),
-                          C.c_uint32(chain), m, _p(bead), _p(disp), _p(acc), C.byref(out))
+    lib().orc_arcs_replay_ext(pr.n, _p(_f32(pr.pos)), _p(fx), _p(_f32(pr.exp_dist)), *la,
+                              C.byref(prm.c()), C.byref(ext) if ext is not None else None,
+                              C.c_float(step), C.c_uint64(seed), C.c_uint32(chain), m,
+                              _p(bead), _p(disp), _p(acc), C.byref(out))
     return _replay_result(out, keep)
 
 

@@ -339,11 +339,24 @@ double orc_arcs_local_score(int n, const float *pos, const float *exp_dist,
  * only where the reference has no counterpart: the Philox source picks among
  * movable beads directly and keeps the pre-move position on rejection (as the
  * CUDA kernels do) instead of subtracting the displacement back. */
+static double ext_full(int n, const float *pos, const orc_ext *x);
+static double ext_local(int n, const float *pos, const orc_ext *x, int moved);
+
 void orc_arcs_anneal(int n, float *pos, const unsigned char *fixed,
                      const float *exp_dist, int n_loops, const int *loop_i,
                      const int *loop_j, const float *loop_k,
                      const float *loop_r0, const orc_params *p,
                      float step_size, orc_rng *rng, orc_result *res) {
+  orc_arcs_anneal_ext(n, pos, fixed, exp_dist, n_loops, loop_i, loop_j, loop_k, loop_r0, p,
+                      NULL, step_size, rng, res);
+}
+
+void orc_arcs_anneal_ext(int n, float *pos, const unsigned char *fixed,
+                         const float *exp_dist, int n_loops, const int *loop_i,
+                         const int *loop_j, const float *loop_k,
+                         const float *loop_r0, const orc_params *p,
+                         const orc_ext *x, float step_size, orc_rng *rng,
+                         orc_result *res) {
   int m;
   loop_ent *e = build_loops(n, n_loops, loop_i, loop_j, loop_k, loop_r0, &m);
   rng_ctx c;
@@ -355,6 +368,8 @@ void orc_arcs_anneal(int n, float *pos, const unsigned char *fixed,
   if (p->sphere_radius > 0.0f)
     for (int k = 0; k < n; ++k)
       score_curr += sphere_pen(pos + 3 * k, p->sphere_radius);
+  if (x)
+    score_curr += ext_full(n, pos, x);
   double score_prev = score_curr, milestone_score = score_curr;
   int64_t success = 0, milestone_success = 0, i = 1;
   int philox = rng->kind == ORC_RNG_PHILOX;
@@ -377,6 +392,8 @@ void orc_arcs_anneal(int n, float *pos, const unsigned char *fixed,
     double lp = arcs_dist_local(n, pos, exp_dist, p, pb) + loop_energy(pos, e, m, pb);
     if (p->sphere_radius > 0.0f)
       lp += sphere_pen(q, p->sphere_radius);
+    if (x)
+      lp += ext_local(n, pos, x, pb);
     float d[3], old[3] = {q[0], q[1], q[2]};
     draw_disp(&c, step_size, p->use2d, d);
     q[0] += d[0];
@@ -385,6 +402,8 @@ void orc_arcs_anneal(int n, float *pos, const unsigned char *fixed,
     double lc = arcs_dist_local(n, pos, exp_dist, p, pb) + loop_energy(pos, e, m, pb);
     if (p->sphere_radius > 0.0f)
       lc += sphere_pen(q, p->sphere_radius);
+    if (x)
+      lc += ext_local(n, pos, x, pb);
     score_curr = score_curr - lp + lc;
     int ok = score_curr <= score_prev;
     if (!ok) {
@@ -651,6 +670,70 @@ double orc_smooth_local_score(int n, const float *pos,
   if (p->sphere_radius > 0.0f)
     sc += sphere_pen(pos + 3 * moved, p->sphere_radius);
   return sc;
+}
+
+/* Extended arc energy: the bond and angle terms above with one target and
+ * the extension's constants, weights 1. */
+static orc_params ext_params(const orc_ext *x) {
+  orc_params q;
+  memset(&q, 0, sizeof(q));
+  q.k_stretch = x->k_stretch;
+  q.k_squeeze = x->k_squeeze;
+  q.k_angle = x->k_angle;
+  q.w_dist = 1.0f;
+  q.w_angle = 1.0f;
+  return q;
+}
+
+static double ext_target(const orc_ext *x) {
+  return x->bond_target < 1e-5 ? 1e-5 : x->bond_target;
+}
+
+static double ext_full(int n, const float *pos, const orc_ext *x) {
+  const orc_params q = ext_params(x);
+  const double t = ext_target(x);
+  double sca = 0.0, scb = 0.0;
+  float v2[3] = {0, 0, 0};
+  for (int i = 0; i + 1 < n; ++i) {
+    const float *a = pos + 3 * i, *b = pos + 3 * (i + 1);
+    float v[3] = {a[0] - b[0], a[1] - b[1], a[2] - b[2]};
+    sca += bond_term(a, b, t, &q);
+    if (i > 0) {
+      double ang = v_angle(v, v2);
+      scb += ang * ang * ang * q.k_angle;
+    }
+    v2[0] = v[0];
+    v2[1] = v[1];
+    v2[2] = v[2];
+  }
+  return sca + scb;
+}
+
+static double ext_local(int n, const float *pos, const orc_ext *x, int moved) {
+  const orc_params q = ext_params(x);
+  const double t = ext_target(x);
+  double sca = 0.0, scb = 0.0;
+  float v2[3] = {0, 0, 0};
+  for (int i = moved - 2; i < moved + 2; i++) {
+    if (i < 0 || i + 1 >= n)
+      continue;
+    const float *a = pos + 3 * i, *b = pos + 3 * (i + 1);
+    float v[3] = {a[0] - b[0], a[1] - b[1], a[2] - b[2]};
+    if (i == moved - 1 || i == moved)
+      sca += bond_term(a, b, t, &q);
+    if (i > moved - 2 && i > 0) {
+      double ang = v_angle(v, v2);
+      scb += ang * ang * ang * q.k_angle;
+    }
+    v2[0] = v[0];
+    v2[1] = v[1];
+    v2[2] = v[2];
+  }
+  return sca + scb;
+}
+
+double orc_arcs_ext_score(int n, const float *pos, const orc_ext *x, int moved) {
+  return moved < 0 ? ext_full(n, pos, x) : ext_local(n, pos, x, moved);
 }
 
 /* MonteCarloArcsSmooth (LooperSolver.hpp:4798-5047), orientation and
@@ -922,6 +1005,7 @@ typedef struct {
   const float *heat;
   int diag, n_bounds;
   const int *bounds;
+  const orc_ext *ext;
 } replay_ctx;
 
 static double arcs_local_cb(void *vc, const float *pos, int moved) {
@@ -930,6 +1014,8 @@ static double arcs_local_cb(void *vc, const float *pos, int moved) {
               loop_energy(pos, c->loops, c->m, moved);
   if (c->p->sphere_radius > 0.0f)
     sc += sphere_pen(pos + 3 * moved, c->p->sphere_radius);
+  if (c->ext)
+    sc += ext_local(c->n, pos, c->ext, moved);
   return sc;
 }
 
@@ -1016,14 +1102,28 @@ void orc_arcs_replay(int n, const float *pos0, const unsigned char *fixed,
                      float step_size, uint64_t seed, uint32_t chain,
                      int n_moves, const int *bead, const float *disp,
                      const int *gpu_acc, orc_replay_out *out) {
+  orc_arcs_replay_ext(n, pos0, fixed, exp_dist, n_loops, loop_i, loop_j, loop_k, loop_r0, p,
+                      NULL, step_size, seed, chain, n_moves, bead, disp, gpu_acc, out);
+}
+
+void orc_arcs_replay_ext(int n, const float *pos0, const unsigned char *fixed,
+                         const float *exp_dist, int n_loops, const int *loop_i,
+                         const int *loop_j, const float *loop_k,
+                         const float *loop_r0, const orc_params *p,
+                         const orc_ext *x, float step_size, uint64_t seed,
+                         uint32_t chain, int n_moves, const int *bead,
+                         const float *disp, const int *gpu_acc,
+                         orc_replay_out *out) {
   int m;
   loop_ent *e = build_loops(n, n_loops, loop_i, loop_j, loop_k, loop_r0, &m);
   float *pos = (float *)malloc(sizeof(float) * 3 * (n > 0 ? n : 1));
   memcpy(pos, pos0, sizeof(float) * 3 * n);
-  replay_ctx c = {n, exp_dist, e, m, p, NULL, NULL, 0, 0, NULL};
+  replay_ctx c = {n, exp_dist, e, m, p, NULL, NULL, 0, 0, NULL, x};
   double E = arcs_dist_full(n, pos, exp_dist, p, 1, 1) + loop_energy(pos, e, m, -1);
   if (p->sphere_radius > 0.0f)
     for (int k = 0; k < n; ++k) E += sphere_pen(pos + 3 * k, p->sphere_radius);
+  if (x)
+    E += ext_full(n, pos, x);
   replay_core(0, &c, arcs_local_cb, n, pos, fixed, p, step_size, E, seed, chain,
               n_moves, bead, disp, gpu_acc, out);
   free(pos);

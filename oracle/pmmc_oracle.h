@@ -104,6 +104,30 @@ void orc_arcs_anneal(int n, float *pos, const unsigned char *fixed,
                      const float *loop_r0, const orc_params *p,
                      float step_size, orc_rng *rng, orc_result *res);
 
+/* Extended arc energy (opt-in; the reference arc level has no bond or angle
+ * term): bond springs on consecutive beads as
+ * calcScoreStructureActiveRegionLengths (LooperSolver.hpp:3375-3412) with
+ * one target for every bead, plus the stiffness angle term
+ * k_angle * angle(v_i, v_{i-1})^3 of calcScoreStructureSmooth
+ * (:3414-3495; angle() thirdparty/common.cpp:39-46), weights 1.  The target
+ * is clamped at 1e-5 in both the full and the local form (the reference
+ * clamps its local length form at 1e-5, :3404-3405). */
+typedef struct orc_ext {
+  double bond_target;  /* dist_to_next of every bead (a double, as Cluster::dist_to_next) */
+  float k_stretch;     /* springConstantStretch of the bonds    */
+  float k_squeeze;     /* springConstantSqueeze of the bonds    */
+  float k_angle;       /* springAngularConstant                 */
+} orc_ext;
+/* moved = -1: the full form; else the terms that bead `moved` changes. */
+double orc_arcs_ext_score(int n, const float *pos, const orc_ext *x, int moved);
+/* orc_arcs_anneal with the extended energy added (x = NULL: none). */
+void orc_arcs_anneal_ext(int n, float *pos, const unsigned char *fixed,
+                         const float *exp_dist, int n_loops, const int *loop_i,
+                         const int *loop_j, const float *loop_k,
+                         const float *loop_r0, const orc_params *p,
+                         const orc_ext *x, float step_size, orc_rng *rng,
+                         orc_result *res);
+
 /* ---------------- heatmap level (chromosome / segment) ---------------- */
 /* calcScoreHeatmapActiveRegion(moved) (:3583-3617); moved = -1 -> full. */
 double orc_heatmap_score(int n, const float *pos, const float *heat, int diag,
@@ -172,6 +196,15 @@ void orc_arcs_replay(int n, const float *pos0, const unsigned char *fixed,
                      float step_size, uint64_t seed, uint32_t chain,
                      int n_moves, const int *bead, const float *disp,
                      const int *gpu_acc, orc_replay_out *out);
+/* orc_arcs_replay with the extended energy added (x = NULL: none). */
+void orc_arcs_replay_ext(int n, const float *pos0, const unsigned char *fixed,
+                         const float *exp_dist, int n_loops, const int *loop_i,
+                         const int *loop_j, const float *loop_k,
+                         const float *loop_r0, const orc_params *p,
+                         const orc_ext *x, float step_size, uint64_t seed,
+                         uint32_t chain, int n_moves, const int *bead,
+                         const float *disp, const int *gpu_acc,
+                         orc_replay_out *out);
 void orc_smooth_replay(int n, const float *pos0, const unsigned char *fixed,
                        const double *dist_to_next, const orc_params *p,
                        float step_size, uint64_t seed, uint32_t chain,

@@ -293,6 +293,19 @@ double ref_smooth_score(int n, const float *pos, const double *dtn,
   return sc;
 }
 
+/* calcScoreStructureActiveRegionLengths() (moved < 0) or
+ * calcScoreStructureActiveRegionLengths(moved) (LooperSolver.hpp:3375-3412):
+ * the bond term the extended arc energy uses. */
+double ref_lengths_score(int n, const float *pos, const double *dtn,
+                         const orc_params *p, int moved) {
+  Quiet q;
+  apply_settings(p, 2);
+  LooperSolver s("ref", "/tmp/");
+  load_clusters(s, n, pos, nullptr, dtn);
+  return moved < 0 ? s.calcScoreStructureActiveRegionLengths()
+                   : s.calcScoreStructureActiveRegionLengths(moved);
+}
+
 /* InteractionArcs::markArcs (src/include/InteractionArcs.hpp:207-336) on a
  * single chromosome "chr1".  Output layout as orc_mark_arcs. */
 int ref_mark_arcs(int n_anchors, const int *a_start, const int *a_end,

@@ -97,6 +97,60 @@ __device__ double arcs_spring_energy(int n, const float4 *spos, const int *srp,
   return warp_sum_d(acc);
 }
 
+// ---------------------------------------------------------------------------
+// Extended energy (opt-in): bond springs ((|p_i - p_i+1| - t)/t)^2 * k (k the
+// stretch constant when longer than t, else the squeeze constant), as
+// calcScoreStructureActiveRegionLengths (LooperSolver.hpp:3375-3412), and
+// k_angle * a^3 with a = (1 - cos)/2 of the angle between p_i-1 - p_i and
+// p_i - p_i+1 at every interior bead, as calcScoreStructureSmooth
+// (:3414-3495, angle() thirdparty/common.cpp:39-46), weights 1.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ float ext_bond(float4 a, float4 b, const ArcsDevParams &P) {
+  const float d = (ref_len(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z)) -
+                   P.bond_t) * P.inv_bond_t;
+  return d * d * (d >= 0.0f ? P.kb_stretch : P.kb_squeeze);
+}
+
+// angle term at the bead between u = a - b and v = b - c (both normalised)
+__device__ __forceinline__ float ext_angle(float4 a, float4 b, float4 c, const ArcsDevParams &P) {
+  const float ux = a.x - b.x, uy = a.y - b.y, uz = a.z - b.z;
+  const float vx = b.x - c.x, vy = b.y - c.y, vz = b.z - c.z;
+  float lu = ref_len(ux, uy, uz), lv = ref_len(vx, vy, vz);
+  lu = lu > 0.0f ? 1.0f / lu : 0.0f;
+  lv = lv > 0.0f ? 1.0f / lv : 0.0f;
+  const float dot = (ux * lu) * (vx * lv) + (uy * lu) * (vy * lv) + (uz * lu) * (vz * lv);
+  const float an = 1.0f - (dot + 1.0f) * 0.5f;
+  return an * an * an * P.k_angle;
+}
+
+// The terms bead b changes (bonds b-1|b, b|b+1; angles at b-1, b, b+1) with
+// bead b at x.
+__device__ float ext_local(const float4 *spos, int n, int b, float4 x, const ArcsDevParams &P) {
+  float4 q[5];
+#pragma unroll
+  for (int k = 0; k < 5; ++k) {
+    const int i = b - 2 + k;
+    q[k] = k == 2 ? x : (i >= 0 && i < n ? spos[i] : make_float4(0.f, 0.f, 0.f, 0.f));
+  }
+  float s = 0.0f;
+  if (b >= 1) s += ext_bond(q[1], q[2], P);
+  if (b + 1 < n) s += ext_bond(q[2], q[3], P);
+  if (b >= 2) s += ext_angle(q[0], q[1], q[2], P);
+  if (b >= 1 && b + 1 < n) s += ext_angle(q[1], q[2], q[3], P);
+  if (b + 2 < n) s += ext_angle(q[2], q[3], q[4], P);
+  return s;
+}
+
+// Full extended energy in FP64 over the warp.
+__device__ double ext_full(int n, const float4 *spos, const ArcsDevParams &P, int lane) {
+  double acc = 0.0;
+  for (int i = lane; i + 1 < n; i += 32) {
+    acc += (double)ext_bond(spos[i], spos[i + 1], P);
+    if (i >= 1) acc += (double)ext_angle(spos[i - 1], spos[i], spos[i + 1], P);
+  }
+  return warp_sum_d(acc);
+}
+
 // The same energy for the periodic resync, which only has to remove the
 // drift of the running total: each term in FP32 (hardware reciprocal square
 // root for the length), summed per lane in float-float (error-free two-sum)
@@ -257,6 +311,7 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
     // ---- initial FP64 energy: repulsion (frozen) + springs/loops/sphere ----
     const double base = arcs_repulsion(n, spos, srp, NB, nulls + U.null_off, U.n_null, lane);
     double E = base + arcs_spring_energy(n, spos, srp, NB, LST, U.n_loops, P, lane);
+    if (P.ext) E += ext_full(n, spos, P, lane);
     // running energy of the chain (identical on every lane): float-float
     // pair on the move path, widened to FP64 at milestones, resyncs, the end
     float e_hi = (float)E, e_lo = (float)(E - (double)(float)E);
@@ -376,8 +431,17 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
             sn += sphere_penalty(nx, ny, nz, R);
           }
           unsigned hit = 0u;
+          if (P.ext) {
+            // bonds and angles reach two beads along the chain: a window
+            // proposal within that distance is a partner too
+            so += ext_local(spos, n, b, pb, P);
+            sn += ext_local(spos, n, b, make_float4(nx, ny, nz, 0.0f), P);
 #pragma unroll
-          for (int j = 0; j < W; ++j) hit |= (unsigned)(b == bj[j]) << j;
+            for (int j = 0; j < W; ++j) hit |= (unsigned)(abs(b - bj[j]) <= 2) << j;
+          } else {
+#pragma unroll
+            for (int j = 0; j < W; ++j) hit |= (unsigned)(b == bj[j]) << j;
+          }
           cm |= hit & ((1u << g) - 1u);
         }
       }
@@ -467,8 +531,8 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
       if (moves == next_rs) {
         next_rs += P.resync;
         if (!flag) {
-          const double es =
-              arcs_spring_energy_ff(n, spos, srp, NB, INV, LST, U.n_loops, P, lane);
+          double es = arcs_spring_energy_ff(n, spos, srp, NB, INV, LST, U.n_loops, P, lane);
+          if (P.ext) es += ext_full(n, spos, P, lane);
           const double Er = base + es;
           e_hi = (float)Er;
           e_lo = (float)(Er - (double)e_hi);
@@ -488,7 +552,8 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
     }
 
     // ---- final FP64 recompute and outputs ----
-    const double es = arcs_spring_energy(n, spos, srp, NB, LST, U.n_loops, P, lane);
+    double es = arcs_spring_energy(n, spos, srp, NB, LST, U.n_loops, P, lane);
+    if (P.ext) es += ext_full(n, spos, P, lane);
     if (lane == 0) {
       ChainOut o;
       o.energy = (double)e_hi + (double)e_lo;
@@ -677,6 +742,13 @@ ArcsDevParams arcs_make_params(const pmmc_anneal_params *prm, uint64_t seed, boo
     P.dtpow[l] = (float)d;
     d *= (double)prm->dt_temp;
   }
+  P.ext = prm->arcs_extended ? 1 : 0;
+  // the reference clamps a bond target at 1e-5 (LooperSolver.hpp:3404-3405)
+  P.bond_t = std::max(prm->bond_target, 1e-5f);
+  P.inv_bond_t = 1.0f / P.bond_t;
+  P.kb_stretch = prm->k_stretch_bond;
+  P.kb_squeeze = prm->k_squeeze_bond;
+  P.k_angle = prm->k_angle_ext;
   return P;
 }
 

@@ -55,6 +55,10 @@ struct ArcsDevParams {
   int pad;
   uint64_t seed;   // default Philox key (each unit carries its own)
   float dtpow[33];  // dt^l, l = 0..32
+  // extended energy (off unless ext): bonds to the next bead with one
+  // target, and the stiffness angle term at every interior bead
+  int ext;
+  float bond_t, inv_bond_t, kb_stretch, kb_squeeze, k_angle;
 };
 
 // per-warp scratch: 32 drawn moves (int4) + their ratio thresholds, and the

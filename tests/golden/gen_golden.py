@@ -7,7 +7,8 @@ outputs on small seeded inputs into tests/golden/*.npz.  The tests then pin
 the plain-C oracle against these files on any machine, including ones without
 the reference tree.
 
-    python tests/golden/gen_golden.py
+    python tests/golden/gen_golden.py            # every group
+    python tests/golden/gen_golden.py ext        # only the named groups
 """
 from __future__ import annotations
 
@@ -57,6 +58,29 @@ def arcs_cases():
                                full=np.array([full]), step=np.array([0.5]),
                                seed=np.array([1000 + k]), out_pos=pos,
                                out_score=np.array([score]), out_moves=np.array([moves]))
+    return out
+
+
+def ext_cases():
+    """The extended arc energy's two terms from the reference's own
+    functions: calcScoreStructureActiveRegionLengths (bonds) and
+    calcScoreStructureSmooth (bonds + angles, weights 1)."""
+    out = {}
+    for k, (n, t, ks, kq, ka) in enumerate([(64, 1.0, 0.1, 0.1, 0.1), (33, 0.7, 0.3, 0.05, 0.4)]):
+        rng = np.random.default_rng(500 + k)
+        pos = (synth.random_walk(n, rng) * 1.1 +
+               rng.normal(0.0, 0.25, (n, 3))).astype(np.float32)
+        dtn = np.full(n, t, np.float64)
+        lp = O.Params(k_stretch=ks, k_squeeze=kq, k_angle=0.0, w_dist=1.0, w_angle=1.0)
+        sp = O.Params(k_stretch=ks, k_squeeze=kq, k_angle=ka, w_dist=1.0, w_angle=1.0)
+        beads = np.array([0, 1, 2, n // 2, n - 2, n - 1], np.int32)
+        sm = O.SmoothProblem(pos, dtn)
+        out[f"ext{k}"] = dict(
+            pos=pos, ext=np.array([t, ks, kq, ka], np.float64), beads=beads,
+            len_full=np.array([O.ref_lengths_score(n, pos, dtn, lp, -1)]),
+            len_local=np.array([O.ref_lengths_score(n, pos, dtn, lp, int(b)) for b in beads]),
+            all_full=np.array([O.ref_smooth_score(sm, sp, -1)]),
+            all_local=np.array([O.ref_smooth_score(sm, sp, int(b)) for b in beads]))
     return out
 
 
@@ -144,11 +168,17 @@ def main():
         O.build()
     if not O.ref_available():
         raise SystemExit("the reference harness could not be built (no reference tree)")
+    # optional arguments name the groups to write (default: all of them)
+    groups = {"arcs": arcs_cases, "ext": ext_cases, "heatmap": heatmap_cases,
+              "smooth": smooth_cases, "mark": mark_cases, "hcm": hcm_cases}
+    want = sys.argv[1:] or list(groups) + ["rng"]
     fixtures = {}
-    for fn in (arcs_cases, heatmap_cases, smooth_cases, mark_cases, hcm_cases):
-        fixtures.update(fn())
-    fixtures["rng"] = dict(random_vectors=O.ref_random_vectors(5, 4, 1.0, False),
-                           random_vectors_2d=O.ref_random_vectors(6, 4, 1.0, True))
+    for g in want:
+        if g in groups:
+            fixtures.update(groups[g]())
+    if "rng" in want:
+        fixtures["rng"] = dict(random_vectors=O.ref_random_vectors(5, 4, 1.0, False),
+                               random_vectors_2d=O.ref_random_vectors(6, 4, 1.0, True))
     for name, d in fixtures.items():
         np.savez_compressed(os.path.join(HERE, f"{name}.npz"), **d)
     print("wrote", len(fixtures), "fixtures")

@@ -61,6 +61,32 @@ def test_arcs_trace_parity(ctx, variant, lanes):
     assert abs(rep["final_energy"] - res[0].energy) <= 1e-5 * abs(rep["final_energy"])
 
 
+@pytest.mark.parametrize("lanes", [2, 8])
+def test_arcs_extended_energy_trace_parity(ctx, lanes):
+    """Opt-in extended energy (bonds to the next bead, target 1.0, k 0.1; the
+    stiffness angle term, k 0.1): per-move local scores and decisions follow
+    the oracle, and the FP64 energy is arcs + loops + bonds + angles."""
+    pr, inp, _ = problem("plain", n=256, arcs=400, seed=42)
+    base = dict(max_temp=5.0, dt_temp=0.9999, milestone_steps=4000, improvement=0.99)
+    ext = dict(arcs_extended=1, bond_target=1.0, k_stretch_bond=0.1, k_squeeze_bond=0.1,
+               k_angle_ext=0.1)
+    prm = capi.default_params(capi.LEVEL_ARCS, schedule=capi.SCHEDULE_CPU, max_moves=12000,
+                              resync_every=1000, **base, **ext)
+    ctx.set_seed(31)
+    b = capi.ArcsBatch(ctx, [inp], prm, [0.5], use_graph=False, trace_cap=12000, lanes=lanes)
+    b.run()
+    pos, res = b.results()
+    m = int(res[0].moves)
+    tr = b.trace(m)
+    ox = O.Ext(1.0, 0.1, 0.1, 0.1)
+    rep = O.arcs_replay(pr, O.Params(**base), 0.5, 31, 0, tr, ext=ox)
+    check_replay(tr, rep)
+    e64 = (O.arcs_repulsion(pr) + O.arcs_full(pr, O.Params(**base), pos=pos[0], repulsion=False)
+           + O.arcs_ext_score(pr.n, pos[0], ox, -1))
+    assert abs(res[0].energy_fp64 - e64) <= 1e-6 * e64
+    assert abs(res[0].energy - e64) <= 1e-4 * e64
+
+
 def test_arcs_fp64_energy_and_resync(ctx):
     pr, inp, _ = problem("plain", n=256, arcs=400, seed=42)
     oprm = O.Params(max_temp=5.0, dt_temp=0.9999, milestone_steps=50000, improvement=0.99)

@@ -62,6 +62,23 @@ def test_arcs_scores_and_anneal(case):
     np.testing.assert_array_equal(pos, g["out_pos"])
 
 
+@pytest.mark.parametrize("case", ["ext0", "ext1"])
+def test_extended_arc_energy_terms(case):
+    """The extended arc energy's bond term against the reference's
+    calcScoreStructureActiveRegionLengths, and bonds + angles against its
+    calcScoreStructureSmooth (weights 1), full and local, bit for bit."""
+    g = load(case)
+    t, ks, kq, ka = g["ext"]
+    n = len(g["pos"])
+    lengths = O.Ext(t, ks, kq, 0.0)
+    both = O.Ext(t, ks, kq, ka)
+    assert O.arcs_ext_score(n, g["pos"], lengths, -1) == g["len_full"][0]
+    assert O.arcs_ext_score(n, g["pos"], both, -1) == g["all_full"][0]
+    for b, wl, wa in zip(g["beads"], g["len_local"], g["all_local"]):
+        assert O.arcs_ext_score(n, g["pos"], lengths, int(b)) == wl
+        assert O.arcs_ext_score(n, g["pos"], both, int(b)) == wa
+
+
 @pytest.mark.parametrize("case", ["heatmap0", "heatmap1"])
 def test_heatmap_scores_and_anneal(case):
     g = load(case)
