@@ -300,7 +300,8 @@ def run_gpu(args, rank, world):
     prm = capi.default_params(capi.LEVEL_ARCS, schedule=capi.SCHEDULE_CPU,
                               resync_every=RESYNC, **ANNEAL)
     steps = [STEP] * len(inputs)
-    batch = capi.ArcsBatch(ctx, inputs, prm, steps, chains=1, use_graph=True)
+    batch = capi.ArcsBatch(ctx, inputs, prm, steps, chains=1, use_graph=True, lanes=args.lanes)
+    classes = batch.classes()
     stream = torch.cuda.Stream()
     l2 = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")  # > 129 MB L2
     # warm-up (graph capture happens on the first run)
@@ -338,7 +339,7 @@ def run_gpu(args, rank, world):
     for k in range(args.e2e_steps):
         torch.cuda.synchronize()
         t = time.perf_counter()
-        p2, r2 = _batch_anneal_host(ctx, inputs, prm, steps)
+        p2, r2 = _batch_anneal_host(ctx, inputs, prm, steps, args.lanes)
         e2e_ms.append((time.perf_counter() - t) * 1e3)
     e2e_moves = sum(r.moves for r in r2)
     h2d, d2h = staged_bytes(inputs)
@@ -354,10 +355,10 @@ def run_gpu(args, rank, world):
     return dict(step_ms=step_ms, moves=moves_per_step, kernel_ms=kernel_ms, wall=t_wall,
                 clocks=clk, rel_err=rel_err, bad=status_bad, e2e_ms=e2e_ms,
                 e2e_moves=e2e_moves, h2d=h2d, d2h=d2h, plain_s=plain_s, n_launch=n_launch,
-                n_units=len(inputs))
+                n_units=len(inputs), classes=classes)
 
 
-def _batch_anneal_host(ctx, inputs, prm, steps):
+def _batch_anneal_host(ctx, inputs, prm, steps, lanes=0):
     import ctypes as C
 
     from pmmc_gb300 import capi
@@ -366,7 +367,7 @@ def _batch_anneal_host(ctx, inputs, prm, steps):
     tot = sum(x.n for x in inputs)
     pos = np.zeros((tot, 3), np.float32)
     res = (capi.Result * len(inputs))()
-    opts = capi.BatchOpts(1, 0, 0)
+    opts = capi.BatchOpts(1, 0, int(lanes))
     ctx.check(capi.lib().pmmc_arcs_batch_anneal(ctx.h, len(inputs), arr, C.byref(prm),
                                                 st.ctypes.data_as(C.c_void_p), C.byref(opts),
                                                 pos.ctypes.data_as(C.c_void_p), res))
@@ -406,6 +407,8 @@ def main():
     ap.add_argument("--maps", type=int, default=0, help="heatmap-batch: number of maps")
     ap.add_argument("--moves", type=int, default=0, help="moves per chain (heatmap/smooth)")
     ap.add_argument("--requests", type=int, default=0, help="serve: requests in the trace")
+    ap.add_argument("--lanes", type=int, default=-1,
+                    help="lanes per proposal of the batched form (2, 4, 8, 32; -1 = autotune)")
     args = ap.parse_args()
     set_workload(args.structures, args.milestone)
     if args.workload == "serve":
@@ -488,7 +491,10 @@ def main():
                    "blocks_per_structure": N_BLOCKS, "regions": r["n_units"] * world,
                    "moves_per_step": total_moves, "fp64_resync_every": RESYNC,
                    "l2": "256 MB buffer written between timed steps",
-                   "parallelism": f"replicas x{world}"},
+                   "parallelism": f"replicas x{world}",
+                   "launch_classes": [{"lanes": la, "warps_per_cta": w, "items": it,
+                                       "arcs_in_smem": nb} for la, w, it, nb in r["classes"]],
+                   "tuning": "autotuned" if args.lanes == -1 else f"lanes={args.lanes}"},
         "structures_per_s": structs,
         "final_energy_rel_error_max": r["rel_err"],
         "chains_not_ok": r["bad"],

@@ -225,8 +225,13 @@ typedef struct pmmc_batch_opts {
   int use_graph;         /* capture the launches in a CUDA graph          */
   int lanes_per_chain;   /* lanes that score one proposal: 2, 4, 8 or 32;
                           * a chain's warp scores 32/lanes proposals at
-                          * once (0 = the default, 2)                      */
+                          * once (0 = the default, 2; PMMC_LANES_AUTO =
+                          * the autotuner picks lanes and warps per CTA
+                          * for each shared-memory class from timed trial
+                          * launches, cached per process and in the JSON
+                          * file named by PMMC_AUTOTUNE_CACHE)            */
 } pmmc_batch_opts;
+#define PMMC_LANES_AUTO (-1)
 pmmc_status pmmc_arcs_batch_create(pmmc_ctx *ctx, int n_units,
                                    const pmmc_arcs_problem *units,
                                    const pmmc_anneal_params *prm,
@@ -269,6 +274,11 @@ pmmc_status pmmc_arcs_batch_create_ex(pmmc_ctx *ctx, int n_units,
                                       const pmmc_batch_opts *opts,
                                       int stop_all, int trace_cap,
                                       pmmc_arcs_batch **out);
+/* The launch configuration of each shared-memory class of a batch (no
+ * reference counterpart): lanes per proposal, warps per CTA, work items and
+ * whether arc lists are staged in shared memory; up to `cap` classes. */
+pmmc_status pmmc_arcs_batch_classes(pmmc_arcs_batch *b, int cap, int *n_classes,
+                                    int *lanes, int *warps, int *items, int *nb_smem);
 /* Copy `count` (<= trace_cap) trace records of the last run to host. */
 pmmc_status pmmc_arcs_batch_trace(pmmc_arcs_batch *b, void *out, int count);
 

@@ -15,6 +15,7 @@ from __future__ import annotations
 import ctypes as C
 import os
 import subprocess
+import sys
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -92,7 +93,7 @@ class Params:
 
 def build() -> None:
     """Compile liboracle.so (and _ref when the reference tree exists)."""
-    subprocess.run(["make", "-C", HERE, "-s"], check=True)
+    subprocess.run(["make", "-C", HERE, "-s"], check=True, stdout=sys.stderr)
 
 
 def _p(a):

@@ -40,8 +40,10 @@ HEADER_SYMBOLS = [
     "pmmc_arcs_batch_create_ex", "pmmc_arcs_batch_trace", "pmmc_smooth_batch_anneal",
     "pmmc_heatmap_batch_anneal", "pmmc_arcs_anneal_noalloc",
     "pmmc_server_create", "pmmc_server_submit", "pmmc_server_poll", "pmmc_server_wait",
-    "pmmc_server_get_stats", "pmmc_server_destroy",
+    "pmmc_server_get_stats", "pmmc_server_destroy", "pmmc_arcs_batch_classes",
 ]
+
+LANES_AUTO = -1  # PMMC_LANES_AUTO: the autotuner picks lanes and warps per class
 
 
 class PmmcError(RuntimeError):
@@ -309,6 +311,14 @@ class ArcsBatch:
         self.ctx.check(lib().pmmc_arcs_batch_stats(self.h, C.byref(ms), C.byref(mv),
                                                    C.byref(lanes)))
         return ms.value, mv.value, lanes.value
+
+    def classes(self):
+        """Per shared-memory class: (lanes, warps per CTA, items, staged)."""
+        cap = 64
+        n = C.c_int()
+        la, wa, it, nb = (C.c_int * cap)(), (C.c_int * cap)(), (C.c_int * cap)(), (C.c_int * cap)()
+        self.ctx.check(lib().pmmc_arcs_batch_classes(self.h, cap, C.byref(n), la, wa, it, nb))
+        return [(la[k], wa[k], it[k], bool(nb[k])) for k in range(min(n.value, cap))]
 
     def trace(self, count=None):
         count = self.trace_cap if count is None else count

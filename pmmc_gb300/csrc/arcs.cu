@@ -29,8 +29,11 @@
 #include <algorithm>
 #include <climits>
 #include <cmath>
+#include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <map>
+#include <string>
 #include <mutex>
 #include <numeric>
 #include <vector>
@@ -624,6 +627,7 @@ struct ArcsClass {
   bool nb_smem = true;
   int smem_per_warp = 0;
   int warps_per_cta = 1;
+  int lanes = 2;          // lanes per proposal
   int grid = 0;
   cudaStream_t stream = nullptr;
   cudaEvent_t join = nullptr;
@@ -906,6 +910,163 @@ void arcs_set_smem_limit(int bytes) {
 
 }  // namespace pmmc
 
+// ---------------------------------------------------------------------------
+// Autotuner: lanes per proposal (G: 2, 4 or 8, i.e. 16, 8 or 4 proposals
+// scored per window) and warps per CTA (1, 2 or 4 chains sharing a CTA's
+// shared memory) for each shared-memory class of a batch.  Every candidate
+// runs the class's largest items (up to 4 per SM) for kTuneMoves moves with
+// milestones and resyncs off, timed with events after one warm-up launch; the
+// fastest in moves/s wins.  Choices are kept per process, keyed by the
+// device (SM count, shared memory) and the class's shape (staged or not,
+// slice size, mean region size and arc degree, loops, extended energy), and
+// mirrored in a JSON file when PMMC_AUTOTUNE_CACHE names one.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int kTuneMoves = 8192;
+
+struct TuneChoice {
+  int lanes = 2, warps = 4;
+  double moves_per_s = 0.0;
+};
+
+std::mutex g_tune_mu;
+std::map<std::string, TuneChoice> g_tune;
+std::string g_tune_loaded;  // the cache file read into g_tune
+
+void tune_load(const std::string &path) {
+  if (path.empty() || path == g_tune_loaded) return;
+  g_tune_loaded = path;
+  FILE *f = fopen(path.c_str(), "r");
+  if (!f) return;
+  char line[512];
+  while (fgets(line, sizeof(line), f)) {
+    char key[256];
+    TuneChoice c;
+    if (sscanf(line, " \"%255[^\"]\": {\"lanes\": %d, \"warps\": %d, \"moves_per_s\": %lf",
+               key, &c.lanes, &c.warps, &c.moves_per_s) == 4)
+      g_tune[key] = c;
+  }
+  fclose(f);
+}
+
+void tune_save(const std::string &path) {
+  if (path.empty()) return;
+  const std::string tmp = path + ".tmp";
+  FILE *f = fopen(tmp.c_str(), "w");
+  if (!f) return;
+  fprintf(f, "{\n  \"pmmc_autotune\": 1,\n  \"entries\": {\n");
+  size_t k = 0;
+  for (auto &kv : g_tune)
+    fprintf(f, "    \"%s\": {\"lanes\": %d, \"warps\": %d, \"moves_per_s\": %.6e}%s\n",
+            kv.first.c_str(), kv.second.lanes, kv.second.warps, kv.second.moves_per_s,
+            ++k < g_tune.size() ? "," : "");
+  fprintf(f, "  }\n}\n");
+  fclose(f);
+  rename(tmp.c_str(), path.c_str());
+}
+
+std::string class_key(const pmmc_arcs_batch *b, const ArcsClass &c, const std::vector<int2> &items) {
+  double n = 0.0, deg = 0.0;
+  int loops = 0;
+  for (int k = c.item_begin; k < c.item_end; ++k) {
+    const ArcsUnit &U = b->h_units[items[k].x];
+    n += U.n;
+    deg += (double)U.nnz / std::max(1, U.n);
+    loops |= U.n_loops > 0;
+  }
+  const int cnt = std::max(1, c.item_end - c.item_begin);
+  n /= cnt;
+  deg /= cnt;
+  char buf[256];
+  snprintf(buf, sizeof(buf), "sm%d_smem%zu_nb%d_slice%d_n%d_deg%d_loops%d_ext%d", b->ctx->sm_count,
+           b->ctx->smem_optin, c.nb_smem ? 1 : 0,
+           (int)std::ceil(std::log2(std::max(16, c.smem_per_warp))),
+           (int)std::lround(2.0 * std::log2(std::max(1.0, n))), (int)std::lround(2.0 * deg),
+           loops, b->P.ext);
+  return buf;
+}
+
+}  // namespace
+
+static cudaError_t autotune_classes(pmmc_arcs_batch *b, cudaStream_t s) {
+  pmmc_ctx *ctx = b->ctx;
+  const char *env = getenv("PMMC_AUTOTUNE_CACHE");
+  const std::string path = env ? env : "";
+  std::vector<int2> items(b->items.n);
+  cudaError_t e = cudaMemcpy(items.data(), b->items.p, sizeof(int2) * items.size(),
+                             cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lock(g_tune_mu);
+  const bool fresh_path = !path.empty() && path != g_tune_loaded;
+  tune_load(path);
+  const size_t cap_smem = ctx->smem_optin - kCtaHeader;
+  ArcsDevParams T = b->P;
+  T.cap = kTuneMoves;
+  T.window = 1 << 30;
+  T.resync = 0;
+  T.stop_all = 0;
+  T.trace_cap = 0;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  bool changed = false;
+  for (size_t k = 0; k < b->classes.size() && e == cudaSuccess; ++k) {
+    ArcsClass &c = b->classes[k];
+    const std::string key = class_key(b, c, items);
+    auto it = g_tune.find(key);
+    TuneChoice best;
+    if (it != g_tune.end()) {
+      best = it->second;
+    } else {
+      const int m = std::min(c.item_end - c.item_begin, 4 * ctx->sm_count);
+      best.moves_per_s = -1.0;
+      for (int lanes : {2, 4, 8}) {
+        for (int w : {4, 2, 1}) {
+          if ((size_t)w * c.smem_per_warp > cap_smem) continue;
+          const int per_sm = arcs_ctas_per_sm(c.nb_smem, lanes, w, c.smem_per_warp);
+          const int grid = std::max(1, std::min(per_sm * ctx->sm_count, (m + w - 1) / w));
+          ArcsLaunch a{b->units.p, b->items.p + c.item_begin, m, b->heads.p + k, b->pos0.p,
+                       b->row_ptr.p, b->nbr.p, b->inv_t.p, b->movable.p, b->lrp.p, b->lent.p,
+                       b->lst.p, b->nulls.p, b->pos_out.p, b->outs.p, b->done.p, nullptr};
+          float ms = 0.0f;
+          for (int rep = 0; rep < 2 && e == cudaSuccess; ++rep) {
+            e = cudaMemsetAsync(b->heads.p + k, 0, sizeof(int), s);
+            if (e == cudaSuccess && rep == 1) e = cudaEventRecord(e0, s);
+            if (e == cudaSuccess) e = arcs_launch(a, T, c.nb_smem, lanes, grid, w, c.smem_per_warp, s);
+            if (e == cudaSuccess && rep == 1) e = cudaEventRecord(e1, s);
+          }
+          if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+          if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+          if (e != cudaSuccess) break;
+          const double rate = (double)m * kTuneMoves / std::max(1e-6, (double)ms * 1e-3);
+          if (rate > best.moves_per_s) {
+            best.lanes = lanes;
+            best.warps = w;
+            best.moves_per_s = rate;
+          }
+        }
+        if (e != cudaSuccess) break;
+      }
+      if (e == cudaSuccess) {
+        g_tune[key] = best;
+        changed = true;
+      }
+    }
+    if (e != cudaSuccess) break;
+    c.lanes = best.lanes;
+    c.warps_per_cta = best.warps;
+    const int per_sm = arcs_ctas_per_sm(c.nb_smem, c.lanes, c.warps_per_cta, c.smem_per_warp);
+    const int items_n = c.item_end - c.item_begin;
+    c.grid = std::max(1, std::min(per_sm * ctx->sm_count,
+                                  (items_n + c.warps_per_cta - 1) / c.warps_per_cta));
+  }
+  if (changed || fresh_path) tune_save(path);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return e;
+}
+
 extern "C" pmmc_status pmmc_arcs_batch_create_ex(
     pmmc_ctx *ctx, int n_units, const pmmc_arcs_problem *units,
     const pmmc_anneal_params *prm, const float *steps,
@@ -962,6 +1123,7 @@ extern "C" pmmc_status pmmc_arcs_batch_create_ex(
     return a.bytes > c.bytes;
   });
   std::vector<int2> h_items;
+  const bool tune = opts && opts->lanes_per_chain == PMMC_LANES_AUTO;
   int lanes = opts && opts->lanes_per_chain > 0 ? opts->lanes_per_chain : 2;
   if (lanes != 2 && lanes != 4 && lanes != 8 && lanes != 32) lanes = 2;
   b->lanes = lanes;
@@ -983,6 +1145,7 @@ extern "C" pmmc_status pmmc_arcs_batch_create_ex(
     int w = 4;
     while (w > 1 && (size_t)w * c.smem_per_warp > cap_smem) w >>= 1;
     c.warps_per_cta = w;
+    c.lanes = lanes;
     const int per_sm = arcs_ctas_per_sm(nbs, lanes, w, c.smem_per_warp);
     const int items_n = c.item_end - c.item_begin;
     c.grid = std::max(1, std::min(per_sm * ctx->sm_count, (items_n + w - 1) / w));
@@ -1022,11 +1185,13 @@ extern "C" pmmc_status pmmc_arcs_batch_create_ex(
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&c.join, cudaEventDisableTiming);
   }
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e == cudaSuccess && tune) e = autotune_classes(b, s);
   if (e != cudaSuccess) {
     delete b;
     return fail(ctx, e == cudaErrorMemoryAllocation ? PMMC_ERR_NOMEM : PMMC_ERR_CUDA,
                 "arcs batch upload: %s", cudaGetErrorString(e));
   }
+  if (!b->classes.empty()) b->lanes = b->classes[0].lanes;
   *out = b;
   return PMMC_OK;
 }
@@ -1046,7 +1211,7 @@ cudaError_t enqueue_pass(pmmc_arcs_batch *b, cudaStream_t s) {
                  b->heads.p + k, b->pos0.p, b->row_ptr.p, b->nbr.p, b->inv_t.p, b->movable.p,
                  b->lrp.p, b->lent.p, b->lst.p, b->nulls.p, b->pos_out.p, b->outs.p,
                  b->done.p, b->trace};
-    e = arcs_launch(a, b->P, c.nb_smem, b->lanes, c.grid, c.warps_per_cta, c.smem_per_warp,
+    e = arcs_launch(a, b->P, c.nb_smem, c.lanes, c.grid, c.warps_per_cta, c.smem_per_warp,
                     c.stream);
     if (e == cudaSuccess) e = cudaEventRecord(c.join, c.stream);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(s, c.join, 0);
@@ -1173,6 +1338,21 @@ extern "C" pmmc_status pmmc_arcs_batch_stats(pmmc_arcs_batch *b, double *kernel_
     int multi = 0;
     for (auto &U : b->h_units) multi |= U.chains > 1;
     *launches_per_run = (int)b->classes.size() + multi;
+  }
+  return PMMC_OK;
+}
+
+extern "C" pmmc_status pmmc_arcs_batch_classes(pmmc_arcs_batch *b, int cap, int *n_classes,
+                                               int *lanes, int *warps, int *items,
+                                               int *nb_smem) {
+  if (!b || !n_classes) return PMMC_ERR_INVALID;
+  *n_classes = (int)b->classes.size();
+  for (int k = 0; k < (int)b->classes.size() && k < cap; ++k) {
+    const ArcsClass &c = b->classes[k];
+    if (lanes) lanes[k] = c.lanes;
+    if (warps) warps[k] = c.warps_per_cta;
+    if (items) items[k] = c.item_end - c.item_begin;
+    if (nb_smem) nb_smem[k] = c.nb_smem ? 1 : 0;
   }
   return PMMC_OK;
 }

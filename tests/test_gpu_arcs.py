@@ -135,6 +135,40 @@ def test_arcs_batch_units_match_oracle(ctx, lanes):
     assert same >= len(regs) - 1
 
 
+def test_arcs_batch_autotune(ctx, tmp_path, monkeypatch):
+    """PMMC_LANES_AUTO: every class gets lanes and warps from timed trials,
+    the choices land in the JSON cache, the batch still follows the oracle,
+    and a second batch of the same shape reuses the cached choices."""
+    import json
+    path = tmp_path / "tune.json"
+    monkeypatch.setenv("PMMC_AUTOTUNE_CACHE", str(path))
+    sizes = [32, 57, 130, 300, 80, 41, 1500, 2048]
+    regs = [synth.arcs_region(n, int(1.5 * n), seed=s) for s, n in enumerate(sizes)]
+    inputs = [capi.ArcsInput.from_dense(r.pos, r.dense()) for r in regs]
+    base = dict(max_temp=5.0, dt_temp=0.9999, milestone_steps=1000, improvement=0.99)
+    prm = capi.default_params(capi.LEVEL_ARCS, schedule=capi.SCHEDULE_CPU, max_moves=3000, **base)
+    ctx.set_seed(99)
+    b = capi.ArcsBatch(ctx, inputs, prm, [0.5] * len(inputs), lanes=capi.LANES_AUTO)
+    cls = b.classes()
+    assert cls and all(la in (2, 4, 8) and w in (1, 2, 4) for la, w, _, _ in cls)
+    assert sum(it for _, _, it, _ in cls) == len(inputs)
+    data = json.load(open(path))
+    assert len(data["entries"]) >= len(cls)
+    assert all(v["moves_per_s"] > 0 for v in data["entries"].values())
+    b.run()
+    pos, res = b.results()
+    same = 0
+    for u, r in enumerate(regs):
+        pr = O.ArcsProblem(r.pos, r.dense())
+        opos, ores = O.arcs_anneal(pr, O.Params(max_moves=3000, **base), 0.5, 99,
+                                   rng=O.RNG_PHILOX, chain=u)
+        assert abs(ores.score - res[u].energy) <= 1e-3 * abs(ores.score)
+        same += int(ores.moves == res[u].moves and np.allclose(opos, pos[u], atol=1e-3))
+    assert same >= len(regs) - 1
+    b2 = capi.ArcsBatch(ctx, inputs, prm, [0.5] * len(inputs), lanes=capi.LANES_AUTO)
+    assert b2.classes() == cls
+
+
 def test_arcs_batch_graph_replay_is_deterministic(ctx):
     regs = [synth.arcs_region(n, int(1.5 * n), seed=s) for s, n in enumerate([64, 200, 700])]
     inputs = [capi.ArcsInput.from_dense(r.pos, r.dense()) for r in regs]
