@@ -262,10 +262,11 @@ def traffic_per_launch():
     return None
 
 
-def make_inputs(rank: int):
+def make_inputs(rank: int, world: int = 1):
     from pmmc_gb300 import capi, synth
-    ens = synth.arcs_ensemble(N_STRUCT, N_BLOCKS, seeds=range(N_STRUCT * rank,
-                                                               N_STRUCT * (rank + 1)))
+    from pmmc_gb300.replicas import shard_seeds
+    ens = synth.arcs_ensemble(N_STRUCT, N_BLOCKS, seeds=shard_seeds(rank, max(world, rank + 1),
+                                                                    N_STRUCT))
     regs = [r for s in ens for r in s]
     inputs = [capi.ArcsInput(r.pos, *r.csr()) for r in regs]
     return regs, inputs
@@ -296,7 +297,7 @@ def run_gpu(args, rank, world):
     dev = torch.cuda.current_device()
     ctx = capi.Context(dev)
     ctx.set_seed(2024 + rank)
-    regs, inputs = make_inputs(rank)
+    regs, inputs = make_inputs(rank, world)
     prm = capi.default_params(capi.LEVEL_ARCS, schedule=capi.SCHEDULE_CPU,
                               resync_every=RESYNC, **ANNEAL)
     steps = [STEP] * len(inputs)
@@ -458,19 +459,13 @@ def main():
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", rank)))
         dist.init_process_group("nccl")
     r = run_gpu(args, rank, world)
-    # max over ranks
+    # max over ranks (replicas: the only cross-rank step)
+    from pmmc_gb300.replicas import combine
+    step_ms, total_moves = combine(r["step_ms"], float(r["moves"]),
+                                   device="cuda" if world > 1 else None)
     if world > 1:
-        import torch
         import torch.distributed as dist
-        t = torch.tensor([r["step_ms"], float(r["moves"])], dtype=torch.float64, device="cuda")
-        gathered = [torch.zeros_like(t) for _ in range(world)]
-        dist.all_gather(gathered, t)
-        step_ms = max(float(g[0]) for g in gathered)
-        total_moves = sum(float(g[1]) for g in gathered)
         dist.destroy_process_group()
-    else:
-        step_ms = r["step_ms"]
-        total_moves = float(r["moves"])
     if rank != 0:
         return
     value = total_moves / (step_ms * 1e-3)
