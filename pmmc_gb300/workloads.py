@@ -37,6 +37,18 @@ def _peak():
     return 6800.0, "fallback"
 
 
+def _traffic(kernel: str, workload: str):
+    """DRAM bytes per launch from the committed ncu summary, if recorded."""
+    p = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))),
+                     "profiles", "traffic_per_launch.txt")
+    if os.path.exists(p):
+        for line in open(p):
+            f = line.split()
+            if len(f) >= 3 and f[0] == kernel and f[1] == workload:
+                return float(f[2])
+    return None
+
+
 def _heatmap(args, n_maps):
     import torch
     torch.cuda.init()
@@ -61,8 +73,12 @@ def _heatmap(args, n_maps):
             total = sum(r.moves for r in res)
     ms = float(np.mean(times))
     row_bytes = 4 * 2048
-    achieved = total * row_bytes / (ms * 1e-3) / 1e9
+    # one launch reads each move's row once and each map twice in full (the
+    # FP64 start and end scores)
+    alg = total * row_bytes + 2 * n_maps * 2048 * 2048 * 4
+    achieved = alg / (ms * 1e-3) / 1e9
     peak, kind = _peak()
+    traffic = _traffic("heatmap_anneal_kernel", f"heatmap_{n_maps}x2048_moves{moves}")
     line = {
         "metric": "MC moves/s", "value": total / (ms * 1e-3), "unit": "moves/s",
         "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
@@ -72,8 +88,9 @@ def _heatmap(args, n_maps):
                    "maps": n_maps, "moves_per_step": total},
         "final_energy_rel_error_max": max(r.rel_error for r in res),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "traffic": None, "peak_source": kind,
-                     "algorithmic_bytes_per_move": row_bytes},
+                     "frac": achieved / peak, "traffic": traffic, "peak_source": kind,
+                     "algorithmic_bytes_per_move": row_bytes,
+                     "algorithmic_bytes_per_launch": alg},
     }
     print(json.dumps(line))
 
