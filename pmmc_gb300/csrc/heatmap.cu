@@ -49,7 +49,7 @@ struct HeatUnit {
   int chain_id;
   long long out_off;
   float step;
-  int pad;
+  int single;        // 1: one chromosome block (every bead's block is [0, n-1])
 };
 
 struct HeatDevParams {
@@ -202,7 +202,7 @@ __device__ double heat_full(const HeatUnit &U, const float4 *spos, const float *
   for (int i = threadIdx.x; i < U.n; i += blockDim.x)
     acc += sphere_penalty(spos[i].x, spos[i].y, spos[i].z, R);
   for (int m = warp; m < U.n; m += nw) {
-    const int2 r = blk[m];
+    const int2 r = U.single ? make_int2(0, U.n - 1) : blk[m];
     const float *row = rheat + U.heat_off + (long long)m * U.pitch;
     const float4 pm = spos[m];
     float part = 0.0f;
@@ -251,6 +251,12 @@ struct WinPlan {
   int pad[2];
 };
 
+// Bytes of the kernel's shared-memory header (barriers, reduction scratch,
+// partial sums, pair corrections, window plan, draw ring), as carved below.
+constexpr size_t kHeadBytes =
+    ((((16 * 8 + 32 * 8 + 16 * kWin * 4 + kWin * kWin * 4 + sizeof(WinPlan)) + 15) / 16 * 16 +
+      128 * sizeof(MoveRec) + 128 * 4) + 127) / 128 * 128;
+
 // Exact in-order windows: every thread scores its slice of the rows of up to
 // kWin moves against the window-start positions; pair corrections restore the
 // terms between two beads of the same window once the earlier one has been
@@ -295,10 +301,12 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
   p += (size_t)D * pitch * 4;
   float4 *spos = reinterpret_cast<float4 *>(p);
   p += (size_t)n * 16;
-  // per-bead chromosome block and the movable list: staged next to the positions
+  // per-bead chromosome block (maps with boundaries) and the movable list
+  // (regions with fixed beads): staged next to the positions
   int2 *blk = reinterpret_cast<int2 *>(p);
-  p += (size_t)n * 8;
+  if (!U.single) p += (size_t)n * 8;
   int *smov = reinterpret_cast<int *>(p);
+  auto block_of = [&](int b) { return U.single ? make_int2(0, n - 1) : blk[b]; };
 
   const int *MOV = U.mov_off >= 0 ? smov : nullptr;
   const float *rrow0 = rheat + U.heat_off;
@@ -309,7 +317,7 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
   }
   for (int i = tid; i < n; i += nthr) {
     spos[i] = pos0[U.pos_off + i];
-    blk[i] = blk_all[U.blk_off + i];
+    if (!U.single) blk[i] = blk_all[U.blk_off + i];
   }
   if (U.mov_off >= 0)
     for (int k = tid; k < U.n_mov; k += nthr) smov[k] = movable[U.mov_off + k];
@@ -344,7 +352,7 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
       if (lane < cnt) {
         const long long k = issued + lane;
         const int b = recs[k & 127].b;
-        const int2 r = blk[b];
+        const int2 r = block_of(b);
         const int st = r.x & ~3;
         const int en = min((r.y + 4) & ~3, pitch);
         tma_row(slots + (size_t)(k & dmask) * pitch, rrow0 + (long long)b * pitch + st,
@@ -373,7 +381,7 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
     const int ww = lane < L ? lane : 0;
     const long long k = m0 + ww;
     const MoveRec rec = recs[k & 127];
-    const int2 bk = blk[rec.b];
+    const int2 bk = block_of(rec.b);
     const int bx0 = __shfl_sync(0xffffffffu, bk.x, 0), by0 = __shfl_sync(0xffffffffu, bk.y, 0);
     const unsigned diff = __ballot_sync(0xffffffffu, bk.x != bx0 || bk.y != by0);
     bool late = false;
@@ -442,7 +450,7 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
 #pragma unroll
     for (int w = 0; w < kWin; ++w) part[w] = 0.0f;
     if (same) {
-      const int2 r = blk[plan_s->bw[0]];
+      const int2 r = block_of(plan_s->bw[0]);
       for (int i = r.x + tid; i <= r.y; i += nthr) {
         const float4 pi = spos[i];
 #pragma unroll
@@ -453,7 +461,7 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
 #pragma unroll
       for (int w = 0; w < kWin; ++w) {
         if (w < L) {
-          const int2 r = blk[plan_s->bw[w]];
+          const int2 r = block_of(plan_s->bw[w]);
           for (int i = r.x + tid; i <= r.y; i += nthr) {
             const float4 pi = spos[i];
             part[w] += pair_delta(pi.x, pi.y, pi.z, g[w], slots[roff[w] + i]);
@@ -467,7 +475,7 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
       float v = 0.0f;
       if (j < w && w < L) {
         const int bw = plan_s->bw[w], bj = plan_s->bw[j];
-        const int2 r = blk[bw];
+        const int2 r = block_of(bw);
         if (bj >= r.x && bj <= r.y) {
           const float4 gb = plan_s->gb[w];
           const float rv = slots[__float_as_int(gb.w) + bj];
@@ -658,6 +666,7 @@ extern "C" pmmc_status pmmc_heatmap_batch_anneal(pmmc_ctx *ctx, int n_units,
   std::vector<int2> hblk;
   long long heat_floats = 0, out_off = 0;
   int max_n = 0, max_pitch = 0;
+  size_t max_bead_bytes = 0;
   for (int u = 0; u < n_units; ++u) {
     const pmmc_heatmap_problem &pr = units[u];
     if (pr.n < 2 || !pr.pos || !pr.heat || pr.diag < 0 || pr.n_bounds < 0 ||
@@ -678,6 +687,11 @@ extern "C" pmmc_status pmmc_heatmap_batch_anneal(pmmc_ctx *ctx, int n_units,
     if (U.n_mov < pr.n) hmov.insert(hmov.end(), mv.begin(), mv.end());
     U.blk_off = (int)hblk.size();
     bead_blocks(pr.n, pr.n_bounds, pr.bounds, hblk);
+    U.single = 1;
+    for (int i = 0; i < pr.n; ++i) {
+      const int2 b = hblk[(size_t)U.blk_off + i];
+      if (b.x != 0 || b.y != pr.n - 1) U.single = 0;
+    }
     U.heat_off = heat_floats;
     heat_floats += (long long)U.pitch * pr.n;
     U.chain_id = u;
@@ -686,6 +700,9 @@ extern "C" pmmc_status pmmc_heatmap_batch_anneal(pmmc_ctx *ctx, int n_units,
     U.step = steps[u] * 0.5f;  // MonteCarloHeatmap halves the step (:1426)
     max_n = std::max(max_n, pr.n);
     max_pitch = std::max(max_pitch, U.pitch);
+    // staged per bead: position, block (maps with boundaries), movable index
+    max_bead_bytes = std::max(max_bead_bytes, (size_t)pr.n * (16 + (U.single ? 0 : 8) +
+                                                               (U.mov_off >= 0 ? 4 : 0)));
     hu[u] = U;
   }
   if (hmov.empty()) hmov.push_back(0);
@@ -709,19 +726,31 @@ extern "C" pmmc_status pmmc_heatmap_batch_anneal(pmmc_ctx *ctx, int n_units,
     P.dtpow[l] = dp;
     dp *= (double)prm->dt_temp;
   }
-  // shared memory: header + D row slots + positions
-  const size_t head = 6144;
-  const size_t pos_bytes = (size_t)max_n * (16 + 8 + 4);  // positions, blocks, movable
+  // Shared memory: header + D row slots + per-bead arrays.  With at least two
+  // chains per SM of work, two CTAs of 256 threads share an SM (one chain's
+  // serial decisions overlap the other's row pass) when a ring of 8 rows
+  // still fits in half the SM's shared memory; otherwise one CTA per SM.
+  const size_t head = kHeadBytes;
   const size_t row_bytes = (size_t)max_pitch * 4;
-  const size_t avail = ctx->smem_optin;
-  if (head + pos_bytes + 2 * row_bytes > avail)
+  int depth = 0, ctas_per_sm = 1;
+  size_t smem = 0;
+  for (int mode : {2, 1}) {
+    if (mode == 2 && n_units < 2 * ctx->sm_count) continue;
+    const size_t avail = mode == 2 ? std::min(ctx->smem_optin, ctx->smem_per_sm / 2 - 1024)
+                                   : ctx->smem_optin;
+    if (head + max_bead_bytes + 2 * row_bytes > avail) continue;
+    const size_t fit = (avail - head - max_bead_bytes) / row_bytes;
+    int d = 2;
+    while (d < 16 && (size_t)d * 2 <= fit) d *= 2;
+    if (mode == 2 && d < kWin) continue;
+    depth = d;
+    ctas_per_sm = mode;
+    smem = head + (size_t)d * row_bytes + max_bead_bytes;
+    break;
+  }
+  if (depth == 0)
     return fail(ctx, PMMC_ERR_INVALID, "heatmap region of %d beads does not fit shared memory", max_n);
-  // ring depth: a power of two up to 16 that fits
-  const size_t fit = (avail - head - pos_bytes) / row_bytes;
-  int depth = 2;
-  while (depth < 16 && (size_t)depth * 2 <= fit) depth *= 2;
   P.depth = depth;
-  const size_t smem = head + (size_t)depth * row_bytes + pos_bytes;
 
   cudaStream_t s = ctx->stream;
   // The kernels read r = 1/h, rows padded to a 16-byte pitch, with r = 0
@@ -771,13 +800,17 @@ extern "C" pmmc_status pmmc_heatmap_batch_anneal(pmmc_ctx *ctx, int n_units,
                 "heatmap upload: %s", cudaGetErrorString(e));
   PMMC_CUDA(ctx, cudaFuncSetAttribute(heatmap_anneal_kernel,
                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+  PMMC_CUDA(ctx, cudaFuncSetAttribute(heatmap_anneal_kernel,
+                                      cudaFuncAttributePreferredSharedMemoryCarveout, 100));
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   cudaEventRecord(e0, s);
-  // threads per chain: about four row entries per thread, 128..512
+  // threads per chain: about four row entries per thread, 128..512 (at most
+  // 256 when two chains share an SM)
   int threads = 128;
-  while (threads < kHeatMaxThreads && threads * 4 < max_n) threads *= 2;
+  const int max_threads = ctas_per_sm == 2 ? 256 : kHeatMaxThreads;
+  while (threads < max_threads && threads * 4 < max_n) threads *= 2;
   heatmap_anneal_kernel<<<n_units, threads, smem, s>>>(
       d_units.p, d_pos.p, d_rheat.p, d_mov.p, d_blk.p, P, d_out.p, d_outs.p,
       trace_cap > 0 ? d_trace.p : nullptr);

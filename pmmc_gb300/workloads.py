@@ -5,9 +5,10 @@ heatmap        one chain on a 2048-bead map (contact map |i-j|^-1 x
                lognormal(0.5), 20 TADs x3, expected distance c^-1/3), T0 5,
                cooling 0.9999, milestones every 100k moves: moves/s.
 heatmap-batch  one chain per distinct 2048-bead map (16 MB each; the
-               generated map scaled by a per-map factor), one map per SM by
+               generated map scaled by a per-map factor), two maps per SM by
                default: the form whose rows stream from HBM; reports HBM GB/s
-               of the row traffic (4 bytes per row entry per move).
+               of the row traffic (4 bytes per row entry per move) and of the
+               two FP64 full scores per map.
 smooth         genome-scale smoothing: 23 chromosomes (~300k beads, anchors
                every Poisson(10) beads, fixed), split at the anchors into
                independent regions; 20k sweeps (moves = 20k x free beads).
@@ -53,6 +54,8 @@ def _heatmap(args, n_maps):
     import torch
     torch.cuda.init()
     ctx = capi.Context(0)
+    if n_maps <= 0:          # two distinct maps per SM (two chains share an SM)
+        n_maps = 2 * ctx.sm_count
     base = synth.heatmap_region(2048, seed=7)
     # distinct maps in memory (the rows of every chain stream from HBM): the
     # generated map scaled by a per-map factor
@@ -263,6 +266,6 @@ def main(args):
     if args.workload == "heatmap":
         _heatmap(args, 1)
     elif args.workload == "heatmap-batch":
-        _heatmap(args, args.maps or 152)
+        _heatmap(args, args.maps or 0)
     else:
         _smooth(args)

@@ -58,3 +58,27 @@ def test_heatmap_statistics_match_reference(ctx):
     out, res, ms, _ = capi.heatmap_batch_anneal(ctx, [capi.HeatmapInput(h.pos, h.heat)] * 16,
                                                 prm, [1.0] * 16)
     assert ks_2samp_p(ref_e, [r.energy for r in res]) > 0.05
+
+
+def test_heatmap_two_chains_per_sm(ctx):
+    """With at least two chains per SM the batch runs two 256-thread CTAs per
+    SM; chains still follow the oracle (trace of chain 0, energies of a
+    sample of the others)."""
+    n_units = 2 * ctx.sm_count + 3
+    hs = [synth.heatmap_region(96 + (u % 5) * 8, seed=1000 + u, n_tads=3, tad_min=8, tad_max=20)
+          for u in range(n_units)]
+    base = dict(max_temp=5.0, dt_temp=0.9999, milestone_steps=1500, improvement=0.99)
+    prm = capi.default_params(capi.LEVEL_HEATMAP, schedule=capi.SCHEDULE_CPU, max_moves=1500, **base)
+    ctx.set_seed(21)
+    out, res, ms, tr = capi.heatmap_batch_anneal(
+        ctx, [capi.HeatmapInput(h.pos, h.heat) for h in hs], prm, [1.0] * n_units, trace_cap=1500)
+    m = int(res[0].moves)
+    pr0 = O.HeatmapProblem(hs[0].pos, hs[0].heat)
+    rep = O.heatmap_replay(pr0, O.Params(**base), 1.0, 21, 0, tr[:m])
+    check_replay(tr[:m], rep, scale_factor=2.0, delta_only=True)
+    for u in range(0, n_units, 37):
+        pr = O.HeatmapProblem(hs[u].pos, hs[u].heat)
+        opos, ores = O.heatmap_anneal(pr, O.Params(max_moves=1500, **base), 1.0, 21,
+                                      rng=O.RNG_PHILOX, incremental=True, chain=u)
+        assert abs(ores.score - res[u].energy) <= 1e-3 * ores.score
+        assert res[u].rel_error < 1e-6 and res[u].status == 0
