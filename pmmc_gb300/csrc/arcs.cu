@@ -210,6 +210,46 @@ __device__ double arcs_spring_energy_ff(int n, const float4 *spos, const int *sr
   return warp_sum_d(t);
 }
 
+// The same recompute from the region's flat spring list: every lane takes
+// every 32nd spring, four at a time with independent accumulators, so no lane
+// waits for another's longer arc list.
+__device__ double arcs_spring_energy_list(int n, const float4 *spos, const int4 *arcl,
+                                          int n_arcs, const int4 *loops, int n_loops,
+                                          const ArcsDevParams &P, int lane) {
+  const float ks = P.k_stretch, kq = P.k_squeeze, R = P.sphere_r;
+  float hi[4] = {0.f, 0.f, 0.f, 0.f}, lo[4] = {0.f, 0.f, 0.f, 0.f};
+  if (R > 0.0f)
+    for (int i = lane; i < n; i += 32) {
+      const float4 q = spos[i];
+      ff_add(hi[1], lo[1], sphere_penalty(q.x, q.y, q.z, R));
+    }
+  int c = lane;
+  for (; c + 96 < n_arcs; c += 128) {
+    int4 a[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) a[r] = arcl[c + 32 * r];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const float v = spring_fast(resync_len(spos[a[r].x], spos[a[r].y]), __int_as_float(a[r].z),
+                                  __int_as_float(a[r].w), ks, kq);
+      ff_add(hi[r], lo[r], v);
+    }
+  }
+  for (; c < n_arcs; c += 32) {
+    const int4 a = arcl[c];
+    ff_add(hi[0], lo[0], spring_fast(resync_len(spos[a.x], spos[a.y]), __int_as_float(a.z),
+                                     __int_as_float(a.w), ks, kq));
+  }
+  for (int k = lane; k < n_loops; k += 32) {
+    const int4 L = loops[k];
+    const float d = (L.x == L.y ? 0.0f : resync_len(spos[L.x], spos[L.y])) - __int_as_float(L.w);
+    ff_add(hi[2], lo[2], __int_as_float(L.z) * d * d);
+  }
+  const double t = ((double)hi[0] + (double)lo[0]) + ((double)hi[1] + (double)lo[1]) +
+                   ((double)hi[2] + (double)lo[2]) + ((double)hi[3] + (double)lo[3]);
+  return warp_sum_d(t);
+}
+
 // FP64 sum of 1/d over every pair (i<j) that the arc lists do not name.
 __device__ double arcs_repulsion(int n, const float4 *spos, const int *srp,
                                  const int2 *nb, const int2 *nulls, int n_null,
@@ -534,7 +574,10 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
       if (moves == next_rs) {
         next_rs += P.resync;
         if (!flag) {
-          double es = arcs_spring_energy_ff(n, spos, srp, NB, INV, LST, U.n_loops, P, lane);
+          double es = U.n_arcs >= 0
+                          ? arcs_spring_energy_list(n, spos, lst + U.arc_off, U.n_arcs, LST,
+                                                    U.n_loops, P, lane)
+                          : arcs_spring_energy_ff(n, spos, srp, NB, INV, LST, U.n_loops, P, lane);
           if (P.ext) es += ext_full(n, spos, P, lane);
           const double Er = base + es;
           e_hi = (float)Er;
@@ -838,6 +881,18 @@ void ArcsPack::add(const pmmc_arcs_problem &pr, int n_chains, float step, uint64
     U.lent_off = 0;
     U.n_lent = 0;
   }
+  // every spring once (entries whose partner precedes the row), for the
+  // periodic recompute: a flat list balances the lanes
+  U.arc_off = (int)lst.size();
+  U.n_arcs = 0;
+  for (int i = 0; i < pr.n; ++i)
+    for (int e = pr.row_ptr[i]; e < pr.row_ptr[i + 1]; ++e) {
+      const float t = pr.target[e];
+      if (pr.col[e] < i && t >= 1e-6f) {
+        lst.push_back(make_int4(pr.col[e], i, __float_as_int_host(t), __float_as_int_host(1.0f / t)));
+        ++U.n_arcs;
+      }
+    }
   U.chains = n_chains;
   U.chain_base = chains;
   U.out_off = out_floats;
@@ -862,6 +917,7 @@ void ArcsPack::append(const ArcsPack &o) {
     if (U.lrp_off >= 0) U.lrp_off += lrp0;
     U.lent_off += lent0;
     U.lst_off += lst0;
+    if (U.n_arcs >= 0) U.arc_off += lst0;
     U.chain_base += chains;
     U.out_off += out_floats;
     units.push_back(U);
@@ -1512,6 +1568,8 @@ __global__ void noalloc_stage_kernel(NoAllocScratch *S, int n, int nnz, const fl
     U.step = step;
     U.rng_chain = 0;
     U.seed = seed;
+    U.arc_off = 0;
+    U.n_arcs = -1;  // no spring list: the recompute walks the arc lists
     S->unit = U;
     S->item = make_int2(0, 0);
     S->head = 0;

@@ -33,6 +33,9 @@ struct ArcsUnit {
   float step;
   int rng_chain;  // Philox chain id of the unit's chain 0
   uint64_t seed;  // Philox key of the unit's chains
+  int arc_off;    // index into the int4 list array of the region's springs,
+  int n_arcs;     // one entry {i, j, target bits, 1/target bits} per arc;
+                  // n_arcs < 0: no list (recomputes walk the arc lists)
 };
 
 struct ArcsDevParams {
@@ -76,7 +79,7 @@ struct ArcsPack {
   std::vector<int2> nbr, nulls;
   std::vector<float> inv;
   std::vector<float4> lent;
-  std::vector<int4> lst;
+  std::vector<int4> lst;      // loop constraints, then each region's spring list
   long long out_floats = 0;  // xyz floats over all chains
   int chains = 0;            // chains over all units
   // Appends one region with `chains` chains; Philox key `seed`, chain ids
