@@ -223,7 +223,7 @@ typedef struct pmmc_arcs_batch pmmc_arcs_batch;
 typedef struct pmmc_batch_opts {
   int chains_per_unit;   /* independent chains per unit (>= 1)           */
   int use_graph;         /* capture the launches in a CUDA graph          */
-  int lanes_per_chain;   /* lanes that score one proposal: 2, 4, 8 or 32;
+  int lanes_per_chain;   /* lanes that score one proposal: 1, 2, 4, 8 or 32;
                           * a chain's warp scores 32/lanes proposals at
                           * once (0 = the default, 2; PMMC_LANES_AUTO =
                           * the autotuner picks lanes and warps per CTA
@@ -346,7 +346,7 @@ typedef struct {
   size_t budget_bytes;    /* device bytes of resident regions; 0 = half the free memory */
   int max_waves;          /* launches in flight at once; 0 = 8 */
   int max_wave_requests;  /* regions per launch; 0 = 4 x SM count */
-  int lanes_per_chain;    /* 2, 4, 8 or 32 lanes per proposal; 0 = 2 */
+  int lanes_per_chain;    /* 1, 2, 4, 8 or 32 lanes per proposal; 0 = 2 */
 } pmmc_server_opts;
 
 typedef struct {

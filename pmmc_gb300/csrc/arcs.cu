@@ -323,7 +323,9 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
 
     // ---- stage the region in this warp's shared-memory slice ----
     int *srp = reinterpret_cast<int *>(spos + n);
-    size_t off = (size_t)kMoveBufBytes + (size_t)n * 16 + (size_t)(n + 1) * 4;
+    // per-bead mask of the current window's slots holding that bead
+    unsigned *smask = reinterpret_cast<unsigned *>(srp + n + 1);
+    size_t off = (size_t)kMoveBufBytes + (size_t)n * 16 + (size_t)(n + 1) * 4 + (size_t)n * 4;
     off = (off + 7) & ~(size_t)7;
     int2 *snb = reinterpret_cast<int2 *>(wbase + off);
     float *sinv = reinterpret_cast<float *>(wbase + off + (size_t)U.nnz * 8);
@@ -334,6 +336,7 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
 
     for (int i = lane; i < n; i += 32) spos[i] = pos0[U.pos_off + i];
     for (int i = lane; i <= n; i += 32) srp[i] = row_ptr[U.rp_off + i];
+    for (int i = lane; i < n; i += 32) smask[i] = 0u;
     if (NB_SMEM) {
       for (int e = lane; e < U.nnz; e += 32) {
         snb[e] = nbr[U.nbr_off + e];
@@ -376,7 +379,9 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
     // accepted proposal of the same window closes the window there: it is
     // re-scored from the updated positions as the first proposal of the next
     // window.  The accepted sequence is therefore the one the one-move-at-a-
-    // time algorithm produces.
+    // time algorithm produces.  Which slots hold a bead is a per-bead bit mask
+    // in shared memory (set for the window, cleared after it), so a partner
+    // check is one load whatever the window size.
     constexpr int W = 32 / G;
     const int g = lane / G;    // proposal slot of this lane
     const int sub = lane % G;  // lane within the slot
@@ -414,9 +419,8 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
       const int4 mv = active ? s_mv[k0 + g] : make_int4(0, 0, 0, 0);
       const float thr = active ? s_thr[k0 + g] : 0.0f;
       const int b = mv.x;
-      int bj[W];
-#pragma unroll
-      for (int j = 0; j < W; ++j) bj[j] = __shfl_sync(0xffffffffu, b, j * G);
+      if (active && sub == 0) atomicOr(&smask[b], 1u << g);
+      __syncwarp();
       float so = 0.0f, sn = 0.0f;
       unsigned cm = 0u;
       float4 pb = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -445,11 +449,7 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
           const float n2 = spring_fast(fast_len(nx, ny, nz, q2), t2, iv2, ks, kq);
           so += o1 + (two ? o2 : 0.0f);
           sn += n1 + (two ? n2 : 0.0f);
-          unsigned hit = 0u;
-#pragma unroll
-          for (int j = 0; j < W; ++j)
-            hit |= (unsigned)(ent.x == bj[j] || ent2.x == bj[j]) << j;
-          cm |= hit & earlier;
+          cm |= (smask[ent.x] | (two ? smask[ent2.x] : 0u)) & earlier;
         }
         if (has_loops) {
           const int l1 = LRP[b + 1];
@@ -462,10 +462,7 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
             const float d1 = (pj == b ? 0.0f : fast_len(nx, ny, nz, q)) - le.z;
             so += le.y * d0 * d0;
             sn += le.y * d1 * d1;
-            unsigned hit = 0u;
-#pragma unroll
-            for (int j = 0; j < W; ++j) hit |= (unsigned)(pj == bj[j]) << j;
-            cm |= hit & ((1u << g) - 1u);
+            cm |= smask[pj] & ((1u << g) - 1u);
           }
         }
         if (sub == 0) {
@@ -473,17 +470,16 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
             so += sphere_penalty(pb.x, pb.y, pb.z, R);
             sn += sphere_penalty(nx, ny, nz, R);
           }
-          unsigned hit = 0u;
+          unsigned hit = smask[b];
           if (P.ext) {
             // bonds and angles reach two beads along the chain: a window
             // proposal within that distance is a partner too
             so += ext_local(spos, n, b, pb, P);
             sn += ext_local(spos, n, b, make_float4(nx, ny, nz, 0.0f), P);
-#pragma unroll
-            for (int j = 0; j < W; ++j) hit |= (unsigned)(abs(b - bj[j]) <= 2) << j;
-          } else {
-#pragma unroll
-            for (int j = 0; j < W; ++j) hit |= (unsigned)(b == bj[j]) << j;
+            if (b >= 1) hit |= smask[b - 1];
+            if (b >= 2) hit |= smask[b - 2];
+            if (b + 1 < n) hit |= smask[b + 1];
+            if (b + 2 < n) hit |= smask[b + 2];
           }
           cm |= hit & ((1u << g) - 1u);
         }
@@ -550,6 +546,8 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
           }
         }
       }
+      __syncwarp();
+      if (active && sub == 0) smask[b] = 0u;  // every reader is past the window
       __syncwarp();
       if (accm) ff_add(e_hi, e_lo, pacc);
       const int na = __popc(accm);
@@ -650,6 +648,7 @@ using ArcsKernelFn = void (*)(const ArcsUnit *, const int2 *, int, int *, const 
 // The instantiation for a launch: arc lists staged or not, G lanes per move.
 inline ArcsKernelFn arcs_kernel_for(bool nb_smem, int lanes) {
   switch (lanes) {
+    case 1: return nb_smem ? arcs_anneal_kernel<true, 1> : arcs_anneal_kernel<false, 1>;
     case 2: return nb_smem ? arcs_anneal_kernel<true, 2> : arcs_anneal_kernel<false, 2>;
     case 8: return nb_smem ? arcs_anneal_kernel<true, 8> : arcs_anneal_kernel<false, 8>;
     case 32: return nb_smem ? arcs_anneal_kernel<true, 32> : arcs_anneal_kernel<false, 32>;
@@ -724,7 +723,7 @@ struct pmmc_arcs_batch {
 namespace pmmc {
 
 size_t arcs_unit_smem(int n, int nnz, int n_mov, bool has_mov) {
-  size_t s = (size_t)kMoveBufBytes + (size_t)n * 16 + (size_t)(n + 1) * 4;
+  size_t s = (size_t)kMoveBufBytes + (size_t)n * 16 + (size_t)(n + 1) * 4 + (size_t)n * 4;
   s = (s + 7) & ~(size_t)7;
   s += (size_t)nnz * 12;
   if (has_mov) s += (size_t)n_mov * 4;
@@ -732,7 +731,7 @@ size_t arcs_unit_smem(int n, int nnz, int n_mov, bool has_mov) {
 }
 
 size_t arcs_unit_smem_min(int n) {
-  size_t s = (size_t)kMoveBufBytes + (size_t)n * 16 + (size_t)(n + 1) * 4;
+  size_t s = (size_t)kMoveBufBytes + (size_t)n * 16 + (size_t)(n + 1) * 4 + (size_t)n * 4;
   return (s + 7) & ~(size_t)7;
 }
 
@@ -958,7 +957,7 @@ int arcs_ctas_per_sm(bool nb_smem, int lanes, int warps, int smem_per_warp) {
 }
 
 void arcs_set_smem_limit(int bytes) {
-  for (int lanes : {2, 4, 8, 32})
+  for (int lanes : {1, 2, 4, 8, 32})
     for (bool nbs : {true, false})
       cudaFuncSetAttribute(arcs_kernel_for(nbs, lanes),
                            cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
@@ -1077,7 +1076,7 @@ static cudaError_t autotune_classes(pmmc_arcs_batch *b, cudaStream_t s) {
     } else {
       const int m = std::min(c.item_end - c.item_begin, 4 * ctx->sm_count);
       best.moves_per_s = -1.0;
-      for (int lanes : {2, 4, 8}) {
+      for (int lanes : {1, 2, 4, 8}) {
         for (int w : {4, 2, 1}) {
           if ((size_t)w * c.smem_per_warp > cap_smem) continue;
           const int per_sm = arcs_ctas_per_sm(c.nb_smem, lanes, w, c.smem_per_warp);
@@ -1181,7 +1180,7 @@ extern "C" pmmc_status pmmc_arcs_batch_create_ex(
   std::vector<int2> h_items;
   const bool tune = opts && opts->lanes_per_chain == PMMC_LANES_AUTO;
   int lanes = opts && opts->lanes_per_chain > 0 ? opts->lanes_per_chain : 2;
-  if (lanes != 2 && lanes != 4 && lanes != 8 && lanes != 32) lanes = 2;
+  if (lanes != 1 && lanes != 2 && lanes != 4 && lanes != 8 && lanes != 32) lanes = 2;
   b->lanes = lanes;
   arcs_set_smem_limit((int)ctx->smem_optin);
   size_t i0 = 0;

@@ -361,8 +361,8 @@ extern "C" pmmc_status pmmc_server_create(pmmc_ctx *ctx, const pmmc_anneal_param
   sv->P = arcs_make_params(prm, 0, false);
   sv->P.trace_cap = 0;
   int lanes = opts && opts->lanes_per_chain > 0 ? opts->lanes_per_chain : 2;
-  if (lanes != 2 && lanes != 4 && lanes != 8 && lanes != 32)
-    return fail(ctx, PMMC_ERR_INVALID, "server: lanes_per_chain must be 2, 4, 8 or 32");
+  if (lanes != 1 && lanes != 2 && lanes != 4 && lanes != 8 && lanes != 32)
+    return fail(ctx, PMMC_ERR_INVALID, "server: lanes_per_chain must be 1, 2, 4, 8 or 32");
   sv->lanes = lanes;
   size_t budget = opts ? opts->budget_bytes : 0;
   if (budget == 0) {

@@ -42,7 +42,8 @@ def problem(variant, n=96, arcs=160, seed=3):
 @pytest.mark.parametrize("variant,lanes", [("plain", 4), ("loops_sphere", 4), ("fixed", 4),
                                            ("2d", 4), ("inert_pairs", 4), ("hub", 4),
                                            ("plain", 2), ("plain", 8), ("plain", 32),
-                                           ("hub", 2), ("loops_sphere", 8)])
+                                           ("hub", 2), ("loops_sphere", 8), ("plain", 1),
+                                           ("loops_sphere", 1), ("hub", 1), ("fixed", 1)])
 def test_arcs_trace_parity(ctx, variant, lanes):
     """Windows of 32/lanes proposals resolve to the one-move-at-a-time chain."""
     pr, inp, kw = problem(variant)
@@ -61,7 +62,7 @@ def test_arcs_trace_parity(ctx, variant, lanes):
     assert abs(rep["final_energy"] - res[0].energy) <= 1e-5 * abs(rep["final_energy"])
 
 
-@pytest.mark.parametrize("lanes", [2, 8])
+@pytest.mark.parametrize("lanes", [1, 2, 8])
 def test_arcs_extended_energy_trace_parity(ctx, lanes):
     """Opt-in extended energy (bonds to the next bead, target 1.0, k 0.1; the
     stiffness angle term, k 0.1): per-move local scores and decisions follow
@@ -114,7 +115,7 @@ def test_arcs_dropin_multichain(ctx):
     assert abs(res.energy_fp64 - e64) <= 1e-6 * e64
 
 
-@pytest.mark.parametrize("lanes", [2, 4, 8])
+@pytest.mark.parametrize("lanes", [1, 2, 4, 8])
 def test_arcs_batch_units_match_oracle(ctx, lanes):
     """Every unit of a batch follows the oracle's Philox-mode annealer."""
     regs = [synth.arcs_region(n, int(1.5 * n), seed=s) for s, n in enumerate([32, 57, 130, 300, 80, 41])]
@@ -150,7 +151,7 @@ def test_arcs_batch_autotune(ctx, tmp_path, monkeypatch):
     ctx.set_seed(99)
     b = capi.ArcsBatch(ctx, inputs, prm, [0.5] * len(inputs), lanes=capi.LANES_AUTO)
     cls = b.classes()
-    assert cls and all(la in (2, 4, 8) and w in (1, 2, 4) for la, w, _, _ in cls)
+    assert cls and all(la in (1, 2, 4, 8) and w in (1, 2, 4) for la, w, _, _ in cls)
     assert sum(it for _, _, it, _ in cls) == len(inputs)
     data = json.load(open(path))
     assert len(data["entries"]) >= len(cls)
