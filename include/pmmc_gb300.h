@@ -274,6 +274,12 @@ pmmc_status pmmc_arcs_batch_create_ex(pmmc_ctx *ctx, int n_units,
                                       const pmmc_batch_opts *opts,
                                       int stop_all, int trace_cap,
                                       pmmc_arcs_batch **out);
+/* Tests only (no reference counterpart): compares the kernels' square root
+ * with the IEEE single-precision routine on the float bit patterns
+ * [lo, lo + count); returns the number of differing results and the lowest
+ * differing pattern (0xFFFFFFFF if none). */
+pmmc_status pmmc_selftest_sqrt(pmmc_ctx *ctx, uint32_t lo, uint32_t count,
+                               uint64_t *mismatches, uint32_t *first_bad);
 /* The launch configuration of each shared-memory class of a batch (no
  * reference counterpart): lanes per proposal, warps per CTA, work items and
  * whether arc lists are staged in shared memory; up to `cap` classes. */

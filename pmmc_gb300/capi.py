@@ -41,6 +41,7 @@ HEADER_SYMBOLS = [
     "pmmc_heatmap_batch_anneal", "pmmc_arcs_anneal_noalloc",
     "pmmc_server_create", "pmmc_server_submit", "pmmc_server_poll", "pmmc_server_wait",
     "pmmc_server_get_stats", "pmmc_server_destroy", "pmmc_arcs_batch_classes",
+    "pmmc_selftest_sqrt",
 ]
 
 LANES_AUTO = -1  # PMMC_LANES_AUTO: the autotuner picks lanes and warps per class
@@ -487,6 +488,16 @@ def heatmap_anneal(ctx: Context, inp: HeatmapInput, params: AnnealParams, step: 
     ctx.check(lib().pmmc_heatmap_anneal(ctx.h, C.byref(s), C.byref(params), C.c_float(step),
                                         _p(pos), C.byref(res)))
     return pos, res
+
+
+def selftest_sqrt(ctx: Context, lo: int, count: int):
+    """(mismatches, lowest differing bit pattern) of the kernels' square root
+    against the IEEE routine on float bit patterns [lo, lo + count)."""
+    bad = C.c_uint64()
+    first = C.c_uint32()
+    ctx.check(lib().pmmc_selftest_sqrt(ctx.h, C.c_uint32(lo), C.c_uint32(count), C.byref(bad),
+                                       C.byref(first)))
+    return bad.value, first.value
 
 
 def mark_arcs(ctx: Context, anchors, raw):

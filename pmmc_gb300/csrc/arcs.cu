@@ -432,24 +432,30 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
         nz = pb.z + __int_as_float(mv.w);
         const int beg = srp[b], end = srp[b + 1];
         const unsigned earlier = (1u << g) - 1u;  // slots before this one
-        // two arcs per lane per iteration: independent loads in flight
-        for (int e = beg + sub; e < end; e += 2 * G) {
-          const int e2 = e + G;
-          const bool two = e2 < end;
-          const int2 ent = NB[e];
-          const float iv = INV[e];
-          const int2 ent2 = two ? NB[e2] : ent;
-          const float iv2 = two ? INV[e2] : 0.0f;
-          const float4 q = spos[ent.x];
-          const float4 q2 = spos[ent2.x];
-          const float t = __int_as_float(ent.y), t2 = __int_as_float(ent2.y);
-          const float o1 = spring_fast(fast_len(pb.x, pb.y, pb.z, q), t, iv, ks, kq);
-          const float n1 = spring_fast(fast_len(nx, ny, nz, q), t, iv, ks, kq);
-          const float o2 = spring_fast(fast_len(pb.x, pb.y, pb.z, q2), t2, iv2, ks, kq);
-          const float n2 = spring_fast(fast_len(nx, ny, nz, q2), t2, iv2, ks, kq);
-          so += o1 + (two ? o2 : 0.0f);
-          sn += n1 + (two ? n2 : 0.0f);
-          cm |= (smask[ent.x] | (two ? smask[ent2.x] : 0u)) & earlier;
+        // two arcs per lane per iteration: independent loads and lengths in
+        // flight
+        constexpr int UA = 2;
+        for (int e = beg + sub; e < end; e += UA * G) {
+          int2 ent[UA];
+          float iv[UA];
+#pragma unroll
+          for (int k = 0; k < UA; ++k) {
+            const int ek = e + k * G;
+            const bool ok = ek < end;
+            ent[k] = NB[ok ? ek : e];
+            iv[k] = ok ? INV[ek] : 0.0f;
+          }
+#pragma unroll
+          for (int k = 0; k < UA; ++k) {
+            const bool ok = e + k * G < end;
+            const float4 q = spos[ent[k].x];
+            const float t = __int_as_float(ent[k].y);
+            const float o1 = spring_fast(fast_len(pb.x, pb.y, pb.z, q), t, iv[k], ks, kq);
+            const float n1 = spring_fast(fast_len(nx, ny, nz, q), t, iv[k], ks, kq);
+            so += ok ? o1 : 0.0f;
+            sn += ok ? n1 : 0.0f;
+            cm |= ok ? (smask[ent[k].x] & earlier) : 0u;
+          }
         }
         if (has_loops) {
           const int l1 = LRP[b + 1];
@@ -503,30 +509,41 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
           s_d[g] = d;
         }
       }
-      // ---- resolution, exactly the in-order loop: every unresolved slot
-      // tests acceptance against the running partial sum at once, a ballot
-      // finds the first acceptance, and the window ends at the first later
-      // slot that depends on an accepted bead ----
+      // ---- resolution, equivalent to the in-order loop.  A downhill slot
+      // is always accepted, an uphill slot's test needs the sum of the
+      // accepted changes before it: all downhill slots are taken at once;
+      // then, repeatedly, a warp scan gives every slot the sum of the
+      // accepted changes before it and the first uphill slot that passes is
+      // accepted (every slot before it is then final).  The window ends at
+      // the first slot that depends on an accepted earlier slot ----
       const bool leader = active && sub == 0;
-      unsigned accm = 0u;
-      float pacc = 0.0f;
-      int lend = L;
-      int first = 0;
-      for (;;) {
-        const float ef = e_hi + pacc;
-        const bool t = leader && g >= first && g < lend &&
-                       (d <= 0.0f || d < ef * (thr - 1.0f));
-        const unsigned am = __ballot_sync(0xffffffffu, t);
-        if (am == 0u) break;
-        const int j = (__ffs(am) - 1) / G;
-        accm |= 1u << j;
-        pacc += __shfl_sync(0xffffffffu, d, j * G);
-        const unsigned km = __ballot_sync(0xffffffffu, leader && g > j && g < lend &&
-                                                            ((cm >> j) & 1u));
-        if (km) lend = (__ffs(km) - 1) / G;
-        first = j + 1;
-        if (first >= lend) break;
+      unsigned acc_l = __ballot_sync(0xffffffffu, leader && d <= 0.0f);  // by lane
+      float inc;  // inclusive scan of the accepted changes over lanes
+      for (int from = 0;;) {
+        const float v = ((acc_l >> lane) & 1u) ? d : 0.0f;
+        inc = v;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+          const float t = __shfl_up_sync(0xffffffffu, inc, o);
+          if (lane >= o) inc += t;
+        }
+        const float pre = __shfl_up_sync(0xffffffffu, inc, 1);
+        const float ef = e_hi + (lane == 0 ? 0.0f : pre);
+        const bool up = leader && lane >= from && !((acc_l >> lane) & 1u) &&
+                        d < ef * (thr - 1.0f);
+        const unsigned um = __ballot_sync(0xffffffffu, up);
+        if (um == 0u) break;
+        const int l1 = __ffs(um) - 1;
+        acc_l |= 1u << l1;
+        from = l1 + 1;
       }
+      unsigned accm =
+          __reduce_or_sync(0xffffffffu, (leader && ((acc_l >> lane) & 1u)) ? 1u << g : 0u);
+      const unsigned dep =
+          __ballot_sync(0xffffffffu, leader && (cm & accm & ((1u << g) - 1u)) != 0u);
+      const int lend = dep ? (__ffs(dep) - 1) / G : L;
+      accm &= lend >= 32 ? 0xffffffffu : (1u << lend) - 1u;
+      const float pacc = __shfl_sync(0xffffffffu, inc, lend * G - 1);
       if (leader && g < lend && ((accm >> g) & 1u)) spos[b] = make_float4(nx, ny, nz, 0.0f);
       if (tracing) {
         __syncwarp();

@@ -1,6 +1,7 @@
 // capi.cu -- context, parameters and format conversions of the C ABI.
 #include <cstring>
 
+#include "common.cuh"
 #include "internal.h"
 
 using namespace pmmc;
@@ -121,5 +122,52 @@ extern "C" pmmc_status pmmc_arcs_dense_to_csr(int n, const float *dense, int *ro
     row_ptr[i + 1] = (int)k;
   }
   if (nnz) *nnz = k;
+  return PMMC_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Self-test of the kernels' square root: sqrt_rn against the IEEE routine
+// on the float bit patterns [lo, lo + count).
+// ---------------------------------------------------------------------------
+namespace {
+__global__ void selftest_sqrt_kernel(uint32_t lo, uint32_t count, unsigned long long *bad,
+                                     unsigned int *first) {
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t k = blockIdx.x * blockDim.x + threadIdx.x; k < count; k += stride) {
+    const uint32_t bits = lo + k;
+    const float s = __uint_as_float(bits);
+    const float a = pmmc::sqrt_rn(s), b = __fsqrt_rn(s);
+    if (__float_as_uint(a) != __float_as_uint(b) && !(a != a && b != b)) {
+      atomicAdd(bad, 1ull);
+      atomicMin(first, bits);
+    }
+  }
+}
+}  // namespace
+
+extern "C" pmmc_status pmmc_selftest_sqrt(pmmc_ctx *ctx, uint32_t lo, uint32_t count,
+                                          uint64_t *mismatches, uint32_t *first_bad) {
+  if (!ctx || !mismatches || !first_bad) return PMMC_ERR_INVALID;
+  unsigned long long *d_bad = nullptr;
+  unsigned int *d_first = nullptr;
+  PMMC_CUDA(ctx, cudaMalloc(&d_bad, sizeof(unsigned long long)));
+  PMMC_CUDA(ctx, cudaMalloc(&d_first, sizeof(unsigned int)));
+  const unsigned int init_first = 0xFFFFFFFFu;
+  cudaError_t e = cudaMemset(d_bad, 0, sizeof(unsigned long long));
+  if (e == cudaSuccess) e = cudaMemcpy(d_first, &init_first, sizeof(init_first), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) {
+    selftest_sqrt_kernel<<<ctx->sm_count * 8, 256, 0, ctx->stream>>>(lo, count, d_bad, d_first);
+    e = cudaGetLastError();
+  }
+  unsigned long long nb = 0;
+  unsigned int fb = 0;
+  if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+  if (e == cudaSuccess) e = cudaMemcpy(&nb, d_bad, sizeof(nb), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(&fb, d_first, sizeof(fb), cudaMemcpyDeviceToHost);
+  cudaFree(d_bad);
+  cudaFree(d_first);
+  if (e != cudaSuccess) return fail(ctx, PMMC_ERR_CUDA, "sqrt self-test: %s", cudaGetErrorString(e));
+  *mismatches = nb;
+  *first_bad = fb;
   return PMMC_OK;
 }
