@@ -36,6 +36,7 @@
 #include <string>
 #include <mutex>
 #include <numeric>
+#include <thread>
 #include <vector>
 
 #include "arcs_impl.h"
@@ -1148,9 +1149,39 @@ extern "C" pmmc_status pmmc_arcs_batch_create_ex(
     return fail(ctx, PMMC_ERR_INVALID, "arcs batch: bad arguments");
   *out = nullptr;
   const int chains = opts && opts->chains_per_unit > 0 ? opts->chains_per_unit : 1;
-  for (int u = 0; u < n_units; ++u) {
-    pmmc_status s = arcs_validate(ctx, &units[u]);
-    if (s != PMMC_OK) return s;
+  // validation and packing of many regions run on several host threads
+  const int n_threads = n_units >= 64
+      ? (int)std::max(1u, std::min(std::thread::hardware_concurrency(), 16u)) : 1;
+  auto parallel = [&](auto &&fn) {  // fn(first, last) over unit ranges
+    if (n_threads == 1) {
+      fn(0, n_units);
+      return;
+    }
+    std::vector<std::thread> th;
+    const int per = (n_units + n_threads - 1) / n_threads;
+    for (int t = 0; t < n_threads; ++t) {
+      const int a = t * per, z = std::min(n_units, a + per);
+      if (a < z) th.emplace_back([&fn, a, z] { fn(a, z); });
+    }
+    for (auto &x : th) x.join();
+  };
+  {
+    std::vector<int> bad(n_threads > 1 ? n_units : 0, 0);
+    int first_bad = -1;
+    if (n_threads == 1) {
+      for (int u = 0; u < n_units; ++u)
+        if (arcs_validate(nullptr, &units[u]) != PMMC_OK) {
+          first_bad = u;
+          break;
+        }
+    } else {
+      parallel([&](int a, int z) {
+        for (int u = a; u < z; ++u) bad[u] = arcs_validate(nullptr, &units[u]) != PMMC_OK;
+      });
+      for (int u = 0; u < n_units && first_bad < 0; ++u)
+        if (bad[u]) first_bad = u;
+    }
+    if (first_bad >= 0) return arcs_validate(ctx, &units[first_bad]);  // records the message
   }
   auto *b = new pmmc_arcs_batch();
   b->ctx = ctx;
@@ -1159,10 +1190,19 @@ extern "C" pmmc_status pmmc_arcs_batch_create_ex(
   b->P = arcs_make_params(prm, next_key(ctx), stop_all != 0);
   b->P.trace_cap = trace_cap;
 
-  // ---- pack host arrays ----
+  // ---- pack host arrays (unit u's chains have global ids u*chains...) ----
   ArcsPack pk;
-  for (int u = 0; u < n_units; ++u)
-    pk.add(units[u], chains, steps[u], b->P.seed, pk.chains);
+  if (n_threads == 1) {
+    for (int u = 0; u < n_units; ++u) pk.add(units[u], chains, steps[u], b->P.seed, u * chains);
+  } else {
+    const int per = (n_units + n_threads - 1) / n_threads;
+    std::vector<ArcsPack> parts((n_units + per - 1) / per);
+    parallel([&](int a, int z) {
+      ArcsPack &q = parts[a / per];
+      for (int u = a; u < z; ++u) q.add(units[u], chains, steps[u], b->P.seed, u * chains);
+    });
+    for (auto &q : parts) pk.append(q);
+  }
   pk.finish();
   b->h_units = pk.units;
   b->h_n.resize(n_units);
@@ -1357,14 +1397,26 @@ extern "C" pmmc_status pmmc_arcs_batch_results(pmmc_arcs_batch *b, float *pos_ou
   if (multi)
     PMMC_CUDA(ctx, cudaMemcpy(best.data(), b->best.p, sizeof(int) * b->n_units,
                               cudaMemcpyDeviceToHost));
+  // positions: one copy; with one chain per unit the device layout is the
+  // caller's, otherwise the best chain of each unit is gathered on the host
+  std::vector<float> all;
+  if (pos_out) {
+    if (!multi) {
+      PMMC_CUDA(ctx, cudaMemcpy(pos_out, b->pos_out.p, sizeof(float) * b->total_pos_out,
+                                cudaMemcpyDeviceToHost));
+    } else {
+      all.resize((size_t)b->total_pos_out);
+      PMMC_CUDA(ctx, cudaMemcpy(all.data(), b->pos_out.p, sizeof(float) * all.size(),
+                                cudaMemcpyDeviceToHost));
+    }
+  }
   long long dst = 0;
   for (int u = 0; u < b->n_units; ++u) {
     const ArcsUnit &U = b->h_units[u];
     const int c = best[u];
-    if (pos_out) {
-      PMMC_CUDA(ctx, cudaMemcpy(pos_out + dst, b->pos_out.p + U.out_off + (long long)c * U.n * 3,
-                                sizeof(float) * U.n * 3, cudaMemcpyDeviceToHost));
-    }
+    if (pos_out && multi)
+      memcpy(pos_out + dst, all.data() + U.out_off + (long long)c * U.n * 3,
+             sizeof(float) * U.n * 3);
     dst += (long long)U.n * 3;
     if (res) {
       const ChainOut &o = outs[U.chain_base + c];
