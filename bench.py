@@ -158,6 +158,83 @@ def cpu_serve_baseline(n_req: int, budget_s: float = 20.0):
             "latency_ms_p99_at_200rps": float(np.percentile(lat, 99))}
 
 
+def _cpu_plain(seed):
+    from oracle import oracle as O
+    from pmmc_gb300 import workloads as W
+    r = W.plain_region()
+    pr = O.ArcsProblem(r.pos, r.dense())
+    t = time.perf_counter()
+    _, res = O.arcs_anneal(pr, O.Params(**W.PLAIN_ANNEAL), 0.5, seed)
+    return res.moves, time.perf_counter() - t
+
+
+def distmap_main(args):
+    """Expected-distance map line beside the reference's host transform (the
+    oracle port, bit-identical to it) on one core, timed on a 4096 x 4096
+    sample and scaled per entry."""
+    from oracle import oracle as O
+    from pmmc_gb300 import workloads as W
+    O.build()
+    cs = W.distmap_contact(4096, seed=6)
+    t = time.perf_counter()
+    O.distance_heatmap(cs, 1, 100.0, -0.333, 2.0)
+    dt = time.perf_counter() - t
+    cpu = {"value": cs.size / dt, "unit": "entries/s", "cores": 1, "kind": "port",
+           "sample": f"one 4096 x 4096 map ({dt:.2f} s)"}
+    if args.impl == "reference":
+        if int(os.environ.get("RANK", "0")) != 0:
+            return
+        print(json.dumps({"metric": "matrix entries/s", "value": cpu["value"],
+                          "unit": "entries/s", "n_gpus": 0, "steps": 1, "warmup": 0,
+                          "ms_per_step": dt * 1e3, "higher_is_better": True,
+                          "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                          "data": "synthetic", "impl": "reference",
+                          "config": {"workload": "distance_heatmap"}, "cpu_baseline": cpu,
+                          "e2e": {"value": cpu["value"], "unit": "entries/s",
+                                  "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+        return
+    sampler = ClockSampler(0)
+    sampler.start()
+    line = W.distmap(args)
+    line["clocks"] = sampler.stop()
+    line["gpu_launches"] = 3 * args.steps
+    line["cpu_baseline"] = cpu
+    print(json.dumps(line))
+
+
+def plain_main(args):
+    """Config-0 line: the plain drop-in call beside the reference CPU
+    annealer (the oracle port, bit-identical to it) on one core."""
+    from oracle import oracle as O
+    from pmmc_gb300 import workloads as W
+    if args.impl == "reference":
+        if int(os.environ.get("RANK", "0")) != 0:
+            return
+        O.build()
+        mv, dt = _cpu_plain(42)
+        v = mv / dt
+        print(json.dumps({"metric": "MC moves/s", "value": v, "unit": "moves/s", "n_gpus": 0,
+                          "steps": 1, "warmup": 0, "ms_per_step": dt * 1e3,
+                          "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                          "dtype": "f64", "data": "synthetic", "impl": "reference",
+                          "config": {"workload": "arcs_plain_256beads_400arcs_seed42"},
+                          "cpu_baseline": {"value": v, "unit": "moves/s", "cores": 1,
+                                           "kind": "port", "sample": "one full anneal"},
+                          "e2e": {"value": v, "unit": "moves/s", "h2d_bytes_per_step": 0,
+                                  "d2h_bytes_per_step": 0}}))
+        return
+    sampler = ClockSampler(0)
+    sampler.start()
+    line = W.plain(args)
+    line["clocks"] = sampler.stop()
+    line["gpu_launches"] = args.steps * 2
+    O.build()
+    mv, dt = _cpu_plain(42)
+    line["cpu_baseline"] = {"value": mv / dt, "unit": "moves/s", "cores": 1, "kind": "port",
+                            "sample": f"one full anneal of the region ({mv} moves, {dt:.2f} s)"}
+    print(json.dumps(line))
+
+
 def serve_main(args):
     from pmmc_gb300 import workloads as W
     n_req = args.requests or 5000
@@ -400,7 +477,8 @@ def main():
     ap.add_argument("--milestone", type=int, default=ANNEAL["milestone_steps"],
                     help="milestone interval (smaller for profiling runs)")
     ap.add_argument("--workload", default="ensemble",
-                    choices=["ensemble", "heatmap", "heatmap-batch", "smooth", "serve"],
+                    choices=["ensemble", "plain", "heatmap", "heatmap-batch", "smooth",
+                             "serve", "distmap"],
                     help="ensemble: the batched arc-level ensemble (default line); "
                          "heatmap: one 2048-bead heatmap chain; heatmap-batch: one chain "
                          "per distinct 2048-bead map, one per SM; smooth: genome-scale "
@@ -408,12 +486,19 @@ def main():
     ap.add_argument("--maps", type=int, default=0, help="heatmap-batch: number of maps")
     ap.add_argument("--moves", type=int, default=0, help="moves per chain (heatmap/smooth)")
     ap.add_argument("--requests", type=int, default=0, help="serve: requests in the trace")
+    ap.add_argument("--n", type=int, default=0, help="distmap: matrix size")
     ap.add_argument("--lanes", type=int, default=-1,
                     help="lanes per proposal of the batched form (2, 4, 8, 32; -1 = autotune)")
     args = ap.parse_args()
     set_workload(args.structures, args.milestone)
     if args.workload == "serve":
         serve_main(args)
+        return
+    if args.workload == "plain":
+        plain_main(args)
+        return
+    if args.workload == "distmap":
+        distmap_main(args)
         return
     if args.workload != "ensemble":
         from pmmc_gb300 import workloads

@@ -310,6 +310,29 @@ pmmc_status pmmc_heatmap_batch_anneal(pmmc_ctx *ctx, int n_units,
                                       pmmc_result *res, double *kernel_ms,
                                       void *trace_out, int trace_cap);
 
+/* ---------------- expected-distance heatmap ---------------- */
+/* Replaces LooperSolver::createDistanceHeatmap (src/include/LooperSolver.hpp:
+ * 3042-3085), which builds heatmap_dist from heatmap[level] on the host
+ * before each heatmap level: for i <= j, d = scale * c^power where
+ * c >= 1e-6 (0 below, -1 inside the diagonal band |i-j| < diag), mirrored;
+ * then values above avg * stretching are clamped to it (avg: the mean over
+ * j >= i + w, w the first diagonal holding a value above 1e-6,
+ * Heatmap::getAvg / getDiagonalSize).  The caller passes the level's
+ * constants (freqToDistHeatmapScale/Power, or the Inter ones for level 0, and
+ * heatmapDistanceHeatmapStretching).  Host buffers of n*n floats; avg_out,
+ * max_out and kernel_ms are optional.  The average is summed in FP64 (the
+ * reference sums in float), so the clamp value can differ from the
+ * reference's in its last bits. */
+pmmc_status pmmc_distance_heatmap(pmmc_ctx *ctx, int n, const float *contact, int diag,
+                                  float scale, float power, float stretching,
+                                  float *dist_out, float *avg_out, float *max_out,
+                                  double *kernel_ms);
+/* The same on device buffers, enqueued on `stream` (NULL: the context's);
+ * stats (device, 2 floats) receives avg and the clamp value. */
+pmmc_status pmmc_distance_heatmap_device(pmmc_ctx *ctx, int n, const float *contact, int diag,
+                                         float scale, float power, float stretching,
+                                         float *dist, float *stats, void *stream);
+
 /* ---------------- arc-level anneal that allocates nothing ------------- */
 /* No counterpart in the reference.  For callers that cannot allocate device
  * memory -- code that must not call cudaMalloc because a host framework owns

@@ -362,6 +362,28 @@ def ref_smooth_score(pr: SmoothProblem, prm: Params, moved=-1, pos=None) -> floa
                                   C.byref(prm.c()), int(moved))
 
 
+def distance_heatmap(contact, diag: int, scale: float, power: float, stretching: float):
+    """orc_distance_heatmap: (n x n distance map, avg, clamp value)."""
+    c = _f32(contact)
+    n = c.shape[0]
+    out = np.zeros((n, n), np.float32)
+    avg = C.c_float()
+    mx = C.c_float()
+    lib().orc_distance_heatmap(n, _p(c), int(diag), C.c_float(scale), C.c_float(power),
+                               C.c_float(stretching), _p(out), C.byref(avg), C.byref(mx))
+    return out, avg.value, mx.value
+
+
+def ref_distance_heatmap(contact, diag: int, level: int, scale: float, power: float,
+                         stretching: float):
+    c = _f32(contact)
+    n = c.shape[0]
+    out = np.zeros((n, n), np.float32)
+    ref().ref_distance_heatmap(n, _p(c), int(diag), int(level), C.c_float(scale),
+                               C.c_float(power), C.c_float(stretching), _p(out))
+    return out
+
+
 def ref_lengths_score(n: int, pos, dist_to_next, prm: Params, moved=-1) -> float:
     return ref().ref_lengths_score(int(n), _p(_f32(pos)), _p(_f64(dist_to_next)),
                                    C.byref(prm.c()), int(moved))

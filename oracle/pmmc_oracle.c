@@ -449,6 +449,48 @@ done:
 }
 
 /* ------------------------------------------------------------------ */
+/* Expected-distance heatmap (createDistanceHeatmap)                   */
+/* ------------------------------------------------------------------ */
+void orc_distance_heatmap(int n, const float *contact, int diag, float scale,
+                          float power, float stretching, float *dist,
+                          float *avg_out, float *max_out) {
+  for (int i = 0; i < n; ++i)
+    for (int j = i; j < n; ++j) {
+      const float val = contact[(size_t)i * n + j];
+      float d;
+      if ((double)val < 1e-6)
+        d = 0.0f;
+      else
+        d = abs(i - j) < diag ? -1.0f : scale * powf(val, power);
+      dist[(size_t)i * n + j] = d;
+      dist[(size_t)j * n + i] = d;
+    }
+  /* Heatmap::getDiagonalSize: the first offset with a value above 1e-6 */
+  int w = 0, found = 0;
+  for (int k = 0; k < n && !found; ++k)
+    for (int i = 0; i + k < n; ++i)
+      if (dist[(size_t)i * n + i + k] > 1e-6) {
+        w = k;
+        found = 1;
+        break;
+      }
+  /* Heatmap::getAvg: float running sum in row order */
+  float ret = 0.0f;
+  int cnt = 0;
+  for (int i = 0; i < n; ++i)
+    for (int j = i + w; j < n; ++j) {
+      ret += dist[(size_t)i * n + j];
+      cnt++;
+    }
+  const float avg = ret / cnt;
+  const float max_dist = avg * stretching;
+  for (size_t k = 0; k < (size_t)n * n; ++k)
+    if (dist[k] > max_dist) dist[k] = max_dist;
+  *avg_out = avg;
+  *max_out = max_dist;
+}
+
+/* ------------------------------------------------------------------ */
 /* Heatmap level                                                       */
 /* ------------------------------------------------------------------ */
 /* getChromosomeHeatmapBoundary (LooperSolver.hpp:6034-6050). */

@@ -128,6 +128,18 @@ void orc_arcs_anneal_ext(int n, float *pos, const unsigned char *fixed,
                          const orc_ext *x, float step_size, orc_rng *rng,
                          orc_result *res);
 
+/* ---------------- expected-distance heatmap ---------------- */
+/* LooperSolver::createDistanceHeatmap (src/include/LooperSolver.hpp:
+ * 3042-3085): d_ij = scale * powf(c_ij, power) for c_ij >= 1e-6 (0 below,
+ * -1 inside the diagonal band |i-j| < diag), from the upper triangle and
+ * mirrored; then every value above avg * stretching is clamped to it, avg
+ * being Heatmap::getAvg of the distance map (Heatmap.hpp:440-451: a float
+ * running sum over j >= i + getDiagonalSize(), :356-367).  Writes the n*n
+ * map, the average and the clamp value. */
+void orc_distance_heatmap(int n, const float *contact, int diag, float scale,
+                          float power, float stretching, float *dist,
+                          float *avg_out, float *max_out);
+
 /* ---------------- heatmap level (chromosome / segment) ---------------- */
 /* calcScoreHeatmapActiveRegion(moved) (:3583-3617); moved = -1 -> full. */
 double orc_heatmap_score(int n, const float *pos, const float *heat, int diag,

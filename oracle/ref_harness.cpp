@@ -306,6 +306,33 @@ double ref_lengths_score(int n, const float *pos, const double *dtn,
                    : s.calcScoreStructureActiveRegionLengths(moved);
 }
 
+/* createDistanceHeatmap(level) (LooperSolver.hpp:3042-3085) on one n x n
+ * contact map (level 0: the inter-chromosomal constants); writes the
+ * expected-distance map into dist_out (n*n). */
+int ref_distance_heatmap(int n, const float *contact, int diag, int level, float scale,
+                         float power, float stretching, float *dist_out) {
+  Quiet q;
+  orc_params p;
+  memset(&p, 0, sizeof(p));
+  apply_settings(&p, 1);
+  if (level == 0) {
+    Settings::freqToDistHeatmapScaleInter = scale;
+    Settings::freqToDistHeatmapPowerInter = power;
+  } else {
+    Settings::freqToDistHeatmapScale = scale;
+    Settings::freqToDistHeatmapPower = power;
+  }
+  Settings::heatmapDistanceHeatmapStretching = stretching;
+  LooperSolver s("ref", "/tmp/");
+  s.heatmap.resize(2);
+  load_dense(s.heatmap[level], n, contact);
+  s.heatmap[level].diagonal_size = diag;
+  s.createDistanceHeatmap(level);
+  for (int i = 0; i < n; ++i)
+    for (int j = 0; j < n; ++j) dist_out[(size_t)i * n + j] = s.heatmap_dist.v[i][j];
+  return 0;
+}
+
 /* InteractionArcs::markArcs (src/include/InteractionArcs.hpp:207-336) on a
  * single chromosome "chr1".  Output layout as orc_mark_arcs. */
 int ref_mark_arcs(int n_anchors, const int *a_start, const int *a_end,

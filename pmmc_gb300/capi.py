@@ -41,7 +41,7 @@ HEADER_SYMBOLS = [
     "pmmc_heatmap_batch_anneal", "pmmc_arcs_anneal_noalloc",
     "pmmc_server_create", "pmmc_server_submit", "pmmc_server_poll", "pmmc_server_wait",
     "pmmc_server_get_stats", "pmmc_server_destroy", "pmmc_arcs_batch_classes",
-    "pmmc_selftest_sqrt",
+    "pmmc_selftest_sqrt", "pmmc_distance_heatmap", "pmmc_distance_heatmap_device",
 ]
 
 LANES_AUTO = -1  # PMMC_LANES_AUTO: the autotuner picks lanes and warps per class
@@ -488,6 +488,19 @@ def heatmap_anneal(ctx: Context, inp: HeatmapInput, params: AnnealParams, step: 
     ctx.check(lib().pmmc_heatmap_anneal(ctx.h, C.byref(s), C.byref(params), C.c_float(step),
                                         _p(pos), C.byref(res)))
     return pos, res
+
+
+def distance_heatmap(ctx: Context, contact, diag: int, scale: float, power: float,
+                     stretching: float):
+    """pmmc_distance_heatmap: (n x n distance map, avg, clamp value, kernel ms)."""
+    c = _f32(contact)
+    n = c.shape[0]
+    out = np.zeros((n, n), np.float32)
+    avg, mx, ms = C.c_float(), C.c_float(), C.c_double()
+    ctx.check(lib().pmmc_distance_heatmap(ctx.h, n, _p(c), int(diag), C.c_float(scale),
+                                          C.c_float(power), C.c_float(stretching), _p(out),
+                                          C.byref(avg), C.byref(mx), C.byref(ms)))
+    return out, avg.value, mx.value, ms.value
 
 
 def selftest_sqrt(ctx: Context, lo: int, count: int):

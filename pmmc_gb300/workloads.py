@@ -12,6 +12,14 @@ heatmap-batch  one chain per distinct 2048-bead map (16 MB each; the
 smooth         genome-scale smoothing: 23 chromosomes (~300k beads, anchors
                every Poisson(10) beads, fixed), split at the anchors into
                independent regions; 20k sweeps (moves = 20k x free beads).
+plain          one arc-level region of 256 beads, 400 arcs (seed 42), T0 5,
+               cooling 0.9999, milestones every 50k moves, threshold 0.99,
+               through the plain drop-in call (host buffers, one call per
+               step): one chain, and the reference GPU form's best of
+               4 x SM-count chains.
+distmap        expected-distance map of a 16384-bead contact map (1 GiB:
+               |i-j|^-1 x lognormal(0.5), 10 % zeros, diagonal band 1),
+               createDistanceHeatmap's transform and clamp; HBM GB/s.
 serve          request loop: 5000 arc-level regions, sizes round(exp U[ln 64,
                ln 8192]), 1.5625 arcs per bead (400 per 256 beads), Poisson
                arrivals at 200 requests/s (seed 11), 20k moves each, device
@@ -260,6 +268,102 @@ def serve(args) -> dict:
                 "note": "host arrays in, host results out, through pmmc_server_*"},
     }
     return line
+
+
+PLAIN_ANNEAL = dict(max_temp=5.0, dt_temp=0.9999, milestone_steps=50_000, improvement=0.99)
+
+
+def plain_region():
+    return synth.arcs_region(256, 400, seed=42)
+
+
+def plain(args) -> dict:
+    """One 256-bead region through pmmc_arcs_anneal (the drop-in call, host
+    buffers in and out): moves/s of one chain and of the multi-chain form."""
+    import time as _t
+    r = plain_region()
+    rp, col, tgt = r.csr()
+    inp = capi.ArcsInput(r.pos, rp, col, tgt)
+    ctx = capi.Context(0)
+    prm = capi.default_params(capi.LEVEL_ARCS, schedule=capi.SCHEDULE_CPU, **PLAIN_ANNEAL)
+    out = {}
+    for name, chains in (("one_chain", 1), ("best_of_chains", 0)):
+        for _ in range(max(1, args.warmup)):
+            capi.arcs_anneal(ctx, inp, prm, 0.5, chains)
+        times, moves, tot, err = [], 0, 0, 0.0
+        for k in range(args.steps):
+            ctx.set_seed(42 + k)
+            t = _t.perf_counter()
+            pos, res = capi.arcs_anneal(ctx, inp, prm, 0.5, chains)
+            times.append(_t.perf_counter() - t)
+            moves, tot, err = res.moves, res.total_moves, max(err, res.rel_error)
+        dt = float(np.median(times))
+        out[name] = {"ms_per_call": dt * 1e3, "moves_per_chain": int(moves),
+                     "moves_per_s": tot / dt, "chain_moves_per_s": moves / dt,
+                     "rel_error": err}
+    one = out["one_chain"]
+    return {
+        "metric": "MC moves/s", "value": one["chain_moves_per_s"], "unit": "moves/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": max(1, args.warmup),
+        "ms_per_step": one["ms_per_call"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "arcs_plain_256beads_400arcs_seed42_T0=5_cool0.9999_"
+                               "milestone50k_thr0.99", "call": "pmmc_arcs_anneal"},
+        "forms": out,
+        "e2e": {"value": one["chain_moves_per_s"], "unit": "moves/s",
+                "h2d_bytes_per_step": int(r.pos.nbytes + rp.nbytes + col.nbytes + tgt.nbytes),
+                "d2h_bytes_per_step": int(r.pos.nbytes)},
+        "final_energy_rel_error_max": max(v["rel_error"] for v in out.values()),
+    }
+
+
+def distmap_contact(n: int, seed: int = 5):
+    rng = np.random.default_rng(seed)
+    c = np.empty((n, n), np.float32)
+    step = 1024
+    for a in range(0, n, step):       # row blocks: bounded temporaries
+        i = np.arange(a, min(n, a + step))[:, None]
+        sep = np.abs(i - np.arange(n)[None, :]).astype(np.float32)
+        blk = np.where(sep > 0, 1.0 / np.maximum(sep, 1.0), 2.0).astype(np.float32)
+        blk *= rng.lognormal(0.0, 0.5, blk.shape).astype(np.float32)
+        blk[rng.random(blk.shape) < 0.1] = 0.0
+        c[a:a + step] = blk
+    return c
+
+
+def distmap(args) -> dict:
+    """createDistanceHeatmap on the device: kernel time per call (device
+    buffers) and the host-buffer call."""
+    import time as _t
+    n = args.n or 16384
+    c = distmap_contact(n)
+    ctx = capi.Context(0)
+    ms_k, e2e = [], []
+    for k in range(max(1, args.warmup) + args.steps):
+        t = _t.perf_counter()
+        d, avg, mx, ms = capi.distance_heatmap(ctx, c, 1, 100.0, -0.333, 2.0)
+        dt = _t.perf_counter() - t
+        if k >= max(1, args.warmup):
+            ms_k.append(ms)
+            e2e.append(dt)
+    ms = float(np.median(ms_k))
+    alg = 4.0 * n * n * 2.0          # upper triangle read twice, full map written
+    peak, kind = _peak()
+    achieved = alg / (ms * 1e-3) / 1e9
+    return {
+        "metric": "matrix entries/s", "value": n * n / (ms * 1e-3), "unit": "entries/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": max(1, args.warmup), "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": f"distance_heatmap_{n}x{n}_diag1_scale100_power-0.333_stretch2",
+                   "n": n},
+        "e2e": {"value": n * n / float(np.median(e2e)), "unit": "entries/s",
+                "h2d_bytes_per_step": 4 * n * n, "d2h_bytes_per_step": 4 * n * n},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None, "peak_source": kind,
+                     "algorithmic_bytes_per_launch": alg},
+        "avg": avg, "clamp": mx,
+    }
 
 
 def main(args):

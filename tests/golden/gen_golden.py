@@ -84,6 +84,26 @@ def ext_cases():
     return out
 
 
+def distmap_cases():
+    """createDistanceHeatmap of the reference on seeded contact maps: |i-j|^-1
+    decay with lognormal noise, zeros, a band of diag diagonals."""
+    out = {}
+    for k, (n, diag, level, scale, power, stretch) in enumerate(
+            [(64, 1, 1, 100.0, -0.333, 2.0), (97, 2, 0, 100.0, -1.0, 2.0),
+             (80, 1, 1, 1.0, -1.0 / 3.0, 1.5)]):
+        rng = np.random.default_rng(700 + k)
+        i = np.arange(n)
+        sep = np.abs(i[:, None] - i[None, :]).astype(np.float64)
+        c = np.where(sep > 0, 1.0 / np.maximum(sep, 1.0), 2.0) * rng.lognormal(0.0, 0.5, (n, n))
+        c[rng.random((n, n)) < 0.1] = 0.0           # missing contacts
+        c = np.triu(c) + np.triu(c, 1).T            # symmetric input
+        c = c.astype(np.float32)
+        d = O.ref_distance_heatmap(c, diag, level, scale, power, stretch)
+        out[f"distmap{k}"] = dict(contact=c, params=np.array([diag, scale, power, stretch]),
+                                  dist=d)
+    return out
+
+
 def heatmap_cases():
     out = {}
     specs = [dict(n=64, diag=1, bounds=[], sphere=0.0, seed=4),
@@ -169,7 +189,8 @@ def main():
     if not O.ref_available():
         raise SystemExit("the reference harness could not be built (no reference tree)")
     # optional arguments name the groups to write (default: all of them)
-    groups = {"arcs": arcs_cases, "ext": ext_cases, "heatmap": heatmap_cases,
+    groups = {"arcs": arcs_cases, "ext": ext_cases, "distmap": distmap_cases,
+              "heatmap": heatmap_cases,
               "smooth": smooth_cases, "mark": mark_cases, "hcm": hcm_cases}
     want = sys.argv[1:] or list(groups) + ["rng"]
     fixtures = {}
