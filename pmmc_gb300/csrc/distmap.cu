@@ -9,15 +9,17 @@
 // diagonal holding a value above 1e-6, Heatmap.hpp:356-367, 440-451).  The
 // reference does this on one host core in O(n^2) before every heatmap level.
 //
-// Two passes over the upper triangle, 32 x 32 tiles (coalesced rows):
-//   pass 1  per tile: the sum of the positive distances (FP64), the number
-//           of band entries, the smallest diagonal offset holding a positive
-//           distance; one partial per tile, reduced in a fixed order by a
-//           single block (deterministic), which derives avg and the clamp;
-//   pass 2  per tile: the distances again, clamped, written to the tile and,
-//           through shared memory, to its mirror tile.
-// HBM bound: 4 bytes read per upper-triangle entry in each pass, 4 bytes
-// written per entry of the full map.
+// Two passes over the upper triangle, 64 x 64 tiles (coalesced rows):
+//   pass 1  per tile: the distances (written unclamped to the upper
+//           triangle), the sum of the positive ones (FP64 per warp), the
+//           number of band entries, the smallest diagonal offset holding a
+//           positive distance; one partial per tile, reduced in a fixed order
+//           by a single block (deterministic), which derives avg and the clamp;
+//   pass 2  per tile: the upper triangle read back, clamped in place and
+//           written, through shared memory, to its mirror tile.
+// Per upper-triangle entry: 4 bytes of contact read and 4 bytes written in
+// pass 1, 4 bytes read in pass 2; per lower-triangle entry 4 bytes written;
+// the power function runs once per entry.
 #include <cmath>
 #include <vector>
 
@@ -26,11 +28,22 @@
 
 namespace pmmc {
 
-constexpr int kTile = 32;
+constexpr int kTile = 64;     // tile edge
+constexpr int kRows = 4;      // thread rows of a 256-thread block (64 x 4)
+
+// (double)c < 1e-6 and (double)d > 1e-6, as the reference compares a float
+// with the double constant, in float: 1e-6 lies between the floats
+// 0x358637bd and 0x358637be.
+__device__ __forceinline__ bool below_1e6(float c) {
+  return c < __uint_as_float(0x358637beu);
+}
+__device__ __forceinline__ bool above_1e6(float d) {
+  return d > __uint_as_float(0x358637bdu);
+}
 
 __device__ __forceinline__ float contact_to_dist(float c, int i, int j, int diag, float scale,
                                                  float power) {
-  if ((double)c < 1e-6) return 0.0f;
+  if (below_1e6(c)) return 0.0f;
   if (abs(i - j) < diag) return -1.0f;
   return scale * powf(c, power);
 }
@@ -42,83 +55,77 @@ struct DistPartial {
   int pad;
 };
 
-// Tile (bi, bj), bi <= bj, of the upper triangle: blockIdx.x enumerates them
-// row by row.
-__device__ __forceinline__ void tile_of(int t, int nt, int &bi, int &bj) {
-  // row bi holds nt - bi tiles; invert the prefix count
-  int r = 0, base = 0;
-  while (base + (nt - r) <= t) {
-    base += nt - r;
-    ++r;
-  }
-  bi = r;
-  bj = r + (t - base);
-}
-
-__global__ void __launch_bounds__(kTile * 8)
+// Tile (bi = blockIdx.y, bj = blockIdx.x) of the upper triangle; blocks below
+// the diagonal exit at once.
+__global__ void __launch_bounds__(kTile * kRows)
 distmap_pass1(const float *__restrict__ c, int n, int nt, int diag, float scale, float power,
-              DistPartial *__restrict__ part) {
-  __shared__ double s_sum[8];
-  __shared__ long long s_neg[8];
-  __shared__ int s_min[8];
-  int bi, bj;
-  tile_of(blockIdx.x, nt, bi, bj);
-  const int tx = threadIdx.x & (kTile - 1), ty = threadIdx.x / kTile;  // 32 x 8
+              DistPartial *__restrict__ part, float *__restrict__ dist) {
+  __shared__ double s_sum[kTile * kRows / 32];
+  __shared__ long long s_neg[kTile * kRows / 32];
+  __shared__ int s_min[kTile * kRows / 32];
+  const int bi = blockIdx.y, bj = blockIdx.x;
+  if (bj < bi) return;
+  const int tx = threadIdx.x % kTile, ty = threadIdx.x / kTile;
   const int j = bj * kTile + tx;
-  double sum = 0.0;
-  long long neg = 0;
+  float sum = 0.0f;   // at most 16 terms per thread; widened to FP64 below
+  int neg = 0;
   int mo = 0x7fffffff;
-  for (int r = ty; r < kTile; r += 8) {
+#pragma unroll 4
+  for (int r = ty; r < kTile; r += kRows) {
     const int i = bi * kTile + r;
     if (i < n && j < n && j >= i) {
       const float d = contact_to_dist(c[(size_t)i * n + j], i, j, diag, scale, power);
-      if (d > 0.0f) sum += (double)d;
-      if (d == -1.0f) ++neg;
-      if ((double)d > 1e-6) mo = min(mo, j - i);
+      dist[(size_t)i * n + j] = d;  // unclamped; pass 2 clamps and mirrors
+      sum += d > 0.0f ? d : 0.0f;
+      neg += d == -1.0f ? 1 : 0;
+      if (above_1e6(d)) mo = min(mo, j - i);
     }
   }
-  sum = warp_sum_d(sum);
+  double ds = warp_sum_d((double)sum);
+  long long ng = neg;
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    neg += __shfl_xor_sync(0xffffffffu, neg, o);
+    ng += __shfl_xor_sync(0xffffffffu, ng, o);
     mo = min(mo, __shfl_xor_sync(0xffffffffu, mo, o));
   }
   const int w = threadIdx.x >> 5;
   if ((threadIdx.x & 31) == 0) {
-    s_sum[w] = sum;
-    s_neg[w] = neg;
+    s_sum[w] = ds;
+    s_neg[w] = ng;
     s_min[w] = mo;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
     DistPartial p{0.0, 0, 0x7fffffff, 0};
-    for (int k = 0; k < 8; ++k) {
+    for (int k = 0; k < kTile * kRows / 32; ++k) {
       p.sum_pos += s_sum[k];
       p.n_neg += s_neg[k];
       p.min_off = min(p.min_off, s_min[k]);
     }
-    part[blockIdx.x] = p;
+    part[(size_t)bi * nt + bj] = p;
   }
 }
 
-// One block: the partials in tile order, avg = Heatmap::getAvg of the map and
-// the clamp value.
-__global__ void distmap_finish(const DistPartial *__restrict__ part, int n_part, int n,
+// One block: the partials of the upper-triangle tiles in index order,
+// avg = Heatmap::getAvg of the map and the clamp value.
+__global__ void distmap_finish(const DistPartial *__restrict__ part, int nt, int n,
                                float stretching, float *__restrict__ out2) {
   __shared__ double s_sum[32];
   __shared__ long long s_neg[32];
   __shared__ int s_min[32];
+  const long long total = (long long)nt * nt;
   double sum = 0.0;
   long long neg = 0;
   int mo = 0x7fffffff;
   // each thread a contiguous chunk, then a fixed-order combination
-  const int per = (n_part + blockDim.x - 1) / blockDim.x;
-  for (int k = threadIdx.x * per; k < min(n_part, (int)(threadIdx.x + 1) * per); ++k) {
+  const long long per = (total + blockDim.x - 1) / blockDim.x;
+  const long long k0 = (long long)threadIdx.x * per, k1 = min(total, k0 + per);
+  for (long long k = k0; k < k1; ++k) {
+    if ((int)(k % nt) < (int)(k / nt)) continue;  // below the diagonal: no tile
     sum += part[k].sum_pos;
     neg += part[k].n_neg;
     mo = min(mo, part[k].min_off);
   }
-  // fixed-order tree over the block
   for (int o = 16; o > 0; o >>= 1) {
     sum += shfl_xor_d(sum, o);
     neg += __shfl_xor_sync(0xffffffffu, neg, o);
@@ -142,36 +149,36 @@ __global__ void distmap_finish(const DistPartial *__restrict__ part, int n_part,
     // getDiagonalSize is 0 when no entry exceeds 1e-6; the average then also
     // takes the band entries (-1) on and above the diagonal
     int w = m;
-    double s = t;
+    double sm = t;
     if (m == 0x7fffffff) {
       w = 0;
-      s = -(double)ng;
+      sm = -(double)ng;
     }
     const double cnt = (double)(n - w) * (double)(n - w + 1) * 0.5;
-    const float avg = (float)(s / cnt);
+    const float avg = (float)(sm / cnt);
     out2[0] = avg;
     out2[1] = avg * stretching;
   }
 }
 
-__global__ void __launch_bounds__(kTile * 8)
-distmap_pass2(const float *__restrict__ c, int n, int nt, int diag, float scale, float power,
-              const float *__restrict__ stats, float *__restrict__ dist) {
+__global__ void __launch_bounds__(kTile * kRows)
+distmap_pass2(int n, const float *__restrict__ stats, float *__restrict__ dist) {
   __shared__ float tile[kTile][kTile + 1];
-  int bi, bj;
-  tile_of(blockIdx.x, nt, bi, bj);
+  const int bi = blockIdx.y, bj = blockIdx.x;
+  if (bj < bi) return;
   const float maxd = stats[1];
-  const int tx = threadIdx.x & (kTile - 1), ty = threadIdx.x / kTile;
+  const int tx = threadIdx.x % kTile, ty = threadIdx.x / kTile;
   const int j = bj * kTile + tx;
-  for (int r = ty; r < kTile; r += 8) {
+#pragma unroll 4
+  for (int r = ty; r < kTile; r += kRows) {
     const int i = bi * kTile + r;
     float d = 0.0f;
-    if (i < n && j < n) {
-      // the upper triangle defines both halves; below the diagonal of a
-      // diagonal tile the mirror writes the value
-      if (j >= i) {
-        d = contact_to_dist(c[(size_t)i * n + j], i, j, diag, scale, power);
-        if (d > maxd) d = maxd;
+    // the upper triangle defines both halves; below the diagonal of a
+    // diagonal tile the mirror writes the value
+    if (i < n && j < n && j >= i) {
+      d = dist[(size_t)i * n + j];
+      if (d > maxd) {
+        d = maxd;
         dist[(size_t)i * n + j] = d;
       }
     }
@@ -180,7 +187,8 @@ distmap_pass2(const float *__restrict__ c, int n, int nt, int diag, float scale,
   __syncthreads();
   // mirror: element (i, j) -> (j, i); thread tx now walks i within the tile
   const int i2 = bi * kTile + tx;
-  for (int r = ty; r < kTile; r += 8) {
+#pragma unroll 4
+  for (int r = ty; r < kTile; r += kRows) {
     const int j2 = bj * kTile + r;
     if (i2 < n && j2 < n && j2 > i2) dist[(size_t)j2 * n + i2] = tile[tx][r];
   }
@@ -196,19 +204,18 @@ pmmc_status distmap_run(pmmc_ctx *ctx, int n, const float *d_c, int diag, float 
                         float power, float stretching, float *d_dist, float *d_stats,
                         cudaStream_t s) {
   const int nt = (n + kTile - 1) / kTile;
-  const long long n_tiles = (long long)nt * (nt + 1) / 2;
-  if (n_tiles > 0x7fffffffLL) return fail(ctx, PMMC_ERR_INVALID, "distance heatmap: n too large");
+  if (nt > 65535) return fail(ctx, PMMC_ERR_INVALID, "distance heatmap: n too large");
   DistPartial *d_part = nullptr;
-  PMMC_CUDA(ctx, cudaMallocAsync(&d_part, sizeof(DistPartial) * n_tiles, s));
-  distmap_pass1<<<(unsigned)n_tiles, kTile * 8, 0, s>>>(d_c, n, nt, diag, scale, power, d_part);
+  PMMC_CUDA(ctx, cudaMallocAsync(&d_part, sizeof(DistPartial) * (size_t)nt * nt, s));
+  const dim3 grid(nt, nt);
+  distmap_pass1<<<grid, kTile * kRows, 0, s>>>(d_c, n, nt, diag, scale, power, d_part, d_dist);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) {
-    distmap_finish<<<1, 1024, 0, s>>>(d_part, (int)n_tiles, n, stretching, d_stats);
+    distmap_finish<<<1, 1024, 0, s>>>(d_part, nt, n, stretching, d_stats);
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) {
-    distmap_pass2<<<(unsigned)n_tiles, kTile * 8, 0, s>>>(d_c, n, nt, diag, scale, power,
-                                                          d_stats, d_dist);
+    distmap_pass2<<<grid, kTile * kRows, 0, s>>>(n, d_stats, d_dist);
     e = cudaGetLastError();
   }
   cudaFreeAsync(d_part, s);

@@ -347,7 +347,9 @@ def distmap(args) -> dict:
             ms_k.append(ms)
             e2e.append(dt)
     ms = float(np.median(ms_k))
-    alg = 4.0 * n * n * 2.0          # upper triangle read twice, full map written
+    # contact upper triangle read, upper triangle written and read back, the
+    # lower triangle written (clamped values rewrite a part of the upper one)
+    alg = 4.0 * n * n * 2.0
     peak, kind = _peak()
     achieved = alg / (ms * 1e-3) / 1e9
     return {
