@@ -202,6 +202,43 @@ def distmap_main(args):
     print(json.dumps(line))
 
 
+def equidistant_main(args):
+    """Equidistant-model line beside the reference's CPU interpolation (the
+    oracle port, bit-identical to it: a linear scan of the level per point)
+    on one core, timed on 20000 points from the middle of the chromosome
+    (the scan's average length) and scaled per point."""
+    from oracle import oracle as O
+    from pmmc_gb300 import workloads as W
+    O.build()
+    gpos, start, end, pos = W.equidistant_level()
+    res = args.n or 100
+    mid = int(gpos[len(gpos) // 2])
+    stop = mid + res * 20_000 - 1
+    t = time.perf_counter()
+    pts = O.equidistant(gpos, pos, int(end[0]), int(start[-1]), mid, stop, res)
+    dt = time.perf_counter() - t
+    cpu = {"value": len(pts) / dt, "unit": "points/s", "cores": 1, "kind": "port",
+           "sample": f"{len(pts)} points from mid-chromosome ({dt:.2f} s)"}
+    if args.impl == "reference":
+        if int(os.environ.get("RANK", "0")) != 0:
+            return
+        print(json.dumps({"metric": "points/s", "value": cpu["value"], "unit": "points/s",
+                          "n_gpus": 0, "steps": 1, "warmup": 0, "ms_per_step": dt * 1e3,
+                          "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                          "dtype": "f32", "data": "synthetic", "impl": "reference",
+                          "config": {"workload": "equidistant"}, "cpu_baseline": cpu,
+                          "e2e": {"value": cpu["value"], "unit": "points/s",
+                                  "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+        return
+    sampler = ClockSampler(0)
+    sampler.start()
+    line = W.equidistant(args)
+    line["clocks"] = sampler.stop()
+    line["gpu_launches"] = args.steps
+    line["cpu_baseline"] = cpu
+    print(json.dumps(line))
+
+
 def plain_main(args):
     """Config-0 line: the plain drop-in call beside the reference CPU
     annealer (the oracle port, bit-identical to it) on one core."""
@@ -478,7 +515,7 @@ def main():
                     help="milestone interval (smaller for profiling runs)")
     ap.add_argument("--workload", default="ensemble",
                     choices=["ensemble", "plain", "heatmap", "heatmap-batch", "smooth",
-                             "serve", "distmap"],
+                             "serve", "distmap", "equidistant"],
                     help="ensemble: the batched arc-level ensemble (default line); "
                          "heatmap: one 2048-bead heatmap chain; heatmap-batch: one chain "
                          "per distinct 2048-bead map, one per SM; smooth: genome-scale "
@@ -499,6 +536,9 @@ def main():
         return
     if args.workload == "distmap":
         distmap_main(args)
+        return
+    if args.workload == "equidistant":
+        equidistant_main(args)
         return
     if args.workload != "ensemble":
         from pmmc_gb300 import workloads

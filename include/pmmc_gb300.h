@@ -333,6 +333,21 @@ pmmc_status pmmc_distance_heatmap_device(pmmc_ctx *ctx, int n, const float *cont
                                          float scale, float power, float stretching,
                                          float *dist, float *stats, void *stream);
 
+/* ---------------- equidistant model ---------------- */
+/* Replaces the interpolation of HierarchicalChromosome::createEqidistantModel
+ * (src/HierarchicalChromosome.cu:466-519; gpuHelper :1253-1447 and its
+ * kernel parallelFind3DSmoothPosition :420-464): points every `res` bp from
+ * pos_start, (pos_stop - pos_start + 1) / res + 1 of them, along one
+ * chromosome's current level (n clusters in order: genomic positions gpos and
+ * positions pos, n*3).  first_end is the first cluster's end, last_start the
+ * last cluster's start (the reference's p1_end, p2_start).  *n_out receives
+ * the number of points; with out == NULL or cap < *n_out nothing else
+ * happens (size query).  Bit-identical to the reference's CPU path. */
+pmmc_status pmmc_equidistant_model(pmmc_ctx *ctx, int n, const int *gpos, const float *pos,
+                                   int first_end, int last_start, int pos_start,
+                                   int pos_stop, int res, float *out, int64_t cap,
+                                   int64_t *n_out, double *kernel_ms);
+
 /* ---------------- arc-level anneal that allocates nothing ------------- */
 /* No counterpart in the reference.  For callers that cannot allocate device
  * memory -- code that must not call cudaMalloc because a host framework owns

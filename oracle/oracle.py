@@ -384,6 +384,31 @@ def ref_distance_heatmap(contact, diag: int, level: int, scale: float, power: fl
     return out
 
 
+def equidistant(gpos, pos, first_end: int, last_start: int, pos_start: int, pos_stop: int,
+                res: int):
+    """orc_equidistant: the interpolated points (m x 3)."""
+    g = _i32(gpos)
+    p = _f32(pos).reshape(-1, 3)
+    m = (pos_stop - pos_start + 1) // res + 1
+    out = np.zeros((max(m, 1), 3), np.float32)
+    lib().orc_equidistant.restype = C.c_longlong
+    k = lib().orc_equidistant(len(g), _p(g), _p(p), int(first_end), int(last_start),
+                              int(pos_start), int(pos_stop), int(res), _p(out), C.c_longlong(m))
+    return out[:k]
+
+
+def ref_equidistant(gpos, start, end, pos, pos_start: int, pos_stop: int, res: int):
+    """The reference's gpuHelper (CPU path) on one chromosome level."""
+    L = C.CDLL(os.path.join(HERE, "_ref", "libpmmc_ref_hc.so"))
+    g, st, en = _i32(gpos), _i32(start), _i32(end)
+    p = _f32(pos).reshape(-1, 3)
+    m = (pos_stop - pos_start + 1) // res + 1
+    out = np.zeros((max(m, 1), 3), np.float32)
+    k = L.ref_equidistant(len(g), _p(g), _p(st), _p(en), _p(p), int(pos_start), int(pos_stop),
+                          int(res), _p(out), int(m))
+    return out[:k]
+
+
 def ref_lengths_score(n: int, pos, dist_to_next, prm: Params, moved=-1) -> float:
     return ref().ref_lengths_score(int(n), _p(_f32(pos)), _p(_f64(dist_to_next)),
                                    C.byref(prm.c()), int(moved))

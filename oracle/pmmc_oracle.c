@@ -491,6 +491,50 @@ void orc_distance_heatmap(int n, const float *contact, int diag, float scale,
 }
 
 /* ------------------------------------------------------------------ */
+/* Equidistant model (gpuHelper's CPU path)                            */
+/* ------------------------------------------------------------------ */
+long long orc_equidistant(int n, const int *gpos, const float *pos, int first_end,
+                          int last_start, int pos_start, int pos_stop, int res,
+                          float *out, long long cap) {
+  const long long out_size = (long long)((pos_stop - pos_start + 1) / res + 1);
+  for (long long idx = 0; idx < out_size && idx < cap; ++idx) {
+    const long long p = pos_start + (long long)res * idx;
+    float *o = out + 3 * idx;
+    if (p < first_end) {
+      memcpy(o, pos, 3 * sizeof(float));
+      continue;
+    }
+    if (p >= last_start) {
+      memcpy(o, pos + 3 * (n - 1), 3 * sizeof(float));
+      continue;
+    }
+    int prev = -1, found = 0;
+    for (int i = 0; i < n; ++i) {
+      if (p < gpos[i] && prev >= 0) {
+        const float *p1 = pos + 3 * prev, *p2 = pos + 3 * i;
+        float p0[3], p3[3];
+        for (int c = 0; c < 3; ++c) {
+          p0[c] = i > 1 ? pos[3 * (i - 2) + c] : 2.0f * p1[c] - p2[c];
+          p3[c] = i + 1 < n ? pos[3 * (i + 1) + c] : 2.0f * p2[c] - p1[c];
+        }
+        const float t = (float)(p - gpos[prev]) / (float)(gpos[i] - gpos[prev]);
+        const float t2 = t * t, t3 = t2 * t;
+        const float b1 = 0.5f * (-t3 + 2.0f * t2 - t);
+        const float b2 = 0.5f * (3.0f * t3 - 5.0f * t2 + 2.0f);
+        const float b3 = 0.5f * (-3.0f * t3 + 4.0f * t2 + t);
+        const float b4 = 0.5f * (t3 - t2);
+        for (int c = 0; c < 3; ++c) o[c] = p0[c] * b1 + p1[c] * b2 + p2[c] * b3 + p3[c] * b4;
+        found = 1;
+        break;
+      }
+      prev = i;
+    }
+    if (!found && prev >= 0) memcpy(o, pos + 3 * prev, 3 * sizeof(float));
+  }
+  return out_size;
+}
+
+/* ------------------------------------------------------------------ */
 /* Heatmap level                                                       */
 /* ------------------------------------------------------------------ */
 /* getChromosomeHeatmapBoundary (LooperSolver.hpp:6034-6050). */

@@ -140,6 +140,20 @@ void orc_distance_heatmap(int n, const float *contact, int diag, float scale,
                           float power, float stretching, float *dist,
                           float *avg_out, float *max_out);
 
+/* ---------------- equidistant model ---------------- */
+/* HierarchicalChromosome::gpuHelper's interpolation (src/
+ * HierarchicalChromosome.cu:1253-1447, its CPU path; createEqidistantModel
+ * :466-519): points every res bp from pos_start, (pos_stop - pos_start + 1)
+ * / res + 1 of them; before first_end the first cluster's position, from
+ * last_start on the last one's, otherwise the Catmull-Rom spline
+ * (interpolateSpline, thirdparty/common.cpp:453-462) through the level's
+ * clusters around the point, mirrored end points at the ends.  gpos/pos: the
+ * level's clusters in order.  Returns the number of points (writes at most
+ * cap). */
+long long orc_equidistant(int n, const int *gpos, const float *pos, int first_end,
+                          int last_start, int pos_start, int pos_stop, int res,
+                          float *out, long long cap);
+
 /* ---------------- heatmap level (chromosome / segment) ---------------- */
 /* calcScoreHeatmapActiveRegion(moved) (:3583-3617); moved = -1 -> full. */
 double orc_heatmap_score(int n, const float *pos, const float *heat, int diag,

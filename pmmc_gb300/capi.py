@@ -42,6 +42,7 @@ HEADER_SYMBOLS = [
     "pmmc_server_create", "pmmc_server_submit", "pmmc_server_poll", "pmmc_server_wait",
     "pmmc_server_get_stats", "pmmc_server_destroy", "pmmc_arcs_batch_classes",
     "pmmc_selftest_sqrt", "pmmc_distance_heatmap", "pmmc_distance_heatmap_device",
+    "pmmc_equidistant_model",
 ]
 
 LANES_AUTO = -1  # PMMC_LANES_AUTO: the autotuner picks lanes and warps per class
@@ -501,6 +502,24 @@ def distance_heatmap(ctx: Context, contact, diag: int, scale: float, power: floa
                                           C.c_float(power), C.c_float(stretching), _p(out),
                                           C.byref(avg), C.byref(mx), C.byref(ms)))
     return out, avg.value, mx.value, ms.value
+
+
+def equidistant_model(ctx: Context, gpos, pos, first_end: int, last_start: int,
+                      pos_start: int, pos_stop: int, res: int):
+    """pmmc_equidistant_model: (points m x 3, kernel ms)."""
+    g = _i32(gpos)
+    p = _f32(pos).reshape(-1, 3)
+    m = C.c_int64()
+    ms = C.c_double()
+    ctx.check(lib().pmmc_equidistant_model(ctx.h, len(g), _p(g), _p(p), int(first_end),
+                                           int(last_start), int(pos_start), int(pos_stop),
+                                           int(res), None, C.c_int64(0), C.byref(m), None))
+    out = np.zeros((m.value, 3), np.float32)
+    ctx.check(lib().pmmc_equidistant_model(ctx.h, len(g), _p(g), _p(p), int(first_end),
+                                           int(last_start), int(pos_start), int(pos_stop),
+                                           int(res), _p(out), C.c_int64(m.value), C.byref(m),
+                                           C.byref(ms)))
+    return out, ms.value
 
 
 def selftest_sqrt(ctx: Context, lo: int, count: int):

@@ -20,6 +20,9 @@ plain          one arc-level region of 256 beads, 400 arcs (seed 42), T0 5,
 distmap        expected-distance map of a 16384-bead contact map (1 GiB:
                |i-j|^-1 x lognormal(0.5), 10 % zeros, diagonal band 1),
                createDistanceHeatmap's transform and clamp; HBM GB/s.
+equidistant    equidistant model of the largest chromosome of the genome
+               workload (~24.8k clusters at 10 kb) resampled every 100 bp
+               (~2.5M points); points/s.
 serve          request loop: 5000 arc-level regions, sizes round(exp U[ln 64,
                ln 8192]), 1.5625 arcs per bead (400 per 256 beads), Poisson
                arrivals at 200 requests/s (seed 11), 20k moves each, device
@@ -365,6 +368,52 @@ def distmap(args) -> dict:
                      "frac": achieved / peak, "traffic": None, "peak_source": kind,
                      "algorithmic_bytes_per_launch": alg},
         "avg": avg, "clamp": mx,
+    }
+
+
+def equidistant_level(seed: int = 3):
+    """The largest chromosome of the genome workload as a level: 10 kb
+    clusters, positions from the smoothing chain."""
+    ch = max(synth.smooth_genome(300_000, seed=seed), key=lambda c: c.n)
+    n = ch.n
+    start = (np.arange(n, dtype=np.int64) * 10_000 + 1).astype(np.int32)
+    end = (start + 9_999).astype(np.int32)
+    gpos = ((start.astype(np.int64) + end) // 2).astype(np.int32)
+    return gpos, start, end, ch.pos
+
+
+def equidistant(args) -> dict:
+    import time as _t
+    gpos, start, end, pos = equidistant_level()
+    res = args.n or 100
+    ctx = capi.Context(0)
+    ms_k, e2e, m = [], [], 0
+    for k in range(max(1, args.warmup) + args.steps):
+        t = _t.perf_counter()
+        pts, ms = capi.equidistant_model(ctx, gpos, pos, int(end[0]), int(start[-1]),
+                                         int(gpos[0]), int(gpos[-1]), res)
+        dt = _t.perf_counter() - t
+        m = len(pts)
+        if k >= max(1, args.warmup):
+            ms_k.append(ms)
+            e2e.append(dt)
+    ms = float(np.median(ms_k))
+    peak, kind = _peak()
+    alg = 12.0 * m + 16.0 * len(gpos)   # points written, level read
+    achieved = alg / (ms * 1e-3) / 1e9
+    return {
+        "metric": "points/s", "value": m / (ms * 1e-3), "unit": "points/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": max(1, args.warmup), "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": f"equidistant_{len(gpos)}clusters_10kb_every{res}bp",
+                   "points": m},
+        "e2e": {"value": m / float(np.median(e2e)), "unit": "points/s",
+                "h2d_bytes_per_step": int(gpos.nbytes + pos.nbytes),
+                "d2h_bytes_per_step": 12 * m},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": None, "peak_source": kind,
+                     "algorithmic_bytes_per_launch": alg},
     }
 
 

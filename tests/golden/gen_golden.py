@@ -104,6 +104,24 @@ def distmap_cases():
     return out
 
 
+def equi_cases():
+    """The reference's equidistant-model interpolation (gpuHelper, CPU path)
+    on seeded chromosome levels: uneven cluster spacing, a 2-cluster level,
+    resolutions that do and do not divide the span."""
+    out = {}
+    for k, (n, res) in enumerate([(40, 1000), (2, 333), (300, 7919), (17, 50)]):
+        rng = np.random.default_rng(800 + k)
+        width = rng.integers(500, 30000, n)
+        start = np.concatenate([[10_000], 10_000 + np.cumsum(width)[:-1]]).astype(np.int32)
+        end = (start + width - 1).astype(np.int32)
+        gpos = ((start + end) // 2).astype(np.int32)
+        pos = synth.random_walk(n, rng) * np.float32(2.0)
+        pts = O.ref_equidistant(gpos, start, end, pos, int(gpos[0]), int(gpos[-1]), res)
+        out[f"equi{k}"] = dict(gpos=gpos, start=start, end=end, pos=pos,
+                               res=np.array([res]), points=pts)
+    return out
+
+
 def heatmap_cases():
     out = {}
     specs = [dict(n=64, diag=1, bounds=[], sphere=0.0, seed=4),
@@ -190,6 +208,7 @@ def main():
         raise SystemExit("the reference harness could not be built (no reference tree)")
     # optional arguments name the groups to write (default: all of them)
     groups = {"arcs": arcs_cases, "ext": ext_cases, "distmap": distmap_cases,
+              "equi": equi_cases,
               "heatmap": heatmap_cases,
               "smooth": smooth_cases, "mark": mark_cases, "hcm": hcm_cases}
     want = sys.argv[1:] or list(groups) + ["rng"]

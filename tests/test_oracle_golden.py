@@ -125,3 +125,23 @@ def test_hcm_lines():
            O.hcm_arc_line([1, 2, 300, 400, 5, 6, -1]),
            O.hcm_arc_line([7, 9, -1, -1, 0, 12, 2])]
     assert got == list(g["lines"])
+
+
+@pytest.mark.parametrize("case", ["distmap0", "distmap1", "distmap2"])
+def test_distance_heatmap(case):
+    """createDistanceHeatmap: the oracle reproduces the reference's map bit
+    for bit (transform, band, clamp at the float-summed average)."""
+    g = load(case)
+    diag, sc, pw, st = g["params"]
+    d, _, _ = O.distance_heatmap(g["contact"], int(diag), sc, pw, st)
+    np.testing.assert_array_equal(d, g["dist"])
+
+
+@pytest.mark.parametrize("case", ["equi0", "equi1", "equi2", "equi3"])
+def test_equidistant_model(case):
+    """The equidistant-model interpolation: the oracle reproduces the
+    reference's points bit for bit."""
+    g = load(case)
+    pts = O.equidistant(g["gpos"], g["pos"], int(g["end"][0]), int(g["start"][-1]),
+                        int(g["gpos"][0]), int(g["gpos"][-1]), int(g["res"][0]))
+    np.testing.assert_array_equal(pts, g["points"])
