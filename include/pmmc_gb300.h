@@ -74,7 +74,9 @@ typedef struct pmmc_anneal_params {
   int milestone_fails;   /* [cuda] milestone_fails                 */
   int schedule;          /* PMMC_SCHEDULE_GPU / PMMC_SCHEDULE_CPU  */
   int resync_every;      /* FP64 energy recompute every L moves (0 = off) */
-  int64_t max_moves;     /* hard cap on moves per chain (0 = schedule's) */
+  int64_t max_moves;     /* hard cap on moves per chain (0 = schedule's);
+                          * smoothing: < 0 means -max_moves sweeps, a cap
+                          * of -max_moves x movable beads per region     */
   /* Extended arc energy (off = the reference's arcs+loops+sphere): bond
    * springs on consecutive beads with target `bond_target` and constants
    * k_stretch_bond/k_squeeze_bond, and the smooth-level angle term

@@ -40,6 +40,7 @@ struct SmoothUnit {
   long long work_off;  // float4 index of chain 0's global working copy
   float step;
   int pad2;
+  long long cap;       // hard move cap of the unit's chains
 };
 
 struct SmoothDevParams {
@@ -85,17 +86,18 @@ __device__ __forceinline__ float angle_e(float4 a, float4 b, float4 c,
 
 // Local score of bead p at position q (calcScoreStructureSmooth(p,true,true)
 // plus the bead's sphere term).
-__device__ __forceinline__ float smooth_local(const float4 *P, const float2 *dtn,
+// P[i * st]: bead i of the chain (st = 32 when a warp's chains interleave).
+__device__ __forceinline__ float smooth_local(const float4 *P, int st, const float2 *dtn,
                                               int n, int p, float4 q,
                                               const SmoothDevParams &S) {
   float s = 0.0f;
-  const float4 pm1 = p >= 1 ? P[p - 1] : q;
-  const float4 pp1 = p + 1 < n ? P[p + 1] : q;
+  const float4 pm1 = p >= 1 ? P[(p - 1) * st] : q;
+  const float4 pp1 = p + 1 < n ? P[(p + 1) * st] : q;
   if (p >= 1) s += bond_e(pm1, q, dtn[p - 1], S.ks, S.kq);
   if (p + 1 < n) s += bond_e(q, pp1, dtn[p], S.ks, S.kq);
-  if (p >= 2) s += angle_e(P[p - 2], pm1, q, S.kang);       // angle at p-1
-  if (p >= 1 && p + 1 < n) s += angle_e(pm1, q, pp1, S.kang);  // at p
-  if (p + 2 < n) s += angle_e(q, pp1, P[p + 2], S.kang);    // at p+1
+  if (p >= 2) s += angle_e(P[(p - 2) * st], pm1, q, S.kang);       // angle at p-1
+  if (p >= 1 && p + 1 < n) s += angle_e(pm1, q, pp1, S.kang);      // at p
+  if (p + 2 < n) s += angle_e(q, pp1, P[(p + 2) * st], S.kang);    // at p+1
   s += sphere_penalty(q.x, q.y, q.z, S.R);
   return s;
 }
@@ -120,14 +122,17 @@ __device__ __forceinline__ double angle_exact(float4 a, float4 b, float4 c, floa
 }
 
 // FP64 full score (calcScoreStructureSmooth(true,true) + sphere).
-__device__ double smooth_full(const float4 *P, const float2 *dtn, int n,
+__device__ double smooth_full(const float4 *P, int st, const float2 *dtn, int n,
                               const SmoothDevParams &S) {
   double sa = 0.0, sb = 0.0, sp = 0.0;
   for (int i = 0; i + 1 < n; ++i) {
-    sa += bond_exact(P[i], P[i + 1], dtn[i].x, S.ks, S.kq);
-    if (i > 0) sb += angle_exact(P[i - 1], P[i], P[i + 1], S.kang);
+    sa += bond_exact(P[i * st], P[(i + 1) * st], dtn[i].x, S.ks, S.kq);
+    if (i > 0) sb += angle_exact(P[(i - 1) * st], P[i * st], P[(i + 1) * st], S.kang);
   }
-  for (int i = 0; i < n; ++i) sp += sphere_penalty(P[i].x, P[i].y, P[i].z, S.R);
+  for (int i = 0; i < n; ++i) {
+    const float4 q = P[i * st];
+    sp += sphere_penalty(q.x, q.y, q.z, S.R);
+  }
   return sa * (double)S.wd + sb * (double)S.wa + sp;
 }
 
@@ -158,13 +163,18 @@ smooth_anneal_kernel(const SmoothUnit *__restrict__ units,
   const int chain = it.y;
   const int n = U.n;
   const uint32_t chain_id = (uint32_t)(U.chain_base + chain);
-  float4 *P = SMEM ? reinterpret_cast<float4 *>(smem) + (size_t)threadIdx.x * S.slice
+  // shared-memory path: the 32 chains of a warp interleave bead by bead
+  // (bead i of lane l at i * 32 + l), so that a warp's loads of any beads
+  // fall on distinct banks
+  const int st = SMEM ? 32 : 1;
+  float4 *P = SMEM ? reinterpret_cast<float4 *>(smem) +
+                         (size_t)(threadIdx.x >> 5) * S.slice * 32 + (threadIdx.x & 31)
                    : work + U.work_off + (long long)chain * n;
   const float2 *dtn = dtn_all + U.dtn_off;
   const int *MOV = U.mov_off >= 0 ? movable + U.mov_off : nullptr;
-  for (int i = 0; i < n; ++i) P[i] = pos0[U.pos_off + i];
+  for (int i = 0; i < n; ++i) P[i * st] = pos0[U.pos_off + i];
 
-  const double E0 = smooth_full(P, dtn, n, S);
+  const double E0 = smooth_full(P, st, dtn, n, S);
   // running score: float-float pair per move, widened to FP64 at milestones
   float e_hi = (float)E0, e_lo = (float)(E0 - (double)(float)E0);
   double E_ms = E0;
@@ -173,11 +183,14 @@ smooth_anneal_kernel(const SmoothUnit *__restrict__ units,
   int succ = 0, misses = 0, status = kDevOk;
   bool stop = U.n_mov == 0;
   if (stop) status = kDevNoMovable;
+  // milestone and recompute counters (no 64-bit division per move)
+  long long next_ms = S.window;
+  long long next_rs = S.resync > 0 ? (long long)S.resync : 0x7fffffffffffffffLL;
   while (!stop) {
     const uint4 r = philox_move(S.seed, chain_id, (uint64_t)moves, 0u);
     const int k = uniform_index(r.x, U.n_mov);
     const int b = MOV ? MOV[k] : k;
-    const float4 ob = P[b];
+    const float4 ob = P[b * st];
     const float ddx = (2.0f * u01(r.y) - 1.0f) * U.step;
     const float ddy = (2.0f * u01(r.z) - 1.0f) * U.step;
     const float ddz = S.use2d ? 0.0f : (2.0f * u01(r.w) - 1.0f) * U.step;
@@ -185,8 +198,8 @@ smooth_anneal_kernel(const SmoothUnit *__restrict__ units,
     nb.x += ddx;
     nb.y += ddy;
     nb.z += ddz;
-    const float so = smooth_local(P, dtn, n, b, ob, S);
-    const float sn = smooth_local(P, dtn, n, b, nb, S);
+    const float so = smooth_local(P, st, dtn, n, b, ob, S);
+    const float sn = smooth_local(P, st, dtn, n, b, nb, S);
     const float d = sn - so;
     // strict improvement (LooperSolver.hpp:4974), else the ratio test
     bool acc = d < 0.0f;
@@ -196,7 +209,7 @@ smooth_anneal_kernel(const SmoothUnit *__restrict__ units,
       acc = d < e_hi * (thr - 1.0f);
     }
     if (acc) {
-      P[b] = nb;
+      P[b * st] = nb;
       ff_add(e_hi, e_lo, d);
       ++accepted;
       ++succ;
@@ -214,14 +227,16 @@ smooth_anneal_kernel(const SmoothUnit *__restrict__ units,
       trace[moves] = tr;
     }
     ++moves;
-    if (S.resync > 0 && moves % S.resync == 0) {
+    if (moves == next_rs) {
       // remove the drift of the running score (a region is small: the
       // recompute is a few dozen terms)
-      const double Er = smooth_full(P, dtn, n, S);
+      next_rs += S.resync;
+      const double Er = smooth_full(P, st, dtn, n, S);
       e_hi = (float)Er;
       e_lo = (float)(Er - (double)e_hi);
     }
-    if (moves % S.window == 0) {
+    if (moves == next_ms) {
+      next_ms += S.window;
       const double E = (double)e_hi + (double)e_lo;
       const bool miss = (E > (double)S.improvement * E_ms && succ < S.min_succ) || E < 1e-6;
       misses = miss ? misses + 1 : 0;
@@ -230,11 +245,11 @@ smooth_anneal_kernel(const SmoothUnit *__restrict__ units,
       succ = 0;
     }
     T *= S.dt;
-    if (!stop && moves >= S.cap) stop = true;
+    if (!stop && moves >= U.cap) stop = true;
   }
   ChainOut o;
   o.energy = (double)e_hi + (double)e_lo;
-  o.energy_fp64 = smooth_full(P, dtn, n, S);
+  o.energy_fp64 = smooth_full(P, st, dtn, n, S);
   o.base = 0.0;
   o.score = e_hi;
   o.status = status;
@@ -243,9 +258,10 @@ smooth_anneal_kernel(const SmoothUnit *__restrict__ units,
   outs[U.chain_base + chain] = o;
   float *po = pos_out + U.out_off + (long long)chain * n * 3;
   for (int i = 0; i < n; ++i) {
-    po[3 * i] = P[i].x;
-    po[3 * i + 1] = P[i].y;
-    po[3 * i + 2] = P[i].z;
+    const float4 q = P[i * st];
+    po[3 * i] = q.x;
+    po[3 * i + 1] = q.y;
+    po[3 * i + 2] = q.z;
   }
 }
 
@@ -305,6 +321,7 @@ extern "C" pmmc_status pmmc_smooth_batch_anneal(pmmc_ctx *ctx, int n_units,
   if (!ctx || n_units < 1 || !units || !prm || !steps)
     return fail(ctx, PMMC_ERR_INVALID, "smooth batch: bad arguments");
   if (chains < 1) chains = 1;
+  SmoothDevParams S = smooth_params(prm, next_key(ctx));
   std::vector<SmoothUnit> hu(n_units);
   std::vector<float4> hpos;
   std::vector<float2> hdtn;
@@ -340,6 +357,8 @@ extern "C" pmmc_status pmmc_smooth_batch_anneal(pmmc_ctx *ctx, int n_units,
     U.out_off = out_off;
     U.work_off = work_off;
     U.step = steps[u];
+    // max_moves < 0: -max_moves sweeps (one proposal per movable bead each)
+    U.cap = prm->max_moves < 0 ? std::max(1LL, (long long)(-prm->max_moves) * U.n_mov) : S.cap;
     chain_base += chains;
     out_off += (long long)chains * pr.n * 3;
     work_off += (long long)chains * pr.n;
@@ -357,7 +376,6 @@ extern "C" pmmc_status pmmc_smooth_batch_anneal(pmmc_ctx *ctx, int n_units,
   for (int u : order)
     for (int c = 0; c < chains; ++c) items.push_back(make_int2(u, c));
 
-  SmoothDevParams S = smooth_params(prm, next_key(ctx));
   const int threads = 128;
   // shared-memory slices when a thread's region fits in 1 KB... 4 KB
   int slice = 0;

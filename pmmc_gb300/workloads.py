@@ -149,22 +149,11 @@ def _smooth(args):
 
 
 def _smooth_run(ctx, segs, prm, sweeps):
-    # regions share one move cap per call: group them by free-bead count
-    groups = {}
-    for i, x in enumerate(segs):
-        groups.setdefault(int((x.fixed == 0).sum()), []).append(i)
-    res_all = [None] * len(segs)
-    out_all = [None] * len(segs)
-    ms_total = 0.0
-    for nf, idx in sorted(groups.items()):
-        prm.max_moves = sweeps * max(nf, 1)
-        out, res, ms = capi.smooth_batch_anneal(ctx, [segs[i] for i in idx], prm,
-                                                [0.5] * len(idx))
-        ms_total += ms
-        for j, i in enumerate(idx):
-            res_all[i] = res[j]
-            out_all[i] = out[j]
-    return out_all, res_all, ms_total
+    # one launch: every region anneals `sweeps` proposals per free bead
+    # (max_moves < 0 sets that cap per region)
+    prm.max_moves = -int(sweeps)
+    out, res, ms = capi.smooth_batch_anneal(ctx, segs, prm, [0.5] * len(segs))
+    return out, res, ms
 
 
 SERVE_ANNEAL = dict(max_temp=5.0, dt_temp=0.9999, milestone_steps=20_000, improvement=0.99,

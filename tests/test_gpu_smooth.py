@@ -74,3 +74,17 @@ def test_smooth_statistics_match_reference(ctx):
     inputs = [capi.SmoothInput(c.pos, c.dist_to_next, c.fixed) for _ in range(16)]
     out, res, ms = capi.smooth_batch_anneal(ctx, inputs, prm, [0.5] * 16)
     assert ks_2samp_p(ref_e, [r.energy for r in res]) > 0.05
+
+
+def test_smooth_sweeps_cap_per_region(ctx):
+    """max_moves < 0: every region anneals -max_moves sweeps of its own
+    movable beads, all regions in one launch."""
+    chains = [synth.smooth_chain(n, seed=40 + n) for n in (12, 30, 7, 55)]
+    inputs = [capi.SmoothInput(c.pos, c.dist_to_next, c.fixed) for c in chains]
+    prm = capi.default_params(capi.LEVEL_SMOOTH, max_temp=5.0, dt_temp=0.9999,
+                              milestone_steps=10**9, improvement=0.99,
+                              schedule=capi.SCHEDULE_CPU, max_moves=-50)
+    out, res, ms = capi.smooth_batch_anneal(ctx, inputs, prm, [0.5] * len(inputs))
+    for c, r in zip(chains, res):
+        assert r.moves == 50 * int((c.fixed == 0).sum())
+        assert r.rel_error < 1e-4   # FP32 deltas, no periodic recompute here
