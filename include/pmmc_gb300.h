@@ -392,7 +392,9 @@ typedef struct {
   size_t budget_bytes;    /* device bytes of resident regions; 0 = half the free memory */
   int max_waves;          /* launches in flight at once; 0 = 8 */
   int max_wave_requests;  /* regions per launch; 0 = 4 x SM count */
-  int lanes_per_chain;    /* 1, 2, 4, 8 or 32 lanes per proposal; 0 = 2 */
+  int lanes_per_chain;    /* 1, 2, 4, 8 or 32 lanes per proposal; 0 = by
+                           * region size (1 from 1024 beads, 2 from 128,
+                           * else 4) */
 } pmmc_server_opts;
 
 typedef struct {

@@ -22,9 +22,9 @@
 //            waiting callers and releases the wave's memory and slot.
 //
 // Each region carries its own Philox key (the caller's seed, chain 0), and a
-// region's class (arc lists staged in shared memory or not) and the lanes per
-// move depend only on the region, so its result is bit-identical whether it
-// runs alone or in any mix.
+// region's class (arc lists staged in shared memory or not) and its lanes per
+// proposal (chosen from its size) depend only on the region, so its result is
+// bit-identical whether it runs alone or in any mix.
 #include <algorithm>
 #include <chrono>
 #include <cmath>
@@ -92,6 +92,7 @@ struct Request {
   ArcsPack pack;           // one region, one chain, packed at submit
   int n = 0;
   bool nb_smem = true;     // arc lists staged in shared memory
+  int lanes = 2;           // lanes per proposal (depends on the region only)
   int smem_need = 0;       // bytes of the chain's shared-memory slice
   size_t dev_bytes = 0;    // device footprint alone (budget accounting)
   Clock::time_point t_submit, t_done;
@@ -134,7 +135,7 @@ cudaError_t ensure_pinned(void *&p, size_t &cap, size_t need) {
 struct pmmc_server {
   pmmc_ctx *ctx = nullptr;
   ArcsDevParams P{};
-  int lanes = 2;
+  int lanes = 0;           // 0: by region size
   size_t budget = 0;
   int max_wave = 0;
   size_t cap_smem = 0;
@@ -207,10 +208,11 @@ void pmmc_server::launch(Slot &sl, std::vector<ReqPtr> wave) {
   // merged pack, largest regions first in the work queue
   ArcsPack pk;
   bool nbs = true;
-  int smem_need = 0;
+  int smem_need = 0, lanes = 2;
   for (auto &r : wave) {
     pk.append(r->pack);
     nbs = r->nb_smem;
+    lanes = r->lanes;
     smem_need = std::max(smem_need, r->smem_need);
   }
   pk.finish();
@@ -314,7 +316,7 @@ void pmmc_server::run() {
         size_t bytes = 0;
         for (auto it = queue.begin(); it != queue.end() && (int)wave.size() < max_wave;) {
           const ReqPtr &r = *it;
-          if (r->nb_smem == head->nb_smem &&
+          if (r->nb_smem == head->nb_smem && r->lanes == head->lanes &&
               (wave.empty() || bytes_in_use + bytes + r->dev_bytes <= budget)) {
             bytes += r->dev_bytes;
             r->state = ReqState::Running;
@@ -360,9 +362,9 @@ extern "C" pmmc_status pmmc_server_create(pmmc_ctx *ctx, const pmmc_anneal_param
   sv->ctx = ctx;
   sv->P = arcs_make_params(prm, 0, false);
   sv->P.trace_cap = 0;
-  int lanes = opts && opts->lanes_per_chain > 0 ? opts->lanes_per_chain : 2;
-  if (lanes != 1 && lanes != 2 && lanes != 4 && lanes != 8 && lanes != 32)
-    return fail(ctx, PMMC_ERR_INVALID, "server: lanes_per_chain must be 1, 2, 4, 8 or 32");
+  const int lanes = opts ? opts->lanes_per_chain : 0;
+  if (lanes != 0 && lanes != 1 && lanes != 2 && lanes != 4 && lanes != 8 && lanes != 32)
+    return fail(ctx, PMMC_ERR_INVALID, "server: lanes_per_chain must be 0, 1, 2, 4, 8 or 32");
   sv->lanes = lanes;
   size_t budget = opts ? opts->budget_bytes : 0;
   if (budget == 0) {
@@ -403,6 +405,9 @@ extern "C" pmmc_status pmmc_server_submit(pmmc_server *sv, const pmmc_arcs_probl
                 "server: region of %d beads exceeds the %zu B shared-memory slice a chain "
                 "can hold", U.n, sv->cap_smem);
   r->nb_smem = full <= sv->cap_smem;
+  // lanes per proposal from the region's own size (large regions: one lane
+  // and 32 proposals per window; small ones: more lanes, fewer conflicts)
+  r->lanes = sv->lanes > 0 ? sv->lanes : (pr->n >= 1024 ? 1 : pr->n >= 128 ? 2 : 4);
   r->smem_need = (int)(r->nb_smem ? full : minimal);
   ArcsPack probe = r->pack;
   probe.finish();
