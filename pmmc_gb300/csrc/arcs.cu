@@ -296,7 +296,7 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
                    const int4 *__restrict__ lst, const int2 *__restrict__ nulls,
                    ArcsDevParams P, int smem_per_warp, float *__restrict__ pos_out,
                    ChainOut *__restrict__ outs, int *__restrict__ done,
-                   MoveTrace *__restrict__ trace) {
+                   MoveTrace *__restrict__ trace, const double *__restrict__ bases) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31;
   float *s_dtpow = reinterpret_cast<float *>(smem);
@@ -356,7 +356,10 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
     const int4 *LST = lst + U.lst_off;
 
     // ---- initial FP64 energy: repulsion (frozen) + springs/loops/sphere ----
-    const double base = arcs_repulsion(n, spos, srp, NB, nulls + U.null_off, U.n_null, lane);
+    // (precomputed per region by arcs_base_kernel when the caller has room)
+    const double base = bases ? bases[it.x]
+                              : arcs_repulsion(n, spos, srp, NB, nulls + U.null_off, U.n_null,
+                                               lane);
     double E = base + arcs_spring_energy(n, spos, srp, NB, LST, U.n_loops, P, lane);
     if (P.ext) E += ext_full(n, spos, P, lane);
     // running energy of the chain (identical on every lane): float-float
@@ -661,7 +664,64 @@ __global__ void arcs_pick_best_kernel(const ArcsUnit *__restrict__ units,
 using ArcsKernelFn = void (*)(const ArcsUnit *, const int2 *, int, int *, const float4 *,
                               const int *, const int2 *, const float *, const int *,
                               const int *, const float4 *, const int4 *, const int2 *,
-                              ArcsDevParams, int, float *, ChainOut *, int *, MoveTrace *);
+                              ArcsDevParams, int, float *, ChainOut *, int *, MoveTrace *,
+                              const double *);
+
+// The frozen repulsion sum of every region (the 1/d of every pair the arc
+// lists do not name, in the initial score only): one 512-thread block per
+// region, rows interleaved over its warps, lanes striding the row, float
+// partial sums of 64 terms widened to FP64, a fixed-order block reduction.
+// The per-chain warp would otherwise spend O(n^2 / 32) steps on it before its
+// first move.
+__global__ void __launch_bounds__(512)
+arcs_base_kernel(const ArcsUnit *__restrict__ units, int n_units,
+                 const float4 *__restrict__ pos0, const int *__restrict__ row_ptr,
+                 const int2 *__restrict__ nbr, const int2 *__restrict__ nulls,
+                 double *__restrict__ bases) {
+  __shared__ double red[16];
+  const int u = blockIdx.x;
+  if (u >= n_units) return;
+  const ArcsUnit U = units[u];
+  const float4 *P = pos0 + U.pos_off;
+  const int *rp = row_ptr + U.rp_off;
+  const int2 *NB = nbr + U.nbr_off;
+  const int n = U.n;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  double acc = 0.0;
+  for (int i = warp; i < n; i += nw) {
+    const float4 pi = P[i];
+    float part = 0.0f;
+    int cnt = 0;
+    for (int j = i + 1 + lane; j < n; j += 32) {
+      const float4 pj = P[j];
+      const float x = pi.x - pj.x, y = pi.y - pj.y, z = pi.z - pj.z;
+      part += rsqrtf(fmaf(x, x, fmaf(y, y, z * z)));
+      if (++cnt == 64) {
+        acc += part;
+        part = 0.0f;
+        cnt = 0;
+      }
+    }
+    acc += part;
+    const int e1 = rp[i + 1];
+    for (int e = rp[i] + lane; e < e1; e += 32) {
+      const int j = NB[e].x;
+      if (j < i) acc -= (double)(1.0f / dist3(P[j].x, P[j].y, P[j].z, pi));
+    }
+  }
+  for (int c = threadIdx.x; c < U.n_null; c += blockDim.x) {
+    const int2 q = nulls[U.null_off + c];
+    acc -= (double)(1.0f / dist3(P[q.x].x, P[q.x].y, P[q.x].z, P[q.y]));
+  }
+  acc = warp_sum_d(acc);
+  if (lane == 0) red[warp] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < nw; ++w) t += red[w];
+    bases[u] = t;
+  }
+}
 
 // The instantiation for a launch: arc lists staged or not, G lanes per move.
 inline ArcsKernelFn arcs_kernel_for(bool nb_smem, int lanes) {
@@ -717,6 +777,7 @@ struct pmmc_arcs_batch {
   DevBuf<ChainOut> outs;
   DevBuf<int> done;
   DevBuf<int> best;
+  DevBuf<double> bases;  // frozen repulsion of each region
   MoveTrace *trace = nullptr;  // tests only (owned)
   std::vector<ArcsClass> classes;
   cudaEvent_t ev_fork = nullptr, ev_start = nullptr, ev_stop = nullptr;
@@ -962,7 +1023,15 @@ cudaError_t arcs_launch(const ArcsLaunch &a, const ArcsDevParams &P, bool nb_sme
   const size_t dyn = kCtaHeader + (size_t)warps * smem_per_warp;
   arcs_kernel_for(nb_smem, lanes)<<<grid, 32 * warps, dyn, s>>>(
       a.units, a.items, a.n_items, a.head, a.pos0, a.row_ptr, a.nbr, a.inv_t, a.movable, a.lrp,
-      a.lent, a.lst, a.nulls, P, smem_per_warp, a.pos_out, a.outs, a.done, a.trace);
+      a.lent, a.lst, a.nulls, P, smem_per_warp, a.pos_out, a.outs, a.done, a.trace, a.bases);
+  return cudaGetLastError();
+}
+
+cudaError_t arcs_bases(const ArcsUnit *units, int n_units, const float4 *pos0,
+                       const int *row_ptr, const int2 *nbr, const int2 *nulls, double *bases,
+                       cudaStream_t s) {
+  if (n_units <= 0) return cudaSuccess;
+  arcs_base_kernel<<<n_units, 512, 0, s>>>(units, n_units, pos0, row_ptr, nbr, nulls, bases);
   return cudaGetLastError();
 }
 
@@ -1101,7 +1170,8 @@ static cudaError_t autotune_classes(pmmc_arcs_batch *b, cudaStream_t s) {
           const int grid = std::max(1, std::min(per_sm * ctx->sm_count, (m + w - 1) / w));
           ArcsLaunch a{b->units.p, b->items.p + c.item_begin, m, b->heads.p + k, b->pos0.p,
                        b->row_ptr.p, b->nbr.p, b->inv_t.p, b->movable.p, b->lrp.p, b->lent.p,
-                       b->lst.p, b->nulls.p, b->pos_out.p, b->outs.p, b->done.p, nullptr};
+                       b->lst.p, b->nulls.p, b->pos_out.p, b->outs.p, b->done.p, nullptr,
+                       b->bases.p};
           float ms = 0.0f;
           for (int rep = 0; rep < 2 && e == cudaSuccess; ++rep) {
             e = cudaMemsetAsync(b->heads.p + k, 0, sizeof(int), s);
@@ -1287,6 +1357,9 @@ extern "C" pmmc_status pmmc_arcs_batch_create_ex(
   if (e == cudaSuccess) e = b->outs.alloc((size_t)chain_base);
   if (e == cudaSuccess) e = b->done.alloc((size_t)n_units);
   if (e == cudaSuccess) e = b->best.alloc((size_t)n_units);
+  if (e == cudaSuccess) e = b->bases.alloc((size_t)n_units);
+  if (e == cudaSuccess) e = arcs_bases(b->units.p, n_units, b->pos0.p, b->row_ptr.p, b->nbr.p,
+                                       b->nulls.p, b->bases.p, s);
   if (e == cudaSuccess && trace_cap > 0)
     e = cudaMalloc(&b->trace, sizeof(MoveTrace) * (size_t)trace_cap);
   if (e == cudaSuccess) e = cudaEventCreate(&b->ev_fork);
@@ -1322,7 +1395,7 @@ cudaError_t enqueue_pass(pmmc_arcs_batch *b, cudaStream_t s) {
     ArcsLaunch a{b->units.p, b->items.p + c.item_begin, c.item_end - c.item_begin,
                  b->heads.p + k, b->pos0.p, b->row_ptr.p, b->nbr.p, b->inv_t.p, b->movable.p,
                  b->lrp.p, b->lent.p, b->lst.p, b->nulls.p, b->pos_out.p, b->outs.p,
-                 b->done.p, b->trace};
+                 b->done.p, b->trace, b->bases.p};
     e = arcs_launch(a, b->P, c.nb_smem, c.lanes, c.grid, c.warps_per_cta, c.smem_per_warp,
                     c.stream);
     if (e == cudaSuccess) e = cudaEventRecord(c.join, c.stream);
@@ -1722,7 +1795,7 @@ extern "C" pmmc_status pmmc_arcs_anneal_noalloc(const pmmc_arcs_problem *pr,
   fn<<<1, 32, kCtaHeader + per_warp, s>>>(&S->unit, &S->item, 1, &S->head, S->pos0,
                                           S->row_ptr, S->nbr, S->inv_t, S->movable, nullptr,
                                           nullptr, S->lst, S->nulls, P, (int)per_warp, pos_out,
-                                          &S->out, &S->done, nullptr);
+                                          &S->out, &S->done, nullptr, nullptr);
   if (cudaGetLastError() != cudaSuccess) return PMMC_ERR_CUDA;
   ChainOut o;
   int bad = 0;

@@ -116,11 +116,16 @@ struct ArcsLaunch {
   ChainOut *outs;
   int *done;
   MoveTrace *trace;
+  const double *bases;  // frozen repulsion per unit (NULL: each chain computes it)
 };
 
 // One persistent pass of `grid` CTAs x `warps` warps over the items on `s`.
 cudaError_t arcs_launch(const ArcsLaunch &a, const ArcsDevParams &P, bool nb_smem, int lanes,
                         int grid, int warps, int smem_per_warp, cudaStream_t s);
+// The frozen repulsion of every unit into bases[u] (one block per unit).
+cudaError_t arcs_bases(const ArcsUnit *units, int n_units, const float4 *pos0,
+                       const int *row_ptr, const int2 *nbr, const int2 *nulls, double *bases,
+                       cudaStream_t s);
 // Resident CTAs per SM of that configuration (at least 1).
 int arcs_ctas_per_sm(bool nb_smem, int lanes, int warps, int smem_per_warp);
 // Raise the dynamic shared-memory limit of every instantiation to `bytes`.

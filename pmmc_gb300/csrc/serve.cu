@@ -53,6 +53,7 @@ struct BlobLayout {
   size_t units, items, pos0, rp, nbr, inv, nulls, mov, lrp, lent, lst;
   size_t in_bytes;        // [0, in_bytes) is copied up
   size_t head, done;      // cleared before the launch
+  size_t bases;           // frozen repulsion per region
   size_t pos_out, outs;   // [pos_out, total) is copied back
   size_t total;
 };
@@ -79,6 +80,7 @@ BlobLayout layout_of(const ArcsPack &pk) {
   L.in_bytes = o;
   L.head = take(sizeof(int));
   L.done = take(sizeof(int) * pk.units.size());
+  L.bases = take(sizeof(double) * pk.units.size());
   L.pos_out = take(sizeof(float) * (size_t)pk.out_floats);
   L.outs = take(sizeof(ChainOut) * (size_t)pk.chains);
   L.total = o;
@@ -272,8 +274,11 @@ void pmmc_server::launch(Slot &sl, std::vector<ReqPtr> wave) {
                  reinterpret_cast<float *>(d + L.pos_out),
                  reinterpret_cast<ChainOut *>(d + L.outs),
                  reinterpret_cast<int *>(d + L.done),
-                 nullptr};
-    e = arcs_launch(a, P, nbs, lanes, grid, warps, per_warp, sl.stream);
+                 nullptr,
+                 reinterpret_cast<const double *>(d + L.bases)};
+    e = arcs_bases(a.units, n_items, a.pos0, a.row_ptr, a.nbr, a.nulls,
+                   reinterpret_cast<double *>(d + L.bases), sl.stream);
+    if (e == cudaSuccess) e = arcs_launch(a, P, nbs, lanes, grid, warps, per_warp, sl.stream);
   }
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(sl.h_out, d + L.pos_out, L.total - L.pos_out, cudaMemcpyDeviceToHost,
