@@ -350,6 +350,21 @@ pmmc_status pmmc_equidistant_model(pmmc_ctx *ctx, int n, const int *gpos, const 
                                    int pos_stop, int res, float *out, int64_t cap,
                                    int64_t *n_out, double *kernel_ms);
 
+/* ---------------- HCM model file ---------------- */
+/* Writes the reference's HCM text format, as HierarchicalChromosome::toFile
+ * (src/HierarchicalChromosome.cu:530-552) with Cluster::toFile
+ * (src/include/Cluster.hpp:175-181) and InteractionArc::toFile
+ * (src/include/InteractionArc.hpp:122-125): a header, the factor names, one
+ * line per cluster (start, end, orientation char, position, children given as
+ * CSR child_ptr[n_clusters+1] / children), then per chromosome its name, root
+ * cluster and arcs (CSR arc_ptr[n_chrs+1]; 7 ints per arc: start, end,
+ * genomic_start, genomic_end, score, eff_score, factor).  Host code only. */
+pmmc_status pmmc_hcm_write(const char *path, int n_clusters, const int *start, const int *end,
+                           const char *orientation, const float *pos, const int *child_ptr,
+                           const int *children, int n_factors, const char *const *factors,
+                           int n_chrs, const char *const *chr_names, const int *chr_root,
+                           const int *arc_ptr, const int *arcs);
+
 /* ---------------- arc-level anneal that allocates nothing ------------- */
 /* No counterpart in the reference.  For callers that cannot allocate device
  * memory -- code that must not call cudaMalloc because a host framework owns

@@ -42,7 +42,7 @@ HEADER_SYMBOLS = [
     "pmmc_server_create", "pmmc_server_submit", "pmmc_server_poll", "pmmc_server_wait",
     "pmmc_server_get_stats", "pmmc_server_destroy", "pmmc_arcs_batch_classes",
     "pmmc_selftest_sqrt", "pmmc_distance_heatmap", "pmmc_distance_heatmap_device",
-    "pmmc_equidistant_model",
+    "pmmc_equidistant_model", "pmmc_hcm_write",
 ]
 
 LANES_AUTO = -1  # PMMC_LANES_AUTO: the autotuner picks lanes and warps per class
@@ -520,6 +520,30 @@ def equidistant_model(ctx: Context, gpos, pos, first_end: int, last_start: int,
                                            int(res), _p(out), C.c_int64(m.value), C.byref(m),
                                            C.byref(ms)))
     return out, ms.value
+
+
+def hcm_write(path: str, start, end, orientation, pos, children, factors, chrs):
+    """pmmc_hcm_write.  children: one list per cluster; factors: names;
+    chrs: list of (name, root, arcs as rows of 7 ints)."""
+    n = len(start)
+    st, en = _i32(start), _i32(end)
+    ori = np.frombuffer("".join(orientation).encode(), np.uint8).copy() if n else np.zeros(1, np.uint8)
+    p = _f32(pos).reshape(-1, 3)
+    cp = _i32(np.concatenate([[0], np.cumsum([len(c) for c in children])]) if n else [0])
+    ch = _i32([x for c in children for x in c] or [0])
+    fac = [f.encode() for f in factors]
+    fac_arr = (C.c_char_p * max(len(fac), 1))(*fac)
+    names = [c[0].encode() for c in chrs]
+    names_arr = (C.c_char_p * max(len(names), 1))(*names)
+    roots = _i32([c[1] for c in chrs] or [0])
+    ap = _i32(np.concatenate([[0], np.cumsum([len(c[2]) for c in chrs])]) if chrs else [0])
+    arcs = _i32(np.array([a for c in chrs for a in c[2]], np.int32).reshape(-1) if chrs else [0])
+    if arcs.size == 0:
+        arcs = np.zeros(7, np.int32)
+    st_ = lib().pmmc_hcm_write(path.encode(), n, _p(st), _p(en), _p(ori), _p(p), _p(cp), _p(ch),
+                               len(fac), fac_arr, len(chrs), names_arr, _p(roots), _p(ap),
+                               _p(arcs))
+    _check(None, st_)
 
 
 def selftest_sqrt(ctx: Context, lo: int, count: int):

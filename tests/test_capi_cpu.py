@@ -67,3 +67,20 @@ def test_serve_trace_shape():
     rate = len(a1) / a1[-1]
     assert 180 < rate < 220
     assert np.all(np.diff(a1) >= 0) and a1[0] == 0.0
+
+
+def test_hcm_writer_matches_reference_lines(tmp_path):
+    """pmmc_hcm_write: cluster and arc lines equal the reference's own
+    Cluster::toFile / InteractionArc::toFile output (golden lines)."""
+    g = np.load(os.path.join(os.path.dirname(__file__), "golden", "hcm.npz"))["lines"]
+    path = str(tmp_path / "model.hcm")
+    capi.hcm_write(path, [10, 0], [20, 0], ["N", "L"],
+                   np.array([[1.5, -2.25, 3.125], [1e-7, 123456.789, -0.5]], np.float32),
+                   [[4, 5], []], ["CTCF"],
+                   [("chr1", 0, [[1, 2, 300, 400, 5, 6, -1], [7, 9, -1, -1, 0, 12, 2]])])
+    lines = open(path).read().splitlines(keepends=True)
+    assert lines[0] == "2 1 -1 1\n"
+    assert lines[1] == "CTCF \n"
+    assert lines[2] == str(g[0]) and lines[3] == str(g[1])
+    assert lines[4] == "chr1 0 2\n"
+    assert lines[5] == str(g[2]) and lines[6] == str(g[3])
