@@ -239,6 +239,45 @@ def equidistant_main(args):
     print(json.dumps(line))
 
 
+def targets_main(args):
+    """Anchor-level expected-distance line beside the reference's host
+    builder (the oracle port, bit-identical to it: a linear anchor scan per
+    long-arc end) on one core, timed on the same chromosome with a quarter
+    of the long arcs and scaled per arc."""
+    from oracle import oracle as O
+    from pmmc_gb300 import workloads as W
+    O.build()
+    n_long = args.n or 2_000_000
+    sample = W.targets_problem(n_long // 4)
+    units = len(sample["arc_start"]) + n_long // 4
+    t = time.perf_counter()
+    O.anchor_targets(sample)
+    dt = time.perf_counter() - t
+    cpu = {"value": units / dt, "unit": "arcs/s", "cores": 1, "kind": "port",
+           "sample": f"{W.TARGETS_ANCHORS} anchors, {len(sample['arc_start'])} arcs and "
+                     f"{n_long // 4} long arcs ({dt:.2f} s)"}
+    if args.impl == "reference":
+        if int(os.environ.get("RANK", "0")) != 0:
+            return
+        print(json.dumps({"metric": "arcs/s", "value": cpu["value"], "unit": "arcs/s",
+                          "n_gpus": 0, "steps": 1, "warmup": 0, "ms_per_step": dt * 1e3,
+                          "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                          "dtype": "int32", "data": "synthetic", "impl": "reference",
+                          "config": {"workload": "anchor_targets"}, "cpu_baseline": cpu,
+                          "e2e": {"value": cpu["value"], "unit": "arcs/s",
+                                  "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+        return
+    sampler = ClockSampler(0)
+    sampler.start()
+    line = W.targets(args)
+    line["clocks"] = sampler.stop()
+    # own kernels per call: long_map, long_resolve, pair_emit, csr_finish (the
+    # two radix sorts are the CUDA toolkit's CUB)
+    line["gpu_launches"] = 4 * args.steps
+    line["cpu_baseline"] = cpu
+    print(json.dumps(line))
+
+
 def plain_main(args):
     """Config-0 line: the plain drop-in call beside the reference CPU
     annealer (the oracle port, bit-identical to it) on one core."""
@@ -515,7 +554,7 @@ def main():
                     help="milestone interval (smaller for profiling runs)")
     ap.add_argument("--workload", default="ensemble",
                     choices=["ensemble", "plain", "heatmap", "heatmap-batch", "smooth",
-                             "serve", "distmap", "equidistant"],
+                             "serve", "distmap", "equidistant", "targets"],
                     help="ensemble: the batched arc-level ensemble (default line); "
                          "heatmap: one 2048-bead heatmap chain; heatmap-batch: one chain "
                          "per distinct 2048-bead map, one per SM; smooth: genome-scale "
@@ -523,7 +562,8 @@ def main():
     ap.add_argument("--maps", type=int, default=0, help="heatmap-batch: number of maps")
     ap.add_argument("--moves", type=int, default=0, help="moves per chain (heatmap/smooth)")
     ap.add_argument("--requests", type=int, default=0, help="serve: requests in the trace")
-    ap.add_argument("--n", type=int, default=0, help="distmap: matrix size")
+    ap.add_argument("--n", type=int, default=0,
+                    help="distmap: matrix size; equidistant: resolution; targets: long arcs")
     ap.add_argument("--lanes", type=int, default=-1,
                     help="lanes per proposal of the batched form (2, 4, 8, 32; -1 = autotune)")
     args = ap.parse_args()
@@ -539,6 +579,9 @@ def main():
         return
     if args.workload == "equidistant":
         equidistant_main(args)
+        return
+    if args.workload == "targets":
+        targets_main(args)
         return
     if args.workload != "ensemble":
         from pmmc_gb300 import workloads

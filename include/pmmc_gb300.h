@@ -335,6 +335,70 @@ pmmc_status pmmc_distance_heatmap_device(pmmc_ctx *ctx, int n, const float *cont
                                          float scale, float power, float stretching,
                                          float *dist, float *stats, void *stream);
 
+/* ---------------- anchor-level expected distances ---------------- */
+/* Replaces LooperSolver::calcAnchorExpectedDistancesHeatmap
+ * (LooperSolver.hpp:5494-5627) and the dense n x n matrix it fills: the
+ * expected distances of an anchor-level active region, written directly as
+ * the CSR pmmc_arcs_problem takes (both directions, columns sorted, the
+ * entries pmmc_arcs_dense_to_csr would keep of the reference's matrix).
+ *   short arcs   the arcs of every active cluster (Cluster::arcs, indices
+ *                into the chromosome's arcs, cluster-index ends) whose other
+ *                end is not below it; the last write of a pair wins;
+ *   long arcs    genomic-position arcs (InteractionArcs::long_arcs) resolved
+ *                to anchors (Anchor::contains; the first anchor holding the
+ *                position), then to active slots; a pair that already holds
+ *                a distance >= 0 keeps it (a collision);
+ *   influence    with anchor_heat (the n x n heatmap_anchor, row-major;
+ *                Settings::useAnchorHeatmap on) every distance >= 0 above the
+ *                diagonal is scaled by 1 - min(1, heat / max * influence),
+ *                max the largest heatmap value from the first diagonal
+ *                holding one above 1e-6 (Heatmap::getRange).
+ * Distances are freqToDistance(score, memo = true) (LooperSolver.hpp:
+ * 3949-3967): freq_memo[score] for 1 <= score <= 100 (the reference's
+ * freq_to_distance table; it fills entries 2..100), otherwise the
+ * countToDist* formula in FP64.  An arc end outside the active region maps
+ * to slot 0, as the reference's std::map::operator[] inserts it.
+ * n_anchors == 0 means the chromosome has no anchor list (long arcs are not
+ * used).  cap >= 2 * (arc_ptr[n] + n_long) always suffices; with a smaller
+ * cap or col/target NULL only *nnz is written (size query).  Long-arc
+ * resolution, de-duplication, the influence and the CSR assembly run on the
+ * device. */
+typedef struct pmmc_anchor_targets_problem {
+  int n;                       /* active-region size                       */
+  const int *active;           /* n cluster indices (active_region)        */
+  const int *arc_ptr;          /* n+1: arcs of cluster active[i]           */
+  const int *arc_idx;          /* arc_ptr[n] indices into the arc table    */
+  int n_arcs;                  /* the chromosome's arcs                    */
+  const int *arc_start;        /* cluster index of each arc's start        */
+  const int *arc_end;          /* cluster index of each arc's end          */
+  const int *arc_score;        /* PET count                                */
+  int n_long;                  /* the chromosome's long arcs               */
+  const int *long_start;       /* genomic positions                        */
+  const int *long_end;
+  const int *long_score;
+  int n_anchors;               /* the chromosome's anchors                 */
+  const int *anchor_start;
+  const int *anchor_end;
+  int first_cluster;           /* chr_first_cluster of the chromosome      */
+  const float *freq_memo;      /* 101 entries                              */
+  float count_a, count_scale, count_shift, count_base; /* Settings::countToDist* */
+  const float *anchor_heat;    /* n*n, NULL: no anchor heatmap             */
+  float anchor_influence;      /* Settings::anchorHeatmapInfluence         */
+} pmmc_anchor_targets_problem;
+
+/* The counters the reference prints for the long arcs, and the device time
+ * of each phase (long-arc mapping, its sort, resolution, CSR assembly with
+ * the heatmap passes). */
+typedef struct pmmc_anchor_targets_stats {
+  int64_t applied, out_of_range, inactive, collision;
+  float ms_map, ms_sort, ms_resolve, ms_assemble;
+} pmmc_anchor_targets_stats;
+
+pmmc_status pmmc_anchor_targets(pmmc_ctx *ctx, const pmmc_anchor_targets_problem *pr,
+                                int *row_ptr, int *col, float *target, int64_t cap,
+                                int64_t *nnz, pmmc_anchor_targets_stats *stats,
+                                double *kernel_ms);
+
 /* ---------------- equidistant model ---------------- */
 /* Replaces the interpolation of HierarchicalChromosome::createEqidistantModel
  * (src/HierarchicalChromosome.cu:466-519; gpuHelper :1253-1447 and its

@@ -532,3 +532,49 @@ def ref_random_vectors(seed: int, count: int, max_size: float = 1.0, in2d: bool 
     out = np.zeros((count, 3), np.float32)
     ref().ref_random_vectors(C.c_uint(seed), count, C.c_float(max_size), int(in2d), _p(out))
     return out
+
+
+def _anchor_args(t):
+    a = {k: _i32(t[k]) for k in ("active", "arc_ptr", "arc_idx", "arc_start", "arc_end",
+                                 "arc_score", "long_start", "long_end", "long_score",
+                                 "anc_start", "anc_end")}
+    heat = None if t.get("heat") is None else _f32(t["heat"])
+    ca, cs, csh, cb = (C.c_float(float(x)) for x in t["count"])
+    return a, _f32(t["memo"]), heat, (ca, cs, csh, cb)
+
+
+def anchor_targets(t):
+    """orc_anchor_targets on a problem dict (the keys of
+    pmmc_gb300.capi.anchor_targets_arrays): (dense n x n, stats dict)."""
+    a, memo, heat, cnt = _anchor_args(t)
+    n = len(a["active"])
+    dense = np.zeros((n, n), np.float32)
+    st = np.zeros(4, np.int64)
+    rc = lib().orc_anchor_targets(
+        n, _p(a["active"]), _p(a["arc_ptr"]), _p(a["arc_idx"]), _p(a["arc_start"]),
+        _p(a["arc_end"]), _p(a["arc_score"]), len(a["long_start"]), _p(a["long_start"]),
+        _p(a["long_end"]), _p(a["long_score"]), len(a["anc_start"]), _p(a["anc_start"]),
+        _p(a["anc_end"]), int(t["first_cluster"]), _p(memo), *cnt, _p(heat),
+        C.c_float(float(t.get("influence", 0.0))), _p(dense), _p(st))
+    if rc != 0:
+        raise ValueError("an arc does not touch its cluster")
+    return dense, dict(zip(("applied", "out_of_range", "inactive", "collision"),
+                           (int(x) for x in st)))
+
+
+def ref_anchor_targets(t):
+    """The reference's calcAnchorExpectedDistancesHeatmap on the same dict."""
+    a, memo, heat, cnt = _anchor_args(t)
+    n = len(a["active"])
+    dense = np.zeros((n, n), np.float32)
+    st = np.zeros(4, np.int64)
+    rc = ref().ref_anchor_targets(
+        n, _p(a["active"]), _p(a["arc_ptr"]), _p(a["arc_idx"]), len(a["arc_start"]),
+        _p(a["arc_start"]), _p(a["arc_end"]), _p(a["arc_score"]), len(a["long_start"]),
+        _p(a["long_start"]), _p(a["long_end"]), _p(a["long_score"]), len(a["anc_start"]),
+        _p(a["anc_start"]), _p(a["anc_end"]), int(t["first_cluster"]), _p(memo), *cnt,
+        _p(heat), C.c_float(float(t.get("influence", 0.0))), _p(dense), _p(st))
+    if rc != 0:
+        raise RuntimeError("reference harness failed")
+    return dense, dict(zip(("applied", "out_of_range", "inactive", "collision"),
+                           (int(x) for x in st)))

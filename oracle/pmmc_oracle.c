@@ -1246,3 +1246,179 @@ void orc_heatmap_replay(int n, const float *pos0, const unsigned char *fixed,
               n_moves, bead, disp, gpu_acc, out);
   free(pos);
 }
+
+/* ------------------------------------------------------------------ */
+/* anchor-level expected distances (LooperSolver.hpp:5494-5627)       */
+/* ------------------------------------------------------------------ */
+
+/* freqToDistance(freq, memo = true) (LooperSolver.hpp:3949-3967): the int
+ * count plus the float shift is a float; the rest is FP64. */
+static float orc_freq_to_distance(int freq, const float *memo, float a,
+                                  float scale, float shift, float base) {
+  if (freq >= 1 && freq <= 100)
+    return memo[freq];
+  if (a < 0.0f) {
+    int fi = (int)((float)freq + shift);
+    if (fi < 1)
+      fi = 1;
+    return (float)((double)base + (double)scale * pow((double)fi, (double)a));
+  }
+  return (float)((double)base +
+                 (double)scale / exp((double)a * (double)((float)freq + shift)));
+}
+
+/* std::map<int, int> as a sorted array: lookup, and operator[] inserting 0. */
+typedef struct {
+  int *key, *val;
+  int n, cap;
+} orc_imap;
+
+static int orc_imap_find(const orc_imap *m, int k) {
+  int lo = 0, hi = m->n;
+  while (lo < hi) {
+    int mid = (lo + hi) >> 1;
+    if (m->key[mid] < k)
+      lo = mid + 1;
+    else
+      hi = mid;
+  }
+  return lo;
+}
+
+static int *orc_imap_at(orc_imap *m, int k) {
+  int p = orc_imap_find(m, k);
+  if (p < m->n && m->key[p] == k)
+    return &m->val[p];
+  if (m->n == m->cap) {
+    m->cap = m->cap ? 2 * m->cap : 64;
+    m->key = (int *)realloc(m->key, sizeof(int) * m->cap);
+    m->val = (int *)realloc(m->val, sizeof(int) * m->cap);
+  }
+  memmove(m->key + p + 1, m->key + p, sizeof(int) * (m->n - p));
+  memmove(m->val + p + 1, m->val + p, sizeof(int) * (m->n - p));
+  m->key[p] = k;
+  m->val[p] = 0;
+  m->n++;
+  return &m->val[p];
+}
+
+int orc_anchor_targets(int n, const int *active, const int *arc_ptr,
+                       const int *arc_idx, const int *arc_start,
+                       const int *arc_end, const int *arc_score, int n_long,
+                       const int *long_start, const int *long_end,
+                       const int *long_score, int n_anc, const int *anc_start,
+                       const int *anc_end, int first_cluster,
+                       const float *memo, float count_a, float count_scale,
+                       float count_shift, float count_base, const float *heat,
+                       float influence, float *dense, long long *stats4) {
+  int i, j, k, rc = 0;
+  orc_imap m = {NULL, NULL, 0, 0};
+  for (k = 0; k < 4; ++k)
+    stats4[k] = 0;
+  /* init(n), add(-1), clearDiagonal(1) */
+  for (i = 0; i < n; ++i)
+    for (j = 0; j < n; ++j)
+      dense[(size_t)i * n + j] = i == j ? 0.0f : -1.0f;
+  for (i = 0; i < n; ++i)
+    *orc_imap_at(&m, active[i]) = i;
+  /* the arcs of the active clusters, forward only (:5512-5539) */
+  for (i = 0; i < n && rc == 0; ++i) {
+    int ai = active[i];
+    for (k = arc_ptr[i]; k < arc_ptr[i + 1]; ++k) {
+      int arc = arc_idx[k], other, a, b;
+      float e;
+      if (arc_start[arc] == ai)
+        other = arc_end[arc];
+      else if (arc_end[arc] == ai)
+        other = arc_start[arc];
+      else {
+        rc = -1;
+        break;
+      }
+      if (other < ai)
+        continue;
+      e = (float)(double)orc_freq_to_distance(arc_score[arc], memo, count_a,
+                                              count_scale, count_shift,
+                                              count_base);
+      a = *orc_imap_at(&m, ai);
+      b = *orc_imap_at(&m, other);
+      dense[(size_t)a * n + b] = e;
+      dense[(size_t)b * n + a] = e;
+    }
+  }
+  /* long arcs: linear anchor scan, slots through the same map (:5547-5588) */
+  if (rc == 0 && n_long > 0 && n_anc > 0) {
+    int *anc_to_active = (int *)malloc(sizeof(int) * n_anc);
+    for (i = 0; i < n_anc; ++i)
+      anc_to_active[i] = -1;
+    for (i = 0; i < m.n; ++i)
+      if (m.key[i] >= first_cluster && m.key[i] < first_cluster + n_anc)
+        anc_to_active[m.key[i] - first_cluster] = m.val[i];
+    for (k = 0; k < n_long; ++k) {
+      int ia = -1, ib = -1, a, b;
+      for (i = 0; i < n_anc; ++i)
+        if (long_start[k] >= anc_start[i] && long_start[k] <= anc_end[i]) {
+          ia = i;
+          break;
+        }
+      for (i = 0; i < n_anc; ++i)
+        if (long_end[k] >= anc_start[i] && long_end[k] <= anc_end[i]) {
+          ib = i;
+          break;
+        }
+      if (ia < 0 || ib < 0 || ia == ib) {
+        stats4[1]++;
+        continue;
+      }
+      a = anc_to_active[ia];
+      b = anc_to_active[ib];
+      if (a < 0 || b < 0) {
+        stats4[2]++;
+        continue;
+      }
+      if (dense[(size_t)a * n + b] >= 0.0f) {
+        stats4[3]++;
+        continue;
+      }
+      {
+        float ed = orc_freq_to_distance(long_score[k], memo, count_a,
+                                        count_scale, count_shift, count_base);
+        dense[(size_t)a * n + b] = ed;
+        dense[(size_t)b * n + a] = ed;
+        stats4[0]++;
+      }
+    }
+    free(anc_to_active);
+  }
+  /* the anchor heatmap's influence (:5598-5625): getDiagonalSize, getRange */
+  if (rc == 0 && heat && n > 0) {
+    int w, diag = 0, found = 0;
+    float max_val = 0.0f;
+    for (w = 0; w < n && !found; ++w)
+      for (i = 0; i + w < n; ++i)
+        if ((double)heat[(size_t)i * n + i + w] > 1e-6) {
+          diag = w;
+          found = 1;
+          break;
+        }
+    for (i = 0; i < n; ++i)
+      for (j = i + diag; j < n; ++j)
+        if (heat[(size_t)i * n + j] > max_val)
+          max_val = heat[(size_t)i * n + j];
+    if ((double)max_val > 1e-6)
+      for (i = 0; i < n; ++i)
+        for (j = i + 1; j < n; ++j) {
+          float s;
+          if (dense[(size_t)i * n + j] < 0.0f)
+            continue;
+          s = (heat[(size_t)i * n + j] / max_val) * influence;
+          if (s > 1.0f)
+            s = 1.0f;
+          dense[(size_t)i * n + j] *= (1.0f - s);
+          dense[(size_t)j * n + i] = dense[(size_t)i * n + j];
+        }
+  }
+  free(m.key);
+  free(m.val);
+  return rc;
+}

@@ -243,6 +243,26 @@ void orc_heatmap_replay(int n, const float *pos0, const unsigned char *fixed,
                         int n_moves, const int *bead, const float *disp,
                         const int *gpu_acc, orc_replay_out *out);
 
+/* ---------------- anchor-level expected distances ---------------- */
+/* LooperSolver::calcAnchorExpectedDistancesHeatmap (src/include/
+ * LooperSolver.hpp:5494-5627) written out literally: the dense n x n matrix
+ * (-1, 0 on the diagonal), the arcs of the active clusters through a
+ * cluster -> slot map that inserts a missing cluster as slot 0 (as
+ * std::map::operator[] does), the long arcs through the linear anchor scan,
+ * then the anchor heatmap's influence (heat NULL: off).  n_anc == 0: no
+ * anchor list.  stats4 = applied, out of range, inactive, collision.
+ * Returns 0, or -1 when an arc does not touch its cluster (the reference
+ * exits). */
+int orc_anchor_targets(int n, const int *active, const int *arc_ptr,
+                       const int *arc_idx, const int *arc_start,
+                       const int *arc_end, const int *arc_score, int n_long,
+                       const int *long_start, const int *long_end,
+                       const int *long_score, int n_anc, const int *anc_start,
+                       const int *anc_end, int first_cluster,
+                       const float *memo, float count_a, float count_scale,
+                       float count_shift, float count_base, const float *heat,
+                       float influence, float *dense, long long *stats4);
+
 /* ---------------- HCM text lines ---------------- */
 /* Cluster::toFile (src/include/Cluster.hpp:175-181). Returns bytes written. */
 int orc_hcm_cluster_line(char *buf, int cap, int start, int end, char orient,

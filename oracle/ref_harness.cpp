@@ -333,6 +333,95 @@ int ref_distance_heatmap(int n, const float *contact, int diag, int level, float
   return 0;
 }
 
+/* LooperSolver::calcAnchorExpectedDistancesHeatmap (src/include/
+ * LooperSolver.hpp:5494-5627) on chromosome "chr1": clusters[active[i]].arcs
+ * = arc_idx[arc_ptr[i]..], the chromosome's arcs, long arcs and anchors as
+ * given, freq_to_distance = memo.  dense (n*n) receives
+ * heatmap_exp_dist_anchor; stats4 the applied / oor / inactive / collision
+ * counts the reference prints (read back from its output).  Returns 0, or -1
+ * when the reference did not finish (it exits on an arc that does not touch
+ * its cluster, so callers pass only well-formed arcs). */
+int ref_anchor_targets(int n, const int *active, const int *arc_ptr, const int *arc_idx,
+                       int n_arcs, const int *arc_start, const int *arc_end,
+                       const int *arc_score, int n_long, const int *long_start,
+                       const int *long_end, const int *long_score, int n_anc,
+                       const int *anc_start, const int *anc_end, int first_cluster,
+                       const float *memo, float count_a, float count_scale,
+                       float count_shift, float count_base, const float *heat,
+                       float influence, float *dense, long long *stats4) {
+  char tmpl[] = "/tmp/pmmc_ref_outXXXXXX";
+  int fd = mkstemp(tmpl);
+  if (fd < 0)
+    return -1;
+  orc_params p;
+  memset(&p, 0, sizeof(p));
+  apply_settings(&p, 0);
+  Settings::outputLevel = 0;
+  Settings::countToDistA = count_a;
+  Settings::countToDistScale = count_scale;
+  Settings::countToDistShift = count_shift;
+  Settings::countToDistBaseLevel = count_base;
+  Settings::useAnchorHeatmap = heat != nullptr;
+  Settings::anchorHeatmapInfluence = influence;
+  fflush(stdout);
+  std::cout.flush();
+  int saved = dup(1);
+  dup2(fd, 1);
+  {
+    LooperSolver s("ref", "/tmp/");
+    int max_cluster = first_cluster + n_anc;
+    for (int i = 0; i < n; ++i) max_cluster = std::max(max_cluster, active[i] + 1);
+    for (int k = 0; k < n_arcs; ++k)
+      max_cluster = std::max(max_cluster, std::max(arc_start[k], arc_end[k]) + 1);
+    s.clusters.assign(max_cluster, Cluster());
+    s.active_region.assign(active, active + n);
+    for (int i = 0; i < n; ++i)
+      s.clusters[active[i]].arcs.assign(arc_idx + arc_ptr[i], arc_idx + arc_ptr[i + 1]);
+    const std::string chr = "chr1";
+    s.current_chr = chr;
+    s.chr_first_cluster[chr] = first_cluster;
+    std::vector<InteractionArc> &av = s.arcs.arcs[chr];
+    for (int k = 0; k < n_arcs; ++k) av.push_back(InteractionArc(arc_start[k], arc_end[k], arc_score[k]));
+    std::vector<InteractionArc> &lv = s.arcs.long_arcs[chr];
+    for (int k = 0; k < n_long; ++k)
+      lv.push_back(InteractionArc(long_start[k], long_end[k], long_score[k]));
+    if (n_anc > 0) {
+      std::vector<Anchor> &anc = s.arcs.anchors[chr];
+      for (int i = 0; i < n_anc; ++i) anc.push_back(Anchor(chr, anc_start[i], anc_end[i], 'N'));
+    }
+    for (int i = 0; i <= 100; ++i) s.freq_to_distance[i] = memo[i];
+    if (heat) load_dense(s.heatmap_anchor, n, heat);
+    s.calcAnchorExpectedDistancesHeatmap();
+    for (int i = 0; i < n; ++i)
+      for (int j = 0; j < n; ++j) dense[(size_t)i * n + j] = s.heatmap_exp_dist_anchor.v[i][j];
+  }
+  fflush(stdout);
+  std::cout.flush();
+  dup2(saved, 1);
+  close(saved);
+  for (int k = 0; k < 4; ++k) stats4[k] = 0;
+  FILE *f = fdopen(fd, "r");
+  if (f) {
+    rewind(f);
+    char line[512];
+    while (fgets(line, sizeof(line), f)) {
+      int a, b, c, d;
+      if (sscanf(line, "long_arcs->anchor: applied=%d oor=%d inactive=%d collision=%d", &a, &b,
+                 &c, &d) == 4) {
+        stats4[0] = a;
+        stats4[1] = b;
+        stats4[2] = c;
+        stats4[3] = d;
+      }
+    }
+    fclose(f);
+  } else {
+    close(fd);
+  }
+  unlink(tmpl);
+  return 0;
+}
+
 /* InteractionArcs::markArcs (src/include/InteractionArcs.hpp:207-336) on a
  * single chromosome "chr1".  Output layout as orc_mark_arcs. */
 int ref_mark_arcs(int n_anchors, const int *a_start, const int *a_end,

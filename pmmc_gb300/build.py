@@ -44,7 +44,9 @@ def build(force: bool = False, verbose: bool = False, ptxas_v: bool = False) -> 
     os.makedirs(BUILD, exist_ok=True)
     cc = nvcc()
     hm = _headers_mtime()
-    flags = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
+    # -ffp-contract=off: host arithmetic that restates the reference's
+    # (freqToDistance, energies) rounds alike on x86-64 and aarch64
+    flags = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-ffp-contract=off",
                     "-I", INCLUDE, "-I", CSRC, "--expt-relaxed-constexpr"]
     if ptxas_v:
         flags += ["-Xptxas", "-v"]

@@ -42,7 +42,7 @@ HEADER_SYMBOLS = [
     "pmmc_server_create", "pmmc_server_submit", "pmmc_server_poll", "pmmc_server_wait",
     "pmmc_server_get_stats", "pmmc_server_destroy", "pmmc_arcs_batch_classes",
     "pmmc_selftest_sqrt", "pmmc_distance_heatmap", "pmmc_distance_heatmap_device",
-    "pmmc_equidistant_model", "pmmc_hcm_write",
+    "pmmc_equidistant_model", "pmmc_hcm_write", "pmmc_anchor_targets",
 ]
 
 LANES_AUTO = -1  # PMMC_LANES_AUTO: the autotuner picks lanes and warps per class
@@ -93,6 +93,25 @@ class HeatmapProblem(C.Structure):
         ("n", C.c_int), ("pos", C.c_void_p), ("fixed", C.c_void_p), ("heat", C.c_void_p),
         ("diag", C.c_int), ("n_bounds", C.c_int), ("bounds", C.c_void_p),
     ]
+
+
+class AnchorTargetsProblem(C.Structure):
+    _fields_ = [
+        ("n", C.c_int), ("active", C.c_void_p), ("arc_ptr", C.c_void_p),
+        ("arc_idx", C.c_void_p), ("n_arcs", C.c_int), ("arc_start", C.c_void_p),
+        ("arc_end", C.c_void_p), ("arc_score", C.c_void_p), ("n_long", C.c_int),
+        ("long_start", C.c_void_p), ("long_end", C.c_void_p), ("long_score", C.c_void_p),
+        ("n_anchors", C.c_int), ("anchor_start", C.c_void_p), ("anchor_end", C.c_void_p),
+        ("first_cluster", C.c_int), ("freq_memo", C.c_void_p), ("count_a", C.c_float),
+        ("count_scale", C.c_float), ("count_shift", C.c_float), ("count_base", C.c_float),
+        ("anchor_heat", C.c_void_p), ("anchor_influence", C.c_float),
+    ]
+
+
+class AnchorTargetsStats(C.Structure):
+    _fields_ = [("applied", C.c_int64), ("out_of_range", C.c_int64), ("inactive", C.c_int64),
+                ("collision", C.c_int64), ("ms_map", C.c_float), ("ms_sort", C.c_float),
+                ("ms_resolve", C.c_float), ("ms_assemble", C.c_float)]
 
 
 class SmoothProblem(C.Structure):
@@ -502,6 +521,59 @@ def distance_heatmap(ctx: Context, contact, diag: int, scale: float, power: floa
                                           C.c_float(power), C.c_float(stretching), _p(out),
                                           C.byref(avg), C.byref(mx), C.byref(ms)))
     return out, avg.value, mx.value, ms.value
+
+
+def anchor_targets_arrays(t: dict) -> dict:
+    """The arrays of an anchor-target problem dict (keys: active, arc_ptr,
+    arc_idx, arc_start, arc_end, arc_score, long_start, long_end, long_score,
+    anc_start, anc_end, first_cluster, memo, count = (a, scale, shift, base),
+    heat or None, influence) as contiguous int32 / float32 arrays."""
+    out = {k: _i32(t[k]) for k in ("active", "arc_ptr", "arc_idx", "arc_start", "arc_end",
+                                   "arc_score", "long_start", "long_end", "long_score",
+                                   "anc_start", "anc_end")}
+    out["memo"] = _f32(t["memo"])
+    out["heat"] = None if t.get("heat") is None else _f32(t["heat"])
+    return out
+
+
+def anchor_targets(ctx: Context, t: dict):
+    """pmmc_anchor_targets: (row_ptr, col, target, stats dict, kernel ms).
+    The stats dict holds the long-arc counters; anchor_targets_phases()
+    gives the per-phase device times of the last call."""
+    a = anchor_targets_arrays(t)
+    n = len(a["active"])
+    ca, cs, csh, cb = (float(x) for x in t["count"])
+    pr = AnchorTargetsProblem(
+        n, _p(a["active"]), _p(a["arc_ptr"]), _p(a["arc_idx"]), len(a["arc_start"]),
+        _p(a["arc_start"]), _p(a["arc_end"]), _p(a["arc_score"]), len(a["long_start"]),
+        _p(a["long_start"]), _p(a["long_end"]), _p(a["long_score"]), len(a["anc_start"]),
+        _p(a["anc_start"]), _p(a["anc_end"]), int(t["first_cluster"]), _p(a["memo"]), ca, cs,
+        csh, cb, _p(a["heat"]), float(t.get("influence", 0.0)))
+    cap = 2 * (int(a["arc_ptr"][-1]) + len(a["long_start"]))
+    row_ptr = np.zeros(n + 1, np.int32)
+    col = np.zeros(max(cap, 1), np.int32)
+    tgt = np.zeros(max(cap, 1), np.float32)
+    nnz = C.c_int64()
+    st = AnchorTargetsStats()
+    ms = C.c_double()
+    ctx.check(lib().pmmc_anchor_targets(ctx.h, C.byref(pr), _p(row_ptr), _p(col), _p(tgt),
+                                        C.c_int64(cap), C.byref(nnz), C.byref(st),
+                                        C.byref(ms)))
+    k = nnz.value
+    stats = {"applied": st.applied, "out_of_range": st.out_of_range, "inactive": st.inactive,
+             "collision": st.collision}
+    global _last_target_phases
+    _last_target_phases = {"map": st.ms_map, "sort": st.ms_sort, "resolve": st.ms_resolve,
+                           "assemble": st.ms_assemble}
+    return row_ptr, col[:k].copy(), tgt[:k].copy(), stats, ms.value
+
+
+_last_target_phases: dict = {}
+
+
+def anchor_targets_phases() -> dict:
+    """Device milliseconds per phase of the last anchor_targets call."""
+    return dict(_last_target_phases)
 
 
 def equidistant_model(ctx: Context, gpos, pos, first_end: int, last_start: int,

@@ -16,6 +16,12 @@ every workload is generated here from a seed:
   chr1..22,X at 10 kb per bead, anchors every Poisson(10) beads fixed.
 * ``arcs_ensemble``    -- structures x blocks of arc regions with
   log-uniform block sizes.
+* ``anchor_targets_problem`` -- one chromosome's anchors (genomic intervals
+  of 2-6 kb every ~50 kb), its arcs (1.5 per anchor, spans log-uniform in
+  [1, 200] anchors, PET counts geometric with mean 12) and long arcs at
+  genomic positions (Hi-C style: spans log-uniform up to the chromosome,
+  counts geometric with mean 3), with an active region of consecutive
+  anchors: the inputs of calcAnchorExpectedDistancesHeatmap.
 """
 from __future__ import annotations
 
@@ -215,3 +221,101 @@ def arcs_ensemble(n_structures: int = 64, n_blocks: int = 24, min_size: int = 32
             blocks.append(arcs_region(size, seed=s * 1000 + b, arcs_per_bead=arcs_per_bead))
         out.append(blocks)
     return out
+
+
+def freq_memo(count_a: float, count_scale: float, count_shift: float,
+              count_base: float) -> np.ndarray:
+    """The reference's freq_to_distance table (LooperSolver.hpp:950-951 fills
+    2..100 with freqToDistance(i, false)); entry 1 is filled the same way
+    here, entry 0 is 0."""
+    m = np.zeros(101, np.float32)
+    for i in range(1, 101):
+        fs = np.float32(np.float32(i) + np.float32(count_shift))
+        if count_a < 0:
+            fi = max(int(fs), 1)
+            v = float(np.float32(count_base)) + float(np.float32(count_scale)) * \
+                float(fi) ** float(np.float32(count_a))
+        else:
+            v = float(np.float32(count_base)) + float(np.float32(count_scale)) / \
+                np.exp(float(np.float32(count_a)) * float(fs))
+        m[i] = np.float32(v)
+    return m
+
+
+def anchor_targets_problem(n_anchors: int = 4000, n_active: int | None = None,
+                           active_from: int = 0, arcs_per_anchor: float = 1.5,
+                           n_long: int = 100_000, seed: int = 21, first_cluster: int = 7,
+                           count=(0.5, 20.0, 1.0, 0.01), heat: bool = False,
+                           influence: float = 0.5, outside_arcs: int = 0,
+                           duplicate_arcs: int = 0) -> dict:
+    """Inputs of calcAnchorExpectedDistancesHeatmap for one chromosome as a
+    dict (the keys of capi.anchor_targets_arrays).  The active region is
+    anchors [active_from, active_from + n_active) as cluster indices
+    first_cluster + anchor; `outside_arcs` arcs reach from the region to
+    anchors outside it, `duplicate_arcs` repeat an existing pair with
+    another count."""
+    rng = np.random.default_rng(seed)
+    n_active = n_anchors if n_active is None else n_active
+    gap = rng.integers(40_000, 60_000, n_anchors).astype(np.int64)
+    start = np.cumsum(gap) + 10_000
+    length = rng.integers(2_000, 6_000, n_anchors)
+    anc_start = start.astype(np.int32)
+    anc_end = (start + length).astype(np.int32)
+    lo, hi = active_from, active_from + n_active
+    n_arcs = int(round(arcs_per_anchor * n_active))
+    a = rng.integers(lo, hi - 1, n_arcs)
+    span = np.exp(rng.uniform(0.0, np.log(200.0), n_arcs)).astype(np.int64)
+    b = np.minimum(a + np.maximum(span, 1), hi - 1)
+    keep = b > a
+    a, b = a[keep], b[keep]
+    score = rng.geometric(1.0 / 12.0, len(a)).astype(np.int64)
+    pairs = [(int(x), int(y), int(z)) for x, y, z in zip(a, b, score)]
+    for _ in range(outside_arcs):
+        x = int(rng.integers(lo, hi))
+        y = int(rng.integers(0, n_anchors))
+        if y < lo or y >= hi:
+            pairs.append((min(x, y), max(x, y), int(rng.geometric(1.0 / 12.0))))
+    for _ in range(duplicate_arcs):
+        if pairs:
+            x, y, _s = pairs[int(rng.integers(0, len(pairs)))]
+            pairs.append((x, y, int(rng.geometric(1.0 / 12.0))))
+    pairs.sort()
+    arc_start = np.array([first_cluster + x for x, _, _ in pairs], np.int32)
+    arc_end = np.array([first_cluster + y for _, y, _ in pairs], np.int32)
+    arc_score = np.array([z for _, _, z in pairs], np.int32)
+    active = np.arange(first_cluster + lo, first_cluster + hi, dtype=np.int32)
+    per = [[] for _ in range(n_active)]
+    for k, (x, y, _) in enumerate(pairs):
+        for c in (x, y):
+            if lo <= c < hi:
+                per[c - lo].append(k)
+    arc_ptr = np.zeros(n_active + 1, np.int32)
+    arc_ptr[1:] = np.cumsum([len(p) for p in per])
+    arc_idx = np.array([k for p in per for k in p], np.int32)
+    # long arcs: one end inside an anchor of the chromosome most of the time
+    chrom_end = int(anc_end[-1]) + 20_000
+    i0 = rng.integers(0, n_anchors, n_long)
+    p0 = anc_start[i0] + rng.integers(-500, 6_500, n_long)
+    sp = np.exp(rng.uniform(np.log(5e4), np.log(chrom_end), n_long)).astype(np.int64)
+    p1 = p0 + sp
+    miss = rng.random(n_long) < 0.3        # land between anchors
+    p1 = np.where(miss, p1, anc_start[np.clip(np.searchsorted(anc_start, p1), 0,
+                                               n_anchors - 1)] + 100)
+    long_start = np.minimum(p0, chrom_end).astype(np.int32)
+    long_end = np.minimum(p1, chrom_end).astype(np.int32)
+    long_score = rng.geometric(1.0 / 3.0, n_long).astype(np.int32)
+    long_score[rng.random(n_long) < 0.01] += 100   # counts above the memo table
+    t = {"active": active, "arc_ptr": arc_ptr, "arc_idx": arc_idx, "arc_start": arc_start,
+         "arc_end": arc_end, "arc_score": arc_score, "long_start": long_start,
+         "long_end": long_end, "long_score": long_score, "anc_start": anc_start,
+         "anc_end": anc_end, "first_cluster": first_cluster,
+         "memo": freq_memo(*count), "count": tuple(count), "heat": None,
+         "influence": influence}
+    if heat:
+        n = n_active
+        i = np.arange(n)
+        sep = np.abs(i[:, None] - i[None, :]).astype(np.float32)
+        h = np.where(sep >= 2, 1.0 / np.maximum(sep, 1.0), 0.0).astype(np.float32)
+        h *= rng.lognormal(0.0, 0.5, (n, n)).astype(np.float32)
+        t["heat"] = h
+    return t

@@ -23,6 +23,10 @@ distmap        expected-distance map of a 16384-bead contact map (1 GiB:
 equidistant    equidistant model of the largest chromosome of the genome
                workload (~24.8k clusters at 10 kb) resampled every 100 bp
                (~2.5M points); points/s.
+targets        anchor-level expected distances of one chromosome: 4000
+               anchors, 6000 arcs, 2M genomic-position long arcs (Hi-C style,
+               seed 21), built as the annealer's CSR
+               (calcAnchorExpectedDistancesHeatmap); arcs/s.
 serve          request loop: 5000 arc-level regions, sizes round(exp U[ln 64,
                ln 8192]), 1.5625 arcs per bead (400 per 256 beads), Poisson
                arrivals at 200 requests/s (seed 11), 20k moves each, device
@@ -403,6 +407,73 @@ def equidistant(args) -> dict:
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": None, "peak_source": kind,
                      "algorithmic_bytes_per_launch": alg},
+    }
+
+
+TARGETS_ANCHORS = 4000
+
+
+def targets_problem(n_long: int = 2_000_000):
+    return synth.anchor_targets_problem(n_anchors=TARGETS_ANCHORS, n_long=n_long, seed=21)
+
+
+def targets(args) -> dict:
+    """calcAnchorExpectedDistancesHeatmap on the device: device time per call
+    (L2 flushed between calls) and the host-buffer call end to end."""
+    import time as _t
+    import torch
+    n_long = args.n or 2_000_000
+    t = targets_problem(n_long)
+    ctx = capi.Context(0)
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device="cuda")
+    ms_k, e2e, ph = [], [], []
+    nnz = 0
+    for k in range(max(3, args.warmup) + args.steps):
+        flush.fill_(k & 0xff)
+        torch.cuda.synchronize()
+        t0 = _t.perf_counter()
+        rp, col, tgt, st, ms = capi.anchor_targets(ctx, t)
+        dt = _t.perf_counter() - t0
+        nnz = len(col)
+        if k >= max(3, args.warmup):
+            ms_k.append(ms)
+            e2e.append(dt)
+            ph.append(capi.anchor_targets_phases())
+    ms = float(np.median(ms_k))
+    units = len(t["arc_start"]) + n_long
+    phases = {key: float(np.median([p[key] for p in ph])) for key in ph[0]}
+    # the larger of the two own kernels of the long-arc pass:
+    #   long_map      8 bytes of positions read, 8 + 4 of key and index written
+    #                 per long arc;
+    #   long_resolve  8 + 4 bytes of sorted key and index read per entry, the
+    #                 count of every written long arc (4), 8 + 4 per emitted pair
+    n_items = n_long + len(t["arc_start"])
+    n_emit = nnz // 2
+    algs = {"map": ("long_map", 20.0 * n_long),
+            "resolve": ("long_resolve", 12.0 * n_items + 4.0 * st["applied"] + 12.0 * n_emit)}
+    dom = max(algs, key=lambda key: phases[key])
+    kernel, alg = algs[dom]
+    peak, kind = _peak()
+    achieved = alg / (phases[dom] * 1e-3) / 1e9
+    h2d = sum(int(np.asarray(t[key]).nbytes) for key in
+              ("active", "arc_ptr", "arc_idx", "arc_start", "arc_end", "arc_score",
+               "long_start", "long_end", "long_score", "anc_start", "anc_end", "memo"))
+    return {
+        "metric": "arcs/s", "value": units / (ms * 1e-3), "unit": "arcs/s", "n_gpus": 1,
+        "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "int32",
+        "data": "synthetic",
+        "config": {"workload": f"anchor_targets_{TARGETS_ANCHORS}anchors_"
+                               f"{len(t['arc_start'])}arcs_{n_long}long_arcs",
+                   "l2": "256 MB buffer written between calls", "nnz": nnz,
+                   "stats": st},
+        "phases_ms": phases,
+        "e2e": {"value": units / float(np.median(e2e)), "unit": "arcs/s",
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": int(4 * (len(rp) + 2 * nnz))},
+        "roofline": {"bound": "hbm", "kernel": kernel, "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": achieved / peak,
+                     "traffic": _traffic(kernel, f"targets_{n_long}"),
+                     "peak_source": kind, "algorithmic_bytes_per_launch": alg},
     }
 
 

@@ -201,6 +201,59 @@ def hcm_cases():
     return {"hcm": dict(lines=np.array(lines))}
 
 
+TARGET_KEYS = ("active", "arc_ptr", "arc_idx", "arc_start", "arc_end", "arc_score",
+               "long_start", "long_end", "long_score", "anc_start", "anc_end", "memo")
+
+
+def target_specs():
+    """The anchor-target cases: problem dicts for synth.anchor_targets_problem
+    plus edits that reach the reference's corner cases."""
+    out = []
+    # arcs leaving the active region (slot 0 through std::map insertion),
+    # repeated pairs (the last write wins), collisions with long arcs
+    out.append(synth.anchor_targets_problem(n_anchors=300, n_active=200, active_from=50,
+                                            n_long=3000, seed=31, outside_arcs=12,
+                                            duplicate_arcs=12))
+    # power-law counts (countToDistA < 0) and the anchor heatmap's influence
+    out.append(synth.anchor_targets_problem(n_anchors=300, n_active=200, active_from=50,
+                                            n_long=3000, seed=32, heat=True,
+                                            count=(-0.5, 2.0, 0.0, 0.1), influence=3.0))
+    # overlapping, unsorted anchors: the first anchor holding a position wins
+    t = synth.anchor_targets_problem(n_anchors=120, n_active=120, n_long=2000, seed=33)
+    t["anc_end"] = t["anc_end"].copy()
+    t["anc_end"][10] = t["anc_start"][12] + 100
+    t["anc_start"] = t["anc_start"].copy()
+    t["anc_start"][40], t["anc_start"][41] = t["anc_start"][41], t["anc_start"][40]
+    t["anc_end"][40], t["anc_end"][41] = t["anc_end"][41], t["anc_end"][40]
+    out.append(t)
+    # negative distances (countToDistBaseLevel < 0): long arcs overwrite them
+    out.append(synth.anchor_targets_problem(n_anchors=200, n_active=150, active_from=20,
+                                            n_long=3000, seed=34,
+                                            count=(0.5, 20.0, 1.0, -0.005)))
+    # no anchor list: long arcs unused; a tiny region
+    t = synth.anchor_targets_problem(n_anchors=12, n_active=12, n_long=50, seed=35)
+    t["anc_start"] = t["anc_start"][:0]
+    t["anc_end"] = t["anc_end"][:0]
+    out.append(t)
+    return out
+
+
+def target_cases():
+    out = {}
+    for k, t in enumerate(target_specs()):
+        dense, st = O.ref_anchor_targets(t)
+        d = {key: np.asarray(t[key]) for key in TARGET_KEYS}
+        d["first_cluster"] = np.array([t["first_cluster"]], np.int32)
+        d["count"] = np.array(t["count"], np.float32)
+        d["heat"] = np.zeros((0, 0), np.float32) if t["heat"] is None else t["heat"]
+        d["influence"] = np.array([t["influence"]], np.float32)
+        d["dense"] = dense
+        d["stats"] = np.array([st["applied"], st["out_of_range"], st["inactive"],
+                               st["collision"]], np.int64)
+        out[f"targets{k}"] = d
+    return out
+
+
 def main():
     if not O.ref_available():
         O.build()
@@ -210,7 +263,8 @@ def main():
     groups = {"arcs": arcs_cases, "ext": ext_cases, "distmap": distmap_cases,
               "equi": equi_cases,
               "heatmap": heatmap_cases,
-              "smooth": smooth_cases, "mark": mark_cases, "hcm": hcm_cases}
+              "smooth": smooth_cases, "mark": mark_cases, "hcm": hcm_cases,
+              "targets": target_cases}
     want = sys.argv[1:] or list(groups) + ["rng"]
     fixtures = {}
     for g in want:

@@ -145,3 +145,44 @@ def test_equidistant_model(case):
     pts = O.equidistant(g["gpos"], g["pos"], int(g["end"][0]), int(g["start"][-1]),
                         int(g["gpos"][0]), int(g["gpos"][-1]), int(g["res"][0]))
     np.testing.assert_array_equal(pts, g["points"])
+
+
+def _target_case(g):
+    t = {k: g[k] for k in ("active", "arc_ptr", "arc_idx", "arc_start", "arc_end", "arc_score",
+                           "long_start", "long_end", "long_score", "anc_start", "anc_end",
+                           "memo")}
+    t["first_cluster"] = int(g["first_cluster"][0])
+    t["count"] = tuple(float(x) for x in g["count"])
+    t["heat"] = None if g["heat"].size == 0 else g["heat"]
+    t["influence"] = float(g["influence"][0])
+    return t
+
+
+@pytest.mark.parametrize("case", [f"targets{k}" for k in range(5)])
+def test_anchor_targets(case):
+    """calcAnchorExpectedDistancesHeatmap: the oracle's dense matrix and
+    long-arc counters equal the reference's bit for bit."""
+    g = load(case)
+    dense, st = O.anchor_targets(_target_case(g))
+    np.testing.assert_array_equal(dense.view(np.uint32), g["dense"].view(np.uint32))
+    assert [st["applied"], st["out_of_range"], st["inactive"], st["collision"]] == \
+        list(g["stats"])
+
+
+def test_anchor_targets_fixtures_reach_the_corner_cases():
+    """The fixtures exercise what they are meant to: collisions, slot 0 by
+    map insertion, negative distances overwritten, the heatmap's influence."""
+    g0, g1, g3 = load("targets0"), load("targets1"), load("targets3")
+    assert g0["stats"][3] > 0 and g0["stats"][2] > 0 and g0["stats"][1] > 0
+    # an arc whose other end is outside the active region lands in row 0
+    t = _target_case(g0)
+    fc = t["first_cluster"]
+    act = set(int(x) for x in t["active"])
+    assert any(int(e) not in act and int(e) > int(s)
+               for s, e in zip(t["arc_start"], t["arc_end"]) if int(s) in act)
+    assert fc >= 0
+    # negative distances written by arcs stay; long arcs still apply
+    assert ((g3["dense"] < 0) & (g3["dense"] != -1.0)).any()
+    assert g3["stats"][0] > 0
+    # the influence case carries a heatmap
+    assert g1["heat"].size > 0
