@@ -278,6 +278,42 @@ def targets_main(args):
     print(json.dumps(line))
 
 
+def stress_main(args):
+    """Stress-refinement line beside the reference's host descent (the oracle
+    port, bit-identical to it) on one core, timed over the first 100
+    iterations of the same chromosome (pair building included, as in the
+    reference) and scaled per iteration."""
+    from oracle import oracle as O
+    from pmmc_gb300 import workloads as W
+    O.build()
+    t = W.stress_problem()
+    t0 = time.perf_counter()
+    _, _, out = O.stress_refine(t, 100, W.STRESS_LR)
+    dt = time.perf_counter() - t0
+    cpu = {"value": out["iterations"] / dt, "unit": "iterations/s", "cores": 1, "kind": "port",
+           "sample": f"{out['iterations']} iterations of {W.STRESS_ANCHORS} anchors, "
+                     f"{out['n_pairs']} pairs ({dt:.2f} s)"}
+    if args.impl == "reference":
+        if int(os.environ.get("RANK", "0")) != 0:
+            return
+        print(json.dumps({"metric": "iterations/s", "value": cpu["value"],
+                          "unit": "iterations/s", "n_gpus": 0, "steps": 1, "warmup": 0,
+                          "ms_per_step": dt * 1e3, "higher_is_better": True,
+                          "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+                          "data": "synthetic", "impl": "reference",
+                          "config": {"workload": "stress_refine"}, "cpu_baseline": cpu,
+                          "e2e": {"value": cpu["value"], "unit": "iterations/s",
+                                  "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+        return
+    sampler = ClockSampler(0)
+    sampler.start()
+    line = W.stress(args)
+    line["clocks"] = sampler.stop()
+    line["gpu_launches"] = args.steps
+    line["cpu_baseline"] = cpu
+    print(json.dumps(line))
+
+
 def plain_main(args):
     """Config-0 line: the plain drop-in call beside the reference CPU
     annealer (the oracle port, bit-identical to it) on one core."""
@@ -554,13 +590,14 @@ def main():
                     help="milestone interval (smaller for profiling runs)")
     ap.add_argument("--workload", default="ensemble",
                     choices=["ensemble", "plain", "heatmap", "heatmap-batch", "smooth",
-                             "serve", "distmap", "equidistant", "targets"],
+                             "serve", "distmap", "equidistant", "targets", "stress"],
                     help="ensemble: the batched arc-level ensemble (default line); "
                          "heatmap: one 2048-bead heatmap chain; heatmap-batch: one chain "
                          "per distinct 2048-bead map, one per SM; smooth: genome-scale "
                          "subanchor smoothing; serve: the request loop on a Poisson trace")
     ap.add_argument("--maps", type=int, default=0, help="heatmap-batch: number of maps")
-    ap.add_argument("--moves", type=int, default=0, help="moves per chain (heatmap/smooth)")
+    ap.add_argument("--moves", type=int, default=0,
+                    help="moves per chain (heatmap/smooth); stress: maximum iterations")
     ap.add_argument("--requests", type=int, default=0, help="serve: requests in the trace")
     ap.add_argument("--n", type=int, default=0,
                     help="distmap: matrix size; equidistant: resolution; targets: long arcs")
@@ -582,6 +619,9 @@ def main():
         return
     if args.workload == "targets":
         targets_main(args)
+        return
+    if args.workload == "stress":
+        stress_main(args)
         return
     if args.workload != "ensemble":
         from pmmc_gb300 import workloads

@@ -399,6 +399,57 @@ pmmc_status pmmc_anchor_targets(pmmc_ctx *ctx, const pmmc_anchor_targets_problem
                                 int64_t *nnz, pmmc_anchor_targets_stats *stats,
                                 double *kernel_ms);
 
+/* ---------------- stress refinement ---------------- */
+/* Replaces LooperSolver::stressRefineAnchors(chr, max_iter, lr)
+ * (LooperSolver.hpp:5638-5913): gradient descent on the anchors of one
+ * chromosome after the anchor-level annealing.  The active region is sorted
+ * by genomic position (ties: stable here, unspecified in the reference's
+ * std::sort); pair targets are freqToDistance(score, memo = false) of the
+ * chromosome's arcs (cluster-index ends) and long arcs (genomic positions
+ * through Anchor::contains), the first of a pair wins, targets <= 1e-6 are
+ * dropped, and consecutive anchors are left to the backbone when a backbone
+ * constant exceeds 1e-6.  Energy: backbone k_{stretch|squeeze} ((d - t)/t)^2
+ * with t = genomicLengthToDistance(gap); pairs ((d - t)/t)^2; angles
+ * k_angular acos(c)^3 with its finite-difference gradient (h = 1e-3).  The
+ * step halves when the energy rises (the run stops below 1e-6) and the run
+ * stops when it improves by less than 1e-7 max(1, E) after 20 iterations.
+ * order_out (n) receives the sorted active region, pos_out (n*3) the
+ * refined positions in that order.  One cooperative launch runs every
+ * iteration; each anchor's gradient is summed in the reference's order
+ * (backbone, pairs in pair order, angles), so without the angle term the
+ * positions equal the reference's bit for bit. */
+typedef struct pmmc_stress_problem {
+  int n;                       /* active-region size                       */
+  const int *active;           /* n cluster indices, any order             */
+  const int *genomic_pos;      /* n: Cluster::genomic_pos of each          */
+  const float *pos;            /* n*3                                      */
+  int n_arcs;                  /* arcs.arcs[chr]: cluster-index ends       */
+  const int *arc_start, *arc_end, *arc_score;
+  int n_long;                  /* arcs.long_arcs[chr]: genomic positions   */
+  const int *long_start, *long_end, *long_score;
+  int n_anchors;               /* arcs.anchors[chr]                        */
+  const int *anchor_start, *anchor_end;
+  int first_cluster;           /* chr_first_cluster[chr]                   */
+  float count_a, count_scale, count_shift, count_base;  /* countToDist*    */
+  float glen_base, glen_scale, glen_power;  /* genomicLengthToDist*       */
+  float k_stretch, k_squeeze, k_angular;    /* springConstantStretch,
+                                               springConstantSqueeze,
+                                               springAngularConstant      */
+} pmmc_stress_problem;
+
+typedef struct pmmc_stress_result {
+  int iterations;              /* iterations whose energy was evaluated    */
+  int stop;                    /* 0 max_iter, 1 converged, 2 step < 1e-6  */
+  float lr;                    /* step at exit                             */
+  double total, backbone, hic, angular;  /* terms of the last evaluation   */
+  int64_t n_pairs;             /* pair targets                             */
+  double kernel_ms;            /* device time of the descent               */
+} pmmc_stress_result;
+
+pmmc_status pmmc_stress_refine(pmmc_ctx *ctx, const pmmc_stress_problem *pr, int max_iter,
+                               float lr, int *order_out, float *pos_out,
+                               pmmc_stress_result *res);
+
 /* ---------------- equidistant model ---------------- */
 /* Replaces the interpolation of HierarchicalChromosome::createEqidistantModel
  * (src/HierarchicalChromosome.cu:466-519; gpuHelper :1253-1447 and its

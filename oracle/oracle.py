@@ -578,3 +578,57 @@ def ref_anchor_targets(t):
         raise RuntimeError("reference harness failed")
     return dense, dict(zip(("applied", "out_of_range", "inactive", "collision"),
                            (int(x) for x in st)))
+
+
+class StressParams(C.Structure):
+    _fields_ = [(k, C.c_float) for k in ("count_a", "count_scale", "count_shift", "count_base",
+                                          "glen_base", "glen_scale", "glen_power", "k_stretch",
+                                          "k_squeeze", "k_angular")]
+
+
+class StressOut(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("stop", C.c_int), ("lr", C.c_float),
+                ("total", C.c_double), ("backbone", C.c_double), ("hic", C.c_double),
+                ("angular", C.c_double), ("n_pairs", C.c_longlong)]
+
+
+def _stress_args(t):
+    a = {k: _i32(t[k]) for k in ("active", "genomic_pos", "arc_start", "arc_end", "arc_score",
+                                 "long_start", "long_end", "long_score", "anc_start",
+                                 "anc_end")}
+    prm = StressParams(*(float(x) for x in t["count"]), *(float(x) for x in t["glen"]),
+                       *(float(x) for x in t["springs"]))
+    return a, _f32(t["pos"]).reshape(-1, 3), prm
+
+
+def stress_refine(t, max_iter: int, lr: float):
+    """orc_stress_refine on a problem dict (keys of
+    pmmc_gb300.capi.stress_arrays): (order, positions n x 3, out dict)."""
+    a, pos, prm = _stress_args(t)
+    n = len(a["active"])
+    order = np.zeros(n, np.int32)
+    out_pos = np.zeros((n, 3), np.float32)
+    o = StressOut()
+    lib().orc_stress_refine(n, _p(a["active"]), _p(a["genomic_pos"]), _p(pos),
+                            len(a["arc_start"]), _p(a["arc_start"]), _p(a["arc_end"]),
+                            _p(a["arc_score"]), len(a["long_start"]), _p(a["long_start"]),
+                            _p(a["long_end"]), _p(a["long_score"]), len(a["anc_start"]),
+                            _p(a["anc_start"]), _p(a["anc_end"]), int(t["first_cluster"]),
+                            C.byref(prm), int(max_iter), C.c_float(lr), _p(order), _p(out_pos),
+                            C.byref(o))
+    return order, out_pos, {k: getattr(o, k) for k, _ in StressOut._fields_}
+
+
+def ref_stress_refine(t, max_iter: int, lr: float):
+    """The reference's stressRefineAnchors on the same dict: (order, positions)."""
+    a, pos, prm = _stress_args(t)
+    n = len(a["active"])
+    order = np.zeros(n, np.int32)
+    out_pos = np.zeros((n, 3), np.float32)
+    ref().ref_stress_refine(n, _p(a["active"]), _p(a["genomic_pos"]), _p(pos),
+                            len(a["arc_start"]), _p(a["arc_start"]), _p(a["arc_end"]),
+                            _p(a["arc_score"]), len(a["long_start"]), _p(a["long_start"]),
+                            _p(a["long_end"]), _p(a["long_score"]), len(a["anc_start"]),
+                            _p(a["anc_start"]), _p(a["anc_end"]), int(t["first_cluster"]),
+                            C.byref(prm), int(max_iter), C.c_float(lr), _p(order), _p(out_pos))
+    return order, out_pos

@@ -1422,3 +1422,301 @@ int orc_anchor_targets(int n, const int *active, const int *arc_ptr,
   free(m.val);
   return rc;
 }
+
+/* ------------------------------------------------------------------ */
+/* stress refinement (LooperSolver.hpp:5638-5913)                     */
+/* ------------------------------------------------------------------ */
+
+/* freqToDistance(freq, memo = false) (LooperSolver.hpp:3949-3967). */
+static float orc_freq_to_distance_formula(int freq, const orc_stress_params *p) {
+  if (p->count_a < 0.0f) {
+    int fi = (int)((float)freq + p->count_shift);
+    if (fi < 1)
+      fi = 1;
+    return (float)((double)p->count_base +
+                   (double)p->count_scale * pow((double)fi, (double)p->count_a));
+  }
+  return (float)((double)p->count_base +
+                 (double)p->count_scale /
+                     exp((double)p->count_a * (double)((float)freq + p->count_shift)));
+}
+
+/* genomicLengthToDistance (LooperSolver.hpp:3900-3904). */
+static double orc_genomic_length_to_distance(int length, const orc_stress_params *p) {
+  return (double)p->glen_base +
+         (double)p->glen_scale * pow(length / 1000.0, (double)p->glen_power);
+}
+
+static void orc_merge_sort_idx(int *a, int *tmp, int n, const int *key) {
+  int w, i;
+  for (w = 1; w < n; w *= 2) {
+    for (i = 0; i < n; i += 2 * w) {
+      int lo = i, mid = i + w < n ? i + w : n, hi = i + 2 * w < n ? i + 2 * w : n;
+      int x = lo, y = mid, k = lo;
+      while (x < mid && y < hi)
+        tmp[k++] = key[a[y]] < key[a[x]] ? a[y++] : a[x++];
+      while (x < mid)
+        tmp[k++] = a[x++];
+      while (y < hi)
+        tmp[k++] = a[y++];
+    }
+    memcpy(a, tmp, sizeof(int) * n);
+  }
+}
+
+typedef struct {
+  int i, j;
+  float t, w;
+} orc_pair;
+
+/* The angle energy k * acos(c)^3 of the three beads around i (:5836-5845);
+ * returns 0 with *ok = 0 when a bond is shorter than 1e-9. */
+static float orc_stress_angle(const float *X, int i, float k, int *ok) {
+  float v1[3], v2[3], n1, n2, c, th;
+  int a;
+  for (a = 0; a < 3; ++a) {
+    v1[a] = X[3 * i + a] - X[3 * (i - 1) + a];
+    v2[a] = X[3 * (i + 1) + a] - X[3 * i + a];
+  }
+  n1 = v_len(v1[0], v1[1], v1[2]);
+  n2 = v_len(v2[0], v2[1], v2[2]);
+  if (n1 < 1e-9f || n2 < 1e-9f) {
+    *ok = 0;
+    return 0.0f;
+  }
+  *ok = 1;
+  c = (v1[0] * v2[0] + v1[1] * v2[1] + v1[2] * v2[2]) / (n1 * n2);
+  if (c > 1.0f)
+    c = 1.0f;
+  if (c < -1.0f)
+    c = -1.0f;
+  th = acosf(c);
+  return k * th * th * th;
+}
+
+int orc_stress_refine(int n, const int *active, const int *genomic_pos,
+                      const float *pos, int n_arcs, const int *arc_start,
+                      const int *arc_end, const int *arc_score, int n_long,
+                      const int *long_start, const int *long_end,
+                      const int *long_score, int n_anc, const int *anc_start,
+                      const int *anc_end, int first_cluster,
+                      const orc_stress_params *p, int max_iter, float lr,
+                      int *order_out, float *pos_out, orc_stress_out *out) {
+  int i, k, it, N = n;
+  int *ord, *tmp, *gp, *anc_to_active, *seen;
+  float *X, *G, *bb;
+  orc_pair *pairs;
+  long long np = 0, cap_pairs;
+  int backbone_active;
+  double prev_total = 1e300;
+  float cur_lr = lr;
+  memset(out, 0, sizeof(*out));
+  out->lr = lr;
+  for (i = 0; i < n; ++i)
+    order_out[i] = active[i];
+  memcpy(pos_out, pos, sizeof(float) * 3 * (size_t)n);
+  if (max_iter <= 0 || n < 2)
+    return 0;
+  /* sort active_region by genomic position (:5647-5650) */
+  ord = (int *)malloc(sizeof(int) * n);
+  tmp = (int *)malloc(sizeof(int) * n);
+  for (i = 0; i < n; ++i)
+    ord[i] = i;
+  orc_merge_sort_idx(ord, tmp, n, genomic_pos);
+  gp = (int *)malloc(sizeof(int) * n);
+  X = (float *)malloc(sizeof(float) * 3 * n);
+  G = (float *)malloc(sizeof(float) * 3 * n);
+  for (i = 0; i < n; ++i) {
+    order_out[i] = active[ord[i]];
+    gp[i] = genomic_pos[ord[i]];
+    X[3 * i] = pos[3 * ord[i]];
+    X[3 * i + 1] = pos[3 * ord[i] + 1];
+    X[3 * i + 2] = pos[3 * ord[i] + 2];
+  }
+  anc_to_active = (int *)malloc(sizeof(int) * (n_anc > 0 ? n_anc : 1));
+  for (i = 0; i < n_anc; ++i)
+    anc_to_active[i] = -1;
+  for (i = 0; i < N; ++i) {
+    int ci = order_out[i];
+    if (ci >= first_cluster && ci < first_cluster + n_anc)
+      anc_to_active[ci - first_cluster] = i;
+  }
+  /* unique pair targets, first one wins (:5670-5729) */
+  backbone_active = p->k_stretch > 1e-6f || p->k_squeeze > 1e-6f;
+  seen = (int *)malloc(sizeof(int) * (size_t)N * N);
+  for (k = 0; k < N * N; ++k)
+    seen[k] = -1;
+  cap_pairs = 1024;
+  pairs = (orc_pair *)malloc(sizeof(orc_pair) * cap_pairs);
+#define ORC_ADD_PAIR(AI, AJ, T)                                                \
+  do {                                                                         \
+    int ai_ = (AI), aj_ = (AJ);                                                \
+    if (ai_ != aj_) {                                                          \
+      if (ai_ > aj_) {                                                         \
+        int s_ = ai_;                                                          \
+        ai_ = aj_;                                                             \
+        aj_ = s_;                                                              \
+      }                                                                        \
+      if (!(backbone_active && aj_ - ai_ <= 1) && seen[ai_ * N + aj_] < 0) {   \
+        seen[ai_ * N + aj_] = (int)np;                                         \
+        if (np == cap_pairs) {                                                 \
+          cap_pairs *= 2;                                                      \
+          pairs = (orc_pair *)realloc(pairs, sizeof(orc_pair) * cap_pairs);    \
+        }                                                                      \
+        pairs[np].i = ai_;                                                     \
+        pairs[np].j = aj_;                                                     \
+        pairs[np].t = (T);                                                     \
+        pairs[np].w = 1.0f;                                                    \
+        np++;                                                                  \
+      }                                                                        \
+    }                                                                          \
+  } while (0)
+  for (k = 0; k < n_arcs; ++k) {
+    int a = arc_start[k], b = arc_end[k], ai, aj;
+    float t;
+    if (a < first_cluster || a >= first_cluster + n_anc)
+      continue;
+    if (b < first_cluster || b >= first_cluster + n_anc)
+      continue;
+    ai = anc_to_active[a - first_cluster];
+    aj = anc_to_active[b - first_cluster];
+    if (ai < 0 || aj < 0)
+      continue;
+    t = orc_freq_to_distance_formula(arc_score[k], p);
+    if (t > 1e-6f)
+      ORC_ADD_PAIR(ai, aj, t);
+  }
+  for (k = 0; k < n_long; ++k) {
+    int ia = -1, ib = -1, as, bs;
+    float t;
+    for (i = 0; i < n_anc; ++i)
+      if (long_start[k] >= anc_start[i] && long_start[k] <= anc_end[i]) {
+        ia = i;
+        break;
+      }
+    for (i = 0; i < n_anc; ++i)
+      if (long_end[k] >= anc_start[i] && long_end[k] <= anc_end[i]) {
+        ib = i;
+        break;
+      }
+    if (ia < 0 || ib < 0)
+      continue;
+    as = anc_to_active[ia];
+    bs = anc_to_active[ib];
+    if (as < 0 || bs < 0)
+      continue;
+    t = orc_freq_to_distance_formula(long_score[k], p);
+    if (t > 1e-6f)
+      ORC_ADD_PAIR(as, bs, t);
+  }
+#undef ORC_ADD_PAIR
+  free(seen);
+  out->n_pairs = np;
+  /* backbone targets from the genomic gaps (:5754-5762) */
+  bb = (float *)malloc(sizeof(float) * N);
+  for (i = 0; i < N; ++i)
+    bb[i] = -1.0f;
+  for (i = 0; i + 1 < N; ++i) {
+    int gap = abs(gp[i + 1] - gp[i]);
+    if (gap > 0)
+      bb[i] = (float)orc_genomic_length_to_distance(gap, p);
+  }
+  /* gradient descent (:5786-5906) */
+  for (it = 0; it < max_iter; ++it) {
+    double e_back = 0.0, e_hic = 0.0, e_ang = 0.0, total;
+    long long q;
+    for (k = 0; k < 3 * N; ++k)
+      G[k] = 0.0f;
+    for (i = 0; i + 1 < N; ++i) {
+      float t = bb[i], d[3], dlen, e, kk, g;
+      if (t <= 1e-6f)
+        continue;
+      d[0] = X[3 * i] - X[3 * (i + 1)];
+      d[1] = X[3 * i + 1] - X[3 * (i + 1) + 1];
+      d[2] = X[3 * i + 2] - X[3 * (i + 1) + 2];
+      dlen = v_len(d[0], d[1], d[2]);
+      if (dlen < 1e-9f)
+        dlen = 1e-9f;
+      e = (dlen - t) / t;
+      kk = e >= 0.0f ? p->k_stretch : p->k_squeeze;
+      e_back += (double)kk * e * e;
+      g = 2.0f * kk * (dlen - t) / (t * t * dlen);
+      for (k = 0; k < 3; ++k) {
+        float gv = d[k] * g;
+        G[3 * i + k] += gv;
+        G[3 * (i + 1) + k] -= gv;
+      }
+    }
+    for (q = 0; q < np; ++q) {
+      const orc_pair *pr = &pairs[q];
+      float d[3], dlen, e, g;
+      d[0] = X[3 * pr->i] - X[3 * pr->j];
+      d[1] = X[3 * pr->i + 1] - X[3 * pr->j + 1];
+      d[2] = X[3 * pr->i + 2] - X[3 * pr->j + 2];
+      dlen = v_len(d[0], d[1], d[2]);
+      if (dlen < 1e-9f)
+        dlen = 1e-9f;
+      e = (dlen - pr->t) / pr->t;
+      e_hic += (double)pr->w * e * e;
+      g = 2.0f * pr->w * (dlen - pr->t) / (pr->t * pr->t * dlen);
+      for (k = 0; k < 3; ++k) {
+        float gv = d[k] * g;
+        G[3 * pr->i + k] += gv;
+        G[3 * pr->j + k] -= gv;
+      }
+    }
+    if (p->k_angular > 0.0f) {
+      const float h = 1e-3f;
+      for (i = 1; i + 1 < N; ++i) {
+        int ok, bi, axis;
+        float E0 = orc_stress_angle(X, i, p->k_angular, &ok);
+        if (!ok)
+          continue;
+        e_ang += (double)E0;
+        for (bi = 0; bi < 3; ++bi) {
+          int b = i - 1 + bi;
+          for (axis = 0; axis < 3; ++axis) {
+            float saved = X[3 * b + axis], Ep;
+            X[3 * b + axis] = saved + h;
+            Ep = orc_stress_angle(X, i, p->k_angular, &ok);
+            X[3 * b + axis] = saved;
+            if (!ok)
+              continue;
+            G[3 * b + axis] += (Ep - E0) / h;
+          }
+        }
+      }
+    }
+    total = e_back + e_hic + e_ang;
+    out->iterations = it + 1;
+    out->total = total;
+    out->backbone = e_back;
+    out->hic = e_hic;
+    out->angular = e_ang;
+    if (total > prev_total && it > 0) {
+      cur_lr *= 0.5f;
+      if (cur_lr < 1e-6f) {
+        out->stop = 2;
+        break;
+      }
+    }
+    for (k = 0; k < 3 * N; ++k)
+      X[k] -= cur_lr * G[k];
+    if (prev_total - total < 1e-7 * (total > 1.0 ? total : 1.0) && it > 20) {
+      out->stop = 1;
+      break;
+    }
+    prev_total = total;
+  }
+  out->lr = cur_lr;
+  memcpy(pos_out, X, sizeof(float) * 3 * (size_t)N);
+  free(ord);
+  free(tmp);
+  free(gp);
+  free(X);
+  free(G);
+  free(bb);
+  free(anc_to_active);
+  free(pairs);
+  return 0;
+}

@@ -263,6 +263,35 @@ int orc_anchor_targets(int n, const int *active, const int *arc_ptr,
                        float count_shift, float count_base, const float *heat,
                        float influence, float *dense, long long *stats4);
 
+/* ---------------- stress refinement ---------------- */
+/* LooperSolver::stressRefineAnchors (src/include/LooperSolver.hpp:5638-5913)
+ * written out literally.  active (n cluster indices) with genomic_pos and
+ * pos (n*3) per entry; on return order_out holds active sorted by genomic
+ * position (a stable sort: callers avoid ties, which std::sort orders
+ * arbitrarily) and pos_out the refined positions in that order. */
+typedef struct orc_stress_params {
+  float count_a, count_scale, count_shift, count_base; /* countToDist*        */
+  float glen_base, glen_scale, glen_power;             /* genomicLengthToDist* */
+  float k_stretch, k_squeeze, k_angular;               /* springConstant*      */
+} orc_stress_params;
+
+typedef struct orc_stress_out {
+  int iterations; /* iterations whose energy was evaluated            */
+  int stop;       /* 0 max_iter, 1 converged, 2 step below 1e-6       */
+  float lr;       /* step at exit                                     */
+  double total, backbone, hic, angular; /* terms of the last evaluation */
+  long long n_pairs;
+} orc_stress_out;
+
+int orc_stress_refine(int n, const int *active, const int *genomic_pos,
+                      const float *pos, int n_arcs, const int *arc_start,
+                      const int *arc_end, const int *arc_score, int n_long,
+                      const int *long_start, const int *long_end,
+                      const int *long_score, int n_anc, const int *anc_start,
+                      const int *anc_end, int first_cluster,
+                      const orc_stress_params *p, int max_iter, float lr,
+                      int *order_out, float *pos_out, orc_stress_out *out);
+
 /* ---------------- HCM text lines ---------------- */
 /* Cluster::toFile (src/include/Cluster.hpp:175-181). Returns bytes written. */
 int orc_hcm_cluster_line(char *buf, int cap, int start, int end, char orient,

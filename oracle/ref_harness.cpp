@@ -422,6 +422,60 @@ int ref_anchor_targets(int n, const int *active, const int *arc_ptr, const int *
   return 0;
 }
 
+/* LooperSolver::stressRefineAnchors("chr1", max_iter, lr)
+ * (src/include/LooperSolver.hpp:5638-5913): clusters[active[i]] at pos[i]
+ * with genomic_pos[i]; on return order_out = active_region (sorted by the
+ * reference) and pos_out the positions of those clusters. */
+void ref_stress_refine(int n, const int *active, const int *genomic_pos, const float *pos,
+                       int n_arcs, const int *arc_start, const int *arc_end,
+                       const int *arc_score, int n_long, const int *long_start,
+                       const int *long_end, const int *long_score, int n_anc,
+                       const int *anc_start, const int *anc_end, int first_cluster,
+                       const orc_stress_params *p, int max_iter, float lr, int *order_out,
+                       float *pos_out) {
+  Quiet q;
+  orc_params op;
+  memset(&op, 0, sizeof(op));
+  apply_settings(&op, 0);
+  Settings::countToDistA = p->count_a;
+  Settings::countToDistScale = p->count_scale;
+  Settings::countToDistShift = p->count_shift;
+  Settings::countToDistBaseLevel = p->count_base;
+  Settings::genomicLengthToDistBase = p->glen_base;
+  Settings::genomicLengthToDistScale = p->glen_scale;
+  Settings::genomicLengthToDistPower = p->glen_power;
+  Settings::springConstantStretch = p->k_stretch;
+  Settings::springConstantSqueeze = p->k_squeeze;
+  Settings::springAngularConstant = p->k_angular;
+  LooperSolver s("ref", "/tmp/");
+  int max_cluster = first_cluster + n_anc;
+  for (int i = 0; i < n; ++i) max_cluster = std::max(max_cluster, active[i] + 1);
+  s.clusters.assign(max_cluster, Cluster());
+  s.active_region.assign(active, active + n);
+  for (int i = 0; i < n; ++i) {
+    s.clusters[active[i]].genomic_pos = genomic_pos[i];
+    s.clusters[active[i]].pos.set(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
+  }
+  const std::string chr = "chr1";
+  s.current_chr = chr;
+  s.chr_first_cluster[chr] = first_cluster;
+  std::vector<InteractionArc> &av = s.arcs.arcs[chr];
+  for (int k = 0; k < n_arcs; ++k) av.push_back(InteractionArc(arc_start[k], arc_end[k], arc_score[k]));
+  std::vector<InteractionArc> &lv = s.arcs.long_arcs[chr];
+  for (int k = 0; k < n_long; ++k)
+    lv.push_back(InteractionArc(long_start[k], long_end[k], long_score[k]));
+  std::vector<Anchor> &anc = s.arcs.anchors[chr];
+  for (int i = 0; i < n_anc; ++i) anc.push_back(Anchor(chr, anc_start[i], anc_end[i], 'N'));
+  s.stressRefineAnchors(chr, max_iter, lr);
+  for (int i = 0; i < n; ++i) {
+    order_out[i] = s.active_region[i];
+    const vector3 &v = s.clusters[s.active_region[i]].pos;
+    pos_out[3 * i] = v.x;
+    pos_out[3 * i + 1] = v.y;
+    pos_out[3 * i + 2] = v.z;
+  }
+}
+
 /* InteractionArcs::markArcs (src/include/InteractionArcs.hpp:207-336) on a
  * single chromosome "chr1".  Output layout as orc_mark_arcs. */
 int ref_mark_arcs(int n_anchors, const int *a_start, const int *a_end,

@@ -42,7 +42,7 @@ HEADER_SYMBOLS = [
     "pmmc_server_create", "pmmc_server_submit", "pmmc_server_poll", "pmmc_server_wait",
     "pmmc_server_get_stats", "pmmc_server_destroy", "pmmc_arcs_batch_classes",
     "pmmc_selftest_sqrt", "pmmc_distance_heatmap", "pmmc_distance_heatmap_device",
-    "pmmc_equidistant_model", "pmmc_hcm_write", "pmmc_anchor_targets",
+    "pmmc_equidistant_model", "pmmc_hcm_write", "pmmc_anchor_targets", "pmmc_stress_refine",
 ]
 
 LANES_AUTO = -1  # PMMC_LANES_AUTO: the autotuner picks lanes and warps per class
@@ -112,6 +112,24 @@ class AnchorTargetsStats(C.Structure):
     _fields_ = [("applied", C.c_int64), ("out_of_range", C.c_int64), ("inactive", C.c_int64),
                 ("collision", C.c_int64), ("ms_map", C.c_float), ("ms_sort", C.c_float),
                 ("ms_resolve", C.c_float), ("ms_assemble", C.c_float)]
+
+
+class StressProblem(C.Structure):
+    _fields_ = [
+        ("n", C.c_int), ("active", C.c_void_p), ("genomic_pos", C.c_void_p), ("pos", C.c_void_p),
+        ("n_arcs", C.c_int), ("arc_start", C.c_void_p), ("arc_end", C.c_void_p),
+        ("arc_score", C.c_void_p), ("n_long", C.c_int), ("long_start", C.c_void_p),
+        ("long_end", C.c_void_p), ("long_score", C.c_void_p), ("n_anchors", C.c_int),
+        ("anchor_start", C.c_void_p), ("anchor_end", C.c_void_p), ("first_cluster", C.c_int),
+    ] + [(k, C.c_float) for k in ("count_a", "count_scale", "count_shift", "count_base",
+                                  "glen_base", "glen_scale", "glen_power", "k_stretch",
+                                  "k_squeeze", "k_angular")]
+
+
+class StressResult(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("stop", C.c_int), ("lr", C.c_float),
+                ("total", C.c_double), ("backbone", C.c_double), ("hic", C.c_double),
+                ("angular", C.c_double), ("n_pairs", C.c_int64), ("kernel_ms", C.c_double)]
 
 
 class SmoothProblem(C.Structure):
@@ -574,6 +592,37 @@ _last_target_phases: dict = {}
 def anchor_targets_phases() -> dict:
     """Device milliseconds per phase of the last anchor_targets call."""
     return dict(_last_target_phases)
+
+
+def stress_arrays(t: dict) -> dict:
+    """Arrays of a stress-refinement problem dict (keys: active, genomic_pos,
+    pos, arc_start, arc_end, arc_score, long_start, long_end, long_score,
+    anc_start, anc_end, first_cluster, count = (a, scale, shift, base),
+    glen = (base, scale, power), springs = (k_stretch, k_squeeze, k_angular))."""
+    out = {k: _i32(t[k]) for k in ("active", "genomic_pos", "arc_start", "arc_end",
+                                   "arc_score", "long_start", "long_end", "long_score",
+                                   "anc_start", "anc_end")}
+    out["pos"] = _f32(t["pos"]).reshape(-1, 3)
+    return out
+
+
+def stress_refine(ctx: Context, t: dict, max_iter: int, lr: float):
+    """pmmc_stress_refine: (order, positions n x 3 in that order, result dict)."""
+    a = stress_arrays(t)
+    n = len(a["active"])
+    pr = StressProblem(
+        n, _p(a["active"]), _p(a["genomic_pos"]), _p(a["pos"]), len(a["arc_start"]),
+        _p(a["arc_start"]), _p(a["arc_end"]), _p(a["arc_score"]), len(a["long_start"]),
+        _p(a["long_start"]), _p(a["long_end"]), _p(a["long_score"]), len(a["anc_start"]),
+        _p(a["anc_start"]), _p(a["anc_end"]), int(t["first_cluster"]),
+        *(float(x) for x in t["count"]), *(float(x) for x in t["glen"]),
+        *(float(x) for x in t["springs"]))
+    order = np.zeros(max(n, 1), np.int32)
+    pos = np.zeros((max(n, 1), 3), np.float32)
+    r = StressResult()
+    ctx.check(lib().pmmc_stress_refine(ctx.h, C.byref(pr), int(max_iter), C.c_float(lr),
+                                       _p(order), _p(pos), C.byref(r)))
+    return order[:n], pos[:n], {k: getattr(r, k) for k, _ in StressResult._fields_}
 
 
 def equidistant_model(ctx: Context, gpos, pos, first_end: int, last_start: int,

@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 
+#include <cmath>
 #include <cstdarg>
 #include <cstdint>
 #include <cstdio>
@@ -33,6 +34,19 @@ inline float __int_as_float_host(int i) {
   float f;
   memcpy(&f, &i, 4);
   return f;
+}
+
+// freqToDistance(freq, memo = false) (LooperSolver.hpp:3949-3967) on the
+// host: the int count plus the float shift is a float, the rest FP64 (this
+// code is built with -ffp-contract=off, so it rounds as the reference does).
+inline float count_to_distance(int freq, float a, float scale, float shift, float base) {
+  const float fs = (float)freq + shift;
+  if (a < 0.0f) {
+    int fi = (int)fs;
+    if (fi < 1) fi = 1;
+    return (float)((double)base + (double)scale * std::pow((double)fi, (double)a));
+  }
+  return (float)((double)base + (double)scale / std::exp((double)a * (double)fs));
 }
 
 // Records a message on the context and returns the status.

@@ -75,13 +75,7 @@ __device__ float freq_to_distance_dev(int freq, const float *__restrict__ memo,
 
 float freq_to_distance_host(int freq, const float *memo, const CountToDist c) {
   if (freq >= 1 && freq <= 100) return memo[freq];
-  const float fs = (float)freq + c.shift;
-  if (c.a < 0.0f) {
-    int fi = (int)fs;
-    if (fi < 1) fi = 1;
-    return (float)((double)c.base + (double)c.scale * std::pow((double)fi, (double)c.a));
-  }
-  return (float)((double)c.base + (double)c.scale / std::exp((double)c.a * (double)fs));
+  return count_to_distance(freq, c.a, c.scale, c.shift, c.base);
 }
 
 // Anchor::contains(pos) (Anchor.hpp:87): start <= pos <= end; the first

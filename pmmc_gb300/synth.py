@@ -22,6 +22,10 @@ every workload is generated here from a seed:
   genomic positions (Hi-C style: spans log-uniform up to the chromosome,
   counts geometric with mean 3), with an active region of consecutive
   anchors: the inputs of calcAnchorExpectedDistancesHeatmap.
+* ``stress_problem``   -- the same chromosome as the input of
+  stressRefineAnchors: every anchor active in registration order (shuffled
+  against the genomic order), positions a random walk with steps of the
+  backbone target, power-law count-to-distance constants.
 """
 from __future__ import annotations
 
@@ -299,8 +303,9 @@ def anchor_targets_problem(n_anchors: int = 4000, n_active: int | None = None,
     sp = np.exp(rng.uniform(np.log(5e4), np.log(chrom_end), n_long)).astype(np.int64)
     p1 = p0 + sp
     miss = rng.random(n_long) < 0.3        # land between anchors
-    p1 = np.where(miss, p1, anc_start[np.clip(np.searchsorted(anc_start, p1), 0,
-                                               n_anchors - 1)] + 100)
+    nxt = np.searchsorted(anc_start, p1)   # beyond the last anchor: stays outside
+    p1 = np.where(miss | (nxt >= n_anchors), p1,
+                  anc_start[np.minimum(nxt, n_anchors - 1)] + 100)
     long_start = np.minimum(p0, chrom_end).astype(np.int32)
     long_end = np.minimum(p1, chrom_end).astype(np.int32)
     long_score = rng.geometric(1.0 / 3.0, n_long).astype(np.int32)
@@ -319,3 +324,25 @@ def anchor_targets_problem(n_anchors: int = 4000, n_active: int | None = None,
         h *= rng.lognormal(0.0, 0.5, (n, n)).astype(np.float32)
         t["heat"] = h
     return t
+
+
+def stress_problem(n_anchors: int = 4000, n_long: int = 200_000, seed: int = 51,
+                   count=(-0.5, 10.0, 0.0, 0.5), glen=(0.0, 1.0, 0.5),
+                   springs=(0.1, 0.1, 0.1), shuffle: bool = True,
+                   arcs_per_anchor: float = 1.5, first_cluster: int = 7) -> dict:
+    """Inputs of stressRefineAnchors for one chromosome (the keys of
+    capi.stress_arrays)."""
+    t = anchor_targets_problem(n_anchors=n_anchors, n_long=n_long, seed=seed,
+                               arcs_per_anchor=arcs_per_anchor, first_cluster=first_cluster)
+    rng = np.random.default_rng(seed + 1)
+    center = ((t["anc_start"].astype(np.int64) + t["anc_end"]) // 2).astype(np.int32)
+    order = rng.permutation(n_anchors) if shuffle else np.arange(n_anchors)
+    step = float(np.sqrt(50.0)) * float(glen[1])
+    pos = random_walk(n_anchors, rng, step)
+    return {"active": (first_cluster + order).astype(np.int32),
+            "genomic_pos": center[order], "pos": pos[order],
+            "arc_start": t["arc_start"], "arc_end": t["arc_end"], "arc_score": t["arc_score"],
+            "long_start": t["long_start"], "long_end": t["long_end"],
+            "long_score": t["long_score"], "anc_start": t["anc_start"],
+            "anc_end": t["anc_end"], "first_cluster": first_cluster, "count": tuple(count),
+            "glen": tuple(glen), "springs": tuple(springs)}

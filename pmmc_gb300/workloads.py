@@ -27,6 +27,10 @@ targets        anchor-level expected distances of one chromosome: 4000
                anchors, 6000 arcs, 2M genomic-position long arcs (Hi-C style,
                seed 21), built as the annealer's CSR
                (calcAnchorExpectedDistancesHeatmap); arcs/s.
+stress         stress refinement of one chromosome's anchors (4000 anchors,
+               200k long arcs -> 70k pair targets, seed 51, reference spring
+               and angle constants, step 0.01) for 2000 iterations (the run
+               may converge earlier); iterations/s.
 serve          request loop: 5000 arc-level regions, sizes round(exp U[ln 64,
                ln 8192]), 1.5625 arcs per bead (400 per 256 beads), Poisson
                arrivals at 200 requests/s (seed 11), 20k moves each, device
@@ -474,6 +478,59 @@ def targets(args) -> dict:
                      "unit": "GB/s", "frac": achieved / peak,
                      "traffic": _traffic(kernel, f"targets_{n_long}"),
                      "peak_source": kind, "algorithmic_bytes_per_launch": alg},
+    }
+
+
+STRESS_ANCHORS, STRESS_LONG, STRESS_LR = 4000, 200_000, 0.01
+
+
+def stress_problem():
+    return synth.stress_problem(n_anchors=STRESS_ANCHORS, n_long=STRESS_LONG, seed=51)
+
+
+def stress(args) -> dict:
+    """stressRefineAnchors on the device: one cooperative launch per call;
+    device time of the descent and the host-buffer call end to end (pair
+    list built on the host)."""
+    import time as _t
+    t = stress_problem()
+    it = args.moves or 2000
+    ctx = capi.Context(0)
+    ms_k, e2e, res = [], [], None
+    for k in range(max(3, args.warmup) + args.steps):
+        t0 = _t.perf_counter()
+        _, _, res = capi.stress_refine(ctx, t, it, STRESS_LR)
+        dt = _t.perf_counter() - t0
+        if k >= max(3, args.warmup):
+            ms_k.append(res["kernel_ms"])
+            e2e.append(dt)
+    ms = float(np.median(ms_k))
+    iters = res["iterations"]
+    n, p = STRESS_ANCHORS, res["n_pairs"]
+    # per iteration: each pair entry (8 bytes) and the partner's position
+    # (16) read from both ends, each anchor's position, neighbours, target
+    # and gradient (~80 bytes); the working set (1.2 MB) stays in L2
+    alg = iters * (2.0 * p * 24.0 + 80.0 * n)
+    peak, kind = _peak()
+    achieved = alg / (ms * 1e-3) / 1e9
+    return {
+        "metric": "iterations/s", "value": iters / (ms * 1e-3), "unit": "iterations/s",
+        "n_gpus": 1, "steps": args.steps, "warmup": max(3, args.warmup), "ms_per_step": ms,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic",
+        "config": {"workload": f"stress_refine_{n}anchors_{STRESS_LONG}long_arcs_"
+                               f"{p}pairs_lr{STRESS_LR}_max{it}",
+                   "iterations": iters, "stop": res["stop"], "final_energy": res["total"],
+                   "pair_terms_per_s": iters * p / (ms * 1e-3)},
+        "e2e": {"value": iters / float(np.median(e2e)), "unit": "iterations/s",
+                "h2d_bytes_per_step": int(sum(np.asarray(t[key]).nbytes for key in
+                                              capi.stress_arrays(t))),
+                "d2h_bytes_per_step": 16 * n},
+        "roofline": {"bound": "hbm", "kernel": "stress_kernel", "achieved": achieved,
+                     "peak": peak, "unit": "GB/s", "frac": achieved / peak, "traffic": None,
+                     "peak_source": kind, "algorithmic_bytes_per_launch": alg,
+                     "note": "L2-resident working set; bound by the per-anchor gather "
+                             "latency and two grid barriers per iteration"},
     }
 
 

@@ -254,6 +254,46 @@ def target_cases():
     return out
 
 
+STRESS_KEYS = ("active", "genomic_pos", "pos", "arc_start", "arc_end", "arc_score",
+               "long_start", "long_end", "long_score", "anc_start", "anc_end")
+
+
+def stress_specs():
+    """(problem, max_iter, lr) of the stress-refinement cases."""
+    return [
+        # defaults: converges after the step was halved once
+        (synth.stress_problem(n_anchors=120, n_long=2000, seed=51), 300, 0.05),
+        # no backbone: consecutive anchors stay in the pair list
+        (synth.stress_problem(n_anchors=200, n_long=3000, seed=52, springs=(0.0, 0.0, 0.1)),
+         200, 0.05),
+        # no angle term, squeeze stiffer than stretch
+        (synth.stress_problem(n_anchors=150, n_long=2000, seed=53, springs=(0.1, 0.2, 0.0)),
+         500, 0.05),
+        # a large step: repeated halving, then convergence
+        (synth.stress_problem(n_anchors=80, n_long=1000, seed=54), 400, 5.0),
+        # no angle term, a long run to max_iter
+        (synth.stress_problem(n_anchors=80, n_long=1000, seed=55, springs=(0.1, 0.1, 0.0)),
+         3000, 0.05),
+    ]
+
+
+def stress_cases():
+    out = {}
+    for k, (t, it, lr) in enumerate(stress_specs()):
+        order, pos = O.ref_stress_refine(t, it, lr)
+        d = {key: np.asarray(t[key]) for key in STRESS_KEYS}
+        d["first_cluster"] = np.array([t["first_cluster"]], np.int32)
+        d["count"] = np.array(t["count"], np.float32)
+        d["glen"] = np.array(t["glen"], np.float32)
+        d["springs"] = np.array(t["springs"], np.float32)
+        d["max_iter"] = np.array([it], np.int32)
+        d["lr"] = np.array([lr], np.float32)
+        d["order"] = order
+        d["out_pos"] = pos
+        out[f"stress{k}"] = d
+    return out
+
+
 def main():
     if not O.ref_available():
         O.build()
@@ -264,7 +304,7 @@ def main():
               "equi": equi_cases,
               "heatmap": heatmap_cases,
               "smooth": smooth_cases, "mark": mark_cases, "hcm": hcm_cases,
-              "targets": target_cases}
+              "targets": target_cases, "stress": stress_cases}
     want = sys.argv[1:] or list(groups) + ["rng"]
     fixtures = {}
     for g in want:
