@@ -28,3 +28,41 @@ def test_shim_compiles_against_reference_headers(tmp_path):
                  "InteractionArcs::parallelMarkArcs(bool)", "setGpuSeed(unsigned int)",
                  "GpuResourceCache::init()", "GpuResourceCache::cleanup()"):
         assert f" T {name}" in syms, name
+
+
+def test_reference_program_links_with_the_shim(tmp_path):
+    """The reference's own pMMC-reconstruct program, built from its sources
+    where they lie with the shim in place of its four GPU .cu files
+    (ParallelMonteCarlo{Arcs,Heatmap,Smooth}.cu, ParallelMarkArcs.cu), links
+    against libpmmc_gb300.so with no symbol left undefined, and starts.
+    (Its sources do not travel to GPU hosts, so the pipeline itself is not
+    run there.)"""
+    import concurrent.futures as cf
+    nvcc = "/usr/local/cuda/bin/nvcc"
+    lib = os.path.join(ROOT, "pmmc_gb300", "libpmmc_gb300.so")
+    if not os.path.exists(nvcc) or not os.path.exists(lib):
+        pytest.skip("nvcc or the built library missing")
+    inc = [f"-I{REF}/include", f"-I{REF}/thirdparty", f"-I{ROOT}/include"]
+    jobs = [["g++", "-std=c++17", "-O1", "-fopenmp", "-w", *inc, "-c",
+             f"{REF}/apps/pMMC-reconstruct/main_reconstruct.cpp", "-o", "main.o"],
+            ["g++", "-std=c++17", "-O1", "-w", *inc, "-c",
+             os.path.join(ROOT, "pmmc_gb300", "shim", "looper_solver_gpu.cpp"), "-o", "shim.o"],
+            ["gcc", "-O1", "-w", "-c", f"{REF}/thirdparty/ini.c", "-o", "ini.o"],
+            [nvcc, "-std=c++17", "-O1", "-w", "-gencode", "arch=compute_103a,code=sm_103a", *inc,
+             "-c", f"{REF}/HierarchicalChromosome.cu", "-o", "hc.o"]]
+    jobs += [["g++", "-std=c++17", "-O1", "-w", *inc, "-c", f"{REF}/thirdparty/{f}.cpp", "-o",
+              f"{f}.o"] for f in ("common", "mtxlib", "INIReader", "rmsd")]
+    with cf.ThreadPoolExecutor(8) as ex:
+        res = list(ex.map(lambda c: subprocess.run(c, cwd=tmp_path, capture_output=True,
+                                                   text=True), jobs))
+    for r in res:
+        assert r.returncode == 0, r.stderr[-2000:]
+    objs = ["main.o", "common.o", "mtxlib.o", "INIReader.o", "rmsd.o", "ini.o", "hc.o", "shim.o"]
+    r = subprocess.run(["g++", "-fopenmp", "-o", "pMMC-reconstruct", *objs,
+                        f"-L{os.path.dirname(lib)}", "-lpmmc_gb300", "-L/usr/local/cuda/lib64",
+                        "-lcudart", f"-Wl,-rpath,{os.path.dirname(lib)}"],
+                       cwd=tmp_path, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
+    out = subprocess.run([str(tmp_path / "pMMC-reconstruct")], capture_output=True, text=True,
+                         timeout=60)
+    assert "Usage: pMMC-reconstruct" in out.stdout + out.stderr
