@@ -303,11 +303,11 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
   for (int i = threadIdx.x; i < 33; i += blockDim.x) s_dtpow[i] = P.dtpow[i];
   __syncthreads();
   unsigned char *wbase = smem + kCtaHeader + (size_t)(threadIdx.x >> 5) * smem_per_warp;
-  int4 *s_mv = reinterpret_cast<int4 *>(wbase);
-  float *s_thr = reinterpret_cast<float *>(wbase + 32 * 16);
-  float *s_d = reinterpret_cast<float *>(wbase + 32 * 20);
-  float *s_so = reinterpret_cast<float *>(wbase + 32 * 28);
-  float *s_sn = reinterpret_cast<float *>(wbase + 32 * 32);
+  int4 *s_mv = reinterpret_cast<int4 *>(wbase);               // move m at slot m & 63
+  float *s_thr = reinterpret_cast<float *>(wbase + 64 * 16);
+  float *s_d = reinterpret_cast<float *>(wbase + 64 * 20);
+  float *s_so = reinterpret_cast<float *>(wbase + 64 * 20 + 32 * 4);
+  float *s_sn = reinterpret_cast<float *>(wbase + 64 * 20 + 32 * 8);
   float4 *spos = reinterpret_cast<float4 *>(wbase + kMoveBufBytes);
 
   for (;;) {
@@ -389,7 +389,11 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
     constexpr int W = 32 / G;
     const int g = lane / G;    // proposal slot of this lane
     const int sub = lane % G;  // lane within the slot
-    long long bm = 0;          // first move held by the draw buffer
+    // Draws live in a 64-move ring, refilled 32 moves at a time, so that a
+    // window can always take 32 proposals whatever move it starts at.
+    // [lo, lo + 64) are drawn; T is the temperature of move lo + 64 (the
+    // first move of the next refill).
+    long long lo = 0;
     auto refill = [&](long long first) {
       const uint64_t m = (uint64_t)first + lane;
       const uint4 r = philox_move(U.seed, chain_id, m, 0u);
@@ -400,28 +404,32 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
       const float dy = (2.0f * u01(r.z) - 1.0f) * step;
       const float dz = P.use2d ? 0.0f : (2.0f * u01(r.w) - 1.0f) * step;
       const float Tl = (float)T * s_dtpow[lane];
-      s_mv[lane] = make_int4(b, __float_as_int(dx), __float_as_int(dy), __float_as_int(dz));
-      s_thr[lane] = ratio_threshold(u01(a.x), Tl, P.inv_scale, P.inv_coef);
+      const int slot = (int)(m & 63u);
+      s_mv[slot] = make_int4(b, __float_as_int(dx), __float_as_int(dy), __float_as_int(dz));
+      s_thr[slot] = ratio_threshold(u01(a.x), Tl, P.inv_scale, P.inv_coef);
+      T *= (double)s_dtpow[32];
     };
-    if (!stop) refill(0);
+    if (!stop) {
+      refill(0);
+      refill(32);
+    }
     __syncwarp();
 
     long long next_ms = P.window;
     long long next_rs = P.resync > 0 ? (long long)P.resync : LLONG_MAX;
     while (!stop) {
       const long long lim = min(min(next_ms, next_rs), P.cap);
-      if (moves + W > bm + 32 && bm + 32 < lim) {  // draw the next 32 moves
-        T *= (double)s_dtpow[moves - bm];
-        bm = moves;
+      const int L = (int)min((long long)W, lim - moves);
+      if (moves + L > lo + 64) {  // the oldest 32 are used: draw the next 32
         __syncwarp();
-        refill(bm);
+        refill(lo + 64);
+        lo += 32;
         __syncwarp();
       }
-      const int L = (int)min((long long)W, min(lim, bm + 32) - moves);
-      const int k0 = (int)(moves - bm);
       const bool active = g < L;
-      const int4 mv = active ? s_mv[k0 + g] : make_int4(0, 0, 0, 0);
-      const float thr = active ? s_thr[k0 + g] : 0.0f;
+      const int slot = (int)((moves + g) & 63);
+      const int4 mv = active ? s_mv[slot] : make_int4(0, 0, 0, 0);
+      const float thr = active ? s_thr[slot] : 0.0f;
       const int b = mv.x;
       if (active && sub == 0) atomicOr(&smask[b], 1u << g);
       __syncwarp();
@@ -553,7 +561,7 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
         __syncwarp();
         if (lane == 0) {
           for (int j = 0; j < lend && moves + j < P.trace_cap; ++j) {
-            const int4 m = s_mv[k0 + j];
+            const int4 m = s_mv[(moves + j) & 63];
             MoveTrace tr;
             tr.bead = m.x;
             tr.accepted = (accm >> j) & 1u;
@@ -1058,7 +1066,11 @@ void arcs_set_smem_limit(int bytes) {
 // shared memory) for each shared-memory class of a batch.  Every candidate
 // runs the class's largest items (up to 4 per SM) for kTuneMoves moves with
 // milestones and resyncs off, timed with events after one warm-up launch; the
-// fastest in moves/s wins.  Choices are kept per process, keyed by the
+// fastest in moves/s wins.  The trial chains run at the temperature the
+// schedule reaches after kTuneCool moves: almost every move of a long chain
+// is made cold, where few proposals are accepted and long windows pay, while
+// the first moves at the start temperature accept many proposals and favour
+// short windows.  Choices are kept per process, keyed by the
 // device (SM count, shared memory) and the class's shape (staged or not,
 // slice size, mean region size and arc degree, loops, extended energy), and
 // mirrored in a JSON file when PMMC_AUTOTUNE_CACHE names one.
@@ -1066,6 +1078,7 @@ void arcs_set_smem_limit(int bytes) {
 namespace {
 
 constexpr int kTuneMoves = 8192;
+constexpr int kTuneCool = 50000;
 
 struct TuneChoice {
   int lanes = 2, warps = 4;
@@ -1121,7 +1134,8 @@ std::string class_key(const pmmc_arcs_batch *b, const ArcsClass &c, const std::v
   n /= cnt;
   deg /= cnt;
   char buf[256];
-  snprintf(buf, sizeof(buf), "sm%d_smem%zu_nb%d_slice%d_n%d_deg%d_loops%d_ext%d", b->ctx->sm_count,
+  snprintf(buf, sizeof(buf), "sm%d_smem%zu_nb%d_slice%d_n%d_deg%d_loops%d_ext%d_cold",
+           b->ctx->sm_count,
            b->ctx->smem_optin, c.nb_smem ? 1 : 0,
            (int)std::ceil(std::log2(std::max(16, c.smem_per_warp))),
            (int)std::lround(2.0 * std::log2(std::max(1.0, n))), (int)std::lround(2.0 * deg),
@@ -1144,6 +1158,7 @@ static cudaError_t autotune_classes(pmmc_arcs_batch *b, cudaStream_t s) {
   tune_load(path);
   const size_t cap_smem = ctx->smem_optin - kCtaHeader;
   ArcsDevParams T = b->P;
+  T.max_temp = (float)((double)b->P.max_temp * std::pow((double)b->P.dtpow[1], (double)kTuneCool));
   T.cap = kTuneMoves;
   T.window = 1 << 30;
   T.resync = 0;

@@ -66,7 +66,9 @@ struct ArcsDevParams {
 
 // per-warp scratch: 32 drawn moves (int4) + their ratio thresholds, and the
 // window's per-slot delta, conflict mask and (tracing) local scores
-constexpr int kMoveBufBytes = 32 * 16 + 32 * 4 + 4 * 32 * 4;
+// per warp: a ring of 64 drawn moves (16 B) and thresholds (4 B), then three
+// 32-float trace rows
+constexpr int kMoveBufBytes = 64 * 16 + 64 * 4 + 3 * 32 * 4;
 constexpr int kCtaHeader = 256;                    // dt^l table shared by the CTA
 
 // Host-side packing of regions into the flat arrays the kernel reads: float4
