@@ -38,7 +38,7 @@ sys.path.insert(0, ROOT)
 
 N_STRUCT, N_BLOCKS = 64, 24
 ANNEAL = dict(max_temp=5.0, dt_temp=0.9999, milestone_steps=50000, improvement=0.99)
-RESYNC = 1000
+RESYNC = 4096
 STEP = 0.5
 WORKLOAD = (f"arcs_ensemble_{N_STRUCT}x{N_BLOCKS}_blocks32-2048_1.5arcs_per_bead_"
             f"T0=5_cool0.9999_milestone50k_thr0.99")
@@ -488,7 +488,7 @@ def run_gpu(args, rank, world):
     ctx.set_seed(2024 + rank)
     regs, inputs = make_inputs(rank, world)
     prm = capi.default_params(capi.LEVEL_ARCS, schedule=capi.SCHEDULE_CPU,
-                              resync_every=RESYNC, **ANNEAL)
+                              resync_every=args.resync, **ANNEAL)
     steps = [STEP] * len(inputs)
     batch = capi.ArcsBatch(ctx, inputs, prm, steps, chains=1, use_graph=True, lanes=args.lanes)
     classes = batch.classes()
@@ -582,6 +582,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--resync", type=int, default=RESYNC,
+                    help="FP64 energy recompute every this many moves of a chain")
     ap.add_argument("--no-plain", dest="plain", action="store_false")
     ap.add_argument("--cpu-budget", type=float, default=20.0)
     ap.add_argument("--structures", type=int, default=N_STRUCT,
@@ -692,7 +694,7 @@ def main():
         "data": "synthetic",
         "config": {"workload": WORKLOAD, "structures": N_STRUCT * world,
                    "blocks_per_structure": N_BLOCKS, "regions": r["n_units"] * world,
-                   "moves_per_step": total_moves, "fp64_resync_every": RESYNC,
+                   "moves_per_step": total_moves, "fp64_resync_every": args.resync,
                    "l2": "256 MB buffer written between timed steps",
                    "parallelism": f"replicas x{world}",
                    "launch_classes": [{"lanes": la, "warps_per_cta": w, "items": it,
