@@ -490,7 +490,8 @@ def run_gpu(args, rank, world):
     prm = capi.default_params(capi.LEVEL_ARCS, schedule=capi.SCHEDULE_CPU,
                               resync_every=args.resync, **ANNEAL)
     steps = [STEP] * len(inputs)
-    batch = capi.ArcsBatch(ctx, inputs, prm, steps, chains=1, use_graph=True, lanes=args.lanes)
+    batch = capi.ArcsBatch(ctx, inputs, prm, steps, chains=1, use_graph=True, lanes=args.lanes,
+                           drawing_warp=args.drawing_warp)
     classes = batch.classes()
     stream = torch.cuda.Stream()
     l2 = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device="cuda")  # > 129 MB L2
@@ -529,7 +530,7 @@ def run_gpu(args, rank, world):
     for k in range(args.e2e_steps):
         torch.cuda.synchronize()
         t = time.perf_counter()
-        p2, r2 = _batch_anneal_host(ctx, inputs, prm, steps, args.lanes)
+        p2, r2 = _batch_anneal_host(ctx, inputs, prm, steps, args.lanes, args.drawing_warp)
         e2e_ms.append((time.perf_counter() - t) * 1e3)
     e2e_moves = sum(r.moves for r in r2)
     h2d, d2h = staged_bytes(inputs)
@@ -548,7 +549,7 @@ def run_gpu(args, rank, world):
                 n_units=len(inputs), classes=classes)
 
 
-def _batch_anneal_host(ctx, inputs, prm, steps, lanes=0):
+def _batch_anneal_host(ctx, inputs, prm, steps, lanes=0, drawing_warp=False):
     import ctypes as C
 
     from pmmc_gb300 import capi
@@ -557,7 +558,7 @@ def _batch_anneal_host(ctx, inputs, prm, steps, lanes=0):
     tot = sum(x.n for x in inputs)
     pos = np.zeros((tot, 3), np.float32)
     res = (capi.Result * len(inputs))()
-    opts = capi.BatchOpts(1, 0, int(lanes))
+    opts = capi.BatchOpts(1, 0, int(lanes), int(bool(drawing_warp)))
     ctx.check(capi.lib().pmmc_arcs_batch_anneal(ctx.h, len(inputs), arr, C.byref(prm),
                                                 st.ctypes.data_as(C.c_void_p), C.byref(opts),
                                                 pos.ctypes.data_as(C.c_void_p), res))
@@ -582,6 +583,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--drawing-warp", action="store_true",
+                    help="with fixed --lanes 1 or 2: a second warp per chain draws the moves")
     ap.add_argument("--resync", type=int, default=RESYNC,
                     help="FP64 energy recompute every this many moves of a chain")
     ap.add_argument("--no-plain", dest="plain", action="store_false")
@@ -697,8 +700,9 @@ def main():
                    "moves_per_step": total_moves, "fp64_resync_every": args.resync,
                    "l2": "256 MB buffer written between timed steps",
                    "parallelism": f"replicas x{world}",
-                   "launch_classes": [{"lanes": la, "warps_per_cta": w, "items": it,
-                                       "arcs_in_smem": nb} for la, w, it, nb in r["classes"]],
+                   "launch_classes": [{"lanes": la, "chains_per_cta": w, "items": it,
+                                       "arcs_in_smem": nb, "drawing_warp": dw}
+                                      for la, w, it, nb, dw in r["classes"]],
                    "tuning": "autotuned" if args.lanes == -1 else f"lanes={args.lanes}"},
         "structures_per_s": structs,
         "final_energy_rel_error_max": r["rel_err"],

@@ -231,7 +231,12 @@ typedef struct pmmc_batch_opts {
                           * the autotuner picks lanes and warps per CTA
                           * for each shared-memory class from timed trial
                           * launches, cached per process and in the JSON
-                          * file named by PMMC_AUTOTUNE_CACHE)            */
+                          * file named by PMMC_AUTOTUNE_CACHE, and
+                          * whether chains get a drawing warp)            */
+  int drawing_warp;      /* with lanes 1 or 2: 1 = every chain gets a second
+                          * warp that draws its moves (Philox proposals and
+                          * thresholds) ahead of it, 0 = the chain's warp
+                          * draws them itself; the moves are the same     */
 } pmmc_batch_opts;
 #define PMMC_LANES_AUTO (-1)
 pmmc_status pmmc_arcs_batch_create(pmmc_ctx *ctx, int n_units,
@@ -283,10 +288,13 @@ pmmc_status pmmc_arcs_batch_create_ex(pmmc_ctx *ctx, int n_units,
 pmmc_status pmmc_selftest_sqrt(pmmc_ctx *ctx, uint32_t lo, uint32_t count,
                                uint64_t *mismatches, uint32_t *first_bad);
 /* The launch configuration of each shared-memory class of a batch (no
- * reference counterpart): lanes per proposal, warps per CTA, work items and
- * whether arc lists are staged in shared memory; up to `cap` classes. */
+ * reference counterpart): lanes per proposal, chains per CTA, work items,
+ * whether arc lists are staged in shared memory and whether each chain has a
+ * second warp drawing its moves ahead; up to `cap` classes.  Any output
+ * pointer may be NULL. */
 pmmc_status pmmc_arcs_batch_classes(pmmc_arcs_batch *b, int cap, int *n_classes,
-                                    int *lanes, int *warps, int *items, int *nb_smem);
+                                    int *lanes, int *warps, int *items, int *nb_smem,
+                                    int *drawing_warp);
 /* Copy `count` (<= trace_cap) trace records of the last run to host. */
 pmmc_status pmmc_arcs_batch_trace(pmmc_arcs_batch *b, void *out, int count);
 

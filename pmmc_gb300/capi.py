@@ -141,7 +141,7 @@ class SmoothProblem(C.Structure):
 
 class BatchOpts(C.Structure):
     _fields_ = [("chains_per_unit", C.c_int), ("use_graph", C.c_int),
-                ("lanes_per_chain", C.c_int)]
+                ("lanes_per_chain", C.c_int), ("drawing_warp", C.c_int)]
 
 
 class ServerOpts(C.Structure):
@@ -315,13 +315,13 @@ class ArcsBatch:
     """Device-resident batch of arc regions (pmmc_arcs_batch_*)."""
 
     def __init__(self, ctx: Context, inputs, params: AnnealParams, steps, chains=1,
-                 use_graph=True, stop_all=False, trace_cap=0, lanes=0):
+                 use_graph=True, stop_all=False, trace_cap=0, lanes=0, drawing_warp=False):
         self.ctx = ctx
         self.inputs = list(inputs)
         arr = (ArcsProblem * len(self.inputs))(*[x.struct() for x in self.inputs])
         self._arr = arr
         self.steps = _f32(steps)
-        opts = BatchOpts(int(chains), int(bool(use_graph)), int(lanes))
+        opts = BatchOpts(int(chains), int(bool(use_graph)), int(lanes), int(bool(drawing_warp)))
         h = C.c_void_p()
         ctx.check(lib().pmmc_arcs_batch_create_ex(
             ctx.h, len(self.inputs), arr, C.byref(params), _p(self.steps), C.byref(opts),
@@ -352,12 +352,14 @@ class ArcsBatch:
         return ms.value, mv.value, lanes.value
 
     def classes(self):
-        """Per shared-memory class: (lanes, warps per CTA, items, staged)."""
+        """Per shared-memory class: (lanes, chains per CTA, items, staged,
+        drawing warp)."""
         cap = 64
         n = C.c_int()
-        la, wa, it, nb = (C.c_int * cap)(), (C.c_int * cap)(), (C.c_int * cap)(), (C.c_int * cap)()
-        self.ctx.check(lib().pmmc_arcs_batch_classes(self.h, cap, C.byref(n), la, wa, it, nb))
-        return [(la[k], wa[k], it[k], bool(nb[k])) for k in range(min(n.value, cap))]
+        la, wa, it, nb, dw = ((C.c_int * cap)() for _ in range(5))
+        self.ctx.check(lib().pmmc_arcs_batch_classes(self.h, cap, C.byref(n), la, wa, it, nb, dw))
+        return [(la[k], wa[k], it[k], bool(nb[k]), bool(dw[k]))
+                for k in range(min(n.value, cap))]
 
     def trace(self, count=None):
         count = self.trace_cap if count is None else count

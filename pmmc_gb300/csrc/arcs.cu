@@ -284,8 +284,16 @@ __device__ double arcs_repulsion(int n, const float4 *spos, const int *srp,
   return warp_sum_d(acc);
 }
 
-template <bool NB_SMEM, int G>
-__global__ void __launch_bounds__(128, 4)
+// Bounded wait of one lane on a shared-memory word written by the other warp
+// of a chain's pair: returns false when the time limit ran out.
+constexpr unsigned long long kPairWaitNs = 2000000000ull;
+
+__device__ __forceinline__ void pair_sync(int slot) {
+  asm volatile("bar.sync %0, 64;" ::"r"(1 + slot) : "memory");
+}
+
+template <bool NB_SMEM, int G, bool PROD>
+__global__ void __launch_bounds__(PROD ? 256 : 128, PROD ? 2 : 4)
 arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
                    const int2 *__restrict__ items, int n_items,
                    int *__restrict__ head, const float4 *__restrict__ pos0,
@@ -299,21 +307,33 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
                    MoveTrace *__restrict__ trace, const double *__restrict__ bases) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int lane = threadIdx.x & 31;
+  // PROD: warps come in pairs, the even one runs the chain, the odd one
+  // draws its moves into the ring ahead of it
+  const int wid = threadIdx.x >> 5;
+  const int slot_w = PROD ? (wid >> 1) : wid;
+  const bool producer = PROD && (wid & 1) != 0;
   float *s_dtpow = reinterpret_cast<float *>(smem);
   for (int i = threadIdx.x; i < 33; i += blockDim.x) s_dtpow[i] = P.dtpow[i];
   __syncthreads();
-  unsigned char *wbase = smem + kCtaHeader + (size_t)(threadIdx.x >> 5) * smem_per_warp;
-  int4 *s_mv = reinterpret_cast<int4 *>(wbase);               // move m at slot m & 63
-  float *s_thr = reinterpret_cast<float *>(wbase + 64 * 16);
-  float *s_d = reinterpret_cast<float *>(wbase + 64 * 20);
-  float *s_so = reinterpret_cast<float *>(wbase + 64 * 20 + 32 * 4);
-  float *s_sn = reinterpret_cast<float *>(wbase + 64 * 20 + 32 * 8);
+  unsigned char *wbase = smem + kCtaHeader + (size_t)slot_w * smem_per_warp;
+  ArcsRingCtl *ctl = reinterpret_cast<ArcsRingCtl *>(wbase + kRingCtlOffset);
+  int4 *s_mv = reinterpret_cast<int4 *>(wbase);  // move m at slot m % kRing
+  float *s_thr = reinterpret_cast<float *>(wbase + kRing * 16);
+  float *s_d = reinterpret_cast<float *>(wbase + kRing * 20);
+  float *s_so = reinterpret_cast<float *>(wbase + kRing * 20 + 32 * 4);
+  float *s_sn = reinterpret_cast<float *>(wbase + kRing * 20 + 32 * 8);
   float4 *spos = reinterpret_cast<float4 *>(wbase + kMoveBufBytes);
 
   for (;;) {
     int item = 0;
-    if (lane == 0) item = atomicAdd(head, 1);
-    item = __shfl_sync(0xffffffffu, item, 0);
+    if (PROD) {
+      if (!producer && lane == 0) *(volatile int *)&ctl->item = atomicAdd(head, 1);
+      pair_sync(slot_w);
+      item = *(volatile int *)&ctl->item;
+    } else {
+      if (lane == 0) item = atomicAdd(head, 1);
+      item = __shfl_sync(0xffffffffu, item, 0);
+    }
     if (item >= n_items) break;
     const int2 it = items[item];
     const ArcsUnit U = units[it.x];
@@ -335,6 +355,61 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
     const bool mov_smem = has_mov && off + (size_t)U.n_mov * 4 <= (size_t)smem_per_warp;
     int *smov = reinterpret_cast<int *>(wbase + off);
 
+    if (producer) {
+      // ---- the drawing warp: moves [next, next + 32) into the ring once
+      // the chain has used the moves that held those slots ----
+      const int *MOVp = has_mov ? (mov_smem ? smov : movable + U.mov_off) : nullptr;
+      pair_sync(slot_w);  // staging done (the movable list may be in shared memory)
+      if (U.n_mov > 0) {
+        double Tp = P.max_temp;
+        const float step = U.step;
+        int4 *s_mv = reinterpret_cast<int4 *>(wbase);
+        float *s_thr = reinterpret_cast<float *>(wbase + kRing * 16);
+        for (long long next = 0;; next += 32) {
+          int st = 0;
+          if (lane == 0) {
+            unsigned long long t0 = 0;
+            for (unsigned spins = 0;; ++spins) {
+              st = *(volatile int *)&ctl->state;
+              if (st != 0) break;
+              if (next <= *(volatile long long *)&ctl->consumed + (kRing - 32)) break;
+              if ((spins & 63u) == 63u) {
+                const unsigned long long t = globaltimer_ns();
+                if (t0 == 0) t0 = t;
+                else if (t - t0 > kPairWaitNs) {
+                  st = 2;
+                  *(volatile int *)&ctl->state = 2;
+                  break;
+                }
+              }
+              __nanosleep(20);
+            }
+          }
+          st = __shfl_sync(0xffffffffu, st, 0);
+          if (st != 0) break;
+          __threadfence_block();  // the chain's reads of these slots are done
+          const uint64_t m = (uint64_t)next + lane;
+          const uint4 r = philox_move(U.seed, chain_id, m, 0u);
+          const uint4 a = philox_move(U.seed, chain_id, m, 1u);
+          const int k = uniform_index(r.x, U.n_mov);
+          const int b = MOVp ? MOVp[k] : k;
+          const float dx = (2.0f * u01(r.y) - 1.0f) * step;
+          const float dy = (2.0f * u01(r.z) - 1.0f) * step;
+          const float dz = P.use2d ? 0.0f : (2.0f * u01(r.w) - 1.0f) * step;
+          const float Tl = (float)Tp * s_dtpow[lane];
+          const int sl = (int)(m & (uint64_t)(kRing - 1));
+          s_mv[sl] = make_int4(b, __float_as_int(dx), __float_as_int(dy), __float_as_int(dz));
+          s_thr[sl] = ratio_threshold(u01(a.x), Tl, P.inv_scale, P.inv_coef);
+          Tp *= (double)s_dtpow[32];
+          __syncwarp();
+          __threadfence_block();
+          if (lane == 0) *(volatile long long *)&ctl->filled = next + 32;
+        }
+      }
+      pair_sync(slot_w);  // the chain is finished
+      continue;
+    }
+
     for (int i = lane; i < n; i += 32) spos[i] = pos0[U.pos_off + i];
     for (int i = lane; i <= n; i += 32) srp[i] = row_ptr[U.rp_off + i];
     for (int i = lane; i < n; i += 32) smask[i] = 0u;
@@ -346,7 +421,16 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
     }
     if (mov_smem)
       for (int k = lane; k < U.n_mov; k += 32) smov[k] = movable[U.mov_off + k];
+    if (PROD && lane == 0) {
+      *(volatile long long *)&ctl->filled = 0;
+      *(volatile long long *)&ctl->consumed = 0;
+      *(volatile int *)&ctl->state = 0;
+    }
     __syncwarp();
+    if (PROD) {
+      __threadfence_block();
+      pair_sync(slot_w);  // staging done: the drawing warp starts
+    }
     const int2 *NB = NB_SMEM ? snb : nbr + U.nbr_off;
     const float *INV = NB_SMEM ? sinv : inv_t + U.nbr_off;
     const int *MOV = has_mov ? (mov_smem ? smov : movable + U.mov_off) : nullptr;
@@ -389,10 +473,11 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
     constexpr int W = 32 / G;
     const int g = lane / G;    // proposal slot of this lane
     const int sub = lane % G;  // lane within the slot
-    // Draws live in a 64-move ring, refilled 32 moves at a time, so that a
-    // window can always take 32 proposals whatever move it starts at.
-    // [lo, lo + 64) are drawn; T is the temperature of move lo + 64 (the
-    // first move of the next refill).
+    // Draws live in a kRing-move ring, refilled 32 moves at a time, so that
+    // a window can always take 32 proposals whatever move it starts at.
+    // [lo, lo + kRing) are drawn; T is the temperature of move lo + kRing
+    // (the first move of the next refill).  With a drawing warp (PROD) that
+    // warp fills the ring and this one only waits for it.
     long long lo = 0;
     auto refill = [&](long long first) {
       const uint64_t m = (uint64_t)first + lane;
@@ -404,15 +489,14 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
       const float dy = (2.0f * u01(r.z) - 1.0f) * step;
       const float dz = P.use2d ? 0.0f : (2.0f * u01(r.w) - 1.0f) * step;
       const float Tl = (float)T * s_dtpow[lane];
-      const int slot = (int)(m & 63u);
+      const int slot = (int)(m & (uint64_t)(kRing - 1));
       s_mv[slot] = make_int4(b, __float_as_int(dx), __float_as_int(dy), __float_as_int(dz));
       s_thr[slot] = ratio_threshold(u01(a.x), Tl, P.inv_scale, P.inv_coef);
       T *= (double)s_dtpow[32];
     };
-    if (!stop) {
-      refill(0);
-      refill(32);
-    }
+    long long have = 0;  // PROD: moves the drawing warp has published
+    if (!PROD && !stop)
+      for (int r = 0; r < kRing; r += 32) refill(r);
     __syncwarp();
 
     long long next_ms = P.window;
@@ -420,14 +504,45 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
     while (!stop) {
       const long long lim = min(min(next_ms, next_rs), P.cap);
       const int L = (int)min((long long)W, lim - moves);
-      if (moves + L > lo + 64) {  // the oldest 32 are used: draw the next 32
+      if (PROD) {
+        if (moves + L > have) {  // wait for the drawing warp
+          long long f = 0;
+          int ok = 1;
+          if (lane == 0) {
+            unsigned long long t0 = 0;
+            for (unsigned spins = 0;; ++spins) {
+              f = *(volatile long long *)&ctl->filled;
+              if (f >= moves + L) break;
+              if (*(volatile int *)&ctl->state == 2) {
+                ok = 0;
+                break;
+              }
+              if ((spins & 63u) == 63u) {
+                const unsigned long long t = globaltimer_ns();
+                if (t0 == 0) t0 = t;
+                else if (t - t0 > kPairWaitNs) {
+                  ok = 0;
+                  break;
+                }
+              }
+              __nanosleep(32);
+            }
+          }
+          have = __shfl_sync(0xffffffffu, f, 0);
+          if (!__shfl_sync(0xffffffffu, ok, 0)) {
+            status = kDevDrawWait;
+            break;
+          }
+          __threadfence_block();  // the slots up to `have` are written
+        }
+      } else if (moves + L > lo + kRing) {  // the oldest 32 are used: draw the next 32
         __syncwarp();
-        refill(lo + 64);
+        refill(lo + kRing);
         lo += 32;
         __syncwarp();
       }
       const bool active = g < L;
-      const int slot = (int)((moves + g) & 63);
+      const int slot = (int)((moves + g) & (kRing - 1));
       const int4 mv = active ? s_mv[slot] : make_int4(0, 0, 0, 0);
       const float thr = active ? s_thr[slot] : 0.0f;
       const int b = mv.x;
@@ -561,7 +676,7 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
         __syncwarp();
         if (lane == 0) {
           for (int j = 0; j < lend && moves + j < P.trace_cap; ++j) {
-            const int4 m = s_mv[(moves + j) & 63];
+            const int4 m = s_mv[(moves + j) & (kRing - 1)];
             MoveTrace tr;
             tr.bead = m.x;
             tr.accepted = (accm >> j) & 1u;
@@ -584,6 +699,10 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
       succ_ms += na;
       moves += lend;
       ++batch_no;
+      if (PROD && lane == 0) {
+        __threadfence_block();  // this window's reads of the ring are done
+        *(volatile long long *)&ctl->consumed = moves;
+      }
 
       // ---- milestone (the reference CPU predicate, FP64, every lane) ----
       bool flag = false;
@@ -646,6 +765,10 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
       po[3 * i + 2] = p.z;
     }
     __syncwarp();
+    if (PROD) {
+      if (lane == 0 && *(volatile int *)&ctl->state == 0) *(volatile int *)&ctl->state = 1;
+      pair_sync(slot_w);  // the drawing warp has stopped
+    }
   }
 }
 
@@ -731,15 +854,21 @@ arcs_base_kernel(const ArcsUnit *__restrict__ units, int n_units,
   }
 }
 
-// The instantiation for a launch: arc lists staged or not, G lanes per move.
-inline ArcsKernelFn arcs_kernel_for(bool nb_smem, int lanes) {
+// The instantiation for a launch: arc lists staged or not, G lanes per move,
+// a drawing warp per chain or not (lanes 1 and 2 only).
+inline ArcsKernelFn arcs_kernel_for(bool nb_smem, int lanes, bool prod = false) {
+  if (prod && lanes == 1)
+    return nb_smem ? arcs_anneal_kernel<true, 1, true> : arcs_anneal_kernel<false, 1, true>;
+  if (prod && lanes == 2)
+    return nb_smem ? arcs_anneal_kernel<true, 2, true> : arcs_anneal_kernel<false, 2, true>;
   switch (lanes) {
-    case 1: return nb_smem ? arcs_anneal_kernel<true, 1> : arcs_anneal_kernel<false, 1>;
-    case 2: return nb_smem ? arcs_anneal_kernel<true, 2> : arcs_anneal_kernel<false, 2>;
-    case 8: return nb_smem ? arcs_anneal_kernel<true, 8> : arcs_anneal_kernel<false, 8>;
-    case 32: return nb_smem ? arcs_anneal_kernel<true, 32> : arcs_anneal_kernel<false, 32>;
-    case 4: return nb_smem ? arcs_anneal_kernel<true, 4> : arcs_anneal_kernel<false, 4>;
-    default: return nb_smem ? arcs_anneal_kernel<true, 2> : arcs_anneal_kernel<false, 2>;
+    case 1: return nb_smem ? arcs_anneal_kernel<true, 1, false> : arcs_anneal_kernel<false, 1, false>;
+    case 2: return nb_smem ? arcs_anneal_kernel<true, 2, false> : arcs_anneal_kernel<false, 2, false>;
+    case 8: return nb_smem ? arcs_anneal_kernel<true, 8, false> : arcs_anneal_kernel<false, 8, false>;
+    case 32:
+      return nb_smem ? arcs_anneal_kernel<true, 32, false> : arcs_anneal_kernel<false, 32, false>;
+    case 4: return nb_smem ? arcs_anneal_kernel<true, 4, false> : arcs_anneal_kernel<false, 4, false>;
+    default: return nb_smem ? arcs_anneal_kernel<true, 2, false> : arcs_anneal_kernel<false, 2, false>;
   }
 }
 
@@ -756,6 +885,7 @@ struct ArcsClass {
   int smem_per_warp = 0;
   int warps_per_cta = 1;
   int lanes = 2;          // lanes per proposal
+  bool prod = false;      // a drawing warp per chain
   int grid = 0;
   cudaStream_t stream = nullptr;
   cudaEvent_t join = nullptr;
@@ -1027,9 +1157,10 @@ void ArcsPack::finish() {
 }
 
 cudaError_t arcs_launch(const ArcsLaunch &a, const ArcsDevParams &P, bool nb_smem, int lanes,
-                        int grid, int warps, int smem_per_warp, cudaStream_t s) {
+                        int grid, int warps, int smem_per_warp, cudaStream_t s, bool prod) {
+  prod = prod && (lanes == 1 || lanes == 2);
   const size_t dyn = kCtaHeader + (size_t)warps * smem_per_warp;
-  arcs_kernel_for(nb_smem, lanes)<<<grid, 32 * warps, dyn, s>>>(
+  arcs_kernel_for(nb_smem, lanes, prod)<<<grid, 32 * warps * (prod ? 2 : 1), dyn, s>>>(
       a.units, a.items, a.n_items, a.head, a.pos0, a.row_ptr, a.nbr, a.inv_t, a.movable, a.lrp,
       a.lent, a.lst, a.nulls, P, smem_per_warp, a.pos_out, a.outs, a.done, a.trace, a.bases);
   return cudaGetLastError();
@@ -1043,19 +1174,21 @@ cudaError_t arcs_bases(const ArcsUnit *units, int n_units, const float4 *pos0,
   return cudaGetLastError();
 }
 
-int arcs_ctas_per_sm(bool nb_smem, int lanes, int warps, int smem_per_warp) {
+int arcs_ctas_per_sm(bool nb_smem, int lanes, int warps, int smem_per_warp, bool prod) {
+  prod = prod && (lanes == 1 || lanes == 2);
   int per_sm = 0;
   const size_t dyn = kCtaHeader + (size_t)warps * smem_per_warp;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, arcs_kernel_for(nb_smem, lanes),
-                                                32 * warps, dyn);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, arcs_kernel_for(nb_smem, lanes, prod),
+                                                32 * warps * (prod ? 2 : 1), dyn);
   return per_sm < 1 ? 1 : per_sm;
 }
 
 void arcs_set_smem_limit(int bytes) {
   for (int lanes : {1, 2, 4, 8, 32})
     for (bool nbs : {true, false})
-      cudaFuncSetAttribute(arcs_kernel_for(nbs, lanes),
-                           cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+      for (bool prod : {false, true})
+        cudaFuncSetAttribute(arcs_kernel_for(nbs, lanes, prod),
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
 }
 
 }  // namespace pmmc
@@ -1070,7 +1203,15 @@ void arcs_set_smem_limit(int bytes) {
 // schedule reaches after kTuneCool moves: almost every move of a long chain
 // is made cold, where few proposals are accepted and long windows pay, while
 // the first moves at the start temperature accept many proposals and favour
-// short windows.  Choices are kept per process, keyed by the
+// short windows.  Classes holding regions within an eighth of the size of
+// the batch's largest are not tuned for throughput: their chains set, or come
+// close to, the length of the pass, so they take the configuration with the
+// lowest latency per move (one lane per proposal, a drawing warp, one chain
+// per CTA).  On the benchmark ensemble (sizes 32-2048) giving that
+// configuration to the classes above 1/2, 1/3, 1/4 and all of the largest
+// size measured 152, 147, 148 and 143 ms per pass: the throughput trials,
+// run with a class alone on the device, choose configurations that lose
+// once the classes share it.  Choices are kept per process, keyed by the
 // device (SM count, shared memory) and the class's shape (staged or not,
 // slice size, mean region size and arc degree, loops, extended energy), and
 // mirrored in a JSON file when PMMC_AUTOTUNE_CACHE names one.
@@ -1081,7 +1222,7 @@ constexpr int kTuneMoves = 8192;
 constexpr int kTuneCool = 50000;
 
 struct TuneChoice {
-  int lanes = 2, warps = 4;
+  int lanes = 2, warps = 4, prod = 0;
   double moves_per_s = 0.0;
 };
 
@@ -1098,8 +1239,10 @@ void tune_load(const std::string &path) {
   while (fgets(line, sizeof(line), f)) {
     char key[256];
     TuneChoice c;
-    if (sscanf(line, " \"%255[^\"]\": {\"lanes\": %d, \"warps\": %d, \"moves_per_s\": %lf",
-               key, &c.lanes, &c.warps, &c.moves_per_s) == 4)
+    if (sscanf(line,
+               " \"%255[^\"]\": {\"lanes\": %d, \"warps\": %d, \"prod\": %d, "
+               "\"moves_per_s\": %lf",
+               key, &c.lanes, &c.warps, &c.prod, &c.moves_per_s) == 5)
       g_tune[key] = c;
   }
   fclose(f);
@@ -1113,9 +1256,10 @@ void tune_save(const std::string &path) {
   fprintf(f, "{\n  \"pmmc_autotune\": 1,\n  \"entries\": {\n");
   size_t k = 0;
   for (auto &kv : g_tune)
-    fprintf(f, "    \"%s\": {\"lanes\": %d, \"warps\": %d, \"moves_per_s\": %.6e}%s\n",
-            kv.first.c_str(), kv.second.lanes, kv.second.warps, kv.second.moves_per_s,
-            ++k < g_tune.size() ? "," : "");
+    fprintf(f,
+            "    \"%s\": {\"lanes\": %d, \"warps\": %d, \"prod\": %d, \"moves_per_s\": %.6e}%s\n",
+            kv.first.c_str(), kv.second.lanes, kv.second.warps, kv.second.prod,
+            kv.second.moves_per_s, ++k < g_tune.size() ? "," : "");
   fprintf(f, "  }\n}\n");
   fclose(f);
   rename(tmp.c_str(), path.c_str());
@@ -1168,20 +1312,41 @@ static cudaError_t autotune_classes(pmmc_arcs_batch *b, cudaStream_t s) {
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   bool changed = false;
+  // the regions whose chains set the pass's length: within an eighth of the
+  // size of the batch's largest (move counts grow with the region)
+  int n_max = 0;
+  for (const ArcsUnit &U : b->h_units) n_max = std::max(n_max, U.n);
   for (size_t k = 0; k < b->classes.size() && e == cudaSuccess; ++k) {
     ArcsClass &c = b->classes[k];
-    const std::string key = class_key(b, c, items);
-    auto it = g_tune.find(key);
+    int c_max = 0;
+    for (int q = c.item_begin; q < c.item_end; ++q)
+      c_max = std::max(c_max, b->h_units[items[q].x].n);
     TuneChoice best;
-    if (it != g_tune.end()) {
+    const bool critical = 8 * c_max >= n_max;
+    const std::string key = class_key(b, c, items) + (critical ? "_critical" : "");
+    auto it = g_tune.find(key);
+    if (critical) {
+      // the lowest latency per move, not the highest throughput: one lane
+      // per proposal, a drawing warp, a chain per CTA
+      best.lanes = 1;
+      best.warps = 1;
+      best.prod = 1;
+      best.moves_per_s = 0.0;
+      if (it == g_tune.end()) {
+        g_tune[key] = best;
+        changed = true;
+      }
+    } else if (it != g_tune.end()) {
       best = it->second;
     } else {
       const int m = std::min(c.item_end - c.item_begin, 4 * ctx->sm_count);
       best.moves_per_s = -1.0;
-      for (int lanes : {1, 2, 4, 8}) {
+      for (int cand = 0; cand < 6; ++cand) {  // lanes 1, 2 with and without drawing warp; 4, 8
+        const int lanes = cand < 2 ? 1 : cand < 4 ? 2 : cand == 4 ? 4 : 8;
+        const bool prod = cand < 4 && (cand & 1);
         for (int w : {4, 2, 1}) {
           if ((size_t)w * c.smem_per_warp > cap_smem) continue;
-          const int per_sm = arcs_ctas_per_sm(c.nb_smem, lanes, w, c.smem_per_warp);
+          const int per_sm = arcs_ctas_per_sm(c.nb_smem, lanes, w, c.smem_per_warp, prod);
           const int grid = std::max(1, std::min(per_sm * ctx->sm_count, (m + w - 1) / w));
           ArcsLaunch a{b->units.p, b->items.p + c.item_begin, m, b->heads.p + k, b->pos0.p,
                        b->row_ptr.p, b->nbr.p, b->inv_t.p, b->movable.p, b->lrp.p, b->lent.p,
@@ -1191,7 +1356,8 @@ static cudaError_t autotune_classes(pmmc_arcs_batch *b, cudaStream_t s) {
           for (int rep = 0; rep < 2 && e == cudaSuccess; ++rep) {
             e = cudaMemsetAsync(b->heads.p + k, 0, sizeof(int), s);
             if (e == cudaSuccess && rep == 1) e = cudaEventRecord(e0, s);
-            if (e == cudaSuccess) e = arcs_launch(a, T, c.nb_smem, lanes, grid, w, c.smem_per_warp, s);
+            if (e == cudaSuccess)
+              e = arcs_launch(a, T, c.nb_smem, lanes, grid, w, c.smem_per_warp, s, prod);
             if (e == cudaSuccess && rep == 1) e = cudaEventRecord(e1, s);
           }
           if (e == cudaSuccess) e = cudaEventSynchronize(e1);
@@ -1201,6 +1367,7 @@ static cudaError_t autotune_classes(pmmc_arcs_batch *b, cudaStream_t s) {
           if (rate > best.moves_per_s) {
             best.lanes = lanes;
             best.warps = w;
+            best.prod = prod ? 1 : 0;
             best.moves_per_s = rate;
           }
         }
@@ -1214,7 +1381,9 @@ static cudaError_t autotune_classes(pmmc_arcs_batch *b, cudaStream_t s) {
     if (e != cudaSuccess) break;
     c.lanes = best.lanes;
     c.warps_per_cta = best.warps;
-    const int per_sm = arcs_ctas_per_sm(c.nb_smem, c.lanes, c.warps_per_cta, c.smem_per_warp);
+    c.prod = best.prod != 0;
+    const int per_sm =
+        arcs_ctas_per_sm(c.nb_smem, c.lanes, c.warps_per_cta, c.smem_per_warp, c.prod);
     const int items_n = c.item_end - c.item_begin;
     c.grid = std::max(1, std::min(per_sm * ctx->sm_count,
                                   (items_n + c.warps_per_cta - 1) / c.warps_per_cta));
@@ -1324,6 +1493,7 @@ extern "C" pmmc_status pmmc_arcs_batch_create_ex(
   int lanes = opts && opts->lanes_per_chain > 0 ? opts->lanes_per_chain : 2;
   if (lanes != 1 && lanes != 2 && lanes != 4 && lanes != 8 && lanes != 32) lanes = 2;
   b->lanes = lanes;
+  const bool prod_fixed = opts && opts->drawing_warp != 0 && (lanes == 1 || lanes == 2);
   arcs_set_smem_limit((int)ctx->smem_optin);
   size_t i0 = 0;
   while (i0 < needs.size()) {
@@ -1343,7 +1513,8 @@ extern "C" pmmc_status pmmc_arcs_batch_create_ex(
     while (w > 1 && (size_t)w * c.smem_per_warp > cap_smem) w >>= 1;
     c.warps_per_cta = w;
     c.lanes = lanes;
-    const int per_sm = arcs_ctas_per_sm(nbs, lanes, w, c.smem_per_warp);
+    c.prod = prod_fixed;
+    const int per_sm = arcs_ctas_per_sm(nbs, lanes, w, c.smem_per_warp, c.prod);
     const int items_n = c.item_end - c.item_begin;
     c.grid = std::max(1, std::min(per_sm * ctx->sm_count, (items_n + w - 1) / w));
     b->classes.push_back(c);
@@ -1412,7 +1583,7 @@ cudaError_t enqueue_pass(pmmc_arcs_batch *b, cudaStream_t s) {
                  b->lrp.p, b->lent.p, b->lst.p, b->nulls.p, b->pos_out.p, b->outs.p,
                  b->done.p, b->trace, b->bases.p};
     e = arcs_launch(a, b->P, c.nb_smem, c.lanes, c.grid, c.warps_per_cta, c.smem_per_warp,
-                    c.stream);
+                    c.stream, c.prod);
     if (e == cudaSuccess) e = cudaEventRecord(c.join, c.stream);
     if (e == cudaSuccess) e = cudaStreamWaitEvent(s, c.join, 0);
   }
@@ -1556,7 +1727,7 @@ extern "C" pmmc_status pmmc_arcs_batch_stats(pmmc_arcs_batch *b, double *kernel_
 
 extern "C" pmmc_status pmmc_arcs_batch_classes(pmmc_arcs_batch *b, int cap, int *n_classes,
                                                int *lanes, int *warps, int *items,
-                                               int *nb_smem) {
+                                               int *nb_smem, int *drawing_warp) {
   if (!b || !n_classes) return PMMC_ERR_INVALID;
   *n_classes = (int)b->classes.size();
   for (int k = 0; k < (int)b->classes.size() && k < cap; ++k) {
@@ -1565,6 +1736,7 @@ extern "C" pmmc_status pmmc_arcs_batch_classes(pmmc_arcs_batch *b, int cap, int 
     if (warps) warps[k] = c.warps_per_cta;
     if (items) items[k] = c.item_end - c.item_begin;
     if (nb_smem) nb_smem[k] = c.nb_smem ? 1 : 0;
+    if (drawing_warp) drawing_warp[k] = c.prod ? 1 : 0;
   }
   return PMMC_OK;
 }
@@ -1588,7 +1760,7 @@ extern "C" pmmc_status pmmc_arcs_batch_anneal(pmmc_ctx *ctx, int n_units,
                                               const pmmc_batch_opts *opts,
                                               float *pos_out, pmmc_result *res) {
   pmmc_arcs_batch *b = nullptr;
-  pmmc_batch_opts o = opts ? *opts : pmmc_batch_opts{1, 0, 0};
+  pmmc_batch_opts o = opts ? *opts : pmmc_batch_opts{1, 0, 0, 0};
   o.use_graph = 0;  // one pass: nothing to replay
   pmmc_status s = pmmc_arcs_batch_create(ctx, n_units, units, prm, step_sizes, &o, &b);
   if (s != PMMC_OK) return s;
@@ -1603,7 +1775,7 @@ extern "C" pmmc_status pmmc_arcs_anneal(pmmc_ctx *ctx, const pmmc_arcs_problem *
                                         int n_chains, float *pos_out, pmmc_result *res) {
   if (!ctx || !pr || !prm) return fail(ctx, PMMC_ERR_INVALID, "arcs anneal: bad arguments");
   if (n_chains <= 0) n_chains = 4 * ctx->sm_count;
-  pmmc_batch_opts o{n_chains, 0, 0};
+  pmmc_batch_opts o{n_chains, 0, 0, 0};
   pmmc_arcs_batch *b = nullptr;
   pmmc_status s =
       pmmc_arcs_batch_create_ex(ctx, 1, pr, prm, &step_size, &o, 1, 0, &b);

@@ -66,9 +66,20 @@ struct ArcsDevParams {
 
 // per-warp scratch: 32 drawn moves (int4) + their ratio thresholds, and the
 // window's per-slot delta, conflict mask and (tracing) local scores
-// per warp: a ring of 64 drawn moves (16 B) and thresholds (4 B), then three
-// 32-float trace rows
-constexpr int kMoveBufBytes = 64 * 16 + 64 * 4 + 3 * 32 * 4;
+// per chain: a ring of kRing drawn moves (16 B) and thresholds (4 B), three
+// 32-float trace rows, and the words a drawing warp and its chain's warp
+// exchange (ArcsRingCtl).  The ring holds four rounds of 32 draws, so a
+// drawing warp stays two rounds ahead of windows that use ~30 moves each.
+constexpr int kRing = 128;
+constexpr int kMoveBufBytes = kRing * 16 + kRing * 4 + 3 * 32 * 4 + 64;
+constexpr int kRingCtlOffset = kRing * 16 + kRing * 4 + 3 * 32 * 4;
+
+struct ArcsRingCtl {
+  long long filled;    // moves [0, filled) are drawn
+  long long consumed;  // moves [0, consumed) are used up
+  int item;            // the pair's current item
+  int state;           // 0 running, 1 chain finished, 2 the drawing warp gave up
+};
 constexpr int kCtaHeader = 256;                    // dt^l table shared by the CTA
 
 // Host-side packing of regions into the flat arrays the kernel reads: float4
@@ -121,15 +132,18 @@ struct ArcsLaunch {
   const double *bases;  // frozen repulsion per unit (NULL: each chain computes it)
 };
 
-// One persistent pass of `grid` CTAs x `warps` warps over the items on `s`.
+// One persistent pass of `grid` CTAs x `warps` chains over the items on `s`.
+// prod: every chain gets a second warp that draws its moves ahead (lanes 1
+// or 2 only).
 cudaError_t arcs_launch(const ArcsLaunch &a, const ArcsDevParams &P, bool nb_smem, int lanes,
-                        int grid, int warps, int smem_per_warp, cudaStream_t s);
+                        int grid, int warps, int smem_per_warp, cudaStream_t s,
+                        bool prod = false);
 // The frozen repulsion of every unit into bases[u] (one block per unit).
 cudaError_t arcs_bases(const ArcsUnit *units, int n_units, const float4 *pos0,
                        const int *row_ptr, const int2 *nbr, const int2 *nulls, double *bases,
                        cudaStream_t s);
 // Resident CTAs per SM of that configuration (at least 1).
-int arcs_ctas_per_sm(bool nb_smem, int lanes, int warps, int smem_per_warp);
+int arcs_ctas_per_sm(bool nb_smem, int lanes, int warps, int smem_per_warp, bool prod = false);
 // Raise the dynamic shared-memory limit of every instantiation to `bytes`.
 void arcs_set_smem_limit(int bytes);
 

@@ -151,11 +151,16 @@ def test_arcs_batch_autotune(ctx, tmp_path, monkeypatch):
     ctx.set_seed(99)
     b = capi.ArcsBatch(ctx, inputs, prm, [0.5] * len(inputs), lanes=capi.LANES_AUTO)
     cls = b.classes()
-    assert cls and all(la in (1, 2, 4, 8) and w in (1, 2, 4) for la, w, _, _ in cls)
-    assert sum(it for _, _, it, _ in cls) == len(inputs)
+    assert cls and all(la in (1, 2, 4, 8) and w in (1, 2, 4) for la, w, _, _, _ in cls)
+    assert all(not dw or la in (1, 2) for la, _, _, _, dw in cls)
+    assert sum(it for _, _, it, _, _ in cls) == len(inputs)
     data = json.load(open(path))
     assert len(data["entries"]) >= len(cls)
-    assert all(v["moves_per_s"] > 0 for v in data["entries"].values())
+    # classes whose regions set the pass's length take the low-latency
+    # configuration without trials; every other class was timed
+    assert all(v["moves_per_s"] > 0 or k.endswith("_critical")
+               for k, v in data["entries"].items())
+    assert any(k.endswith("_critical") for k in data["entries"])
     b.run()
     pos, res = b.results()
     same = 0
@@ -210,3 +215,48 @@ def test_arcs_statistics_match_reference(ctx):
     gpu_p = [distmap_pearson(p, r.pos) for p in pos]
     for a, c in ((ref_e, gpu_e), (ref_rmsd, gpu_rmsd), (ref_p, gpu_p)):
         assert ks_2samp_p(a, c) > 0.05
+
+
+@pytest.mark.parametrize("lanes", [1, 2])
+def test_arcs_drawing_warp_gives_the_same_chains(ctx, lanes):
+    """A second warp per chain drawing the moves ahead changes nothing but
+    the timing: every chain of a batch ends bit-identical (positions, energy,
+    moves) to the single-warp form."""
+    sizes = [40, 300, 1100, 2000, 75]
+    regs = [synth.arcs_region(n, int(1.5 * n), seed=50 + s) for s, n in enumerate(sizes)]
+    inputs = [capi.ArcsInput.from_dense(r.pos, r.dense()) for r in regs]
+    inputs += [problem("fixed")[1], problem("loops_sphere")[1]]  # movable list, loops
+    prm = capi.default_params(capi.LEVEL_ARCS, schedule=capi.SCHEDULE_CPU, max_temp=5.0,
+                              dt_temp=0.9999, milestone_steps=5000, improvement=0.99,
+                              resync_every=1000)
+    out = []
+    for dw in (False, True):
+        ctx.set_seed(321)
+        b = capi.ArcsBatch(ctx, inputs, prm, [0.5] * len(inputs), lanes=lanes, drawing_warp=dw)
+        assert all(c[4] == dw for c in b.classes())
+        b.run()
+        out.append(b.results())
+        b.close()
+    (p0, r0), (p1, r1) = out
+    for a, c in zip(p0, p1):
+        np.testing.assert_array_equal(a, c)
+    assert [(x.moves, x.accepted, x.energy, x.status) for x in r0] == \
+        [(x.moves, x.accepted, x.energy, x.status) for x in r1]
+    assert all(x.status == 0 for x in r1)
+
+
+def test_arcs_drawing_warp_trace_replays(ctx):
+    """The trace of a chain with a drawing warp replays on the oracle."""
+    r = synth.arcs_region(300, 450, seed=77)
+    pr = O.ArcsProblem(r.pos, r.dense())
+    base = dict(max_temp=5.0, dt_temp=0.9999, milestone_steps=2000, improvement=0.99)
+    prm = capi.default_params(capi.LEVEL_ARCS, schedule=capi.SCHEDULE_CPU, max_moves=6000,
+                              **base)
+    ctx.set_seed(777)
+    b = capi.ArcsBatch(ctx, [capi.ArcsInput.from_dense(r.pos, r.dense())], prm, [0.5],
+                       trace_cap=6000, lanes=1, drawing_warp=True)
+    b.run()
+    _, res = b.results()
+    tr = b.trace(int(res[0].moves))
+    rep = O.arcs_replay(pr, O.Params(max_moves=6000, **base), 0.5, 777, 0, tr)
+    check_replay(tr, rep)
