@@ -1775,7 +1775,10 @@ extern "C" pmmc_status pmmc_arcs_anneal(pmmc_ctx *ctx, const pmmc_arcs_problem *
                                         int n_chains, float *pos_out, pmmc_result *res) {
   if (!ctx || !pr || !prm) return fail(ctx, PMMC_ERR_INVALID, "arcs anneal: bad arguments");
   if (n_chains <= 0) n_chains = 4 * ctx->sm_count;
-  pmmc_batch_opts o{n_chains, 0, 0, 0};
+  // a few chains: latency per move decides (one lane per proposal and a
+  // drawing warp); many: throughput (two lanes, the chain draws itself)
+  const bool few = n_chains <= ctx->sm_count;
+  pmmc_batch_opts o{n_chains, 0, few ? 1 : 0, few ? 1 : 0};
   pmmc_arcs_batch *b = nullptr;
   pmmc_status s =
       pmmc_arcs_batch_create_ex(ctx, 1, pr, prm, &step_size, &o, 1, 0, &b);

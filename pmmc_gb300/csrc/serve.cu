@@ -256,7 +256,10 @@ void pmmc_server::launch(Slot &sl, std::vector<ReqPtr> wave) {
     const int per_warp = (smem_need + 15) & ~15;
     while (warps > 1 && (size_t)warps * per_warp > cap_smem) warps >>= 1;
     const int n_items = (int)items.size();
-    const int per_sm = arcs_ctas_per_sm(nbs, lanes, warps, per_warp);
+    // one lane per proposal (large regions): a drawing warp per chain keeps
+    // the proposal draws off the chain's path
+    const bool prod = lanes == 1;
+    const int per_sm = arcs_ctas_per_sm(nbs, lanes, warps, per_warp, prod);
     const int grid = std::max(1, std::min(per_sm * ctx->sm_count, (n_items + warps - 1) / warps));
     ArcsLaunch a{reinterpret_cast<const ArcsUnit *>(d + L.units),
                  reinterpret_cast<const int2 *>(d + L.items),
@@ -278,7 +281,8 @@ void pmmc_server::launch(Slot &sl, std::vector<ReqPtr> wave) {
                  reinterpret_cast<const double *>(d + L.bases)};
     e = arcs_bases(a.units, n_items, a.pos0, a.row_ptr, a.nbr, a.nulls,
                    reinterpret_cast<double *>(d + L.bases), sl.stream);
-    if (e == cudaSuccess) e = arcs_launch(a, P, nbs, lanes, grid, warps, per_warp, sl.stream);
+    if (e == cudaSuccess)
+      e = arcs_launch(a, P, nbs, lanes, grid, warps, per_warp, sl.stream, prod);
   }
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(sl.h_out, d + L.pos_out, L.total - L.pos_out, cudaMemcpyDeviceToHost,
