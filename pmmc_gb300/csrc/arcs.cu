@@ -1445,24 +1445,49 @@ extern "C" pmmc_status pmmc_arcs_batch_create_ex(
   b->P.trace_cap = trace_cap;
 
   // ---- pack host arrays (unit u's chains have global ids u*chains...) ----
-  ArcsPack pk;
-  if (n_threads == 1) {
-    for (int u = 0; u < n_units; ++u) pk.add(units[u], chains, steps[u], b->P.seed, u * chains);
-  } else {
-    const int per = (n_units + n_threads - 1) / n_threads;
-    std::vector<ArcsPack> parts((n_units + per - 1) / per);
-    parallel([&](int a, int z) {
-      ArcsPack &q = parts[a / per];
-      for (int u = a; u < z; ++u) q.add(units[u], chains, steps[u], b->P.seed, u * chains);
-    });
-    for (auto &q : parts) pk.append(q);
+  // Each host thread packs a contiguous range of units into its own part;
+  // the parts are not concatenated on the host (a serial copy of every
+  // array): each is uploaded to its offset in the device arrays, and only
+  // the unit records are rebased.
+  const int per = (n_units + n_threads - 1) / n_threads;
+  std::vector<ArcsPack> parts((n_units + per - 1) / per);
+  parallel([&](int a, int z) {
+    ArcsPack &q = parts[a / per];
+    for (int u = a; u < z; ++u) q.add(units[u], chains, steps[u], b->P.seed, u * chains);
+  });
+  struct PartOff {
+    size_t pos, rp, nbr, nulls, mov, lrp, lent, lst;
+  };
+  std::vector<PartOff> po(parts.size() + 1, PartOff{0, 0, 0, 0, 0, 0, 0, 0});
+  long long out_off = 0;
+  int chain_base = 0;
+  b->h_units.clear();
+  b->h_units.reserve(n_units);
+  for (size_t k = 0; k < parts.size(); ++k) {
+    const ArcsPack &q = parts[k];
+    const PartOff &o = po[k];
+    for (ArcsUnit U : q.units) {
+      U.pos_off += (int)o.pos;
+      U.rp_off += (int)o.rp;
+      U.nbr_off += (int)o.nbr;
+      U.null_off += (int)o.nulls;
+      if (U.mov_off >= 0) U.mov_off += (int)o.mov;
+      if (U.lrp_off >= 0) U.lrp_off += (int)o.lrp;
+      U.lent_off += (int)o.lent;
+      U.lst_off += (int)o.lst;
+      if (U.n_arcs >= 0) U.arc_off += (int)o.lst;
+      U.chain_base += chain_base;
+      U.out_off += out_off;
+      b->h_units.push_back(U);
+    }
+    po[k + 1] = PartOff{o.pos + q.pos.size(),     o.rp + q.rp.size(),   o.nbr + q.nbr.size(),
+                        o.nulls + q.nulls.size(), o.mov + q.mov.size(), o.lrp + q.lrp.size(),
+                        o.lent + q.lent.size(),   o.lst + q.lst.size()};
+    out_off += q.out_floats;
+    chain_base += q.chains;
   }
-  pk.finish();
-  b->h_units = pk.units;
   b->h_n.resize(n_units);
   for (int u = 0; u < n_units; ++u) b->h_n[u] = units[u].n;
-  const long long out_off = pk.out_floats;
-  const int chain_base = pk.chains;
   b->total_pos_out = out_off;
   b->total_chains = chain_base;
 
@@ -1524,19 +1549,27 @@ extern "C" pmmc_status pmmc_arcs_batch_create_ex(
   // ---- upload ----
   cudaStream_t s = ctx->stream;
   cudaError_t e = cudaSuccess;
-#define UP(buf, vec)                                                           \
-  if (e == cudaSuccess) e = b->buf.upload(vec, s);
-  UP(units, pk.units);
-  UP(items, h_items);
-  UP(pos0, pk.pos);
-  UP(row_ptr, pk.rp);
-  UP(nbr, pk.nbr);
-  UP(inv_t, pk.inv);
-  UP(nulls, pk.nulls);
-  UP(movable, pk.mov);
-  UP(lrp, pk.lrp);
-  UP(lent, pk.lent);
-  UP(lst, pk.lst);
+  // every device array at its total size (at least one entry), each part's
+  // slice copied to its offset
+  const PartOff &tot = po.back();
+#define UP(buf, field, member)                                                  \
+  if (e == cudaSuccess) e = b->buf.alloc(std::max<size_t>(1, tot.field));      \
+  for (size_t k = 0; k < parts.size() && e == cudaSuccess; ++k)                \
+    if (!parts[k].member.empty())                                              \
+      e = cudaMemcpyAsync(b->buf.p + po[k].field, parts[k].member.data(),      \
+                          parts[k].member.size() * sizeof(parts[k].member[0]), \
+                          cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = b->units.upload(b->h_units, s);
+  if (e == cudaSuccess) e = b->items.upload(h_items, s);
+  UP(pos0, pos, pos);
+  UP(row_ptr, rp, rp);
+  UP(nbr, nbr, nbr);
+  UP(inv_t, nbr, inv);
+  UP(nulls, nulls, nulls);
+  UP(movable, mov, mov);
+  UP(lrp, lrp, lrp);
+  UP(lent, lent, lent);
+  UP(lst, lst, lst);
 #undef UP
   if (e == cudaSuccess) e = b->heads.alloc(b->classes.size());
   if (e == cudaSuccess) e = b->pos_out.alloc((size_t)out_off);
