@@ -1453,6 +1453,17 @@ extern "C" pmmc_status pmmc_arcs_batch_create_ex(
   std::vector<ArcsPack> parts((n_units + per - 1) / per);
   parallel([&](int a, int z) {
     ArcsPack &q = parts[a / per];
+    size_t beads = 0, entries = 0;
+    for (int u = a; u < z; ++u) {
+      beads += (size_t)units[u].n;
+      entries += (size_t)units[u].row_ptr[units[u].n];
+    }
+    q.units.reserve(z - a);
+    q.pos.reserve(beads);
+    q.rp.reserve(beads + (size_t)(z - a));
+    q.nbr.reserve(entries);
+    q.inv.reserve(entries);
+    q.lst.reserve(entries / 2 + 1);
     for (int u = a; u < z; ++u) q.add(units[u], chains, steps[u], b->P.seed, u * chains);
   });
   struct PartOff {
