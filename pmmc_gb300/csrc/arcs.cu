@@ -1194,9 +1194,10 @@ void arcs_set_smem_limit(int bytes) {
 }  // namespace pmmc
 
 // ---------------------------------------------------------------------------
-// Autotuner: lanes per proposal (G: 2, 4 or 8, i.e. 16, 8 or 4 proposals
-// scored per window) and warps per CTA (1, 2 or 4 chains sharing a CTA's
-// shared memory) for each shared-memory class of a batch.  Every candidate
+// Autotuner: lanes per proposal (G: 1, 2, 4 or 8, i.e. 32, 16, 8 or 4
+// proposals scored per window), a drawing warp per chain or not (G 1 and 2),
+// and chains per CTA (1, 2 or 4 sharing a CTA's shared memory) for each
+// shared-memory class of a batch.  Every candidate
 // runs the class's largest items (up to 4 per SM) for kTuneMoves moves with
 // milestones and resyncs off, timed with events after one warm-up launch; the
 // fastest in moves/s wins.  The trial chains run at the temperature the
