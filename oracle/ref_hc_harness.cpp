@@ -1,7 +1,7 @@
 // ref_hc_harness.cpp -- test infrastructure: drives the reference's
 // equidistant-model interpolation (HierarchicalChromosome::gpuHelper,
-// src/HierarchicalChromosome.cu:1253-1447) through its CPU path (this build
-// host has no GPU, so gpuHelper takes its own CPU fallback) to record golden
+// src/HierarchicalChromosome.cu:1253-1447) through its CPU path (on a host
+// without a GPU, gpuHelper takes its own CPU fallback) to record golden
 // outputs.  Built from the reference sources where they lie by
 // oracle/Makefile into oracle/_ref/libpmmc_ref_hc.so; never shipped.
 #include <fcntl.h>
