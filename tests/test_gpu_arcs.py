@@ -260,3 +260,28 @@ def test_arcs_drawing_warp_trace_replays(ctx):
     tr = b.trace(int(res[0].moves))
     rep = O.arcs_replay(pr, O.Params(max_moves=6000, **base), 0.5, 777, 0, tr)
     check_replay(tr, rep)
+
+
+def test_plain_call_with_one_chain_matches_the_single_warp_batch(ctx):
+    """The drop-in call with at most one chain per SM runs one lane per
+    proposal with a drawing warp; a one-chain call equals the batch form
+    with one lane and no drawing warp, move for move (same Philox key: the
+    seed is reset before each call).  With several chains the first to
+    converge stops the others at a time-dependent move, so only one chain
+    compares exactly."""
+    n_chains = 1
+    r = synth.arcs_region(180, 270, seed=91)
+    inp = capi.ArcsInput.from_dense(r.pos, r.dense())
+    prm = capi.default_params(capi.LEVEL_ARCS, schedule=capi.SCHEDULE_CPU, max_temp=5.0,
+                              dt_temp=0.9999, milestone_steps=3000, improvement=0.99)
+    ctx.set_seed(4242)
+    pos, res = capi.arcs_anneal(ctx, inp, prm, 0.5, n_chains)
+    ctx.set_seed(4242)
+    b = capi.ArcsBatch(ctx, [inp], prm, [0.5], chains=n_chains, use_graph=False,
+                       stop_all=True, lanes=1, drawing_warp=False)
+    b.run()
+    bpos, bres = b.results()
+    b.close()
+    assert res.status == 0 and bres[0].status == 0
+    assert (res.moves, res.energy) == (bres[0].moves, bres[0].energy)
+    np.testing.assert_array_equal(pos, bpos[0])
