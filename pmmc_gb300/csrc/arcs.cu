@@ -1018,97 +1018,105 @@ ArcsDevParams arcs_make_params(const pmmc_anneal_params *prm, uint64_t seed, boo
 void ArcsPack::add(const pmmc_arcs_problem &pr, int n_chains, float step, uint64_t seed,
                    int rng_chain) {
   ArcsUnit U{};
-  U.n = pr.n;
+  const int n = pr.n;
+  U.n = n;
   U.pos_off = (int)pos.size();
-  for (int i = 0; i < pr.n; ++i)
-    pos.push_back(make_float4(pr.pos[3 * i], pr.pos[3 * i + 1], pr.pos[3 * i + 2], 0.0f));
-  // spring entries (target >= 1e-6) with 1/target; listed pairs with
-  // 0 <= target < 1e-6 are inert and only leave the repulsion sum
+  pos.resize(pos.size() + n);
+  float4 *P = pos.data() + U.pos_off;
+  for (int i = 0; i < n; ++i)
+    P[i] = make_float4(pr.pos[3 * i], pr.pos[3 * i + 1], pr.pos[3 * i + 2], 0.0f);
+  // loop constraints first (their records open this unit's slice of lst):
+  // rebuildActiveLoopMap (LooperSolver.hpp:3318-3337): key (min,max), the
+  // last constraint of a key wins, std::map order
+  U.lst_off = (int)lst.size();
+  U.n_loops = 0;
+  U.lrp_off = -1;
+  U.lent_off = 0;
+  U.n_lent = 0;
+  if (pr.n_loops > 0) {
+    std::map<std::pair<int, int>, int> lm;
+    for (int c = 0; c < pr.n_loops; ++c) {
+      int i = pr.loop_i[c], j = pr.loop_j[c];
+      if (i < 0 || j < 0 || i >= n || j >= n) continue;
+      lm[i < j ? std::make_pair(i, j) : std::make_pair(j, i)] = c;
+    }
+    U.n_loops = (int)lm.size();
+    if (!lm.empty()) {
+      std::vector<std::vector<float4>> per(n);
+      for (auto &kv : lm) {
+        const int c = kv.second, i = kv.first.first, j = kv.first.second;
+        lst.push_back(make_int4(i, j, __float_as_int_host(pr.loop_k[c]),
+                                __float_as_int_host(pr.loop_r0[c])));
+        per[i].push_back(make_float4(__int_as_float_host(j), pr.loop_k[c], pr.loop_r0[c], 0.0f));
+        if (j != i)
+          per[j].push_back(make_float4(__int_as_float_host(i), pr.loop_k[c], pr.loop_r0[c], 0.0f));
+      }
+      U.lrp_off = (int)lrp.size();
+      U.lent_off = (int)lent.size();
+      int acc = 0;
+      for (int i = 0; i < n; ++i) {
+        lrp.push_back(acc);
+        for (auto &e : per[i]) lent.push_back(e);
+        acc += (int)per[i].size();
+      }
+      lrp.push_back(acc);
+      U.n_lent = acc;
+    }
+  }
+  // one pass over the arc lists: spring entries (target >= 1e-6) with
+  // 1/target, listed pairs with 0 <= target < 1e-6 (inert: they only leave
+  // the repulsion sum), and every spring once (entries whose partner
+  // precedes the row) in the flat list of the periodic recompute
   U.rp_off = (int)rp.size();
   U.nbr_off = (int)nbr.size();
   U.null_off = (int)nulls.size();
-  int cnt = 0;
-  rp.push_back(0);
-  for (int i = 0; i < pr.n; ++i) {
+  U.arc_off = (int)lst.size();
+  const int n_ent = pr.row_ptr[n];
+  rp.resize(rp.size() + n + 1);
+  int *R = rp.data() + U.rp_off;
+  nbr.resize(nbr.size() + n_ent);
+  inv.resize(inv.size() + n_ent);
+  lst.resize(lst.size() + n_ent);  // trimmed below
+  int2 *NB = nbr.data() + U.nbr_off;
+  float *IV = inv.data() + U.nbr_off;
+  int4 *LS = lst.data() + U.arc_off;
+  int cnt = 0, n_arcs = 0;
+  R[0] = 0;
+  for (int i = 0; i < n; ++i) {
     for (int e = pr.row_ptr[i]; e < pr.row_ptr[i + 1]; ++e) {
+      const int j = pr.col[e];
       const float t = pr.target[e];
-      if (pr.col[e] == i) continue;  // the reference never pairs a bead with itself
+      if (j == i) continue;  // the reference never pairs a bead with itself
       if (t >= 1e-6f) {
-        int2 v;
-        v.x = pr.col[e];
-        v.y = __float_as_int_host(t);
-        nbr.push_back(v);
-        inv.push_back(1.0f / t);
+        const float it = 1.0f / t;
+        NB[cnt] = make_int2(j, __float_as_int_host(t));
+        IV[cnt] = it;
         ++cnt;
-      } else if (t >= 0.0f && pr.col[e] < i) {
-        nulls.push_back(make_int2(pr.col[e], i));
+        if (j < i) LS[n_arcs++] = make_int4(j, i, __float_as_int_host(t), __float_as_int_host(it));
+      } else if (t >= 0.0f && j < i) {
+        nulls.push_back(make_int2(j, i));
       }
     }
-    rp.push_back(cnt);
+    R[i + 1] = cnt;
   }
+  nbr.resize(U.nbr_off + cnt);
+  inv.resize(U.nbr_off + cnt);
+  lst.resize(U.arc_off + n_arcs);
   U.nnz = cnt;
   U.n_null = (int)nulls.size() - U.null_off;
-  std::vector<int> mv;
-  for (int i = 0; i < pr.n; ++i)
-    if (!pr.fixed || !pr.fixed[i]) mv.push_back(i);
-  U.n_mov = (int)mv.size();
-  if (U.n_mov < pr.n) {
+  U.n_arcs = n_arcs;
+  // movable beads, listed only when some bead is fixed
+  int n_mov = n;
+  if (pr.fixed)
+    for (int i = 0; i < n; ++i) n_mov -= pr.fixed[i] ? 1 : 0;
+  U.n_mov = n_mov;
+  if (n_mov < n) {
     U.mov_off = (int)mov.size();
-    mov.insert(mov.end(), mv.begin(), mv.end());
+    for (int i = 0; i < n; ++i)
+      if (!pr.fixed[i]) mov.push_back(i);
   } else {
     U.mov_off = -1;
   }
-  // loop constraints: rebuildActiveLoopMap (LooperSolver.hpp:3318-3337):
-  // key (min,max), the last constraint of a key wins, std::map order.
-  std::map<std::pair<int, int>, int> lm;
-  for (int c = 0; c < pr.n_loops; ++c) {
-    int i = pr.loop_i[c], j = pr.loop_j[c];
-    if (i < 0 || j < 0 || i >= pr.n || j >= pr.n) continue;
-    lm[i < j ? std::make_pair(i, j) : std::make_pair(j, i)] = c;
-  }
-  U.lst_off = (int)lst.size();
-  U.n_loops = (int)lm.size();
-  if (!lm.empty()) {
-    std::vector<std::vector<float4>> per(pr.n);
-    for (auto &kv : lm) {
-      const int c = kv.second, i = kv.first.first, j = kv.first.second;
-      int4 L;
-      L.x = i;
-      L.y = j;
-      L.z = __float_as_int_host(pr.loop_k[c]);
-      L.w = __float_as_int_host(pr.loop_r0[c]);
-      lst.push_back(L);
-      per[i].push_back(make_float4(__int_as_float_host(j), pr.loop_k[c], pr.loop_r0[c], 0.0f));
-      if (j != i)
-        per[j].push_back(make_float4(__int_as_float_host(i), pr.loop_k[c], pr.loop_r0[c], 0.0f));
-    }
-    U.lrp_off = (int)lrp.size();
-    U.lent_off = (int)lent.size();
-    int acc = 0;
-    for (int i = 0; i < pr.n; ++i) {
-      lrp.push_back(acc);
-      for (auto &e : per[i]) lent.push_back(e);
-      acc += (int)per[i].size();
-    }
-    lrp.push_back(acc);
-    U.n_lent = acc;
-  } else {
-    U.lrp_off = -1;
-    U.lent_off = 0;
-    U.n_lent = 0;
-  }
-  // every spring once (entries whose partner precedes the row), for the
-  // periodic recompute: a flat list balances the lanes
-  U.arc_off = (int)lst.size();
-  U.n_arcs = 0;
-  for (int i = 0; i < pr.n; ++i)
-    for (int e = pr.row_ptr[i]; e < pr.row_ptr[i + 1]; ++e) {
-      const float t = pr.target[e];
-      if (pr.col[e] < i && t >= 1e-6f) {
-        lst.push_back(make_int4(pr.col[e], i, __float_as_int_host(t), __float_as_int_host(1.0f / t)));
-        ++U.n_arcs;
-      }
-    }
   U.chains = n_chains;
   U.chain_base = chains;
   U.out_off = out_floats;
@@ -1116,7 +1124,7 @@ void ArcsPack::add(const pmmc_arcs_problem &pr, int n_chains, float step, uint64
   U.rng_chain = rng_chain;
   U.seed = seed;
   chains += n_chains;
-  out_floats += (long long)n_chains * pr.n * 3;
+  out_floats += (long long)n_chains * n * 3;
   units.push_back(U);
 }
 
@@ -1149,6 +1157,21 @@ void ArcsPack::append(const ArcsPack &o) {
   lst.insert(lst.end(), o.lst.begin(), o.lst.end());
   chains += o.chains;
   out_floats += o.out_floats;
+}
+
+void ArcsPack::clear() {
+  units.clear();
+  pos.clear();
+  rp.clear();
+  mov.clear();
+  lrp.clear();
+  nbr.clear();
+  nulls.clear();
+  inv.clear();
+  lent.clear();
+  lst.clear();
+  out_floats = 0;
+  chains = 0;
 }
 
 void ArcsPack::finish() {
@@ -1451,7 +1474,20 @@ extern "C" pmmc_status pmmc_arcs_batch_create_ex(
   // array): each is uploaded to its offset in the device arrays, and only
   // the unit records are rebased.
   const int per = (n_units + n_threads - 1) / n_threads;
-  std::vector<ArcsPack> parts((n_units + per - 1) / per);
+  // The parts live in the context and are reused: their memory is already
+  // paged in, where fresh arrays of this size spend most of their packing
+  // time in first-touch page faults.  One batch creation packs at a time per
+  // context.
+  struct PackCache {
+    std::mutex mu;
+    std::vector<ArcsPack> parts;
+  };
+  if (!ctx->arcs_host_cache) ctx->arcs_host_cache = std::make_shared<PackCache>();
+  PackCache &cache = *static_cast<PackCache *>(ctx->arcs_host_cache.get());
+  std::lock_guard<std::mutex> pack_lock(cache.mu);
+  std::vector<ArcsPack> &parts = cache.parts;
+  parts.resize((n_units + per - 1) / per);
+  for (ArcsPack &q : parts) q.clear();
   parallel([&](int a, int z) {
     ArcsPack &q = parts[a / per];
     size_t beads = 0, entries = 0;

@@ -102,6 +102,8 @@ struct ArcsPack {
   void append(const ArcsPack &o);
   // Placeholder entries so that no device array is empty.
   void finish();
+  // Empties the pack, keeping every array's capacity.
+  void clear();
 };
 
 // Shared-memory bytes of one chain's slice: everything staged / positions only.

@@ -7,6 +7,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <string>
 #include <vector>
 
@@ -14,6 +15,9 @@
 
 struct pmmc_ctx {
   int device = 0;
+  // host-side state a module keeps per context (e.g. packing buffers that
+  // are reused, already paged in, by the next call)
+  std::shared_ptr<void> arcs_host_cache;
   int sm_count = 0;
   size_t smem_optin = 0;       // max dynamic shared memory per block (opt-in)
   size_t smem_per_sm = 0;
