@@ -818,7 +818,9 @@ arcs_base_kernel(const ArcsUnit *__restrict__ units, int n_units,
   const int2 *NB = nbr + U.nbr_off;
   const int n = U.n;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
-  double acc = 0.0;
+  // per-lane float-float accumulation (~48 bits): FP64 arithmetic is a
+  // narrow pipe on this part and a double add per row kept it 85 % busy
+  float hi = 0.0f, lo = 0.0f;
   for (int i = warp; i < n; i += nw) {
     const float4 pi = P[i];
     float part = 0.0f;
@@ -828,23 +830,23 @@ arcs_base_kernel(const ArcsUnit *__restrict__ units, int n_units,
       const float x = pi.x - pj.x, y = pi.y - pj.y, z = pi.z - pj.z;
       part += rsqrtf(fmaf(x, x, fmaf(y, y, z * z)));
       if (++cnt == 64) {
-        acc += part;
+        ff_add(hi, lo, part);
         part = 0.0f;
         cnt = 0;
       }
     }
-    acc += part;
+    ff_add(hi, lo, part);
     const int e1 = rp[i + 1];
     for (int e = rp[i] + lane; e < e1; e += 32) {
       const int j = NB[e].x;
-      if (j < i) acc -= (double)(1.0f / dist3(P[j].x, P[j].y, P[j].z, pi));
+      if (j < i) ff_add(hi, lo, -(1.0f / dist3(P[j].x, P[j].y, P[j].z, pi)));
     }
   }
   for (int c = threadIdx.x; c < U.n_null; c += blockDim.x) {
     const int2 q = nulls[U.null_off + c];
-    acc -= (double)(1.0f / dist3(P[q.x].x, P[q.x].y, P[q.x].z, P[q.y]));
+    ff_add(hi, lo, -(1.0f / dist3(P[q.x].x, P[q.x].y, P[q.x].z, P[q.y])));
   }
-  acc = warp_sum_d(acc);
+  double acc = warp_sum_d((double)hi + (double)lo);
   if (lane == 0) red[warp] = acc;
   __syncthreads();
   if (threadIdx.x == 0) {
