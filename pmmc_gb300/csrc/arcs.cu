@@ -13,19 +13,29 @@
 //   same definition.
 //
 // Layout in device memory: beads as float4 (16 B, one vector load), per-bead
-// arc lists as CSR with {col, target} packed in one int2 (8 B).  A chain is
-// one warp: the region's positions and arc lists are staged in the warp's
-// slice of shared memory (arc lists fall back to L1-cached global loads when
-// the region is too large), the Philox draws of 32 moves are made at once
-// (lane l draws move m+l: bead, displacement and the precomputed Metropolis
-// ratio threshold), and each move evaluates the moved bead's arcs with one
-// lane per arc and an xor-butterfly as wide as the bead's degree.  Lane 0
-// takes the decision and owns the chain state; the running energy is kept in
-// FP64, the per-move delta in FP32.
+// arc lists as CSR with {col, target} packed in one int2 (8 B) and 1/target
+// beside it.  A chain is one warp: the region's positions and arc lists are
+// staged in the warp's slice of shared memory (arc lists fall back to
+// L1-cached global loads when the region is too large).  Proposals come from
+// a counter-based Philox stream (move m: bead, displacement and the
+// precomputed Metropolis ratio threshold), drawn 32 at a time into a
+// 128-move ring -- by the chain's own warp, or by a second "drawing" warp
+// that stays ahead of it.  The chain scores W = 32/G proposals at once (G
+// lanes each) against the positions at the window's start and resolves them
+// in order (downhill slots at once, uphill slots by a warp prefix sum of the
+// accepted changes); the window ends at the first slot whose bead or
+// partner an accepted earlier slot moved (a per-bead slot mask in shared
+// memory finds those), so the accepted sequence is the one-move-at-a-time
+// one.  The per-move delta is FP32, the running total a float-float pair
+// refreshed by an energy recompute every `resync` moves, and the milestones
+// and the end-of-chain recompute are FP64.
 //
-// Work distribution: persistent warps pull (unit, chain) items from an atomic
-// queue (largest regions first), one launch per shared-memory size class, the
-// classes on forked streams and the whole pass captured in a CUDA graph.
+// Work distribution: persistent warps (or warp pairs) pull (unit, chain)
+// items from an atomic queue, largest regions first, one launch per
+// shared-memory size class; the classes run on forked streams and the whole
+// pass is captured in a CUDA graph.  An autotuner picks each class's lanes
+// per proposal, chains per CTA and drawing warp; the classes whose regions
+// set the pass's length take the lowest-latency configuration.
 #include <algorithm>
 #include <climits>
 #include <cmath>
