@@ -12,9 +12,11 @@
 //            regions of one shared-memory class, in arrival order, while the
 //            device bytes of everything resident stay within the budget and a
 //            launch slot is free.  The wave's inputs go up in one copy from a
-//            pinned staging buffer, one persistent launch anneals all of its
-//            regions (one warp per region, work-stealing), and the results
-//            come back in one copy, all on the slot's own stream.
+//            pinned staging buffer, the frozen repulsion of its regions is
+//            computed (one block each), one persistent launch anneals all of
+//            them (one warp per region, plus a drawing warp for one-lane
+//            regions; work-stealing), and the results come back in one copy,
+//            all on the slot's own stream.
 //   overlap  up to max_waves waves are in flight at once on separate streams,
 //            so regions that arrive while others run start as soon as a slot
 //            and memory free up, without waiting for the running waves.
