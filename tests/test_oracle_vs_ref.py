@@ -54,3 +54,35 @@ def test_mark_arcs_random():
                     int(rng.integers(1, 9)), int(rng.integers(0, 4))])
     raw = np.array(raw, np.int32)
     np.testing.assert_array_equal(O.mark_arcs(anchors, raw), O.ref_mark_arcs(anchors, raw))
+
+
+@pytest.mark.parametrize("kw", [
+    dict(n_anchors=400, n_active=300, active_from=60, n_long=6000, seed=71, outside_arcs=20,
+         duplicate_arcs=20),
+    dict(n_anchors=250, n_long=4000, seed=72, heat=True, count=(-0.6, 4.0, 0.5, 0.2),
+         influence=0.8),
+    dict(n_anchors=150, n_long=3000, seed=73, count=(0.4, 15.0, 1.0, -0.01)),
+])
+def test_anchor_targets_random(kw):
+    """calcAnchorExpectedDistancesHeatmap on fresh inputs: the dense matrix
+    and the long-arc counters."""
+    t = synth.anchor_targets_problem(**kw)
+    d1, s1 = O.ref_anchor_targets(t)
+    d2, s2 = O.anchor_targets(t)
+    assert s1 == s2
+    np.testing.assert_array_equal(d1.view(np.uint32), d2.view(np.uint32))
+
+
+@pytest.mark.parametrize("kw,it,lr", [
+    (dict(n_anchors=160, n_long=2500, seed=74, springs=(0.1, 0.1, 0.0)), 400, 0.05),
+    (dict(n_anchors=120, n_long=2000, seed=75, springs=(0.2, 0.05, 0.1)), 150, 0.03),
+    (dict(n_anchors=90, n_long=1500, seed=76, springs=(0.0, 0.0, 0.0)), 300, 0.1),
+])
+def test_stress_refine_random(kw, it, lr):
+    """stressRefineAnchors on fresh inputs: sorted region and positions
+    (this host's libm acosf on both sides)."""
+    t = synth.stress_problem(**kw)
+    o1, x1 = O.ref_stress_refine(t, it, lr)
+    o2, x2, _ = O.stress_refine(t, it, lr)
+    np.testing.assert_array_equal(o1, o2)
+    np.testing.assert_array_equal(x1.view(np.uint32), x2.view(np.uint32))
