@@ -498,11 +498,8 @@ extern "C" pmmc_status pmmc_stress_refine(pmmc_ctx *ctx, const pmmc_stress_probl
   cudaFuncAttributes fa{};
   cudaFuncGetAttributes(&fa, stress_kernel);
   const size_t dyn_max = ctx->smem_optin > fa.sharedSizeBytes ? ctx->smem_optin - fa.sharedSizeBytes : 0;
-  static size_t attr_set = 0;
-  if (attr_set != dyn_max) {
-    cudaFuncSetAttribute(stress_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn_max);
-    attr_set = dyn_max;
-  }
+  // set on every call: the attribute belongs to the current device
+  cudaFuncSetAttribute(stress_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dyn_max);
   const size_t smem = sizeof(float4) * (size_t)n;
   const int staged = smem <= dyn_max ? 1 : 0;
   int per_sm = 0;

@@ -615,12 +615,9 @@ extern "C" pmmc_status pmmc_anchor_targets(pmmc_ctx *ctx, const pmmc_anchor_targ
     // starts and buckets in shared memory up to 96 KB, else through L1/L2
     const size_t smem = 4 * ((size_t)pr->n_anchors + (size_t)nb);
     if (sorted && smem <= 96 * 1024) {
-      static bool attr = false;
-      if (!attr) {
-        cudaFuncSetAttribute(long_map<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             96 * 1024);
-        attr = true;
-      }
+      // set on every call: the attribute belongs to the current device
+      cudaFuncSetAttribute(long_map<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           96 * 1024);
       int per_sm = 0;
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, long_map<true>, T, smem);
       const int grid = (int)std::min<long long>((n_long + T - 1) / T,
