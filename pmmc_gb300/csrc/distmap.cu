@@ -55,16 +55,30 @@ struct DistPartial {
   int pad;
 };
 
-// Tile (bi = blockIdx.y, bj = blockIdx.x) of the upper triangle; blocks below
-// the diagonal exit at once.
+// Upper-triangle tile t (row by row, bi <= bj) as (bi, bj): row b holds
+// nt - b tiles and starts at b*nt - b*(b-1)/2.  The grids launch only these
+// tiles (a square grid would schedule as many blocks below the diagonal that
+// do nothing).
+__device__ __forceinline__ int2 upper_tile(long long t, int nt) {
+  const double a = 2.0 * nt + 1.0;
+  int b = (int)((a - sqrt(a * a - 8.0 * (double)t)) * 0.5);
+  auto start = [nt](long long r) { return r * nt - r * (r - 1) / 2; };
+  if (b < 0) b = 0;
+  if (b > nt - 1) b = nt - 1;
+  while (b > 0 && start(b) > t) --b;
+  while (b + 1 < nt && start(b + 1) <= t) ++b;
+  return make_int2(b, b + (int)(t - start(b)));
+}
+
+// Tile blockIdx.x of the upper triangle; its partial goes to part[blockIdx.x].
 __global__ void __launch_bounds__(kTile * kRows)
 distmap_pass1(const float *__restrict__ c, int n, int nt, int diag, float scale, float power,
               DistPartial *__restrict__ part, float *__restrict__ dist) {
   __shared__ double s_sum[kTile * kRows / 32];
   __shared__ long long s_neg[kTile * kRows / 32];
   __shared__ int s_min[kTile * kRows / 32];
-  const int bi = blockIdx.y, bj = blockIdx.x;
-  if (bj < bi) return;
+  const int2 tb = upper_tile(blockIdx.x, nt);
+  const int bi = tb.x, bj = tb.y;
   const int tx = threadIdx.x % kTile, ty = threadIdx.x / kTile;
   const int j = bj * kTile + tx;
   float sum = 0.0f;   // at most 16 terms per thread; widened to FP64 below
@@ -102,26 +116,23 @@ distmap_pass1(const float *__restrict__ c, int n, int nt, int diag, float scale,
       p.n_neg += s_neg[k];
       p.min_off = min(p.min_off, s_min[k]);
     }
-    part[(size_t)bi * nt + bj] = p;
+    part[blockIdx.x] = p;
   }
 }
 
-// One block: the partials of the upper-triangle tiles in index order,
+// One block: the partials of the upper-triangle tiles (thread t takes every
+// blockDim-th one from t, then a fixed-order combination: deterministic),
 // avg = Heatmap::getAvg of the map and the clamp value.
 __global__ void distmap_finish(const DistPartial *__restrict__ part, int nt, int n,
                                float stretching, float *__restrict__ out2) {
   __shared__ double s_sum[32];
   __shared__ long long s_neg[32];
   __shared__ int s_min[32];
-  const long long total = (long long)nt * nt;
+  const long long total = (long long)nt * (nt + 1) / 2;
   double sum = 0.0;
   long long neg = 0;
   int mo = 0x7fffffff;
-  // each thread a contiguous chunk, then a fixed-order combination
-  const long long per = (total + blockDim.x - 1) / blockDim.x;
-  const long long k0 = (long long)threadIdx.x * per, k1 = min(total, k0 + per);
-  for (long long k = k0; k < k1; ++k) {
-    if ((int)(k % nt) < (int)(k / nt)) continue;  // below the diagonal: no tile
+  for (long long k = threadIdx.x; k < total; k += blockDim.x) {
     sum += part[k].sum_pos;
     neg += part[k].n_neg;
     mo = min(mo, part[k].min_off);
@@ -162,10 +173,10 @@ __global__ void distmap_finish(const DistPartial *__restrict__ part, int nt, int
 }
 
 __global__ void __launch_bounds__(kTile * kRows)
-distmap_pass2(int n, const float *__restrict__ stats, float *__restrict__ dist) {
+distmap_pass2(int n, int nt, const float *__restrict__ stats, float *__restrict__ dist) {
   __shared__ float tile[kTile][kTile + 1];
-  const int bi = blockIdx.y, bj = blockIdx.x;
-  if (bj < bi) return;
+  const int2 tb = upper_tile(blockIdx.x, nt);
+  const int bi = tb.x, bj = tb.y;
   const float maxd = stats[1];
   const int tx = threadIdx.x % kTile, ty = threadIdx.x / kTile;
   const int j = bj * kTile + tx;
@@ -205,9 +216,11 @@ pmmc_status distmap_run(pmmc_ctx *ctx, int n, const float *d_c, int diag, float 
                         cudaStream_t s) {
   const int nt = (n + kTile - 1) / kTile;
   if (nt > 65535) return fail(ctx, PMMC_ERR_INVALID, "distance heatmap: n too large");
+  // (nt x (nt + 1) / 2 tiles stay below the 2^31 - 1 blocks of a 1-D grid)
   DistPartial *d_part = nullptr;
-  PMMC_CUDA(ctx, cudaMallocAsync(&d_part, sizeof(DistPartial) * (size_t)nt * nt, s));
-  const dim3 grid(nt, nt);
+  const long long tiles = (long long)nt * (nt + 1) / 2;
+  PMMC_CUDA(ctx, cudaMallocAsync(&d_part, sizeof(DistPartial) * (size_t)tiles, s));
+  const unsigned grid = (unsigned)tiles;
   distmap_pass1<<<grid, kTile * kRows, 0, s>>>(d_c, n, nt, diag, scale, power, d_part, d_dist);
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess) {
@@ -215,7 +228,7 @@ pmmc_status distmap_run(pmmc_ctx *ctx, int n, const float *d_c, int diag, float 
     e = cudaGetLastError();
   }
   if (e == cudaSuccess) {
-    distmap_pass2<<<grid, kTile * kRows, 0, s>>>(n, d_stats, d_dist);
+    distmap_pass2<<<grid, kTile * kRows, 0, s>>>(n, nt, d_stats, d_dist);
     e = cudaGetLastError();
   }
   cudaFreeAsync(d_part, s);
