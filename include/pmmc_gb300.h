@@ -35,7 +35,8 @@ typedef enum pmmc_status {
   PMMC_ERR_BUDGET = 6,    /* request exceeds the device-memory budget    */
   PMMC_ERR_FIXED = 7,     /* arc level: every bead is fixed              */
   PMMC_ERR_BUSY = 8,      /* server: no free slot right now              */
-  PMMC_ERR_NOT_FOUND = 9  /* server: unknown request id                  */
+  PMMC_ERR_NOT_FOUND = 9, /* server: unknown request id                  */
+  PMMC_ERR_CANCELLED = 10 /* server: the request was cancelled            */
 } pmmc_status;
 
 /* Stopping schedule of a chain. */
@@ -558,6 +559,10 @@ pmmc_status pmmc_server_poll(pmmc_server *sv, long long ticket, int *done);
 pmmc_status pmmc_server_wait(pmmc_server *sv, long long ticket, int timeout_ms,
                              float *pos_out, pmmc_result *res, double *latency_ms);
 pmmc_status pmmc_server_get_stats(pmmc_server *sv, pmmc_server_stats *st);
+/* Withdraws a request that is still queued: its wait then returns
+ * PMMC_ERR_CANCELLED at once.  A request already admitted to a wave runs to
+ * its end (PMMC_ERR_BUSY); an unknown ticket gives PMMC_ERR_NOT_FOUND. */
+pmmc_status pmmc_server_cancel(pmmc_server *sv, long long ticket);
 /* Finishes every queued and running region, then frees the server. */
 void pmmc_server_destroy(pmmc_server *sv);
 

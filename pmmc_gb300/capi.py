@@ -25,6 +25,7 @@ PMMC_ERR_BUDGET = 6
 PMMC_ERR_FIXED = 7
 PMMC_ERR_BUSY = 8
 PMMC_ERR_NOT_FOUND = 9
+PMMC_ERR_CANCELLED = 10
 
 SCHEDULE_GPU = 0
 SCHEDULE_CPU = 1
@@ -43,6 +44,7 @@ HEADER_SYMBOLS = [
     "pmmc_server_get_stats", "pmmc_server_destroy", "pmmc_arcs_batch_classes",
     "pmmc_selftest_sqrt", "pmmc_distance_heatmap", "pmmc_distance_heatmap_device",
     "pmmc_equidistant_model", "pmmc_hcm_write", "pmmc_anchor_targets", "pmmc_stress_refine",
+    "pmmc_server_cancel",
 ]
 
 LANES_AUTO = -1  # PMMC_LANES_AUTO: the autotuner picks lanes and warps per class
@@ -426,6 +428,10 @@ class Server:
                                               _p(pos), C.byref(res), C.byref(lat)))
         self._n.pop(ticket, None)
         return pos, res, lat.value
+
+    def cancel(self, ticket: int) -> int:
+        """pmmc_server_cancel: the status (0 = withdrawn while queued)."""
+        return int(lib().pmmc_server_cancel(self.h, C.c_longlong(ticket)))
 
     def stats(self) -> dict:
         st = ServerStats()

@@ -18,6 +18,7 @@ extern "C" const char *pmmc_status_string(pmmc_status s) {
     case PMMC_ERR_FIXED: return "every bead is fixed";
     case PMMC_ERR_BUSY: return "no free slot";
     case PMMC_ERR_NOT_FOUND: return "unknown request";
+    case PMMC_ERR_CANCELLED: return "request cancelled";
   }
   return "unknown status";
 }

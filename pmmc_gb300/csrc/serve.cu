@@ -89,7 +89,7 @@ BlobLayout layout_of(const ArcsPack &pk) {
   return L;
 }
 
-enum class ReqState { Queued, Running, Done, Failed };
+enum class ReqState { Queued, Running, Done, Failed, Cancelled };
 
 struct Request {
   long long ticket = 0;
@@ -447,7 +447,25 @@ extern "C" pmmc_status pmmc_server_poll(pmmc_server *sv, long long ticket, int *
   auto it = sv->table.find(ticket);
   if (it == sv->table.end()) return PMMC_ERR_NOT_FOUND;
   const ReqState s = it->second->state;
-  *done = (s == ReqState::Done || s == ReqState::Failed) ? 1 : 0;
+  *done = (s == ReqState::Done || s == ReqState::Failed || s == ReqState::Cancelled) ? 1 : 0;
+  return PMMC_OK;
+}
+
+extern "C" pmmc_status pmmc_server_cancel(pmmc_server *sv, long long ticket) {
+  if (!sv) return PMMC_ERR_INVALID;
+  std::lock_guard<std::mutex> lock(sv->mu);
+  auto it = sv->table.find(ticket);
+  if (it == sv->table.end()) return PMMC_ERR_NOT_FOUND;
+  ReqPtr r = it->second;
+  if (r->state != ReqState::Queued) return PMMC_ERR_BUSY;
+  for (auto q = sv->queue.begin(); q != sv->queue.end(); ++q)
+    if (q->get() == r.get()) {
+      sv->queue.erase(q);
+      break;
+    }
+  r->state = ReqState::Cancelled;
+  r->t_done = Clock::now();
+  sv->cv_done.notify_all();
   return PMMC_OK;
 }
 
@@ -458,7 +476,10 @@ extern "C" pmmc_status pmmc_server_wait(pmmc_server *sv, long long ticket, int t
   auto it = sv->table.find(ticket);
   if (it == sv->table.end()) return PMMC_ERR_NOT_FOUND;
   ReqPtr r = it->second;
-  auto ready = [&] { return r->state == ReqState::Done || r->state == ReqState::Failed; };
+  auto ready = [&] {
+    return r->state == ReqState::Done || r->state == ReqState::Failed ||
+           r->state == ReqState::Cancelled;
+  };
   if (timeout_ms < 0) {
     sv->cv_done.wait(lock, ready);
   } else if (!sv->cv_done.wait_for(lock, std::chrono::milliseconds(timeout_ms), ready)) {
@@ -466,6 +487,8 @@ extern "C" pmmc_status pmmc_server_wait(pmmc_server *sv, long long ticket, int t
   }
   sv->table.erase(ticket);
   lock.unlock();
+  if (r->state == ReqState::Cancelled)
+    return fail(sv->ctx, PMMC_ERR_CANCELLED, "server: request %lld was cancelled", ticket);
   if (r->state == ReqState::Failed)
     return fail(sv->ctx, r->error, "server: request %lld failed on the device", ticket);
   if (pos_out) memcpy(pos_out, r->pos_out.data(), sizeof(float) * r->pos_out.size());

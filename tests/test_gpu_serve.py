@@ -109,3 +109,28 @@ def test_server_wait_timeout_and_unknown_ticket(ctx):
         sv.wait(t)
     assert e.value.status == capi.PMMC_ERR_NOT_FOUND
     sv.close()
+
+
+def test_server_cancel_queued_request(ctx):
+    """A request withdrawn while queued comes back cancelled at once; the
+    others run as they would have, and the withdrawn one leaves no trace.
+    One wave of one region at a time keeps the later requests queued."""
+    _, inputs = regions()
+    prm = capi.default_params(capi.LEVEL_ARCS, schedule=capi.SCHEDULE_CPU, max_moves=200_000,
+                              **BASE)
+    sv = capi.Server(ctx, prm, max_waves=1, max_wave_requests=1)
+    tickets = [sv.submit(inputs[k], 0.5, 50 + k) for k in (7, 1, 5, 3)]
+    last = tickets[-1]
+    assert sv.cancel(last) == 0            # still behind the first three
+    assert sv.poll(last)
+    with pytest.raises(capi.PmmcError) as e:
+        sv.wait(last)
+    assert e.value.status == capi.PMMC_ERR_CANCELLED
+    assert sv.cancel(last) == capi.PMMC_ERR_NOT_FOUND   # already collected
+    for t in tickets[:-1]:
+        pos, res, _ = sv.wait(t)
+        assert res.status == 0 and np.isfinite(pos).all()
+        assert sv.cancel(t) == capi.PMMC_ERR_NOT_FOUND
+    st = sv.stats()
+    assert st["queued"] == 0
+    sv.close()
