@@ -370,7 +370,15 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
       // the chain has used the moves that held those slots ----
       const int *MOVp = has_mov ? (mov_smem ? smov : movable + U.mov_off) : nullptr;
       pair_sync(slot_w);  // staging done (the movable list may be in shared memory)
-      if (U.n_mov > 0) {
+      if (P.stall_draws) {
+        // nothing is drawn: wait (bounded) for the chain to give up
+        if (lane == 0) {
+          const unsigned long long t0 = globaltimer_ns();
+          while (*(volatile int *)&ctl->state == 0 && globaltimer_ns() - t0 < 2 * kPairWaitNs)
+            __nanosleep(1000);
+        }
+        __syncwarp();
+      } else if (U.n_mov > 0) {
         double Tp = P.max_temp;
         const float step = U.step;
         int4 *s_mv = reinterpret_cast<int4 *>(wbase);
@@ -1479,6 +1487,9 @@ extern "C" pmmc_status pmmc_arcs_batch_create_ex(
   b->use_graph = !opts || opts->use_graph != 0;
   b->P = arcs_make_params(prm, next_key(ctx), stop_all != 0);
   b->P.trace_cap = trace_cap;
+  // tests only: the wait of a chain on its drawing warp runs out (no fault,
+  // no hang: both sides give up after their 2 s limit)
+  b->P.stall_draws = getenv("PMMC_TEST_STALL_DRAWS") != nullptr ? 1 : 0;
 
   // ---- pack host arrays (unit u's chains have global ids u*chains...) ----
   // Each host thread packs a contiguous range of units into its own part;

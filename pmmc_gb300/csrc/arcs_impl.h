@@ -53,6 +53,8 @@ struct ArcsDevParams {
   int use2d;
   int stop_all;    // the first converged chain stops the unit's others
   int trace_cap;
+  int stall_draws; // tests only: drawing warps never publish (the chain's
+                   // bounded wait runs out and it ends with status 3)
   long long cap;   // hard move cap
   int cap_is_error;
   int pad;

@@ -285,3 +285,31 @@ def test_plain_call_with_one_chain_matches_the_single_warp_batch(ctx):
     assert res.status == 0 and bres[0].status == 0
     assert (res.moves, res.energy) == (bres[0].moves, bres[0].energy)
     np.testing.assert_array_equal(pos, bpos[0])
+
+
+def test_arcs_drawing_warp_wait_runs_out(ctx, monkeypatch):
+    """The chain's wait on its drawing warp is bounded: with the drawing warp
+    told never to publish (a test-only switch), the chain gives up after its
+    2 s limit with status 3 and no move, nothing faults or hangs, and the
+    context runs the next batch normally."""
+    import time
+    r = synth.arcs_region(100, 150, seed=5)
+    inp = capi.ArcsInput.from_dense(r.pos, r.dense())
+    prm = capi.default_params(capi.LEVEL_ARCS, schedule=capi.SCHEDULE_CPU, max_moves=5000,
+                              max_temp=5.0, dt_temp=0.9999, milestone_steps=1000,
+                              improvement=0.99)
+    monkeypatch.setenv("PMMC_TEST_STALL_DRAWS", "1")
+    b = capi.ArcsBatch(ctx, [inp], prm, [0.5], use_graph=False, lanes=1, drawing_warp=True)
+    monkeypatch.delenv("PMMC_TEST_STALL_DRAWS")
+    t0 = time.time()
+    b.run()
+    _, res = b.results()
+    dt = time.time() - t0
+    b.close()
+    assert res[0].status == 3 and res[0].moves == 0
+    assert 1.5 < dt < 20
+    b2 = capi.ArcsBatch(ctx, [inp], prm, [0.5], use_graph=False, lanes=1, drawing_warp=True)
+    b2.run()
+    _, res2 = b2.results()
+    b2.close()
+    assert res2[0].status == 0 and res2[0].moves > 0
