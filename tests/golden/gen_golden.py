@@ -294,6 +294,65 @@ def stress_cases():
     return out
 
 
+def edge_cases():
+    """The smallest and degenerate regions the reference's CPU annealers
+    still finish on: a 2-bead region with one arc, a 3-bead region, a region
+    without arcs (repulsion only), heatmap regions with one to five free
+    beads and a diagonal band wider than most of the map, and smoothing
+    chains of three and four beads (ends fixed).  Regions whose beads are all
+    fixed are left out: the reference redraws a bead until a free one comes
+    up and never returns on them."""
+    out = {}
+    for k, (n, arcs, seed) in enumerate([(2, 1, 9), (3, 2, 9), (16, 0, 9), (5, 3, 9)]):
+        r = synth.arcs_region(n, max(arcs, 1), seed=seed)
+        dense = r.dense()
+        if arcs == 0:
+            dense[:] = -1.0
+        z = np.zeros(0, np.int32)
+        zf = np.zeros(0, np.float32)
+        pr = O.ArcsProblem(r.pos, dense, None, z, z, zf, zf)
+        prm = O.Params(max_temp=5.0, dt_temp=0.9999, milestone_steps=500, improvement=0.99)
+        beads = np.arange(n, dtype=np.int32)
+        pos, score, moves = O.ref_arcs_anneal(pr, prm, 0.5, 77 + k)
+        out[f"edge_arcs{k}"] = dict(
+            pos=r.pos, dense=dense, li=z, lj=z, lk=zf, lr=zf, params=params_array(prm),
+            beads=beads, local=np.array([O.ref_arcs_score(pr, prm, int(b)) for b in beads]),
+            full=np.array([O.ref_arcs_score(pr, prm, -1)]), step=np.array([0.5]),
+            seed=np.array([77 + k]), out_pos=pos, out_score=np.array([score]),
+            out_moves=np.array([moves]))
+    for k, (n, diag, n_free) in enumerate([(4, 1, 3), (8, 3, 2), (6, 1, 5)]):
+        h = synth.heatmap_region(n, seed=11, n_tads=1, tad_min=2, tad_max=3)
+        fixed = np.ones(n, np.uint8)
+        fixed[1:1 + n_free] = 0
+        pr = O.HeatmapProblem(h.pos, h.heat, diag, np.zeros(0, np.int32), fixed)
+        prm = O.Params(max_temp=5.0, dt_temp=0.9999, milestone_steps=300, improvement=0.99)
+        beads = np.arange(n, dtype=np.int32)
+        pos, score, moves = O.ref_heatmap_anneal(pr, prm, 1.0, 5 + k)
+        out[f"edge_heatmap{k}"] = dict(
+            pos=h.pos, heat=h.heat, diag=np.array([diag]), bounds=np.zeros(0, np.int32),
+            fixed=fixed, params=params_array(prm), beads=beads,
+            local=np.array([O.ref_heatmap_score(pr, int(b)) for b in beads]),
+            full=np.array([O.ref_heatmap_score(pr, -1)]), step=np.array([1.0]),
+            seed=np.array([5 + k]), out_pos=pos, out_score=np.array([score]),
+            out_moves=np.array([moves]))
+    for k, (n, sphere) in enumerate([(3, 0.0), (4, 2.0)]):
+        c = synth.smooth_chain(n, seed=12)
+        dtn = c.dist_to_next.copy()
+        pr = O.SmoothProblem(c.pos, dtn, c.fixed)
+        prm = O.Params(max_temp=5.0, dt_temp=0.9999, milestone_steps=300, improvement=0.99,
+                       k_stretch=0.1, k_squeeze=0.1, k_angle=0.1, w_dist=1.0, w_angle=1.0,
+                       sphere_radius=sphere)
+        beads = np.arange(n, dtype=np.int32)
+        pos, score, moves = O.ref_smooth_anneal(pr, prm, 0.5, 6 + k)
+        out[f"edge_smooth{k}"] = dict(
+            pos=c.pos, dtn=dtn, fixed=c.fixed, params=params_array(prm), beads=beads,
+            local=np.array([O.ref_smooth_score(pr, prm, int(b)) for b in beads]),
+            full=np.array([O.ref_smooth_score(pr, prm, -1)]), step=np.array([0.5]),
+            seed=np.array([6 + k]), out_pos=pos, out_score=np.array([score]),
+            out_moves=np.array([moves]))
+    return out
+
+
 def main():
     if not O.ref_available():
         O.build()
@@ -304,7 +363,7 @@ def main():
               "equi": equi_cases,
               "heatmap": heatmap_cases,
               "smooth": smooth_cases, "mark": mark_cases, "hcm": hcm_cases,
-              "targets": target_cases, "stress": stress_cases}
+              "targets": target_cases, "stress": stress_cases, "edge": edge_cases}
     want = sys.argv[1:] or list(groups) + ["rng"]
     fixtures = {}
     for g in want:

@@ -48,7 +48,8 @@ def test_random_vector_draw_order():
         np.testing.assert_array_equal(np.array(vals, np.float32), g[key])
 
 
-@pytest.mark.parametrize("case", ["arcs0", "arcs1", "arcs2"])
+@pytest.mark.parametrize("case", ["arcs0", "arcs1", "arcs2", "edge_arcs0", "edge_arcs1",
+                                  "edge_arcs2", "edge_arcs3"])
 def test_arcs_scores_and_anneal(case):
     g = load(case)
     pr = O.ArcsProblem(g["pos"], g["dense"], None, g["li"], g["lj"], g["lk"], g["lr"])
@@ -79,7 +80,8 @@ def test_extended_arc_energy_terms(case):
         assert O.arcs_ext_score(n, g["pos"], both, int(b)) == wa
 
 
-@pytest.mark.parametrize("case", ["heatmap0", "heatmap1"])
+@pytest.mark.parametrize("case", ["heatmap0", "heatmap1", "edge_heatmap0", "edge_heatmap1",
+                                  "edge_heatmap2"])
 def test_heatmap_scores_and_anneal(case):
     g = load(case)
     pr = O.HeatmapProblem(g["pos"], g["heat"], int(g["diag"][0]), g["bounds"], g["fixed"])
@@ -93,7 +95,7 @@ def test_heatmap_scores_and_anneal(case):
     np.testing.assert_array_equal(pos, g["out_pos"])
 
 
-@pytest.mark.parametrize("case", ["smooth0", "smooth1"])
+@pytest.mark.parametrize("case", ["smooth0", "smooth1", "edge_smooth0", "edge_smooth1"])
 def test_smooth_scores_and_anneal(case):
     g = load(case)
     pr = O.SmoothProblem(g["pos"], g["dtn"], g["fixed"])
@@ -105,6 +107,35 @@ def test_smooth_scores_and_anneal(case):
     assert res.moves == g["out_moves"][0]
     assert res.score == g["out_score"][0]
     np.testing.assert_array_equal(pos, g["out_pos"])
+
+
+def test_all_fixed_regions_make_no_move():
+    """A region without a free bead: the reference's CPU annealers redraw a
+    bead until a free one comes up and never return; the Philox-mode
+    annealers (and the kernels) draw among the movable beads only, so they
+    make no move and return the start.  The heatmap level reports 0 there,
+    as it does for a start score below 1e-6."""
+    from pmmc_gb300 import synth
+    prm = O.Params(max_temp=5.0, dt_temp=0.9999, milestone_steps=300, improvement=0.99,
+                   k_stretch=0.1, k_squeeze=0.1, k_angle=0.1, w_dist=1.0, w_angle=1.0)
+    r = synth.arcs_region(8, 6, seed=9)
+    z = np.zeros(0, np.int32)
+    zf = np.zeros(0, np.float32)
+    pr = O.ArcsProblem(r.pos, r.dense(), np.ones(8, np.uint8), z, z, zf, zf)
+    pos, res = O.arcs_anneal(pr, prm, 0.5, 5, rng=O.RNG_PHILOX)
+    assert res.moves == 0 and res.score == O.arcs_full(pr, prm)
+    np.testing.assert_array_equal(pos, r.pos)
+    h = synth.heatmap_region(6, seed=11, n_tads=1, tad_min=2, tad_max=3)
+    pr = O.HeatmapProblem(h.pos, h.heat, 1, z, np.ones(6, np.uint8))
+    pos, res = O.heatmap_anneal(pr, prm, 1.0, 5, rng=O.RNG_PHILOX)
+    assert res.moves == 0 and res.score == 0.0
+    np.testing.assert_array_equal(pos, h.pos)
+    c = synth.smooth_chain(2, seed=12)
+    assert c.fixed.all()
+    pr = O.SmoothProblem(c.pos, c.dist_to_next.copy(), c.fixed)
+    pos, res = O.smooth_anneal(pr, prm, 0.5, 6, rng=O.RNG_PHILOX)
+    assert res.moves == 0 and res.score == O.smooth_full(pr, prm)
+    np.testing.assert_array_equal(pos, c.pos)
 
 
 def test_mark_arcs():
