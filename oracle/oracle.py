@@ -528,6 +528,39 @@ def heatmap_replay(pr: HeatmapProblem, prm: Params, step: float, seed: int, chai
     return _replay_result(out, keep)
 
 
+def _ref_walk(level: int, n: int, pos, prm: Params, trace, matrix=None, diag: int = 0,
+              bounds=None, dtn=None, pr_loops=None):
+    m, bead, disp, acc, out, keep = _replay_prep(trace)
+    before, after = keep[3], keep[4]
+    mat = _f32(matrix) if matrix is not None else None
+    b = _i32(bounds if bounds is not None else np.zeros(0, np.int32))
+    d = _f64(dtn) if dtn is not None else None
+    if pr_loops is not None:
+        la, lkeep = _loops(pr_loops)
+    else:
+        la = (0, None, None, None, None)
+    ref().ref_local_walk(level, n, _p(_f32(pos)), _p(mat) if mat is not None else None,
+                         int(diag), len(b), _p(b), _p(d) if d is not None else None, *la,
+                         C.byref(prm.c()), m, _p(bead), _p(disp), _p(acc), _p(before),
+                         _p(after))
+    return {"before": before, "after": after}
+
+
+def ref_arcs_walk(pr: ArcsProblem, prm: Params, trace):
+    """The reference's per-proposal local arc energy along a scripted walk
+    (`trace`: bead, dx, dy, dz, accepted), before and after each move."""
+    return _ref_walk(0, pr.n, pr.pos, prm, trace, matrix=pr.exp_dist, pr_loops=pr)
+
+
+def ref_heatmap_walk(pr: HeatmapProblem, prm: Params, trace):
+    return _ref_walk(1, pr.n, pr.pos, prm, trace, matrix=pr.heat, diag=pr.diag,
+                     bounds=pr.bounds)
+
+
+def ref_smooth_walk(pr: SmoothProblem, prm: Params, trace):
+    return _ref_walk(2, pr.n, pr.pos, prm, trace, dtn=pr.dist_to_next)
+
+
 def ref_random_vectors(seed: int, count: int, max_size: float = 1.0, in2d: bool = False):
     out = np.zeros((count, 3), np.float32)
     ref().ref_random_vectors(C.c_uint(seed), count, C.c_float(max_size), int(in2d), _p(out))

@@ -293,6 +293,59 @@ double ref_smooth_score(int n, const float *pos, const double *dtn,
   return sc;
 }
 
+/* Scores a scripted walk with the reference's local energy functions, the
+ * ones its annealers evaluate per proposal.  Move k: before[k] = local score
+ * of bead[k]; the bead moves by disp[3k..3k+2] (vector3 float addition, as
+ * in the annealers); after[k] = local score again; the move stays when
+ * acc[k] != 0, else the saved position comes back.  One solver is set up per
+ * call, so a walk of 10^4 moves costs O(10^4 n).
+ *   level 0: calcScoreDistancesActiveRegion(p) + calcScoreLoopEnergy(p)
+ *            + boundaryPenalty(p)  (MonteCarloArcs, LooperSolver.hpp:4721-4731)
+ *   level 1: calcScoreHeatmapActiveRegion(p) (:3583-3617; MonteCarloHeatmap
+ *            re-scores the whole map per move, :1488, whose change is twice
+ *            the local one)
+ *   level 2: calcScoreStructureSmooth(p, true, true) + boundaryPenalty(p)
+ *                                  (MonteCarloArcsSmooth, :4939-4949)
+ * matrix is the arc-target map (level 0) or the heatmap (level 1). */
+void ref_local_walk(int level, int n, const float *pos, const float *matrix, int diag,
+                    int n_bounds, const int *bounds, const double *dtn, int n_loops,
+                    const int *li, const int *lj, const float *lk, const float *lr0,
+                    const orc_params *p, int n_moves, const int *bead, const float *disp,
+                    const int *acc, double *before, double *after) {
+  Quiet q;
+  apply_settings(p, level);
+  LooperSolver s("ref", "/tmp/");
+  load_clusters(s, n, pos, nullptr, level == 2 ? dtn : nullptr);
+  if (level == 0) {
+    load_dense(s.heatmap_exp_dist_anchor, n, matrix);
+    load_loops(s, n_loops, li, lj, lk, lr0);
+  } else if (level == 1) {
+    load_dense(s.heatmap_dist, n, matrix);
+    s.heatmap_dist.diagonal_size = diag;
+    s.heatmap_chromosome_boundaries.assign(bounds, bounds + n_bounds);
+  }
+  auto local = [&](int b) -> double {
+    double sc;
+    if (level == 0)
+      sc = s.calcScoreDistancesActiveRegion(b) + s.calcScoreLoopEnergy(b);
+    else if (level == 1)
+      return s.calcScoreHeatmapActiveRegion(b);
+    else
+      sc = s.calcScoreStructureSmooth(b, true, true);
+    if (s.spherical_container) sc += s.spherical_container->boundaryPenalty(s.clusters[b].pos);
+    return sc;
+  };
+  for (int k = 0; k < n_moves; ++k) {
+    const int b = bead[k];
+    vector3 &x = s.clusters[b].pos;
+    const vector3 saved = x;
+    before[k] = local(b);
+    x += vector3(disp[3 * k], disp[3 * k + 1], disp[3 * k + 2]);
+    after[k] = local(b);
+    if (!acc[k]) x = saved;
+  }
+}
+
 /* calcScoreStructureActiveRegionLengths() (moved < 0) or
  * calcScoreStructureActiveRegionLengths(moved) (LooperSolver.hpp:3375-3412):
  * the bond term the extended arc energy uses. */

@@ -86,3 +86,72 @@ def test_stress_refine_random(kw, it, lr):
     o2, x2, _ = O.stress_refine(t, it, lr)
     np.testing.assert_array_equal(o1, o2)
     np.testing.assert_array_equal(x1.view(np.uint32), x2.view(np.uint32))
+
+
+def _walk(n: int, moves: int, step: float, seed: int, movable=None, in2d=False):
+    """A scripted walk: uniform beads (among `movable`), uniform displacements
+    in [-step, step) per axis, each move kept with probability 0.3."""
+    rng = np.random.default_rng(seed)
+    t = np.zeros(moves, np.dtype([("bead", np.int32), ("accepted", np.int32),
+                                  ("dx", np.float32), ("dy", np.float32), ("dz", np.float32)]))
+    beads = np.arange(n) if movable is None else np.asarray(movable)
+    t["bead"] = rng.choice(beads, moves)
+    for ax in ("dx", "dy", "dz"):
+        t[ax] = rng.uniform(-step, step, moves).astype(np.float32)
+    if in2d:
+        t["dz"] = 0.0
+    t["accepted"] = rng.random(moves) < 0.3
+    return t
+
+
+WALK_MOVES = 10_000
+
+
+def test_arcs_local_energy_walk():
+    """10^4 proposals on the plain drop-in's region shape (256 beads, 400 arcs)
+    plus loop constraints and a sphere: the oracle's local arc energy before
+    and after every move equals the reference's calcScoreDistancesActiveRegion(p)
+    + calcScoreLoopEnergy(p) + boundaryPenalty bit for bit."""
+    r = synth.arcs_region(256, 400, seed=31)
+    rng = np.random.default_rng(32)
+    li = rng.integers(0, 256, 8).astype(np.int32)
+    lj = rng.integers(0, 256, 8).astype(np.int32)
+    pr = O.ArcsProblem(r.pos, r.dense(), None, li, lj, rng.uniform(0.5, 2.0, 8).astype(np.float32),
+                       rng.uniform(1.0, 3.0, 8).astype(np.float32))
+    prm = O.Params(sphere_radius=6.0)
+    t = _walk(256, WALK_MOVES, 0.5, 33)
+    ref = O.ref_arcs_walk(pr, prm, t)
+    orc = O.arcs_replay(pr, prm, 0.5, 0, 0, t)
+    np.testing.assert_array_equal(orc["before"], ref["before"])
+    np.testing.assert_array_equal(orc["after"], ref["after"])
+    assert np.count_nonzero(ref["after"] != ref["before"]) > WALK_MOVES // 2
+
+
+def test_heatmap_local_energy_walk():
+    """10^4 proposals on a 256-bead map with a diagonal band of 2 and two
+    chromosome blocks: calcScoreHeatmapActiveRegion(p) before and after."""
+    h = synth.heatmap_region(256, seed=34, n_tads=4, tad_min=20, tad_max=60)
+    pr = O.HeatmapProblem(h.pos, h.heat, 2, np.array([0, 100, 256], np.int32))
+    prm = O.Params()
+    t = _walk(256, WALK_MOVES, 0.5, 35)
+    ref = O.ref_heatmap_walk(pr, prm, t)
+    orc = O.heatmap_replay(pr, prm, 1.0, 0, 0, t)
+    np.testing.assert_array_equal(orc["before"], ref["before"])
+    np.testing.assert_array_equal(orc["after"], ref["after"])
+
+
+def test_smooth_local_energy_walk():
+    """10^4 proposals on a 200-bead subanchor chain (anchors fixed, weights
+    0.7/1.3, a sphere): calcScoreStructureSmooth(p, true, true) +
+    boundaryPenalty before and after, 2D moves included."""
+    c = synth.smooth_chain(200, seed=36)
+    pr = O.SmoothProblem(c.pos, c.dist_to_next, c.fixed)
+    prm = O.Params(k_stretch=0.1, k_squeeze=0.1, k_angle=0.1, w_dist=0.7, w_angle=1.3,
+                   sphere_radius=8.0)
+    free = np.flatnonzero(c.fixed == 0)
+    for k, in2d in enumerate((False, True)):
+        t = _walk(200, WALK_MOVES // 2, 0.5, 37 + k, movable=free, in2d=in2d)
+        ref = O.ref_smooth_walk(pr, prm, t)
+        orc = O.smooth_replay(pr, prm, 0.5, 0, 0, t)
+        np.testing.assert_array_equal(orc["before"], ref["before"])
+        np.testing.assert_array_equal(orc["after"], ref["after"])
