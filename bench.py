@@ -314,6 +314,163 @@ def stress_main(args):
     print(json.dumps(line))
 
 
+def _cpu_heatmap(job):
+    scale, cap, incremental = job
+    from oracle import oracle as O
+    from pmmc_gb300 import workloads as W
+    base, _ = W.heatmap_maps(1)
+    heat = base.heat if scale == 1.0 else (base.heat * np.float32(scale)).astype(np.float32)
+    pr = O.HeatmapProblem(base.pos, heat, base.diag, base.bounds)
+    prm = O.Params(**W.HEATMAP_ANNEAL, max_moves=cap)
+    t = time.perf_counter()
+    _, res = O.heatmap_anneal(pr, prm, 1.0, 7, incremental=incremental)
+    return res.moves, time.perf_counter() - t
+
+
+def _cpu_pool(fn, jobs, cores):
+    """Runs one job per core at once; returns the moves, the sum of the jobs'
+    own rates (moves / own time, process start-up excluded) and the wall
+    time."""
+    t0 = time.perf_counter()
+    if cores == 1:
+        res = [fn(j) for j in jobs]
+    else:
+        with mp.get_context("spawn").Pool(cores) as pool:
+            res = pool.map(fn, jobs)
+    return (sum(r[0] for r in res), sum(r[0] / r[1] for r in res),
+            time.perf_counter() - t0)
+
+
+def heatmap_cpu_baseline(n_maps: int, budget_s: float) -> dict:
+    """The reference's heatmap annealer on the host (MonteCarloHeatmap,
+    restated by the oracle bit for bit), one map per core (one core for the
+    single-chain line).  Its own form re-scores the whole 2048-bead map after
+    every move (O(N^2) per move); the baseline reported is an O(N)-incremental
+    form of the same annealer (local scores of the moved bead), the faster
+    CPU code, with the reference's own form beside it."""
+    from oracle import oracle as O
+    from pmmc_gb300 import workloads as W
+    O.build()
+    cores = 1 if n_maps == 1 else max(1, min(os.cpu_count() or 1, n_maps))
+    _, scales = W.heatmap_maps(max(n_maps, cores))
+    mv, dt = _cpu_heatmap((1.0, 2000, True))
+    cap = int(min(100_000, max(2000, mv / dt * budget_s / 2)))
+    _, rate, wall = _cpu_pool(_cpu_heatmap, [(float(scales[k]), cap, True)
+                                             for k in range(cores)], cores)
+    full_cap = 20
+    _, frate, fwall = _cpu_pool(_cpu_heatmap, [(float(scales[k]), full_cap, False)
+                                               for k in range(cores)], cores)
+    return {"value": rate, "unit": "moves/s", "cores": cores, "kind": "port",
+            "sample": f"{cores} map(s) x {cap} moves at once, O(N) local scores per move "
+                      f"({wall:.1f} s)",
+            "reference_form": {"value": frate, "unit": "moves/s", "cores": cores,
+                               "sample": f"{cores} map(s) x {full_cap} moves at once, "
+                                         f"re-scoring the whole map per move ({fwall:.1f} s)"}}
+
+
+def heatmap_main(args, n_maps: int):
+    """Heatmap-level line (one chain, or one chain per distinct map) beside
+    the reference's heatmap annealer on the host cores."""
+    if args.impl == "reference":
+        if int(os.environ.get("RANK", "0")) != 0:
+            return
+        maps = n_maps if n_maps > 0 else 2 * (os.cpu_count() or 1)
+        cpu = heatmap_cpu_baseline(maps, args.cpu_budget)
+        ref = dict(cpu["reference_form"], kind="reference_algorithm_port")
+        print(json.dumps({"metric": "MC moves/s", "value": ref["value"], "unit": "moves/s",
+                          "n_gpus": 0, "steps": 1, "warmup": 0, "ms_per_step": None,
+                          "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                          "dtype": "f64", "data": "synthetic", "impl": "reference",
+                          "config": {"workload": f"heatmap_{maps}x2048"},
+                          "cpu_baseline": ref, "incremental_port": cpu,
+                          "e2e": {"value": ref["value"], "unit": "moves/s",
+                                  "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+        return
+    # CPU baseline first, so that its process pool starts before the first
+    # GPU call; the batch's default (two maps per SM) exceeds the host cores
+    cpu = heatmap_cpu_baseline(n_maps if n_maps > 0 else 2 * (os.cpu_count() or 1),
+                               args.cpu_budget)
+    from pmmc_gb300 import workloads as W
+    sampler = ClockSampler(0)
+    sampler.start()
+    line = W.heatmap(args, n_maps)
+    line["clocks"] = sampler.stop()
+    line["gpu_launches"] = args.steps  # one heatmap_anneal_kernel launch per call
+    line["cpu_baseline"] = cpu
+    print(json.dumps(line))
+
+
+def _cpu_smooth(job):
+    segs, sweeps = job
+    from oracle import oracle as O
+    from pmmc_gb300 import workloads as W
+    moves = 0
+    t = time.perf_counter()
+    for pos, dtn, fixed in segs:
+        free = int((fixed == 0).sum())
+        prm = O.Params(**W.SMOOTH_ANNEAL, k_stretch=0.1, k_squeeze=0.1,
+                       max_moves=sweeps * free)
+        _, res = O.smooth_anneal(O.SmoothProblem(pos, dtn, fixed), prm, 0.5, 3)
+        moves += res.moves
+    return moves, time.perf_counter() - t
+
+
+def smooth_cpu_baseline(sweeps: int, budget_s: float) -> dict:
+    """The reference's smoothing annealer (MonteCarloArcsSmooth, restated by
+    the oracle bit for bit) over the workload's regions on every host core,
+    each region for the same sweeps as the GPU line; a seeded random subset
+    of the regions, as many as about budget_s of wall time covers."""
+    from oracle import oracle as O
+    from pmmc_gb300 import workloads as W
+    O.build()
+    segs = W.smooth_segments()
+    order = np.random.default_rng(5).permutation(len(segs))
+    chunks = [([segs[i] for i in order[k:k + 32]], sweeps) for k in range(0, len(segs), 32)]
+    cores = os.cpu_count() or 1
+    moves, cpu_s, done = 0, 0.0, 0
+    t0 = time.perf_counter()
+    with mp.get_context("spawn").Pool(cores) as pool:
+        for mv, dt in pool.imap_unordered(_cpu_smooth, chunks):
+            moves += mv
+            cpu_s += dt
+            done += 1
+            if time.perf_counter() - t0 > budget_s:
+                pool.terminate()
+                break
+    wall = time.perf_counter() - t0
+    # every core ran chunks at once: the mean rate of a core times the cores
+    return {"value": moves / cpu_s * cores, "unit": "moves/s", "cores": cores, "kind": "port",
+            "sample": f"{done * 32} of {len(segs)} regions x {sweeps} sweeps "
+                      f"({cpu_s:.1f} CPU s in {wall:.1f} s)"}
+
+
+def smooth_main(args):
+    """Genome-smoothing line beside the reference's smoothing annealer on
+    every host core."""
+    sweeps = args.moves or 20_000
+    cpu = smooth_cpu_baseline(sweeps, args.cpu_budget)
+    if args.impl == "reference":
+        if int(os.environ.get("RANK", "0")) != 0:
+            return
+        print(json.dumps({"metric": "MC moves/s", "value": cpu["value"], "unit": "moves/s",
+                          "n_gpus": 0, "steps": 1, "warmup": 0, "ms_per_step": None,
+                          "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+                          "dtype": "f64", "data": "synthetic", "impl": "reference",
+                          "config": {"workload": f"genome_smoothing_{sweeps}sweeps"},
+                          "cpu_baseline": cpu,
+                          "e2e": {"value": cpu["value"], "unit": "moves/s",
+                                  "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
+        return
+    from pmmc_gb300 import workloads as W
+    sampler = ClockSampler(0)
+    sampler.start()
+    line = W.smooth(args)
+    line["clocks"] = sampler.stop()
+    line["gpu_launches"] = args.steps  # one smooth_anneal_kernel launch per call
+    line["cpu_baseline"] = cpu
+    print(json.dumps(line))
+
+
 def plain_main(args):
     """Config-0 line: the plain drop-in call beside the reference CPU
     annealer (the oracle port, bit-identical to it) on one core."""
@@ -628,9 +785,14 @@ def main():
     if args.workload == "stress":
         stress_main(args)
         return
-    if args.workload != "ensemble":
-        from pmmc_gb300 import workloads
-        workloads.main(args)
+    if args.workload == "heatmap":
+        heatmap_main(args, 1)
+        return
+    if args.workload == "heatmap-batch":
+        heatmap_main(args, args.maps or 0)
+        return
+    if args.workload == "smooth":
+        smooth_main(args)
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))

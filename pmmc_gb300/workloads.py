@@ -69,23 +69,31 @@ def _traffic(kernel: str, workload: str):
     return None
 
 
-def _heatmap(args, n_maps):
+HEATMAP_ANNEAL = dict(max_temp=5.0, dt_temp=0.9999, milestone_steps=100_000, improvement=0.99)
+
+
+def heatmap_maps(n_maps: int):
+    """The 2048-bead heatmap region (20 TAD blocks, expected distance c^-1/3)
+    and one scale factor per distinct map: the batch holds the generated map
+    scaled by a per-map factor, so every chain streams its own rows."""
+    base = synth.heatmap_region(2048, seed=7)
+    rng = np.random.default_rng(11)
+    scales = [1.0] + list(rng.uniform(0.8, 1.25, n_maps - 1))
+    return base, scales
+
+
+def heatmap(args, n_maps):
     import torch
     torch.cuda.init()
     ctx = capi.Context(0)
     if n_maps <= 0:          # two distinct maps per SM (two chains share an SM)
         n_maps = 2 * ctx.sm_count
-    base = synth.heatmap_region(2048, seed=7)
-    # distinct maps in memory (the rows of every chain stream from HBM): the
-    # generated map scaled by a per-map factor
-    rng = np.random.default_rng(11)
-    scales = [1.0] + list(rng.uniform(0.8, 1.25, n_maps - 1))
+    base, scales = heatmap_maps(n_maps)
     inputs = [capi.HeatmapInput(base.pos, (base.heat * np.float32(sc)).astype(np.float32),
                                 base.diag, base.bounds) for sc in scales]
     moves = args.moves or (100_000 if n_maps == 1 else 20_000)
-    prm = capi.default_params(capi.LEVEL_HEATMAP, max_temp=5.0, dt_temp=0.9999,
-                              milestone_steps=100_000, improvement=0.99,
-                              schedule=capi.SCHEDULE_CPU, max_moves=moves)
+    prm = capi.default_params(capi.LEVEL_HEATMAP, schedule=capi.SCHEDULE_CPU, max_moves=moves,
+                              **HEATMAP_ANNEAL)
     times, total = [], 0
     for k in range(args.warmup + args.steps):
         ctx.set_seed(7)
@@ -114,27 +122,33 @@ def _heatmap(args, n_maps):
                      "algorithmic_bytes_per_move": row_bytes,
                      "algorithmic_bytes_per_launch": alg},
     }
-    print(json.dumps(line))
+    return line
 
 
-def _smooth(args):
-    ctx = capi.Context(0)
-    chains = synth.smooth_genome(300_000, seed=3)
-    segs = []
-    for ch in chains:
+SMOOTH_ANNEAL = dict(max_temp=5.0, dt_temp=0.9999, milestone_steps=10**9, improvement=0.99)
+
+
+def smooth_segments():
+    """The genome-smoothing workload's regions: about 300k beads over the 23
+    chromosomes, cut at the fixed anchors into (pos, dist_to_next, fixed)
+    segments of at least one free bead."""
+    out = []
+    for ch in synth.smooth_genome(300_000, seed=3):
         a = np.nonzero(ch.fixed)[0]
         for l, r in zip(a[:-1], a[1:]):
             if r - l >= 2:
                 sl = slice(l, r + 1)
-                segs.append(capi.SmoothInput(ch.pos[sl], ch.dist_to_next[sl], ch.fixed[sl]))
+                out.append((ch.pos[sl], ch.dist_to_next[sl], ch.fixed[sl]))
+    return out
+
+
+def smooth(args):
+    ctx = capi.Context(0)
+    segs = [capi.SmoothInput(*x) for x in smooth_segments()]
     free = sum(int((x.fixed == 0).sum()) for x in segs)
     sweeps = args.moves or 20_000
-    prm = capi.default_params(capi.LEVEL_SMOOTH, max_temp=5.0, dt_temp=0.9999,
-                              milestone_steps=10**9, improvement=0.99,
-                              schedule=capi.SCHEDULE_CPU, resync_every=1000)
-    steps = []
-    for x in segs:
-        steps.append(0.5)
+    prm = capi.default_params(capi.LEVEL_SMOOTH, schedule=capi.SCHEDULE_CPU, resync_every=1000,
+                              **SMOOTH_ANNEAL)
     times, total = [], 0
     for k in range(args.warmup + args.steps):
         ctx.set_seed(3)
@@ -153,7 +167,7 @@ def _smooth(args):
                                f"{sweeps}sweeps", "moves_per_step": total},
         "final_energy_rel_error_max": max(r.rel_error for r in res),
     }
-    print(json.dumps(line))
+    return line
 
 
 def _smooth_run(ctx, segs, prm, sweeps):
@@ -532,12 +546,3 @@ def stress(args) -> dict:
                      "note": "L2-resident working set; bound by the per-anchor gather "
                              "latency and two grid barriers per iteration"},
     }
-
-
-def main(args):
-    if args.workload == "heatmap":
-        _heatmap(args, 1)
-    elif args.workload == "heatmap-batch":
-        _heatmap(args, args.maps or 0)
-    else:
-        _smooth(args)
