@@ -448,10 +448,10 @@ def smooth_main(args):
     """Genome-smoothing line beside the reference's smoothing annealer on
     every host core."""
     sweeps = args.moves or 20_000
+    if args.impl == "reference" and int(os.environ.get("RANK", "0")) != 0:
+        return
     cpu = smooth_cpu_baseline(sweeps, args.cpu_budget)
     if args.impl == "reference":
-        if int(os.environ.get("RANK", "0")) != 0:
-            return
         print(json.dumps({"metric": "MC moves/s", "value": cpu["value"], "unit": "moves/s",
                           "n_gpus": 0, "steps": 1, "warmup": 0, "ms_per_step": None,
                           "higher_is_better": True, "scaling": "weak", "vs_baseline": None,

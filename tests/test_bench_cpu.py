@@ -1,0 +1,56 @@
+"""bench.py's reference arm on the CPU: the JSON line the benchmark contract
+asks for (one line on rank 0, nothing on the other ranks, exit status 0).
+The arm times the oracle's restatement of the reference's CPU annealers on
+the host cores, so it needs no GPU."""
+import json
+import os
+import subprocess
+import sys
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+KEYS = {"metric", "value", "unit", "n_gpus", "steps", "warmup", "higher_is_better",
+        "scaling", "vs_baseline", "dtype", "data", "config", "impl", "cpu_baseline", "e2e"}
+
+
+def run_bench(*argv, rank=0):
+    env = dict(os.environ, RANK=str(rank), WORLD_SIZE="2" if rank else "1")
+    p = subprocess.run([sys.executable, "bench.py", *argv], cwd=ROOT, env=env,
+                       capture_output=True, text=True, timeout=600)
+    assert p.returncode == 0, p.stderr[-2000:]
+    return [ln for ln in p.stdout.splitlines() if ln.strip()]
+
+
+def check_line(lines, unit):
+    assert len(lines) == 1, lines
+    d = json.loads(lines[0])
+    assert KEYS <= set(d), KEYS - set(d)
+    assert d["impl"] == "reference"
+    assert d["unit"] == unit and d["value"] > 0
+    cb = d["cpu_baseline"]
+    assert cb["value"] == d["value"] and cb["cores"] >= 1 and cb["kind"] in (
+        "port", "reference", "reference_algorithm_port")
+    assert d["e2e"] == {"value": d["value"], "unit": unit, "h2d_bytes_per_step": 0,
+                        "d2h_bytes_per_step": 0}
+    assert isinstance(d["config"], dict) and "workload" in d["config"]
+    return d
+
+
+def test_reference_arm_ensemble():
+    d = check_line(run_bench("--impl", "reference", "--steps", "1", "--warmup", "0"),
+                   "moves/s")
+    assert d["metric"] == "MC moves/s" and d["higher_is_better"] is True
+
+
+@pytest.mark.parametrize("workload,unit", [("targets", "arcs/s"),
+                                           ("smooth", "moves/s")])
+def test_reference_arm_workloads(workload, unit):
+    check_line(run_bench("--impl", "reference", "--workload", workload, "--cpu-budget", "1"),
+               unit)
+
+
+@pytest.mark.parametrize("workload", ["ensemble", "smooth", "heatmap", "targets"])
+def test_reference_arm_other_ranks_print_nothing(workload):
+    assert run_bench("--impl", "reference", "--workload", workload, "--steps", "1",
+                     "--warmup", "0", rank=1) == []
