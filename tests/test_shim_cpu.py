@@ -66,3 +66,42 @@ def test_reference_program_links_with_the_shim(tmp_path):
     out = subprocess.run([str(tmp_path / "pMMC-reconstruct")], capture_output=True, text=True,
                          timeout=60)
     assert "Usage: pMMC-reconstruct" in out.stdout + out.stderr
+
+
+def test_drop_in_fails_loudly_without_a_device(tmp_path):
+    """The drop-in parallelMonteCarloArcs, called from the reference's own
+    LooperSolver on a host without a CUDA device, ends the program with the
+    library's status (PMMC_ERR_NO_DEVICE = 2) and message, as the reference's
+    gpuErrchk does on a CUDA error: no CPU annealer runs in its place."""
+    import concurrent.futures as cf
+    import torch
+    lib = os.path.join(ROOT, "pmmc_gb300", "libpmmc_gb300.so")
+    if not os.path.exists(lib):
+        pytest.skip("the built library missing")
+    if torch.cuda.is_available():
+        pytest.skip("a CUDA device is present")
+    inc = [f"-I{REF}/include", f"-I{REF}/thirdparty", f"-I{ROOT}/include"]
+    jobs = [["g++", "-std=c++17", "-O1", "-w", *inc, "-c",
+             os.path.join(ROOT, "tests", "shim_no_device.cpp"), "-o", "drv.o"],
+            ["g++", "-std=c++17", "-O1", "-w", *inc, "-c",
+             os.path.join(ROOT, "pmmc_gb300", "shim", "looper_solver_gpu.cpp"), "-o", "shim.o"],
+            ["gcc", "-O1", "-w", "-c", f"{REF}/thirdparty/ini.c", "-o", "ini.o"]]
+    jobs += [["g++", "-std=c++17", "-O1", "-w", *inc, "-c", f"{REF}/thirdparty/{f}.cpp", "-o",
+              f"{f}.o"] for f in ("common", "mtxlib", "INIReader", "rmsd")]
+    with cf.ThreadPoolExecutor(8) as ex:
+        res = list(ex.map(lambda c: subprocess.run(c, cwd=tmp_path, capture_output=True,
+                                                   text=True), jobs))
+    for r in res:
+        assert r.returncode == 0, r.stderr[-2000:]
+    objs = ["drv.o", "shim.o", "common.o", "mtxlib.o", "INIReader.o", "rmsd.o", "ini.o"]
+    r = subprocess.run(["g++", "-fopenmp", "-o", "drv", *objs, f"-L{os.path.dirname(lib)}",
+                        "-lpmmc_gb300", "-L/usr/local/cuda/lib64", "-lcudart",
+                        f"-Wl,-rpath,{os.path.dirname(lib)}"],
+                       cwd=tmp_path, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
+    (tmp_path / "seg.bed").write_text("chr1\t0\t1000000\n")
+    out = subprocess.run([str(tmp_path / "drv"), str(tmp_path / "seg.bed")], cwd=tmp_path,
+                         capture_output=True, text=True, timeout=120)
+    assert out.returncode == 2, (out.returncode, out.stdout[-500:], out.stderr[-500:])
+    assert "GPUassert (pmmc_gb300): context: no usable CUDA device" in out.stderr
+    assert "returned" not in out.stdout
