@@ -6,10 +6,16 @@ the configuration the batched-vs-plain metric is quoted on.
 
 A step anneals every block of the ensemble once (T0 5, cooling 0.9999,
 milestones every 50k moves with improvement threshold 0.99 -- the reference
-CPU schedule of MonteCarloArcs -- and an FP64 energy resync every 1000 moves)
-in one CUDA-graph launch of the persistent work-stealing kernels.  Inputs are
-seeded synthetic regions (no datasets ship with the reference).  Rank r of N
-anneals its own ensemble (seeds 64r..64r+63): weak scaling, no collective.
+CPU schedule of MonteCarloArcs -- and an energy recompute every 4096 moves,
+--resync) in one CUDA-graph launch of the persistent work-stealing kernels.
+Inputs are seeded synthetic regions (no datasets ship with the reference).
+Rank r of N anneals its own ensemble (seeds 64r..64r+63): weak scaling, no
+collective.
+
+Other lines (--workload): plain, heatmap, heatmap-batch, smooth, serve,
+distmap, equidistant, targets, stress (pmmc_gb300/workloads.py describes
+each); every line carries its CPU baseline, and --impl reference prints the
+reference arm of the chosen line.
 
 One JSON line on rank 0: value = MC moves/s over all ranks (device time,
 CUDA events on the launching stream); structures/s beside it; e2e = the same
