@@ -1,5 +1,6 @@
-"""Benchmark lines for the heatmap and smoothing kernels (bench.py
---workload heatmap | heatmap-batch | smooth).
+"""Workloads and GPU legs of bench.py's lines other than the default
+ensemble (bench.py --workload NAME; bench.py adds each line's CPU baseline,
+clocks and launch count).
 
 heatmap        one chain on a 2048-bead map (contact map |i-j|^-1 x
                lognormal(0.5), 20 TADs x3, expected distance c^-1/3), T0 5,
