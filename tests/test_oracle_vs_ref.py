@@ -155,3 +155,43 @@ def test_smooth_local_energy_walk():
         orc = O.smooth_replay(pr, prm, 0.5, 0, 0, t)
         np.testing.assert_array_equal(orc["before"], ref["before"])
         np.testing.assert_array_equal(orc["after"], ref["after"])
+
+
+@pytest.mark.parametrize("seed", [41, 42, 43])
+def test_distance_heatmap_random(seed):
+    """createDistanceHeatmap on fresh contact maps: odd sizes, wide diagonal
+    bands, many zeros, asymmetric inputs, both level constants."""
+    rng = np.random.default_rng(seed)
+    n = int(rng.integers(20, 150))
+    diag = int(rng.integers(0, 4))
+    level = int(rng.integers(0, 2))
+    scale = float(rng.choice([1.0, 100.0]))
+    power = float(rng.uniform(-1.2, -0.2))
+    stretch = float(rng.uniform(1.1, 3.0))
+    c = (rng.lognormal(0.0, 1.0, (n, n)) * (rng.random((n, n)) > 0.3)).astype(np.float32)
+    if seed % 2:
+        c = np.triu(c) + np.triu(c, 1).T
+    d, _, _ = O.distance_heatmap(c, diag, scale, power, stretch)
+    np.testing.assert_array_equal(d, O.ref_distance_heatmap(c, diag, level, scale, power, stretch))
+
+
+@pytest.mark.parametrize("seed", [51, 52, 53])
+def test_equidistant_random(seed):
+    """The equidistant-model interpolation on fresh chromosome levels:
+    uneven spacing, 2 to 200 clusters, resolutions from below the smallest
+    gap to above the largest."""
+    import os
+    if not os.path.exists(os.path.join(os.path.dirname(O.__file__), "_ref", "libpmmc_ref_hc.so")):
+        pytest.skip("the reference's equidistant harness is not built")
+    rng = np.random.default_rng(seed)
+    n = int(rng.integers(2, 200))
+    width = rng.integers(50, 40000, n)
+    start = np.concatenate([[5_000], 5_000 + np.cumsum(width)[:-1]]).astype(np.int32)
+    end = (start + width - 1).astype(np.int32)
+    gpos = ((start + end) // 2).astype(np.int32)
+    pos = synth.random_walk(n, rng) * np.float32(1.5)
+    res = int(rng.choice([37, 500, 5000, 60000]))
+    lo, hi = int(gpos[0]), int(gpos[-1])
+    pts = O.equidistant(gpos, pos, int(end[0]), int(start[-1]), lo, hi, res)
+    ref = O.ref_equidistant(gpos, start, end, pos, lo, hi, res)
+    np.testing.assert_array_equal(pts, ref)
