@@ -122,7 +122,6 @@ def lib():
         if not os.path.exists(LIB_PATH):
             build()
         L = C.CDLL(LIB_PATH)
-        v = C.c_void_p
         L.orc_arcs_full_score.restype = C.c_double
         L.orc_arcs_spring_score.restype = C.c_double
         L.orc_arcs_repulsion.restype = C.c_double
@@ -133,11 +132,7 @@ def lib():
         L.orc_u01.restype = C.c_float
         L.orc_arcs_ext_score.restype = C.c_double
         L.orc_u01.argtypes = [C.c_uint32]
-        for name in ("orc_arcs_full_score", "orc_arcs_spring_score",
-                     "orc_arcs_local_score", "orc_arcs_anneal"):
-            pass
         _lib = L
-        del v
     return _lib
 
 
@@ -155,6 +150,8 @@ def ref():
         R.ref_heatmap_score.restype = C.c_double
         R.ref_smooth_score.restype = C.c_double
         R.ref_lengths_score.restype = C.c_double
+        R.ref_rmsd.restype = C.c_double
+        R.ref_distance_correlation.restype = C.c_double
         _ref = R
     return _ref
 
@@ -559,6 +556,18 @@ def ref_heatmap_walk(pr: HeatmapProblem, prm: Params, trace):
 
 def ref_smooth_walk(pr: SmoothProblem, prm: Params, trace):
     return _ref_walk(2, pr.n, pr.pos, prm, trace, dtn=pr.dist_to_next)
+
+
+def ref_rmsd(a, b) -> float:
+    """The reference's Chromosome::calcRMSD (superposed RMSD, fast_rmsd)."""
+    a, b = _f32(a).reshape(-1, 3), _f32(b).reshape(-1, 3)
+    return ref().ref_rmsd(len(a), _p(a), _p(b))
+
+
+def ref_distance_correlation(a, b) -> float:
+    """The reference's MetricsFramework::distanceCorrelation (all pairs)."""
+    a, b = _f32(a).reshape(-1, 3), _f32(b).reshape(-1, 3)
+    return ref().ref_distance_correlation(len(a), _p(a), _p(b))
 
 
 def ref_random_vectors(seed: int, count: int, max_size: float = 1.0, in2d: bool = False):

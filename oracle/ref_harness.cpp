@@ -39,6 +39,7 @@
 #include <AppCommon.hpp>
 #include <Static.hpp>
 #include <LooperSolver.hpp>
+#include <MetricsFramework.hpp>
 #undef private
 #undef protected
 
@@ -344,6 +345,32 @@ void ref_local_walk(int level, int n, const float *pos, const float *matrix, int
     after[k] = local(b);
     if (!acc[k]) x = saved;
   }
+}
+
+/* The structural metrics the distribution tests compare: RMSD after optimal
+ * superposition (Chromosome::calcRMSD -> fast_rmsd, Chromosome.hpp:613-634)
+ * and the Pearson correlation of all pairwise distances
+ * (MetricsFramework::distanceCorrelation, MetricsFramework.hpp:238-286). */
+static void load_chromosome(Chromosome &c, int n, const float *pos) {
+  c.points.clear();
+  for (int i = 0; i < n; ++i)
+    c.points.push_back(vector3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]));
+  c.size = n;
+}
+
+double ref_rmsd(int n, const float *a, const float *b) {
+  Chromosome ca, cb;
+  load_chromosome(ca, n, a);
+  load_chromosome(cb, n, b);
+  return ca.calcRMSD(cb);
+}
+
+double ref_distance_correlation(int n, const float *a, const float *b) {
+  Chromosome ca, cb;
+  load_chromosome(ca, n, a);
+  load_chromosome(cb, n, b);
+  MetricsFramework m;
+  return m.distanceCorrelation(ca, cb, 1);
 }
 
 /* calcScoreStructureActiveRegionLengths() (moved < 0) or

@@ -195,3 +195,22 @@ def test_equidistant_random(seed):
     pts = O.equidistant(gpos, pos, int(end[0]), int(start[-1]), lo, hi, res)
     ref = O.ref_equidistant(gpos, start, end, pos, lo, hi, res)
     np.testing.assert_array_equal(pts, ref)
+
+
+@pytest.mark.parametrize("n,seed", [(16, 61), (256, 62), (700, 63)])
+def test_parity_metrics_match_reference(n, seed):
+    """The structural metrics of the 16-seed distribution tests equal the
+    reference's own: Kabsch RMSD against Chromosome::calcRMSD (fast_rmsd,
+    float result) and the pairwise-distance Pearson correlation against
+    MetricsFramework::distanceCorrelation (float distances, double sums,
+    float result)."""
+    from parity import distmap_pearson, kabsch_rmsd
+    rng = np.random.default_rng(seed)
+    a = synth.random_walk(n, rng)
+    # a rotated, shifted, perturbed copy (and a mirror image for one case)
+    q, _ = np.linalg.qr(rng.normal(size=(3, 3)))
+    if seed % 2 == 0 and np.linalg.det(q) > 0:
+        q[:, 0] *= -1.0
+    b = (a @ q.T + rng.normal(0.0, 0.3, (n, 3)) + 5.0).astype(np.float32)
+    assert kabsch_rmsd(a, b) == pytest.approx(O.ref_rmsd(a, b), rel=1e-5, abs=1e-5)
+    assert distmap_pearson(a, b) == pytest.approx(O.ref_distance_correlation(a, b), rel=1e-6)
