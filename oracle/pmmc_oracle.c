@@ -1223,7 +1223,7 @@ void orc_smooth_replay(int n, const float *pos0, const unsigned char *fixed,
                        const int *gpu_acc, orc_replay_out *out) {
   float *pos = (float *)malloc(sizeof(float) * 3 * (n > 0 ? n : 1));
   memcpy(pos, pos0, sizeof(float) * 3 * n);
-  replay_ctx c = {n, NULL, NULL, 0, p, dist_to_next, NULL, 0, 0, NULL};
+  replay_ctx c = {n, NULL, NULL, 0, p, dist_to_next, NULL, 0, 0, NULL, NULL};
   double E = orc_smooth_full_score(n, pos, dist_to_next, p);
   replay_core(2, &c, smooth_local_cb, n, pos, fixed, p, step_size, E, seed, chain,
               n_moves, bead, disp, gpu_acc, out);
@@ -1238,7 +1238,7 @@ void orc_heatmap_replay(int n, const float *pos0, const unsigned char *fixed,
                         const int *gpu_acc, orc_replay_out *out) {
   float *pos = (float *)malloc(sizeof(float) * 3 * (n > 0 ? n : 1));
   memcpy(pos, pos0, sizeof(float) * 3 * n);
-  replay_ctx c = {n, NULL, NULL, 0, p, NULL, heat, diag, n_bounds, bounds};
+  replay_ctx c = {n, NULL, NULL, 0, p, NULL, heat, diag, n_bounds, bounds, NULL};
   double E = orc_heatmap_score(n, pos, heat, diag, n_bounds, bounds, -1);
   if (p->sphere_radius > 0.0f)
     for (int k = 0; k < n; ++k) E += sphere_pen(pos + 3 * k, p->sphere_radius);
