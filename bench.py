@@ -705,7 +705,6 @@ def run_gpu(args, rank, world):
             capi.arcs_anneal(ctx, x, prm, STEP, 1)
         plain_s = time.perf_counter() - t
     batch.close()
-    from pmmc_gb300.capi import lib  # noqa: F401
     return dict(step_ms=step_ms, moves=moves_per_step, kernel_ms=kernel_ms, wall=t_wall,
                 clocks=clk, rel_err=rel_err, bad=status_bad, e2e_ms=e2e_ms,
                 e2e_moves=e2e_moves, h2d=h2d, d2h=d2h, plain_s=plain_s, n_launch=n_launch,
