@@ -162,7 +162,8 @@ const char *pmmc_last_error(const pmmc_ctx *ctx);
  * Philox key of every later call.  Each call also advances a per-context
  * call counter so that consecutive calls draw fresh streams. */
 void pmmc_set_seed(pmmc_ctx *ctx, uint64_t seed);
-/* Number of SMs of the context's device. */
+/* Number of SMs of the context's device (the reference caches it in
+ * GpuResourceCache::sm_count, ParallelMonteCarloArcs.cu:89-90). */
 int pmmc_sm_count(const pmmc_ctx *ctx);
 /* Reference defaults of a level (Settings.hpp:397-505). */
 void pmmc_default_params(int level, pmmc_anneal_params *out);
