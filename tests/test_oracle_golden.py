@@ -245,3 +245,55 @@ def test_stress_refine(case):
     np.testing.assert_array_equal(order, g["order"])
     np.testing.assert_array_equal(pos.view(np.uint32), g["out_pos"].view(np.uint32))
     assert out["n_pairs"] > 0
+
+
+def _dist_check(fn, start, seeds=64):
+    """Final energy, superposed RMSD to the start and distance-map Pearson
+    over `seeds` runs of the libc-mode annealer (bit-identical to the
+    reference's) and the Philox-mode annealer (the stream the kernels follow
+    move for move): two-sample KS and Welch tests, p > 0.01 for each."""
+    from scipy import stats
+    from parity import distmap_pearson, kabsch_rmsd, ks_2samp_p
+    out = []
+    for mode in (O.RNG_LIBC, O.RNG_PHILOX):
+        e, r, p = [], [], []
+        for s in range(seeds):
+            pos, res = fn(mode, s)
+            e.append(res.score)
+            r.append(kabsch_rmsd(pos, start))
+            p.append(distmap_pearson(pos, start))
+        out.append((e, r, p))
+    for a, b in zip(*out):
+        assert ks_2samp_p(a, b) > 0.01
+        assert stats.ttest_ind(a, b, equal_var=False).pvalue > 0.01
+
+
+@pytest.mark.parametrize("n,arcs,milestone", [(64, 100, 5000), (128, 200, 10000)])
+def test_philox_stream_matches_reference_stream_arcs(n, arcs, milestone):
+    """The kernels draw from Philox4x32-10 where the reference draws from libc
+    rand(): the two streams give the same distributions of the annealed
+    structures (the GPU tests then hold each kernel to the Philox-mode
+    annealer move by move)."""
+    from pmmc_gb300 import synth
+    r = synth.arcs_region(n, arcs, seed=8)
+    pr = O.ArcsProblem(r.pos, r.dense())
+    prm = O.Params(max_temp=5.0, dt_temp=0.9999, milestone_steps=milestone, improvement=0.99)
+    _dist_check(lambda mode, s: O.arcs_anneal(pr, prm, 0.5, 700 + s, rng=mode, chain=s), r.pos)
+
+
+def test_philox_stream_matches_reference_stream_heatmap():
+    from pmmc_gb300 import synth
+    h = synth.heatmap_region(40, seed=4, n_tads=2, tad_min=6, tad_max=12)
+    pr = O.HeatmapProblem(h.pos, h.heat, 1, np.zeros(0, np.int32))
+    prm = O.Params(max_temp=5.0, dt_temp=0.9999, milestone_steps=2000, improvement=0.99)
+    _dist_check(lambda mode, s: O.heatmap_anneal(pr, prm, 1.0, 900 + s, rng=mode, chain=s),
+                h.pos)
+
+
+def test_philox_stream_matches_reference_stream_smooth():
+    from pmmc_gb300 import synth
+    c = synth.smooth_chain(60, seed=6)
+    pr = O.SmoothProblem(c.pos, c.dist_to_next, c.fixed)
+    prm = O.Params(max_temp=5.0, dt_temp=0.9999, milestone_steps=3000, improvement=0.99,
+                   k_stretch=0.1, k_squeeze=0.1)
+    _dist_check(lambda mode, s: O.smooth_anneal(pr, prm, 0.5, 950 + s, rng=mode, chain=s), c.pos)
