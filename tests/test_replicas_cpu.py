@@ -1,5 +1,5 @@
-"""Replica sharding and the cross-rank timing reduction, world size 2 over
-gloo on the CPU (the multi-GPU bench path without GPUs)."""
+"""Replica sharding and the cross-rank timing reduction, world sizes 2 and 3
+over gloo on the CPU (the multi-GPU bench path without GPUs)."""
 import os
 import socket
 
@@ -41,19 +41,20 @@ def test_combine_without_process_group_is_local():
     assert combine(12.5, 7.0) == (12.5, 7.0)
 
 
-def test_two_rank_gloo_max_and_sum():
+@pytest.mark.parametrize("world", [2, 3])
+def test_gloo_ranks_max_and_sum(world):
     ctx = mp.get_context("spawn")
     q = ctx.Queue()
     port = _free_port()
-    procs = [ctx.Process(target=_rank, args=(r, 2, port, q)) for r in range(2)]
+    procs = [ctx.Process(target=_rank, args=(r, world, port, q)) for r in range(world)]
     for p in procs:
         p.start()
-    got = sorted(q.get(timeout=120) for _ in range(2))
+    got = sorted(q.get(timeout=120) for _ in range(world))
     for p in procs:
         p.join(timeout=60)
         assert p.exitcode == 0
-    (r0, s0, t0, m0), (r1, s1, t1, m1) = got
-    assert (r0, r1) == (0, 1)
-    assert s0 == list(range(0, 64)) and s1 == list(range(64, 128))
-    assert t0 == t1 == 150.0          # the slowest rank
-    assert m0 == m1 == 3000.0         # all ranks' moves
+    assert [g[0] for g in got] == list(range(world))
+    for r, seeds, step, moves in got:
+        assert seeds == list(range(64 * r, 64 * (r + 1)))
+        assert step == 100.0 + 50.0 * (world - 1)                     # the slowest rank
+        assert moves == 1000.0 * world * (world + 1) / 2              # all ranks' moves
