@@ -105,3 +105,19 @@ def test_drop_in_fails_loudly_without_a_device(tmp_path):
     assert out.returncode == 2, (out.returncode, out.stdout[-500:], out.stderr[-500:])
     assert "GPUassert (pmmc_gb300): context: no usable CUDA device" in out.stderr
     assert "returned" not in out.stdout
+
+
+def test_shim_reads_every_setting_the_reference_gpu_files_read():
+    """Every Settings:: parameter the reference's four replaced GPU files read
+    is read by the shim, except the heatmap kernel's launch geometry
+    ([cuda] num_threads, blocks_multiplier), which this library chooses
+    itself."""
+    import re
+    pat = re.compile(r"Settings::(\w+)")
+    ref = set()
+    for f in ("ParallelMonteCarloArcs.cu", "ParallelMonteCarloHeatmap.cu",
+              "ParallelMonteCarloSmooth.cu", "ParallelMarkArcs.cu"):
+        ref |= set(pat.findall(open(os.path.join(REF, f)).read()))
+    shim = set(pat.findall(open(os.path.join(ROOT, "pmmc_gb300", "shim",
+                                             "looper_solver_gpu.cpp")).read()))
+    assert ref - shim == {"cudaThreadsPerBlock", "cudaBlocksMultiplier"}
