@@ -84,3 +84,40 @@ def test_hcm_writer_matches_reference_lines(tmp_path):
     assert lines[2] == str(g[0]) and lines[3] == str(g[1])
     assert lines[4] == "chr1 0 2\n"
     assert lines[5] == str(g[2]) and lines[6] == str(g[3])
+
+
+def test_ctypes_structs_match_header_layouts(tmp_path):
+    """Every struct the binding mirrors has the header's size and field
+    offsets (a C program built against include/pmmc_gb300.h prints them)."""
+    import ctypes
+    import shutil
+    import subprocess
+    if shutil.which("gcc") is None:
+        pytest.skip("no C compiler")
+    pairs = {"AnnealParams": "pmmc_anneal_params", "Result": "pmmc_result",
+             "ArcsProblem": "pmmc_arcs_problem", "HeatmapProblem": "pmmc_heatmap_problem",
+             "SmoothProblem": "pmmc_smooth_problem", "BatchOpts": "pmmc_batch_opts",
+             "AnchorTargetsProblem": "pmmc_anchor_targets_problem",
+             "AnchorTargetsStats": "pmmc_anchor_targets_stats",
+             "StressProblem": "pmmc_stress_problem", "StressResult": "pmmc_stress_result",
+             "ServerOpts": "pmmc_server_opts", "ServerStats": "pmmc_server_stats"}
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "pmmc_gb300.h"',
+             "int main(void) {"]
+    want = []
+    for py, c in pairs.items():
+        cls = getattr(capi, py)
+        lines.append(f'  printf("%zu\\n", sizeof({c}));')
+        want.append(ctypes.sizeof(cls))
+        for name, _ in cls._fields_:
+            lines.append(f'  printf("%zu\\n", offsetof({c}, {name}));')
+            want.append(getattr(cls, name).offset)
+    lines += ["  return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines) + "\n")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    r = subprocess.run(["gcc", "-std=c11", f"-I{root}/include", str(src), "-o",
+                        str(tmp_path / "layout")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-2000:]
+    got = [int(x) for x in subprocess.run([str(tmp_path / "layout")], capture_output=True,
+                                          text=True).stdout.split()]
+    assert got == want
