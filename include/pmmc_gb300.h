@@ -33,7 +33,8 @@ typedef enum pmmc_status {
   PMMC_ERR_NOMEM = 4,     /* device allocation failed                    */
   PMMC_ERR_TIMEOUT = 5,   /* a bounded device wait ran out               */
   PMMC_ERR_BUDGET = 6,    /* request exceeds the device-memory budget    */
-  PMMC_ERR_FIXED = 7,     /* arc level: every bead is fixed              */
+  PMMC_ERR_FIXED = 7,     /* reserved, not returned: a region whose beads
+                           * are all fixed makes no move                 */
   PMMC_ERR_BUSY = 8,      /* server: no free slot right now              */
   PMMC_ERR_NOT_FOUND = 9, /* server: unknown request id                  */
   PMMC_ERR_CANCELLED = 10 /* server: the request was cancelled            */

@@ -300,8 +300,9 @@ def edge_cases():
     without arcs (repulsion only), heatmap regions with one to five free
     beads and a diagonal band wider than most of the map, and smoothing
     chains of three and four beads (ends fixed).  Regions whose beads are all
-    fixed are left out: the reference redraws a bead until a free one comes
-    up and never returns on them."""
+    fixed are left out: the reference's heatmap and smoothing annealers
+    redraw a bead until a free one comes up and never return on them, its
+    arc annealer stops the program."""
     out = {}
     for k, (n, arcs, seed) in enumerate([(2, 1, 9), (3, 2, 9), (16, 0, 9), (5, 3, 9)]):
         r = synth.arcs_region(n, max(arcs, 1), seed=seed)

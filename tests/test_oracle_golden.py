@@ -110,11 +110,12 @@ def test_smooth_scores_and_anneal(case):
 
 
 def test_all_fixed_regions_make_no_move():
-    """A region without a free bead: the reference's CPU annealers redraw a
-    bead until a free one comes up and never return; the Philox-mode
-    annealers (and the kernels) draw among the movable beads only, so they
-    make no move and return the start.  The heatmap level reports 0 there,
-    as it does for a start score below 1e-6."""
+    """A region without a free bead: the reference's CPU heatmap and
+    smoothing annealers redraw a bead until a free one comes up and never
+    return, its CPU arc annealer stops the program on a fixed bead; the
+    Philox-mode annealers (and the kernels) draw among the movable beads
+    only, so they make no move and return the start.  The heatmap level
+    reports 0 there, as it does for a start score below 1e-6."""
     from pmmc_gb300 import synth
     prm = O.Params(max_temp=5.0, dt_temp=0.9999, milestone_steps=300, improvement=0.99,
                    k_stretch=0.1, k_squeeze=0.1, k_angle=0.1, w_dist=1.0, w_angle=1.0)
