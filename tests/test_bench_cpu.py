@@ -43,8 +43,9 @@ def test_reference_arm_ensemble():
     assert d["metric"] == "MC moves/s" and d["higher_is_better"] is True
 
 
-@pytest.mark.parametrize("workload,unit", [("targets", "arcs/s"),
-                                           ("smooth", "moves/s")])
+@pytest.mark.parametrize("workload,unit", [("targets", "arcs/s"), ("smooth", "moves/s"),
+                                           ("heatmap", "moves/s"), ("plain", "moves/s"),
+                                           ("stress", "iterations/s")])
 def test_reference_arm_workloads(workload, unit):
     check_line(run_bench("--impl", "reference", "--workload", workload, "--cpu-budget", "1"),
                unit)
