@@ -298,3 +298,20 @@ def test_philox_stream_matches_reference_stream_smooth():
     prm = O.Params(max_temp=5.0, dt_temp=0.9999, milestone_steps=3000, improvement=0.99,
                    k_stretch=0.1, k_squeeze=0.1)
     _dist_check(lambda mode, s: O.smooth_anneal(pr, prm, 0.5, 950 + s, rng=mode, chain=s), c.pos)
+
+
+@pytest.mark.parametrize("n,seed", [(64, 4), (128, 5)])
+def test_incremental_heatmap_baseline_anneals_the_same(n, seed):
+    """The O(N)-incremental form of the heatmap annealer, timed as the CPU
+    baseline beside the reference's full re-score per move, makes the same
+    decisions: same moves, same final positions, its running score within
+    1e-6 of the re-scored one."""
+    from pmmc_gb300 import synth
+    h = synth.heatmap_region(n, seed=seed, n_tads=3, tad_min=8, tad_max=30)
+    pr = O.HeatmapProblem(h.pos, h.heat, 1, np.zeros(0, np.int32))
+    prm = O.Params(max_temp=5.0, dt_temp=0.9999, milestone_steps=1000, improvement=0.99)
+    pf, rf = O.heatmap_anneal(pr, prm, 1.0, 11)
+    pi, ri = O.heatmap_anneal(pr, prm, 1.0, 11, incremental=True)
+    assert rf.moves == ri.moves
+    np.testing.assert_array_equal(pf, pi)
+    assert abs(rf.score - ri.score) <= 1e-6 * abs(rf.score)
