@@ -42,10 +42,18 @@ typedef enum pmmc_status {
 
 /* Stopping schedule of a chain. */
 enum {
-  /* The reference CUDA kernels (ParallelMonteCarloArcs.cu:520-658,
-   * ParallelMonteCarloSmooth.cu:267-337): milestones every 256 moves, stop
-   * after `milestone_fails` consecutive misses, at most `milestone_steps`
-   * moves (rounded up to 256). */
+  /* The reference CUDA kernels: moves in blocks of 256 while fewer than
+   * `milestone_steps` are done (so at most `milestone_steps` rounded up to
+   * 256, none when it is <= 0).  Arc level (ParallelMonteCarloArcs.cu:
+   * 520-655): a milestone after every block, the CPU predicate with its
+   * ratio test guarded by milestone energy > 1e-10, stop after
+   * `milestone_fails` consecutive misses or below 1e-5; an uphill move is
+   * tested only when T > 0 and the previous energy is > 0; with several
+   * chains the first to stop ends the others at their next milestone.
+   * Smoothing (ParallelMonteCarloSmooth.cu:267-337): every chain makes the
+   * whole cap (the kernel's milestone test cannot fire before its last
+   * block), and the reported chain is the one whose running energy reached
+   * the lowest value. */
   PMMC_SCHEDULE_GPU = 0,
   /* The reference CPU loops (LooperSolver.hpp:4764-4783, 1529-1553,
    * 5014-5034): a milestone every `milestone_steps` moves, stop at the first
@@ -129,7 +137,11 @@ typedef struct pmmc_arcs_problem {
 /* Heatmap-level active region: dense n x n expected-distance matrix
  * (row-major, symmetric as createDistanceHeatmap builds it,
  * LooperSolver.hpp:3042-3085), diagonal band width and optional chromosome
- * boundaries. */
+ * boundaries.  The annealers change the full score by twice a move's local
+ * change, which holds only for a symmetric map: a map whose pairs (i, m)
+ * inside one block and outside the diagonal band differ from (m, i) -- one
+ * side below 1e-6 and the other not, or unequal values -- is refused with
+ * PMMC_ERR_INVALID. */
 typedef struct pmmc_heatmap_problem {
   int n;
   const float *pos;            /* n*3                        */
@@ -273,10 +285,12 @@ pmmc_status pmmc_arcs_batch_anneal(pmmc_ctx *ctx, int n_units,
                                    pmmc_result *res);
 
 /* pmmc_arcs_batch_create with two more knobs: stop_all != 0 lets the first
- * converged chain of a unit stop its other chains (the reference's shared
- * d_isDone flag, ParallelMonteCarloArcs.cu:522,650); trace_cap > 0 records
- * the first trace_cap moves of chain 0 (bead, local scores before/after,
- * decision, displacement; 32 bytes each) for per-move parity checks. */
+ * converged chain of a unit stop its other chains at their next milestone
+ * (the reference's shared d_isDone flag, read once per 256-move block,
+ * ParallelMonteCarloArcs.cu:520,650); trace_cap > 0 records the first
+ * trace_cap moves of every chain of region 0 (bead, local scores
+ * before/after, decision, displacement; 32 bytes each) for per-move parity
+ * checks. */
 pmmc_status pmmc_arcs_batch_create_ex(pmmc_ctx *ctx, int n_units,
                                       const pmmc_arcs_problem *units,
                                       const pmmc_anneal_params *prm,
@@ -298,8 +312,18 @@ pmmc_status pmmc_selftest_sqrt(pmmc_ctx *ctx, uint32_t lo, uint32_t count,
 pmmc_status pmmc_arcs_batch_classes(pmmc_arcs_batch *b, int cap, int *n_classes,
                                     int *lanes, int *warps, int *items, int *nb_smem,
                                     int *drawing_warp);
-/* Copy `count` (<= trace_cap) trace records of the last run to host. */
+/* Copy `count` (<= trace_cap) trace records of chain 0 of the last run to
+ * host (tests; no reference counterpart). */
 pmmc_status pmmc_arcs_batch_trace(pmmc_arcs_batch *b, void *out, int count);
+/* The same for chain `chain` of region 0. */
+pmmc_status pmmc_arcs_batch_trace_chain(pmmc_arcs_batch *b, int chain, void *out, int count);
+/* The result of every chain of region `unit` of the last run, in chain order
+ * (up to `cap`; best_chain holds the chain's own index, total_moves the
+ * region's total), and the region's chain count.  The reference keeps the
+ * per-warp scores of its drop-in call in d_best_score
+ * (ParallelMonteCarloArcs.cu:661-667); this exposes the same per chain. */
+pmmc_status pmmc_arcs_batch_chain_results(pmmc_arcs_batch *b, int unit, int cap,
+                                          pmmc_result *res, int *n_chains);
 
 /* ---------------- batched smoothing and heatmap annealing -------------- */
 /* Many smoothing regions (genome-scale smoothing splits chromosomes at their
@@ -498,17 +522,25 @@ pmmc_status pmmc_hcm_write(const char *path, int n_clusters, const int *start, c
  * under a fixed memory budget.  Every pointer in *pr is a DEVICE pointer (the
  * caller's inputs: positions, optional fixed flags, row_ptr/col/target);
  * pos_out is a device buffer of n*3 floats; res is a host struct.  One chain
- * is annealed with the same kernel and Philox stream as pmmc_arcs_batch_*
- * with one chain (key = seed, chain 0), on `stream` (NULL = legacy default).
- * All intermediates live in one fixed device array of the library (about
- * 0.4 MB, held by every GPU that loads it until the process exits): regions
- * of at most 4096 beads and 16384 arc-list entries, no loop constraints;
- * larger regions return PMMC_ERR_BUDGET, loop constraints PMMC_ERR_INVALID.
- * Nothing is allocated: no cudaMalloc/cudaFree and no allocating library
- * call.  The first call on a device looks up the array's device address
- * (with that device current) and should come before any stream capture.
- * Calls share the array and each starts by re-initialising it; calls whose
- * work overlaps on the GPU (two streams, two host threads) race on it. */
+ * is annealed exactly as pmmc_arcs_batch_* anneals a one-chain region with
+ * two lanes per proposal and no drawing warp (key = seed, chain 0): the same
+ * kernel, arc-list staging, repulsion sum and recompute order, so positions,
+ * energies and move counts are bit-identical to that call.  All
+ * intermediates live in one fixed device array of the library (688,352
+ * bytes, about 0.69 MB), reserved on a device when the library's module is
+ * loaded there -- lazily, at its first use, under CUDA's default lazy module
+ * loading -- and held until the process exits: regions of at most 4096 beads
+ * and 16384 arc-list entries, no loop constraints; a larger region returns
+ * PMMC_ERR_BUDGET, loop constraints or malformed arc lists (row pointers out
+ * of order, a column out of range) PMMC_ERR_INVALID, and a rejected call
+ * writes nothing to pos_out.  Nothing is allocated: no cudaMalloc/cudaFree
+ * and no allocating library call.  The array's device address is looked up
+ * (with the device current) at the first call on each device and again after
+ * the device's context changed (a cudaDeviceReset); that first call should
+ * come before any stream capture.  The call blocks: it waits on `stream`
+ * twice, for the check of the arc lists and for the result.  Calls share the
+ * array, each one re-initialises it; calls whose work overlaps on the GPU
+ * (two streams, two host threads) race on it. */
 pmmc_status pmmc_arcs_anneal_noalloc(const pmmc_arcs_problem *pr,
                                      const pmmc_anneal_params *prm,
                                      float step_size, uint64_t seed,

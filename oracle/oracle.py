@@ -26,6 +26,10 @@ REF_PATH = os.path.join(HERE, "_ref", "libpmmc_ref.so")
 
 RNG_LIBC = 0
 RNG_PHILOX = 1
+# stopping schedules (orc_params.schedule): the reference's CPU loops, or the
+# schedule of its CUDA kernels (256-move blocks, milestone_fails)
+SCHEDULE_CPU = 0
+SCHEDULE_GPU = 1
 
 
 class OrcParams(C.Structure):
@@ -45,6 +49,8 @@ class OrcParams(C.Structure):
         ("sphere_radius", C.c_float),
         ("use2d", C.c_int),
         ("max_moves", C.c_int64),
+        ("schedule", C.c_int),
+        ("milestone_fails", C.c_int),
     ]
 
 
@@ -63,6 +69,7 @@ class OrcResult(C.Structure):
         ("moves", C.c_int64),
         ("accepted", C.c_int64),
         ("proposals", C.c_int64),
+        ("best", C.c_double),
     ]
 
 
@@ -86,6 +93,8 @@ class Params:
     sphere_radius: float = 0.0
     use2d: int = 0
     max_moves: int = 0
+    schedule: int = SCHEDULE_CPU
+    milestone_fails: int = 3
 
     def c(self) -> OrcParams:
         return OrcParams(*[getattr(self, f[0]) for f in OrcParams._fields_])
@@ -470,7 +479,8 @@ def philox(ctr, key):
 class ReplayOut(C.Structure):
     _fields_ = [("before", C.c_void_p), ("after", C.c_void_p), ("orc_acc", C.c_void_p),
                 ("margin", C.c_void_p), ("proposal_mismatch", C.c_int),
-                ("final_energy", C.c_double)]
+                ("final_energy", C.c_double), ("stop_at", C.c_int64),
+                ("stop_margin", C.c_double)]
 
 
 def _replay_prep(trace):
@@ -483,14 +493,15 @@ def _replay_prep(trace):
     after = np.zeros(m, np.float64)
     oacc = np.zeros(m, np.int32)
     margin = np.zeros(m, np.float64)
-    out = ReplayOut(_p(before), _p(after), _p(oacc), _p(margin), 0, 0.0)
+    out = ReplayOut(_p(before), _p(after), _p(oacc), _p(margin), 0, 0.0, -1, 0.0)
     keep = (bead, disp, acc, before, after, oacc, margin)
     return m, bead, disp, acc, out, keep
 
 
 def _replay_result(out, keep):
     return {"before": keep[3], "after": keep[4], "orc_acc": keep[5], "margin": keep[6],
-            "proposal_mismatch": out.proposal_mismatch, "final_energy": out.final_energy}
+            "proposal_mismatch": out.proposal_mismatch, "final_energy": out.final_energy,
+            "stop_at": out.stop_at, "stop_margin": out.stop_margin}
 
 
 def arcs_replay(pr: ArcsProblem, prm: Params, step: float, seed: int, chain: int, trace,

@@ -338,7 +338,20 @@ double orc_arcs_local_score(int n, const float *pos, const float *exp_dist,
 /* LooperSolver::MonteCarloArcs (LooperSolver.hpp:4670-4796).  Differences
  * only where the reference has no counterpart: the Philox source picks among
  * movable beads directly and keeps the pre-move position on rejection (as the
- * CUDA kernels do) instead of subtracting the displacement back. */
+ * CUDA kernels do) instead of subtracting the displacement back.
+ *
+ * ORC_SCHEDULE_GPU restates the schedule of the reference's arc kernel
+ * (MonteCarloArcsKernel, src/ParallelMonteCarloArcs.cu:494-655) around the
+ * same moves: blocks of 256 moves while fewer than milestone_steps moves are
+ * done (:522,631), so the cap is milestone_steps rounded up to 256 and no
+ * move at all when it is <= 0; an uphill move is tested only when T > 0 and
+ * the previous score is > 0 (:598-603), otherwise it is rejected without a
+ * draw; after every block the milestone predicate (:635-641) -- the CPU one
+ * with the ratio test guarded by milestone_score > 1e-10 -- counts
+ * consecutive misses (:643-646), and the chain stops when they reach
+ * milestone_fails or the score drops below 1e-5 (:648-650).  The kernel keeps
+ * its score in float; this restatement keeps it in double, the precision
+ * form the GPU path reproduces. */
 static double ext_full(int n, const float *pos, const orc_ext *x);
 static double ext_local(int n, const float *pos, const orc_ext *x, int moved);
 
@@ -373,8 +386,12 @@ void orc_arcs_anneal_ext(int n, float *pos, const unsigned char *fixed,
   double score_prev = score_curr, milestone_score = score_curr;
   int64_t success = 0, milestone_success = 0, i = 1;
   int philox = rng->kind == ORC_RNG_PHILOX;
+  int gpu = p->schedule == ORC_SCHEDULE_GPU;
+  int64_t cap = p->milestone_steps > 0 ? ((int64_t)p->milestone_steps + 255) / 256 * 256 : 0;
+  int misses = 0;
 
-  if (philox && c.n_movable == 0) { /* nothing can move */
+  res->best = score_curr;
+  if ((philox && c.n_movable == 0) || (gpu && cap == 0)) { /* nothing moves */
     res->score = score_curr;
     goto done;
   }
@@ -406,13 +423,14 @@ void orc_arcs_anneal_ext(int n, float *pos, const unsigned char *fixed,
       lc += ext_local(n, pos, x, pb);
     score_curr = score_curr - lp + lc;
     int ok = score_curr <= score_prev;
-    if (!ok) {
+    if (!ok && (!gpu || (T > 0.0 && score_prev > 0.0))) {
       tp = p->jump_scale * exp(-p->jump_coef * (score_curr / score_prev) / T);
       ok = draw_chance(&c, (float)tp);
     }
     if (ok) {
       success++;
       milestone_success++;
+      if (score_curr < res->best) res->best = score_curr;
     } else {
       if (philox) {
         q[0] = old[0];
@@ -427,7 +445,21 @@ void orc_arcs_anneal_ext(int n, float *pos, const unsigned char *fixed,
     }
     end_move(&c);
     T *= dt;
-    if (i % p->milestone_steps == 0) {
+    if (gpu) {
+      if (i % 256 == 0) {
+        int miss = (score_curr > p->improvement * milestone_score &&
+                    milestone_success < p->min_successes) ||
+                   score_curr < 1e-5 ||
+                   (milestone_score > 1e-10 && score_curr / milestone_score > 0.9999);
+        misses = miss ? misses + 1 : 0;
+        if (misses >= p->milestone_fails || score_curr < 1e-5)
+          break;
+        milestone_score = score_curr;
+        milestone_success = 0;
+        if (i >= cap)
+          break;
+      }
+    } else if (i % p->milestone_steps == 0) {
       if ((score_curr > p->improvement * milestone_score &&
            milestone_success < p->min_successes) ||
           score_curr < 1e-5 || score_curr / milestone_score > 0.9999)
@@ -823,7 +855,19 @@ double orc_arcs_ext_score(int n, const float *pos, const orc_ext *x, int moved) 
 }
 
 /* MonteCarloArcsSmooth (LooperSolver.hpp:4798-5047), orientation and
- * subanchor-heatmap terms off. */
+ * subanchor-heatmap terms off.
+ *
+ * ORC_SCHEDULE_GPU restates the schedule of the reference's smoothing kernel
+ * (MonteCarloSmoothKernelMultiWarp, src/ParallelMonteCarloSmooth.cu:258-337):
+ * blocks of 256 moves while fewer than milestone_steps moves are done
+ * (:267-269,317), so exactly milestone_steps rounded up to 256 moves (none
+ * when it is <= 0).  Its milestone test (:320-335) runs only when
+ * iterations % milestone_steps < 256, which inside that loop happens only
+ * after the last block, so it never shortens the chain and is not restated.
+ * An uphill move is tested against
+ * scale * exp(-coef * (E_new / max(E_prev, 1e-12)) / T) when T > 0 (:291-296).
+ * res->best is the lowest running score of the chain (:299-301), by which the
+ * reference's host picks the reported warp (:462-472). */
 void orc_smooth_anneal(int n, float *pos, const unsigned char *fixed,
                        const double *dist_to_next, const orc_params *p,
                        float step_size, orc_rng *rng, orc_result *res) {
@@ -837,7 +881,10 @@ void orc_smooth_anneal(int n, float *pos, const unsigned char *fixed,
   double score_curr = curr_structure + 0.0 + 0.0;
   double score_prev = score_curr, milestone_score = score_curr;
   int64_t success = 0, milestone_success = 0, i = 1;
-  if (philox && c.n_movable == 0) {
+  int gpu = p->schedule == ORC_SCHEDULE_GPU;
+  int64_t cap = p->milestone_steps > 0 ? ((int64_t)p->milestone_steps + 255) / 256 * 256 : 0;
+  res->best = score_curr;
+  if ((philox && c.n_movable == 0) || (gpu && cap == 0)) {
     res->score = score_curr;
     rng_end(&c);
     return;
@@ -859,7 +906,8 @@ void orc_smooth_anneal(int n, float *pos, const unsigned char *fixed,
     score_curr = curr_structure + 0.0 + 0.0;
     int ok = score_curr < score_prev;
     if (!ok && T > 0.0) {
-      tp = p->jump_scale * exp(-p->jump_coef * (score_curr / score_prev) / T);
+      double den = gpu && score_prev < 1e-12 ? 1e-12 : score_prev;
+      tp = p->jump_scale * exp(-p->jump_coef * (score_curr / den) / T);
       ok = draw_chance(&c, (float)tp);
     }
     if (ok) {
@@ -867,6 +915,7 @@ void orc_smooth_anneal(int n, float *pos, const unsigned char *fixed,
       milestone_success++;
       score_prev = score_curr;
       prev_structure = curr_structure;
+      if (score_curr < res->best) res->best = score_curr;
     } else {
       if (philox) {
         q[0] = old[0];
@@ -881,7 +930,9 @@ void orc_smooth_anneal(int n, float *pos, const unsigned char *fixed,
       curr_structure = prev_structure;
     }
     end_move(&c);
-    if (i % p->milestone_steps == 0) {
+    if (gpu) {
+      if (i >= cap) break;
+    } else if (i % p->milestone_steps == 0) {
       if ((score_curr > p->improvement * milestone_score &&
            milestone_success < p->min_successes) ||
           score_curr < 1e-6)
@@ -1115,8 +1166,60 @@ static double heat_local_cb(void *vc, const float *pos, int moved) {
   return hm_local(c->n, pos, c->heat, c->diag, c->n_bounds, c->bounds, moved);
 }
 
-/* kind: 0 arcs (<=, no T check), 1 heatmap (<=, T>0, delta counted twice),
- * 2 smoothing (strict <, T>0). */
+/* Relative distance of a from the threshold b (for the stop margin). */
+static double rel_gap(double a, double b) {
+  double s = fabs(b) > 0.0 ? fabs(b) : 1.0;
+  return fabs(a - b) / s;
+}
+
+/* The milestone predicate of `kind` under p->schedule at counted move i,
+ * with the running energy E, the milestone energy *E_ms and the successes
+ * since it; updates the milestone state and returns 1 when the annealer
+ * stops after move i.  CPU schedule: MonteCarloArcs :4765-4783,
+ * MonteCarloHeatmap :1543-1553, MonteCarloArcsSmooth :5015-5034; GPU
+ * schedule: ParallelMonteCarloArcs.cu:631-655 (arcs),
+ * ParallelMonteCarloSmooth.cu:267-317 (smoothing: the cap alone). */
+static int schedule_stop(int kind, const orc_params *p, int64_t i, double E,
+                         double *E_ms, int64_t *succ, int *misses, double *margin) {
+  int gpu = p->schedule == ORC_SCHEDULE_GPU && kind != 1;
+  int stop = 0;
+  if (gpu && kind == 2) {
+    int64_t cap = p->milestone_steps > 0 ? ((int64_t)p->milestone_steps + 255) / 256 * 256 : 0;
+    stop = i >= cap;
+  } else if (gpu) {
+    if (i % 256 == 0) {
+      int64_t cap = p->milestone_steps > 0 ? ((int64_t)p->milestone_steps + 255) / 256 * 256 : 0;
+      int slow = *succ < p->min_successes;
+      int guard = *E_ms > 1e-10;
+      int miss = (E > p->improvement * *E_ms && slow) || E < 1e-5 ||
+                 (guard && E / *E_ms > 0.9999);
+      if (slow) *margin = fmin(*margin, rel_gap(E, p->improvement * *E_ms));
+      if (guard) *margin = fmin(*margin, rel_gap(E / *E_ms, 0.9999));
+      *margin = fmin(*margin, rel_gap(E, 1e-5));
+      *misses = miss ? *misses + 1 : 0;
+      stop = *misses >= p->milestone_fails || E < 1e-5 || i >= cap;
+      *E_ms = E;
+      *succ = 0;
+    }
+  } else if (p->milestone_steps > 0 && i % p->milestone_steps == 0) {
+    double floor = kind == 0 ? 1e-5 : 1e-6;
+    int slow = *succ < p->min_successes;
+    int miss = (E > p->improvement * *E_ms && slow) || E < floor;
+    if (kind == 0) miss = miss || E / *E_ms > 0.9999;
+    if (slow) *margin = fmin(*margin, rel_gap(E, p->improvement * *E_ms));
+    if (kind == 0) *margin = fmin(*margin, rel_gap(E / *E_ms, 0.9999));
+    *margin = fmin(*margin, rel_gap(E, floor));
+    stop = miss;
+    *E_ms = E;
+    *succ = 0;
+  }
+  if (!stop && p->max_moves > 0 && i >= p->max_moves) stop = 1;
+  return stop;
+}
+
+/* kind: 0 arcs (<=; CPU schedule: no T check, GPU schedule: T > 0 and
+ * E > 0), 1 heatmap (<=, T>0, delta counted twice), 2 smoothing (strict <,
+ * T>0; GPU schedule: the ratio's denominator at least 1e-12). */
 static void replay_core(int kind, void *ctx, local_fn fn, int n, float *pos,
                         const unsigned char *fixed, const orc_params *p,
                         float step, double E, uint64_t seed, uint32_t chain,
@@ -1130,7 +1233,13 @@ static void replay_core(int kind, void *ctx, local_fn fn, int n, float *pos,
   rng_ctx c;
   rng_begin(&c, &r, n, fixed);
   double T = p->max_temp;
+  int gpu = p->schedule == ORC_SCHEDULE_GPU;
+  double E_ms = E;
+  int64_t succ = 0;
+  int misses = 0;
   out->proposal_mismatch = 0;
+  out->stop_at = -1;
+  out->stop_margin = 1e300;
   for (int k = 0; k < n_moves; ++k) {
     int b = draw_bead(&c, n);
     float d[3];
@@ -1154,8 +1263,10 @@ static void replay_core(int kind, void *ctx, local_fn fn, int n, float *pos,
     uint32_t o[4];
     philox_block(&r, 1u, o);
     float u = orc_u01(o[0]);
-    if (!ok && (kind == 0 || T > 0.0)) {
-      double tp = p->jump_scale * exp(-p->jump_coef * (En / E) / T);
+    int test = kind == 0 ? (!gpu || (T > 0.0 && E > 0.0)) : T > 0.0;
+    if (!ok && test) {
+      double den = (kind == 2 && gpu && E < 1e-12) ? 1e-12 : E;
+      double tp = p->jump_scale * exp(-p->jump_coef * (En / den) / T);
       ok = u < (float)tp;
     }
     /* distance of the decision from its threshold, in log-ratio units */
@@ -1169,11 +1280,15 @@ static void replay_core(int kind, void *ctx, local_fn fn, int n, float *pos,
     out->margin[k] = margin;
     if (gpu_acc[k]) {
       E = En;
+      succ++;
     } else {
       q[0] = old[0];
       q[1] = old[1];
       q[2] = old[2];
     }
+    if (out->stop_at < 0 &&
+        schedule_stop(kind, p, (int64_t)k + 1, E, &E_ms, &succ, &misses, &out->stop_margin))
+      out->stop_at = (int64_t)k + 1;
     r.move++;
     T *= p->dt_temp;
   }

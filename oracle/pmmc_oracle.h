@@ -44,7 +44,23 @@ typedef struct orc_params {
   float sphere_radius; /* sphere_radius (0 = no container)                  */
   int use2d;           /* use2D                                             */
   int64_t max_moves;   /* oracle-only safety cap on counted moves (0: none) */
+  int schedule;        /* ORC_SCHEDULE_CPU (0) or ORC_SCHEDULE_GPU (1)       */
+  int milestone_fails; /* milestoneFailsThreshold ([cuda] milestone_fails)   */
 } orc_params;
+
+/* Stopping schedule of an annealer.
+ *  ORC_SCHEDULE_CPU : the reference's CPU loops (MonteCarloArcs,
+ *                     MonteCarloHeatmap, MonteCarloArcsSmooth): a milestone
+ *                     every milestone_steps moves, stop at the first miss.
+ *  ORC_SCHEDULE_GPU : the reference's CUDA kernels, restated from their
+ *                     source (src/ParallelMonteCarloArcs.cu:494-655,
+ *                     src/ParallelMonteCarloSmooth.cu:258-337): moves in
+ *                     blocks of 256, milestone_steps caps the moves; the arc
+ *                     kernel tests a milestone after every block and stops
+ *                     after milestone_fails consecutive misses, the
+ *                     smoothing kernel runs every block of its cap.  The
+ *                     heatmap annealer has only the CPU schedule. */
+enum { ORC_SCHEDULE_CPU = 0, ORC_SCHEDULE_GPU = 1 };
 
 /* Random-number source of an oracle annealer.
  *  ORC_RNG_LIBC   : the reference's own stream -- libc rand() after
@@ -66,6 +82,9 @@ typedef struct orc_result {
   int64_t moves;       /* counted moves (the reference's loop index i)  */
   int64_t accepted;    /* accepted moves                                */
   int64_t proposals;   /* proposals drawn, incl. skipped fixed beads    */
+  double best;         /* lowest running score seen, the start included
+                        * (the smoothing kernel's per-warp best score,
+                        * ParallelMonteCarloSmooth.cu:299,341)          */
 } orc_result;
 
 /* ---------------- Philox4x32-10 (Salmon et al., SC'11) ---------------- */
@@ -213,6 +232,14 @@ typedef struct orc_replay_out {
   double *margin;
   int proposal_mismatch;
   double final_energy; /* oracle running energy after the last move */
+  /* Stopping point of p->schedule along the kernel's decisions and the
+   * oracle's FP64 running energy: the counted moves after which the
+   * annealer stops (-1: not within the trace), and the smallest relative
+   * distance of a milestone comparison that decided it from its threshold
+   * (a kernel whose running energy differs in the last bits can stop
+   * elsewhere only when this is tiny). */
+  int64_t stop_at;
+  double stop_margin;
 } orc_replay_out;
 
 void orc_arcs_replay(int n, const float *pos0, const unsigned char *fixed,

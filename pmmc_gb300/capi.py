@@ -44,7 +44,7 @@ HEADER_SYMBOLS = [
     "pmmc_server_get_stats", "pmmc_server_destroy", "pmmc_arcs_batch_classes",
     "pmmc_selftest_sqrt", "pmmc_distance_heatmap", "pmmc_distance_heatmap_device",
     "pmmc_equidistant_model", "pmmc_hcm_write", "pmmc_anchor_targets", "pmmc_stress_refine",
-    "pmmc_server_cancel",
+    "pmmc_server_cancel", "pmmc_arcs_batch_trace_chain", "pmmc_arcs_batch_chain_results",
 ]
 
 LANES_AUTO = -1  # PMMC_LANES_AUTO: the autotuner picks lanes and warps per class
@@ -363,11 +363,23 @@ class ArcsBatch:
         return [(la[k], wa[k], it[k], bool(nb[k]), bool(dw[k]))
                 for k in range(min(n.value, cap))]
 
-    def trace(self, count=None):
+    def trace(self, count=None, chain=0):
+        """The first `count` trace records of chain `chain` of region 0."""
         count = self.trace_cap if count is None else count
         out = np.zeros(count, TRACE_DTYPE)
-        self.ctx.check(lib().pmmc_arcs_batch_trace(self.h, _p(out), int(count)))
+        self.ctx.check(lib().pmmc_arcs_batch_trace_chain(self.h, int(chain), _p(out),
+                                                         int(count)))
         return out
+
+    def chain_results(self, unit=0):
+        """The result of every chain of region `unit`, in chain order."""
+        n = C.c_int()
+        self.ctx.check(lib().pmmc_arcs_batch_chain_results(self.h, int(unit), 0, None,
+                                                           C.byref(n)))
+        res = (Result * max(n.value, 1))()
+        self.ctx.check(lib().pmmc_arcs_batch_chain_results(self.h, int(unit), n.value, res,
+                                                           C.byref(n)))
+        return [res[k] for k in range(n.value)]
 
     def close(self):
         if self.h:

@@ -49,6 +49,8 @@
 #include <thread>
 #include <vector>
 
+#include <cuda.h>  // driver types only (CUcontext); no link to the driver library
+
 #include "arcs_impl.h"
 
 namespace pmmc {
@@ -471,12 +473,12 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
     double T = P.max_temp;
     long long moves = 0, accepted = 0;
     int succ_ms = 0, misses = 0, status = kDevOk;
-    bool stop = U.n_mov == 0;
-    if (stop) status = kDevNoMovable;
+    bool stop = U.n_mov == 0 || P.cap <= 0;
+    if (U.n_mov == 0) status = kDevNoMovable;
     const float step = U.step;
     const float ks = P.k_stretch, kq = P.k_squeeze, R = P.sphere_r;
-    const bool tracing = trace != nullptr && chain_id == 0;
-    int batch_no = 0;
+    const bool tracing = trace != nullptr && chain_id < (uint32_t)P.trace_chains;
+    MoveTrace *const ctrace = tracing ? trace + (size_t)chain_id * P.trace_cap : nullptr;
 
     // ---- windows of W = 32/G proposals, G lanes each ----
     // Every proposal of a window is scored against the positions at the
@@ -704,7 +706,7 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
             tr.dy = __int_as_float(m.z);
             tr.dz = __int_as_float(m.w);
             tr.pad = s_d[j];
-            trace[moves + j] = tr;
+            ctrace[moves + j] = tr;
           }
         }
       }
@@ -716,20 +718,21 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
       accepted += na;
       succ_ms += na;
       moves += lend;
-      ++batch_no;
       if (PROD && lane == 0) {
         __threadfence_block();  // this window's reads of the ring are done
         *(volatile long long *)&ctl->consumed = moves;
       }
 
-      // ---- milestone (the reference CPU predicate, FP64, every lane) ----
+      // ---- milestone (the reference predicate, FP64, every lane; the
+      // reference kernel guards the ratio test by E_ms > 1e-10) ----
       bool flag = false;
-      if (moves == next_ms) {
+      const bool at_ms = moves == next_ms;
+      if (at_ms) {
         next_ms += P.window;
         const double E = (double)e_hi + (double)e_lo;
         const bool miss =
             (E > (double)P.improvement * E_ms && succ_ms < P.min_successes) ||
-            E < 1e-5 || E / E_ms > 0.9999;
+            E < 1e-5 || ((!P.ms_guard || E_ms > 1e-10) && E / E_ms > 0.9999);
         misses = miss ? misses + 1 : 0;
         if (misses >= P.fails || E < 1e-5) flag = true;
         E_ms = E;
@@ -752,11 +755,13 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
         flag = true;
         if (P.cap_is_error) status = kDevMoveCap;
       }
+      // the first chain to stop ends its unit's others at their next
+      // milestone (the reference's shared d_isDone, read once per 256-move
+      // block, ParallelMonteCarloArcs.cu:520,650)
       int f = flag ? 1 : 0;
       if (lane == 0) {
         if (f && P.stop_all) atomicExch(done_flag, 1);
-        if (!f && P.stop_all && (batch_no & 31) == 0 && *((volatile int *)done_flag) != 0)
-          f = 1;
+        if (!f && P.stop_all && at_ms && *((volatile int *)done_flag) != 0) f = 1;
       }
       stop = __shfl_sync(0xffffffffu, f, 0) != 0;
     }
@@ -769,6 +774,7 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
       o.energy = (double)e_hi + (double)e_lo;
       o.energy_fp64 = base + es;
       o.base = base;
+      o.best = o.energy;  // not tracked at the arc level
       o.score = e_hi;
       o.status = status;
       o.moves = moves;
@@ -1012,10 +1018,15 @@ ArcsDevParams arcs_make_params(const pmmc_anneal_params *prm, uint64_t seed, boo
     P.cap = prm->max_moves > 0 ? prm->max_moves : 200ll * P.window;
     P.cap_is_error = 0;
   } else {
+    // MonteCarloArcsKernel (ParallelMonteCarloArcs.cu:520-655): blocks of
+    // 256 moves while fewer than stop_condition_steps are done, a milestone
+    // after each block, stop after milestone_fails consecutive misses (a
+    // threshold <= 0 stops at the first milestone, as there)
     P.window = 256;
-    P.fails = std::max(1, prm->milestone_fails);
-    long long cap = std::max(1, prm->milestone_steps);
-    cap = (cap + 255) / 256 * 256;
+    P.fails = prm->milestone_fails;
+    P.ms_guard = 1;
+    long long cap = prm->milestone_steps > 0 ? ((long long)prm->milestone_steps + 255) / 256 * 256
+                                             : 0;
     if (prm->max_moves > 0) cap = std::min(cap, (long long)prm->max_moves);
     P.cap = cap;
     P.cap_is_error = 0;
@@ -1650,8 +1661,10 @@ extern "C" pmmc_status pmmc_arcs_batch_create_ex(
   if (e == cudaSuccess) e = b->bases.alloc((size_t)n_units);
   if (e == cudaSuccess) e = arcs_bases(b->units.p, n_units, b->pos0.p, b->row_ptr.p, b->nbr.p,
                                        b->nulls.p, b->bases.p, s);
+  // tests: the first trace_cap moves of every chain of region 0
+  b->P.trace_chains = trace_cap > 0 ? b->h_units[0].chains : 0;
   if (e == cudaSuccess && trace_cap > 0)
-    e = cudaMalloc(&b->trace, sizeof(MoveTrace) * (size_t)trace_cap);
+    e = cudaMalloc(&b->trace, sizeof(MoveTrace) * (size_t)trace_cap * b->P.trace_chains);
   if (e == cudaSuccess) e = cudaEventCreate(&b->ev_fork);
   if (e == cudaSuccess) e = cudaEventCreate(&b->ev_start);
   if (e == cudaSuccess) e = cudaEventCreate(&b->ev_stop);
@@ -1845,13 +1858,51 @@ extern "C" pmmc_status pmmc_arcs_batch_classes(pmmc_arcs_batch *b, int cap, int 
   return PMMC_OK;
 }
 
-// Tests only: copy the per-move trace of chain 0 of the batch.
-extern "C" pmmc_status pmmc_arcs_batch_trace(pmmc_arcs_batch *b, void *out, int count) {
-  if (!b || !b->trace || count < 0 || count > b->P.trace_cap) return PMMC_ERR_INVALID;
+// Tests only: copy the per-move trace of chain `chain` of region 0.
+extern "C" pmmc_status pmmc_arcs_batch_trace_chain(pmmc_arcs_batch *b, int chain, void *out,
+                                                   int count) {
+  if (!b || !b->trace || !out || count < 0 || count > b->P.trace_cap || chain < 0 ||
+      chain >= b->P.trace_chains)
+    return PMMC_ERR_INVALID;
   pmmc_ctx *ctx = b->ctx;
   PMMC_CUDA(ctx, cudaEventSynchronize(b->ev_stop));
-  PMMC_CUDA(ctx, cudaMemcpy(out, b->trace, sizeof(MoveTrace) * (size_t)count,
-                            cudaMemcpyDeviceToHost));
+  PMMC_CUDA(ctx, cudaMemcpy(out, b->trace + (size_t)chain * b->P.trace_cap,
+                            sizeof(MoveTrace) * (size_t)count, cudaMemcpyDeviceToHost));
+  return PMMC_OK;
+}
+
+extern "C" pmmc_status pmmc_arcs_batch_trace(pmmc_arcs_batch *b, void *out, int count) {
+  return pmmc_arcs_batch_trace_chain(b, 0, out, count);
+}
+
+// Every chain of one region (positions aside), in chain order.
+extern "C" pmmc_status pmmc_arcs_batch_chain_results(pmmc_arcs_batch *b, int unit, int cap,
+                                                     pmmc_result *res, int *n_chains) {
+  if (!b || !b->ran || unit < 0 || unit >= b->n_units || (cap > 0 && !res))
+    return PMMC_ERR_INVALID;
+  pmmc_ctx *ctx = b->ctx;
+  const ArcsUnit &U = b->h_units[unit];
+  if (n_chains) *n_chains = U.chains;
+  PMMC_CUDA(ctx, cudaEventSynchronize(b->ev_stop));
+  std::vector<ChainOut> outs((size_t)U.chains);
+  PMMC_CUDA(ctx, cudaMemcpy(outs.data(), b->outs.p + U.chain_base,
+                            sizeof(ChainOut) * outs.size(), cudaMemcpyDeviceToHost));
+  long long tot = 0;
+  for (const ChainOut &o : outs) tot += o.moves;
+  for (int c = 0; c < U.chains && c < cap; ++c) {
+    const ChainOut &o = outs[c];
+    pmmc_result r{};
+    r.score = o.score;
+    r.energy = o.energy;
+    r.energy_fp64 = o.energy_fp64;
+    r.rel_error = std::fabs(o.energy - o.energy_fp64) / std::max(std::fabs(o.energy_fp64), 1e-30);
+    r.moves = o.moves;
+    r.accepted = o.accepted;
+    r.total_moves = tot;
+    r.best_chain = c;
+    r.status = o.status;
+    res[c] = r;
+  }
   return PMMC_OK;
 }
 
@@ -1903,7 +1954,9 @@ extern "C" pmmc_status pmmc_arcs_anneal(pmmc_ctx *ctx, const pmmc_arcs_problem *
 // between stream-capture phases that must not trigger allocations).  The
 // caller passes device-resident inputs and an output buffer; every
 // intermediate the anneal needs lives in one file-scope device array of
-// fixed size, which every GPU that loads this library holds until exit.
+// fixed size, reserved on a device when this library's module is loaded
+// there (lazily, at its first use, under CUDA's default lazy loading) and
+// held until the process exits.
 namespace {
 
 constexpr int kNoAllocMaxBeads = 4096;      // beads of the region
@@ -1916,57 +1969,92 @@ struct NoAllocScratch {
   int done;
   int best;
   int n_null;
-  int status;
-  int pad[3];
+  // written by noalloc_check_kernel, read back by the host in one copy
+  int status;     // 0 ok, 1 malformed arc lists, 2 more entries than the scratch holds
+  int nnz;        // entries of the caller's arc lists (row_ptr[n])
+  int n_spring;   // spring entries (target >= 1e-6, partner != bead)
+  int n_mov;      // movable beads
   ChainOut out;
+  double base;    // frozen repulsion of the start (arcs_base_kernel)
   float4 pos0[kNoAllocMaxBeads];
   int row_ptr[kNoAllocMaxBeads + 1];
   int movable[kNoAllocMaxBeads];
   int2 nbr[kNoAllocMaxEntries];
   float inv_t[kNoAllocMaxEntries];
   int2 nulls[kNoAllocMaxEntries];
-  int4 lst[1];
+  int4 lst[kNoAllocMaxEntries];  // every spring once: the energy recompute's list
 };
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[sizeof(NoAllocScratch)];
 
-// One block packs the caller's region into the scratch array: float4
-// positions, spring-only arc lists with reciprocals, inert pairs, movable
-// list, work item and counters (the counters must start at zero).
-__global__ void noalloc_stage_kernel(NoAllocScratch *S, int n, int nnz, const float *pos,
+// One block checks the caller's arc lists before anything reads through
+// them (row pointers in order and within row_ptr[n], columns in range, the
+// entry count within the scratch) and counts the spring entries and the
+// movable beads, which decide the shared-memory layout as in the batched
+// path.  A rejected region leaves every caller buffer untouched.
+__global__ void noalloc_check_kernel(NoAllocScratch *S, int n, const unsigned char *fixed,
+                                     const int *row_ptr, const int *col, const float *target,
+                                     int lists_given) {
+  __shared__ int s_bad, s_spring, s_mov;
+  const int t = threadIdx.x;
+  const int nnz = row_ptr[n];
+  if (t == 0) {
+    s_bad = (row_ptr[0] != 0 || nnz < 0 || (nnz > 0 && !lists_given)) ? 1 : 0;
+    if (nnz > kNoAllocMaxEntries) s_bad = 2;
+    s_spring = 0;
+    s_mov = 0;
+  }
+  __syncthreads();
+  if (s_bad == 0)
+    for (int i = t; i < n; i += blockDim.x) {
+      const int a = row_ptr[i], z = row_ptr[i + 1];
+      if (a < 0 || z < a || z > nnz) atomicOr(&s_bad, 1);
+    }
+  __syncthreads();
+  if (s_bad == 0) {
+    int sp = 0, mv = 0;
+    for (int i = t; i < n; i += blockDim.x) {
+      mv += (fixed && fixed[i]) ? 0 : 1;
+      for (int e = row_ptr[i]; e < row_ptr[i + 1]; ++e) {
+        const int j = col[e];
+        if (j < 0 || j >= n) atomicOr(&s_bad, 1);
+        sp += (target[e] >= 1e-6f && j != i) ? 1 : 0;
+      }
+    }
+    atomicAdd(&s_spring, sp);
+    atomicAdd(&s_mov, mv);
+  }
+  __syncthreads();
+  if (t == 0) {
+    S->status = s_bad;
+    S->nnz = nnz;
+    S->n_spring = s_spring;
+    S->n_mov = s_mov;
+  }
+}
+
+// One block packs a checked region into the scratch array as the batched
+// path packs it on the host: float4 positions, spring-only arc lists with
+// reciprocals, inert pairs, the flat spring list, the movable list, the
+// work item and counters (which must start at zero).
+__global__ void noalloc_stage_kernel(NoAllocScratch *S, int n, const float *pos,
                                      const unsigned char *fixed, const int *row_ptr,
                                      const int *col, const float *target, float step,
                                      uint64_t seed) {
   __shared__ int s_cnt[kNoAllocMaxBeads + 1];
   __shared__ int s_mov[kNoAllocMaxBeads + 1];
-  __shared__ int s_bad;
   const int t = threadIdx.x;
-  if (t == 0) s_bad = 0;
-  __syncthreads();
-  // the caller's arc lists are checked before anything reads through them
-  for (int i = t; i < n; i += blockDim.x) {
-    const int a = row_ptr[i], z = row_ptr[i + 1];
-    if (a < 0 || z < a || z > nnz) atomicOr(&s_bad, 1);
-  }
-  if (t == 0 && row_ptr[0] != 0) atomicOr(&s_bad, 1);
-  __syncthreads();
-  if (!s_bad)
-    for (int e = t; e < nnz; e += blockDim.x)
-      if (col[e] < 0 || col[e] >= n) atomicOr(&s_bad, 1);
-  __syncthreads();
-  const bool bad = s_bad != 0;
   for (int i = t; i < n; i += blockDim.x) {
     S->pos0[i] = make_float4(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2], 0.0f);
     int c = 0;
-    if (!bad)
-      for (int e = row_ptr[i]; e < row_ptr[i + 1]; ++e)
-        c += (target[e] >= 1e-6f && col[e] != i) ? 1 : 0;
+    for (int e = row_ptr[i]; e < row_ptr[i + 1]; ++e)
+      c += (target[e] >= 1e-6f && col[e] != i) ? 1 : 0;
     s_cnt[i] = c;
-    s_mov[i] = (bad || (fixed && fixed[i])) ? 0 : 1;
+    s_mov[i] = (fixed && fixed[i]) ? 0 : 1;
   }
   __syncthreads();
-  if (t == 0) {  // prefix sums (n <= 4096: one thread is fast enough here)
-    int acc = 0, m = 0, nn = 0;
+  if (t == 0) {  // prefix sums and the ordered lists (n <= 4096: one thread)
+    int acc = 0, m = 0, nn = 0, na = 0;
     for (int i = 0; i < n; ++i) {
       const int c = s_cnt[i];
       s_cnt[i] = acc;
@@ -1974,17 +2062,24 @@ __global__ void noalloc_stage_kernel(NoAllocScratch *S, int n, int nnz, const fl
       const int mv = s_mov[i];
       s_mov[i] = m;
       m += mv;
-      if (!bad)
-        for (int e = row_ptr[i]; e < row_ptr[i + 1]; ++e)
-          if (target[e] >= 0.0f && target[e] < 1e-6f && col[e] < i)
-            S->nulls[nn++] = make_int2(col[e], i);
+      for (int e = row_ptr[i]; e < row_ptr[i + 1]; ++e) {
+        const int j = col[e];
+        const float tg = target[e];
+        if (j == i) continue;
+        if (tg >= 1e-6f) {
+          if (j < i)
+            S->lst[na++] = make_int4(j, i, __float_as_int(tg), __float_as_int(1.0f / tg));
+        } else if (tg >= 0.0f && j < i) {
+          S->nulls[nn++] = make_int2(j, i);
+        }
+      }
     }
     s_cnt[n] = acc;
     s_mov[n] = m;
     S->n_null = nn;
     ArcsUnit U{};
     U.n = n;
-    U.n_mov = m;  // 0 for a malformed region: the kernel then makes no move
+    U.n_mov = m;
     U.pos_off = 0;
     U.rp_off = 0;
     U.nbr_off = 0;
@@ -2004,20 +2099,17 @@ __global__ void noalloc_stage_kernel(NoAllocScratch *S, int n, int nnz, const fl
     U.rng_chain = 0;
     U.seed = seed;
     U.arc_off = 0;
-    U.n_arcs = -1;  // no spring list: the recompute walks the arc lists
+    U.n_arcs = na;
     S->unit = U;
     S->item = make_int2(0, 0);
     S->head = 0;
     S->done = 0;
     S->best = 0;
-    S->status = bad ? 1 : 0;
-    S->lst[0] = make_int4(0, 0, 0, 0);
   }
   __syncthreads();
   for (int i = t; i <= n; i += blockDim.x) S->row_ptr[i] = s_cnt[i];
   for (int i = t; i < n; i += blockDim.x) {
-    if (!bad && !(fixed && fixed[i])) S->movable[s_mov[i]] = i;
-    if (bad) continue;
+    if (!(fixed && fixed[i])) S->movable[s_mov[i]] = i;
     int k = s_cnt[i];
     for (int e = row_ptr[i]; e < row_ptr[i + 1]; ++e) {
       const float tg = target[e];
@@ -2030,8 +2122,65 @@ __global__ void noalloc_stage_kernel(NoAllocScratch *S, int n, int nnz, const fl
   }
 }
 
+// The unique id of the calling thread's current CUDA context (0 when there
+// is none or the driver cannot say), through the runtime's driver entry
+// points, so that the library needs no link to the driver library.
+unsigned long long current_context_id() {
+  typedef CUresult (*GetCurrentFn)(CUcontext *);
+  typedef CUresult (*GetIdFn)(CUcontext, unsigned long long *);
+  static GetCurrentFn get_current = nullptr;
+  static GetIdFn get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<GetCurrentFn>(p);
+    p = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &p, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess && q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<GetIdFn>(p);
+    cudaGetLastError();
+  });
+  CUcontext c = nullptr;
+  unsigned long long id = 0;
+  if (!get_current || !get_id || get_current(&c) != CUDA_SUCCESS || !c ||
+      get_id(c, &id) != CUDA_SUCCESS)
+    return 0;
+  return id;
+}
+
+// Device address of the scratch array for the current device: looked up
+// (cudaGetSymbolAddress, with the device current) once per device and
+// context, and again whenever the context changed (a cudaDeviceReset, a
+// caller's own context), since the array moves with its module.
 std::mutex g_noalloc_mutex;
-NoAllocScratch *g_noalloc_ptr[64] = {};
+struct NoAllocAddr {
+  unsigned long long ctx_id;
+  NoAllocScratch *ptr;
+};
+NoAllocAddr g_noalloc_addr[64] = {};
+
+cudaError_t noalloc_scratch(int dev, NoAllocScratch **out) {
+  std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+  NoAllocAddr &a = g_noalloc_addr[dev];
+  const unsigned long long id = current_context_id();
+  if (a.ptr && id != 0 && a.ctx_id == id) {
+    *out = a.ptr;
+    return cudaSuccess;
+  }
+  void *p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+  if (e != cudaSuccess || !p) {
+    cudaGetLastError();
+    return e != cudaSuccess ? e : cudaErrorInvalidSymbol;
+  }
+  a.ptr = reinterpret_cast<NoAllocScratch *>(p);
+  a.ctx_id = current_context_id();  // the lookup made the context current
+  *out = a.ptr;
+  return cudaSuccess;
+}
 
 }  // namespace
 
@@ -2047,36 +2196,29 @@ extern "C" pmmc_status pmmc_arcs_anneal_noalloc(const pmmc_arcs_problem *pr,
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return PMMC_ERR_NO_DEVICE;
   NoAllocScratch *S = nullptr;
-  {
-    // once per device, with that device current: the host-side name of a
-    // __device__ array is not a device address, so look the address up
-    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (!g_noalloc_ptr[dev]) {
-      void *p = nullptr;
-      if (cudaGetSymbolAddress(&p, g_noalloc_scratch) != cudaSuccess || !p) {
-        cudaGetLastError();
-        return PMMC_ERR_CUDA;
-      }
-      g_noalloc_ptr[dev] = reinterpret_cast<NoAllocScratch *>(p);
-    }
-    S = g_noalloc_ptr[dev];
-  }
+  if (noalloc_scratch(dev, &S) != cudaSuccess) return PMMC_ERR_CUDA;
   cudaStream_t s = (cudaStream_t)stream;
-  int nnz = 0;
-  if (cudaMemcpyAsync(&nnz, pr->row_ptr + pr->n, sizeof(int), cudaMemcpyDeviceToHost, s) !=
-          cudaSuccess ||
+  const int n = pr->n;
+  // 1. check the caller's arc lists and count what the layout depends on
+  noalloc_check_kernel<<<1, 256, 0, s>>>(S, n, pr->fixed, pr->row_ptr, pr->col, pr->target,
+                                         pr->col && pr->target ? 1 : 0);
+  int hdr[4] = {0, 0, 0, 0};  // status, nnz, n_spring, n_mov
+  if (cudaGetLastError() != cudaSuccess ||
+      cudaMemcpyAsync(hdr, &S->status, sizeof(hdr), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
       cudaStreamSynchronize(s) != cudaSuccess)
     return PMMC_ERR_CUDA;
-  if (nnz > kNoAllocMaxEntries) return PMMC_ERR_BUDGET;
-  if (nnz < 0 || (nnz > 0 && (!pr->col || !pr->target))) return PMMC_ERR_INVALID;
+  if (hdr[0] == 2) return PMMC_ERR_BUDGET;   // more arc-list entries than the scratch holds
+  if (hdr[0] != 0) return PMMC_ERR_INVALID;  // malformed arc lists: nothing was written
+  const int n_spring = hdr[2], n_mov = hdr[3];
+  // 2. the batched path's shared-memory decision for this region
   int dev_smem = 0;
   cudaDeviceGetAttribute(&dev_smem, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  const int n = pr->n;
+  const size_t cap_smem = (size_t)dev_smem - kCtaHeader;
+  const size_t full = arcs_unit_smem(n, n_spring, n_mov, n_mov < n);
   const size_t minimal = arcs_unit_smem_min(n);
-  const size_t full = arcs_unit_smem(n, nnz, n, true);
-  const bool nbs = kCtaHeader + full <= (size_t)dev_smem;
+  const bool nbs = full <= cap_smem;
+  if (!nbs && minimal > cap_smem) return PMMC_ERR_INVALID;
   const size_t per_warp = ((nbs ? full : minimal) + 15) & ~(size_t)15;
-  if (kCtaHeader + per_warp > (size_t)dev_smem) return PMMC_ERR_INVALID;
   ArcsDevParams P = arcs_make_params(prm, seed, false);
   ArcsKernelFn fn = arcs_kernel_for(nbs, 2);
   // the device's opt-in maximum, as the batched path sets it: never lower
@@ -2084,20 +2226,21 @@ extern "C" pmmc_status pmmc_arcs_anneal_noalloc(const pmmc_arcs_problem *pr,
   if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, dev_smem) !=
       cudaSuccess)
     return PMMC_ERR_CUDA;
-  noalloc_stage_kernel<<<1, 256, 0, s>>>(S, n, nnz, pr->pos, pr->fixed, pr->row_ptr, pr->col,
+  // 3. stage, the frozen repulsion, one chain
+  noalloc_stage_kernel<<<1, 256, 0, s>>>(S, n, pr->pos, pr->fixed, pr->row_ptr, pr->col,
                                          pr->target, step_size, seed);
+  if (arcs_bases(&S->unit, 1, S->pos0, S->row_ptr, S->nbr, S->nulls, &S->base, s) !=
+      cudaSuccess)
+    return PMMC_ERR_CUDA;
   fn<<<1, 32, kCtaHeader + per_warp, s>>>(&S->unit, &S->item, 1, &S->head, S->pos0,
                                           S->row_ptr, S->nbr, S->inv_t, S->movable, nullptr,
                                           nullptr, S->lst, S->nulls, P, (int)per_warp, pos_out,
-                                          &S->out, &S->done, nullptr, nullptr);
+                                          &S->out, &S->done, nullptr, &S->base);
   if (cudaGetLastError() != cudaSuccess) return PMMC_ERR_CUDA;
   ChainOut o;
-  int bad = 0;
   if (cudaMemcpyAsync(&o, &S->out, sizeof(o), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-      cudaMemcpyAsync(&bad, &S->status, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
       cudaStreamSynchronize(s) != cudaSuccess)
     return PMMC_ERR_CUDA;
-  if (bad) return PMMC_ERR_INVALID;  // malformed arc lists: nothing was annealed
   pmmc_result r{};
   r.score = o.score;
   r.energy = o.energy;

@@ -51,13 +51,15 @@ struct ArcsDevParams {
   int fails;       // consecutive misses that stop a chain
   int resync;      // FP64 recompute interval (0 = off)
   int use2d;
-  int stop_all;    // the first converged chain stops the unit's others
-  int trace_cap;
+  int stop_all;    // the first converged chain stops the unit's others (the
+                   // others read the flag at their milestones)
+  int trace_cap;   // trace records per traced chain (tests)
+  int trace_chains; // chains 0..trace_chains-1 (region 0's) are traced
   int stall_draws; // tests only: drawing warps never publish (the chain's
                    // bounded wait runs out and it ends with status 3)
-  long long cap;   // hard move cap
+  long long cap;   // hard move cap (0: no move)
   int cap_is_error;
-  int pad;
+  int ms_guard;    // reference-kernel rule: ratio test only when E_ms > 1e-10
   uint64_t seed;   // default Philox key (each unit carries its own)
   float dtpow[33];  // dt^l, l = 0..32
   // extended energy (off unless ext): bonds to the next bead with one

@@ -604,6 +604,7 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
     o.energy = E;
     o.energy_fp64 = run ? Efin : 0.0;
     o.base = 0.0;
+    o.best = E;
     o.score = (float)E;
     o.status = status;
     o.moves = moves;
@@ -751,6 +752,10 @@ extern "C" pmmc_status pmmc_heatmap_batch_anneal(pmmc_ctx *ctx, int n_units,
   // wherever the reference skips the pair: h < 1e-6, |i - m| < diag, i == m,
   // and i outside bead m's chromosome block (LooperSolver.hpp:3597-3611).
   std::vector<float> hrheat((size_t)heat_floats, 0.0f);
+  // A move changes the full score by twice its local change only when the
+  // map is symmetric over the pairs the score reads (createDistanceHeatmap
+  // mirrors it, LooperSolver.hpp:3062); an asymmetric map is refused.
+  std::vector<long long> asym(n_units, -1);
   {
     auto pack = [&](int u) {
       const HeatUnit &U = hu[u];
@@ -764,6 +769,24 @@ extern "C" pmmc_status pmmc_heatmap_batch_anneal(pmmc_ctx *ctx, int n_units,
           if (std::abs(i - m) >= U.diag && i != m && h >= 1e-6f) dst[i] = 1.0f / h;
         }
       }
+      // pairs (m, i), m < i, in 32 x 32 tiles: h_mi and h_im must both be
+      // skipped (< 1e-6) or be equal
+      const int n = pr.n;
+      const float *H = pr.heat;
+      for (int m0 = 0; m0 < n && asym[u] < 0; m0 += 32)
+        for (int i0 = m0; i0 < n && asym[u] < 0; i0 += 32)
+          for (int m = m0; m < std::min(m0 + 32, n); ++m) {
+            const int2 b = hblk[(size_t)U.blk_off + m];
+            for (int i = std::max(i0, m + 1); i < std::min(i0 + 32, n); ++i) {
+              if (i < b.x || i > b.y || i - m < U.diag) continue;
+              const float a = H[(size_t)m * n + i], c = H[(size_t)i * n + m];
+              const bool ua = a >= 1e-6f, uc = c >= 1e-6f;
+              if (ua != uc || (ua && a != c)) {
+                asym[u] = (long long)m * n + i;
+                break;
+              }
+            }
+          }
     };
     const int nt = (int)std::max(1u, std::min<unsigned>(std::thread::hardware_concurrency(), 32u));
     std::vector<std::thread> pool;
@@ -774,6 +797,11 @@ extern "C" pmmc_status pmmc_heatmap_batch_anneal(pmmc_ctx *ctx, int n_units,
       });
     for (auto &th : pool) th.join();
   }
+  for (int u = 0; u < n_units; ++u)
+    if (asym[u] >= 0)
+      return fail(ctx, PMMC_ERR_INVALID,
+                  "heatmap region %d: the map is not symmetric at (%lld, %lld)", u,
+                  asym[u] / units[u].n, asym[u] % units[u].n);
   DevBuf<HeatUnit> d_units;
   DevBuf<float4> d_pos;
   DevBuf<float> d_rheat, d_out;

@@ -56,6 +56,9 @@ struct SmoothDevParams {
   int use2d;
   int resync;     // full recompute every `resync` moves (0 = off)
   int slice;      // beads per thread slice (shared-memory path)
+  int gpu_sched;  // the reference kernel's schedule: no milestone, fixed cap,
+                  // ratio denominator at least 1e-12
+  int pad;
   long long cap;
   uint64_t seed;
 };
@@ -177,14 +180,14 @@ smooth_anneal_kernel(const SmoothUnit *__restrict__ units,
   const double E0 = smooth_full(P, st, dtn, n, S);
   // running score: float-float pair per move, widened to FP64 at milestones
   float e_hi = (float)E0, e_lo = (float)(E0 - (double)(float)E0);
-  double E_ms = E0;
+  double E_ms = E0, best = E0;
   float T = S.max_temp;
   long long moves = 0, accepted = 0;
   int succ = 0, misses = 0, status = kDevOk;
-  bool stop = U.n_mov == 0;
-  if (stop) status = kDevNoMovable;
+  bool stop = U.n_mov == 0 || U.cap <= 0;
+  if (U.n_mov == 0) status = kDevNoMovable;
   // milestone and recompute counters (no 64-bit division per move)
-  long long next_ms = S.window;
+  long long next_ms = S.window > 0 ? (long long)S.window : 0x7fffffffffffffffLL;
   long long next_rs = S.resync > 0 ? (long long)S.resync : 0x7fffffffffffffffLL;
   while (!stop) {
     const uint4 r = philox_move(S.seed, chain_id, (uint64_t)moves, 0u);
@@ -206,13 +209,17 @@ smooth_anneal_kernel(const SmoothUnit *__restrict__ units,
     if (!acc && T > 0.0f) {
       const uint4 a = philox_move(S.seed, chain_id, (uint64_t)moves, 1u);
       const float thr = ratio_threshold(u01(a.x), T, S.inv_scale, S.inv_coef);
-      acc = d < e_hi * (thr - 1.0f);
+      // the reference kernel divides by max(E_prev, 1e-12)
+      // (ParallelMonteCarloSmooth.cu:293-294)
+      acc = (S.gpu_sched && e_hi < 1e-12f) ? d < 1e-12f * thr - e_hi
+                                           : d < e_hi * (thr - 1.0f);
     }
     if (acc) {
       P[b * st] = nb;
       ff_add(e_hi, e_lo, d);
       ++accepted;
       ++succ;
+      if (S.gpu_sched) best = fmin(best, (double)e_hi + (double)e_lo);
     }
     if (trace != nullptr && chain_id == 0 && moves < trace_cap) {
       MoveTrace tr;
@@ -251,6 +258,7 @@ smooth_anneal_kernel(const SmoothUnit *__restrict__ units,
   o.energy = (double)e_hi + (double)e_lo;
   o.energy_fp64 = smooth_full(P, st, dtn, n, S);
   o.base = 0.0;
+  o.best = S.gpu_sched ? best : o.energy;
   o.score = e_hi;
   o.status = status;
   o.moves = moves;
@@ -296,12 +304,16 @@ SmoothDevParams smooth_params(const pmmc_anneal_params *prm, uint64_t seed) {
     S.fails = 1;
     S.cap = prm->max_moves > 0 ? prm->max_moves : 200ll * S.window;
   } else {
-    // ParallelMonteCarloSmooth.cu:267-337: 256-move milestones, fails
-    // threshold, at most stop_condition_steps moves.
-    S.window = 256;
-    S.fails = std::max(1, prm->milestone_fails);
-    long long cap = std::max(1, prm->milestone_steps);
-    cap = (cap + 255) / 256 * 256;
+    // MonteCarloSmoothKernelMultiWarp (ParallelMonteCarloSmooth.cu:267-337):
+    // blocks of 256 moves while fewer than stop_condition_steps are done.
+    // Its milestone test runs only when iterations % steps < 256, which
+    // inside that loop is only after the last block: every chain makes
+    // exactly the cap's moves, so no milestone is evaluated here.
+    S.window = 0;
+    S.fails = 1;
+    S.gpu_sched = 1;
+    long long cap = prm->milestone_steps > 0 ? ((long long)prm->milestone_steps + 255) / 256 * 256
+                                             : 0;
     if (prm->max_moves > 0) cap = std::min(cap, (long long)prm->max_moves);
     S.cap = cap;
   }
@@ -444,9 +456,15 @@ extern "C" pmmc_status pmmc_smooth_batch_anneal(pmmc_ctx *ctx, int n_units,
   long long dst = 0;
   for (int u = 0; u < n_units; ++u) {
     const SmoothUnit &U = hu[u];
+    // the reported chain: the lowest final running energy; under the
+    // reference kernel's schedule, the lowest running energy ever reached
+    // (its per-warp best score, ParallelMonteCarloSmooth.cu:299-301,462-472),
+    // ties to the lower index
     int best = 0;
-    for (int c = 1; c < U.chains; ++c)
-      if (outs[U.chain_base + c].energy < outs[U.chain_base + best].energy) best = c;
+    for (int c = 1; c < U.chains; ++c) {
+      const ChainOut &oc = outs[U.chain_base + c], &ob = outs[U.chain_base + best];
+      if (S.gpu_sched ? oc.best < ob.best : oc.energy < ob.energy) best = c;
+    }
     const ChainOut &o = outs[U.chain_base + best];
     if (pos_out) {
       PMMC_CUDA(ctx, cudaMemcpy(pos_out + dst, d_out.p + U.out_off + (long long)best * U.n * 3,

@@ -48,3 +48,9 @@ def distmap_pearson(a, b):
 def ks_2samp_p(x, y):
     from scipy import stats
     return float(stats.ks_2samp(x, y).pvalue)
+
+
+def welch_p(x, y):
+    """Two-sided Welch t-test p-value (equal means, unequal variances)."""
+    from scipy import stats
+    return float(stats.ttest_ind(x, y, equal_var=False).pvalue)

@@ -82,3 +82,115 @@ def test_heatmap_two_chains_per_sm(ctx):
                                       rng=O.RNG_PHILOX, incremental=True, chain=u)
         assert abs(ores.score - res[u].energy) <= 1e-3 * ores.score
         assert res[u].rel_error < 1e-6 and res[u].status == 0
+
+
+def test_heatmap_refuses_asymmetric_map(ctx):
+    """A move changes the full score by twice its local change only on a
+    symmetric map (createDistanceHeatmap mirrors it): an asymmetric pair
+    that the score reads is refused; pairs it never reads (the diagonal band,
+    across chromosome blocks) may differ."""
+    h = synth.heatmap_region(64, seed=3, n_tads=2, tad_min=6, tad_max=10)
+    prm = capi.default_params(capi.LEVEL_HEATMAP, schedule=capi.SCHEDULE_CPU, max_moves=500,
+                              max_temp=5.0, dt_temp=0.9999, milestone_steps=250)
+    assert (h.heat == h.heat.T).all()
+    bad_value = h.heat.copy()
+    bad_value[3, 40] *= 1.5
+    bad_skip = h.heat.copy()
+    bad_skip[50, 5] = 0.0           # one side skipped (< 1e-6), the other not
+    for heat in (bad_value, bad_skip):
+        with pytest.raises(capi.PmmcError) as e:
+            capi.heatmap_anneal(ctx, capi.HeatmapInput(h.pos, heat), prm, 1.0)
+        assert e.value.status == capi.PMMC_ERR_INVALID
+        assert "not symmetric" in str(e.value)
+    unread = h.heat.copy()
+    unread[7, 8] = 9.0              # inside a diagonal band of width 2
+    unread[3, 40] *= 1.5            # across the block boundary at 32
+    pos, res = capi.heatmap_anneal(
+        ctx, capi.HeatmapInput(h.pos, unread, 2, np.array([0, 32, 64], np.int32)), prm, 1.0)
+    assert res.moves == 500 and np.isfinite(pos).all()
+
+
+def _config1_region():
+    # the 2048-bead heatmap workload: c_ij = |i-j|^-1 x lognormal(0.5), 20 TAD
+    # blocks x3, expected distance c^-1/3, seed 7
+    return synth.heatmap_region(2048, seed=7)
+
+
+def test_heatmap_trace_parity_config1(ctx):
+    """Per-move parity on the 2048-bead map, one chain: the launch the
+    single-chain workload takes (one CTA of 512 threads, 16-row ring)."""
+    h = _config1_region()
+    base = dict(max_temp=5.0, dt_temp=0.9999, milestone_steps=100_000, improvement=0.99)
+    moves = 20_000
+    prm = capi.default_params(capi.LEVEL_HEATMAP, schedule=capi.SCHEDULE_CPU, max_moves=moves,
+                              **base)
+    ctx.set_seed(7)
+    out, res, ms, tr = capi.heatmap_batch_anneal(ctx, [capi.HeatmapInput(h.pos, h.heat)], prm,
+                                                 [1.0], trace_cap=moves)
+    m = int(res[0].moves)
+    assert m == moves and res[0].status == 0
+    pr = O.HeatmapProblem(h.pos, h.heat)
+    rep = O.heatmap_replay(pr, O.Params(**base), 1.0, 7, 0, tr[:m])
+    check_replay(tr[:m], rep, scale_factor=2.0, delta_only=True)
+    e64 = O.heatmap_score(pr, -1, pos=out[0])
+    assert abs(res[0].energy_fp64 - e64) <= 1e-6 * e64
+    assert abs(res[0].energy - e64) <= 1e-5 * e64
+    assert abs(rep["final_energy"] - res[0].energy) <= 1e-5 * abs(res[0].energy)
+
+
+def test_heatmap_two_chains_per_sm_config1(ctx):
+    """The batch form at 2048 beads with two chains per SM (two 256-thread
+    CTAs share an SM, 8-row rings): chain 0's moves replay on the oracle and
+    a sample of the other chains ends where the oracle's annealer ends."""
+    h = _config1_region()
+    n_units = 2 * ctx.sm_count
+    base = dict(max_temp=5.0, dt_temp=0.9999, milestone_steps=100_000, improvement=0.99)
+    moves = 3000
+    prm = capi.default_params(capi.LEVEL_HEATMAP, schedule=capi.SCHEDULE_CPU, max_moves=moves,
+                              **base)
+    inp = capi.HeatmapInput(h.pos, h.heat)
+    ctx.set_seed(19)
+    out, res, ms, tr = capi.heatmap_batch_anneal(ctx, [inp] * n_units, prm, [1.0] * n_units,
+                                                 trace_cap=moves)
+    pr = O.HeatmapProblem(h.pos, h.heat)
+    rep = O.heatmap_replay(pr, O.Params(**base), 1.0, 19, 0, tr[:moves])
+    check_replay(tr[:moves], rep, scale_factor=2.0, delta_only=True)
+    for u in range(0, n_units, 29):
+        opos, ores = O.heatmap_anneal(pr, O.Params(max_moves=moves, **base), 1.0, 19,
+                                      rng=O.RNG_PHILOX, incremental=True, chain=u)
+        assert res[u].moves == moves and res[u].status == 0
+        assert abs(ores.score - res[u].energy) <= 1e-4 * ores.score
+        assert res[u].rel_error < 1e-6
+
+
+def test_heatmap_structures_match_reference_config1(ctx):
+    """16 seeds on the 2048-bead map: final energy, RMSD to the start and
+    distance-map Pearson against the start, GPU vs the reference's CPU
+    annealer (MonteCarloHeatmap: the oracle in libc mode with local scores,
+    which anneals exactly as the reference's full re-score).  Two-sample KS
+    and Welch tests, p > 0.01 each."""
+    from concurrent.futures import ThreadPoolExecutor
+    from parity import distmap_pearson, kabsch_rmsd, welch_p
+    h = _config1_region()
+    pr = O.HeatmapProblem(h.pos, h.heat)
+    base = dict(max_temp=5.0, dt_temp=0.9999, milestone_steps=5000, improvement=0.99)
+    cap = 20_000
+
+    def ref(s):   # ctypes releases the GIL: the seeds run on all host cores
+        return O.heatmap_anneal(pr, O.Params(max_moves=cap, **base), 1.0, 300 + s,
+                                incremental=True)
+
+    with ThreadPoolExecutor(16) as ex:
+        outs = list(ex.map(ref, range(16)))
+    prm = capi.default_params(capi.LEVEL_HEATMAP, schedule=capi.SCHEDULE_CPU, max_moves=cap,
+                              **base)
+    ctx.set_seed(3030)
+    gpos, gres, _, _ = capi.heatmap_batch_anneal(ctx, [capi.HeatmapInput(h.pos, h.heat)] * 16,
+                                                 prm, [1.0] * 16)
+    ref_m = [[o[1].score for o in outs], [kabsch_rmsd(o[0], h.pos) for o in outs],
+             [distmap_pearson(o[0], h.pos) for o in outs]]
+    gpu_m = [[r.energy for r in gres], [kabsch_rmsd(p, h.pos) for p in gpos],
+             [distmap_pearson(p, h.pos) for p in gpos]]
+    for name, a, b in zip(("energy", "rmsd", "pearson"), ref_m, gpu_m):
+        assert ks_2samp_p(a, b) > 0.01, name
+        assert welch_p(a, b) > 0.01, name

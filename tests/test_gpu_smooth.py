@@ -88,3 +88,31 @@ def test_smooth_sweeps_cap_per_region(ctx):
     for c, r in zip(chains, res):
         assert r.moves == 50 * int((c.fixed == 0).sum())
         assert r.rel_error < 1e-4   # FP32 deltas, no periodic recompute here
+
+
+def test_smooth_structures_match_reference(ctx):
+    """16 seeds on a 400-bead chromosome stretch with anchors every
+    Poisson(10) beads held fixed (the genome-smoothing shape): final energy,
+    RMSD to the start and distance-map Pearson against the start, GPU vs the
+    reference's CPU MonteCarloArcsSmooth (the oracle in libc mode, bit-
+    identical to it).  Two-sample KS and Welch tests, p > 0.01 each."""
+    from parity import distmap_pearson, kabsch_rmsd, welch_p
+    c = synth.smooth_chain(400, seed=31)
+    pr = O.SmoothProblem(c.pos, c.dist_to_next, c.fixed)
+    base = dict(max_temp=5.0, dt_temp=0.9999, milestone_steps=4000, improvement=0.99,
+                k_stretch=0.1, k_squeeze=0.1, k_angle=0.1)
+    cap = 40_000
+    outs = [O.smooth_anneal(pr, O.Params(max_moves=cap, **base), 0.5, 800 + s)
+            for s in range(16)]
+    prm = capi.default_params(capi.LEVEL_SMOOTH, schedule=capi.SCHEDULE_CPU, max_moves=cap,
+                              **base)
+    ctx.set_seed(8080)
+    inp = capi.SmoothInput(c.pos, c.dist_to_next, c.fixed)
+    gpos, gres, _ = capi.smooth_batch_anneal(ctx, [inp] * 16, prm, [0.5] * 16)
+    ref_m = [[o[1].score for o in outs], [kabsch_rmsd(o[0], c.pos) for o in outs],
+             [distmap_pearson(o[0], c.pos) for o in outs]]
+    gpu_m = [[r.energy for r in gres], [kabsch_rmsd(p, c.pos) for p in gpos],
+             [distmap_pearson(p, c.pos) for p in gpos]]
+    for name, a, b in zip(("energy", "rmsd", "pearson"), ref_m, gpu_m):
+        assert ks_2samp_p(a, b) > 0.01, name
+        assert welch_p(a, b) > 0.01, name
