@@ -6,23 +6,31 @@ the configuration the batched-vs-plain metric is quoted on.
 
 A step anneals every block of the ensemble once (T0 5, cooling 0.9999,
 milestones every 50k moves with improvement threshold 0.99 -- the reference
-CPU schedule of MonteCarloArcs -- and an energy recompute every 4096 moves,
---resync) in one CUDA-graph launch of the persistent work-stealing kernels.
-Inputs are seeded synthetic regions (no datasets ship with the reference).
-Rank r of N anneals its own ensemble (seeds 64r..64r+63): weak scaling, no
-collective.
+CPU schedule of MonteCarloArcs -- and an FP64 energy recompute every 1000
+moves, --resync) in one CUDA-graph launch of the persistent work-stealing
+kernels.  Inputs are seeded synthetic regions (no datasets ship with the
+reference).  Rank r of N anneals its own ensemble (seeds 64r..64r+63): weak
+scaling, no collective.
+
+One JSON line on rank 0: value = MC moves/s over all ranks (device time,
+CUDA events on the launching stream); structures/s beside it; e2e = the same
+metric through the host-buffer C-ABI call (staging, copies and result reads
+inside the timed region), the max over ranks; roofline of the annealing
+kernel against the measured HBM peak, its per-move shared-memory/FP32 basis
+and the latency bound of the critical chain; cpu_baseline = the reference's
+CPU annealer (the oracle's bit-identical restatement) on one equal part of
+the same ensemble on all host cores.  At N = 1 the line also carries a
+sub-record per other configuration ("configs": plain, heatmap, heatmap
+batch, smoothing, serving), each with its CPU baseline timed on this host.
+
+--impl reference anneals the same ensemble's blocks with the reference's CPU
+annealer on all host cores (warm-up and timed parts of equal size
+distribution) and prints the same config.
 
 Other lines (--workload): plain, heatmap, heatmap-batch, smooth, serve,
 distmap, equidistant, targets, stress (pmmc_gb300/workloads.py describes
 each); every line carries its CPU baseline, and --impl reference prints the
 reference arm of the chosen line.
-
-One JSON line on rank 0: value = MC moves/s over all ranks (device time,
-CUDA events on the launching stream); structures/s beside it; e2e = the same
-metric through the host-buffer C-ABI call (staging, copies and result reads
-inside the timed region); roofline of the annealing kernel against the
-measured HBM peak; cpu_baseline = the reference's CPU annealer (the oracle's
-bit-identical restatement) on a bounded sample on all host cores.
 """
 from __future__ import annotations
 
@@ -44,7 +52,7 @@ sys.path.insert(0, ROOT)
 
 N_STRUCT, N_BLOCKS = 64, 24
 ANNEAL = dict(max_temp=5.0, dt_temp=0.9999, milestone_steps=50000, improvement=0.99)
-RESYNC = 4096
+RESYNC = 1000
 STEP = 0.5
 WORKLOAD = (f"arcs_ensemble_{N_STRUCT}x{N_BLOCKS}_blocks32-2048_1.5arcs_per_bead_"
             f"T0=5_cool0.9999_milestone50k_thr0.99")
@@ -76,37 +84,51 @@ def _cpu_block(args):
     return res.moves, time.perf_counter() - t, n
 
 
-def cpu_sample(budget_s: float = 20.0):
-    """Anneal a bounded sample of the ensemble's blocks on every host core.
-    Block sizes follow the workload's distribution; the sample grows until it
-    holds about budget_s of CPU work."""
+def ensemble_blocks(rank: int = 0, world: int = 1):
+    """(beads, region seed) of every block of a rank's ensemble, the regions
+    the GPU leg anneals (synth.ensemble_block_specs)."""
+    from pmmc_gb300 import synth
+    from pmmc_gb300.replicas import shard_seeds
+    seeds = shard_seeds(rank, max(world, rank + 1), N_STRUCT)
+    return [b for st in synth.ensemble_block_specs(N_STRUCT, N_BLOCKS, seeds=seeds) for b in st]
+
+
+def size_shares(blocks, shares: int):
+    """The blocks split into `shares` parts of the same size distribution:
+    block of size rank i (largest first) goes to part i mod shares."""
+    order = sorted(range(len(blocks)), key=lambda k: (-blocks[k][0], k))
+    parts = [[] for _ in range(shares)]
+    for i, k in enumerate(order):
+        parts[i % shares].append(blocks[k])
+    return parts
+
+
+def cpu_anneal_blocks(pool, blocks):
+    """The reference CPU annealer (MonteCarloArcs, restated by the oracle
+    bit for bit, libc stream seeded by the region seed) over `blocks` on the
+    pool's processes, largest block first.  Returns moves, wall s, CPU s."""
+    jobs = sorted(blocks, key=lambda b: -b[0])
+    t0 = time.perf_counter()
+    moves = cpu_s = 0.0
+    for mv, dt, _ in pool.imap_unordered(_cpu_block, jobs):
+        moves += mv
+        cpu_s += dt
+    return moves, time.perf_counter() - t0, cpu_s
+
+
+def cpu_ensemble_sample(share: int = 8):
+    """CPU baseline of the default line, bounded: one of `share` equal parts
+    of the ensemble's own blocks (same size distribution) annealed on every
+    host core at once."""
     from oracle import oracle as O
     O.build()
     cores = os.cpu_count() or 1
-    rng = np.random.default_rng(123)
-    sizes = [int(round(math.exp(rng.uniform(math.log(32), math.log(2048)))))
-             for _ in range(4 * cores)]
-    jobs = [(n, 9000 + k) for k, n in enumerate(sizes)]
-    ctx = mp.get_context("spawn")
-    t0 = time.perf_counter()
-    moves = cpu_s = 0.0
-    done = 0
-    with ctx.Pool(cores) as pool:
-        for mv, dt, n in pool.imap_unordered(_cpu_block, jobs):
-            moves += mv
-            cpu_s += dt
-            done += 1
-            if cpu_s > budget_s * cores or time.perf_counter() - t0 > budget_s:
-                pool.terminate()
-                break
-    wall = time.perf_counter() - t0
-    # The rate: a core's mean rate over its own blocks, all cores running at
-    # once, times the cores.  Process start-up and the sample's idle tail (a
-    # few large blocks finishing last) are excluded; a whole ensemble keeps
-    # every core busy until its last blocks.  moves / wall is kept beside it.
-    return {"moves": moves, "cpu_s": cpu_s, "wall_s": wall, "blocks": done,
-            "cores": cores, "moves_per_s": moves / cpu_s * cores if cpu_s > 0 else 0.0,
-            "wall_moves_per_s": moves / wall}
+    part = size_shares(ensemble_blocks(0), share)[0]
+    with mp.get_context("spawn").Pool(cores) as pool:
+        pool.map(_cpu_block, [(32, 7 + k) for k in range(cores)])  # start-up, imports
+        moves, wall, cpu_s = cpu_anneal_blocks(pool, part)
+    return {"moves": moves, "wall_s": wall, "cpu_s": cpu_s, "blocks": len(part),
+            "cores": cores, "moves_per_s": moves / wall, "share": share}
 
 
 def _cpu_request(args):
@@ -379,9 +401,30 @@ def heatmap_cpu_baseline(n_maps: int, budget_s: float) -> dict:
                                          f"re-scoring the whole map per move ({fwall:.1f} s)"}}
 
 
+def heatmap_record(args, n_maps: int) -> dict:
+    """Heatmap-level line (one chain, or one chain per distinct map) with the
+    reference's heatmap annealer on the host cores beside it: its own form
+    (a full re-score per move) timed on a capped number of moves and
+    extrapolated to the line's moves, and the O(N)-incremental form."""
+    # CPU baseline first, so that its process pool starts before the first
+    # GPU call; the batch's default (two maps per SM) exceeds the host cores
+    cpu = heatmap_cpu_baseline(n_maps if n_maps > 0 else 2 * (os.cpu_count() or 1),
+                               args.cpu_budget)
+    from pmmc_gb300 import workloads as W
+    sampler = ClockSampler(0)
+    sampler.start()
+    line = W.heatmap(args, n_maps)
+    line["clocks"] = sampler.stop()
+    line["gpu_launches"] = args.steps  # one heatmap_anneal_kernel launch per call
+    moves = line["config"]["moves_per_step"] / line["config"]["maps"]
+    ref = cpu["reference_form"]
+    ref["extrapolated_s_per_chain"] = moves / (ref["value"] / ref["cores"])
+    line["cpu_baseline"] = cpu
+    return line
+
+
 def heatmap_main(args, n_maps: int):
-    """Heatmap-level line (one chain, or one chain per distinct map) beside
-    the reference's heatmap annealer on the host cores."""
+    """Heatmap-level line beside the reference's heatmap annealer."""
     if args.impl == "reference":
         if int(os.environ.get("RANK", "0")) != 0:
             return
@@ -397,18 +440,7 @@ def heatmap_main(args, n_maps: int):
                           "e2e": {"value": ref["value"], "unit": "moves/s",
                                   "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
         return
-    # CPU baseline first, so that its process pool starts before the first
-    # GPU call; the batch's default (two maps per SM) exceeds the host cores
-    cpu = heatmap_cpu_baseline(n_maps if n_maps > 0 else 2 * (os.cpu_count() or 1),
-                               args.cpu_budget)
-    from pmmc_gb300 import workloads as W
-    sampler = ClockSampler(0)
-    sampler.start()
-    line = W.heatmap(args, n_maps)
-    line["clocks"] = sampler.stop()
-    line["gpu_launches"] = args.steps  # one heatmap_anneal_kernel launch per call
-    line["cpu_baseline"] = cpu
-    print(json.dumps(line))
+    print(json.dumps(heatmap_record(args, n_maps)))
 
 
 def _cpu_smooth(job):
@@ -455,14 +487,29 @@ def smooth_cpu_baseline(sweeps: int, budget_s: float) -> dict:
                       f"({cpu_s:.1f} CPU s in {wall:.1f} s)"}
 
 
+def smooth_record(args) -> dict:
+    """Genome-smoothing line with the reference's smoothing annealer on every
+    host core beside it."""
+    sweeps = args.moves or 20_000
+    cpu = smooth_cpu_baseline(sweeps, args.cpu_budget)
+    from pmmc_gb300 import workloads as W
+    sampler = ClockSampler(0)
+    sampler.start()
+    line = W.smooth(args)
+    line["clocks"] = sampler.stop()
+    line["gpu_launches"] = args.steps  # one smooth_anneal_kernel launch per call
+    line["cpu_baseline"] = cpu
+    return line
+
+
 def smooth_main(args):
     """Genome-smoothing line beside the reference's smoothing annealer on
     every host core."""
     sweeps = args.moves or 20_000
-    if args.impl == "reference" and int(os.environ.get("RANK", "0")) != 0:
-        return
-    cpu = smooth_cpu_baseline(sweeps, args.cpu_budget)
     if args.impl == "reference":
+        if int(os.environ.get("RANK", "0")) != 0:
+            return
+        cpu = smooth_cpu_baseline(sweeps, args.cpu_budget)
         print(json.dumps({"metric": "MC moves/s", "value": cpu["value"], "unit": "moves/s",
                           "n_gpus": 0, "steps": 1, "warmup": 0, "ms_per_step": None,
                           "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -472,21 +519,46 @@ def smooth_main(args):
                           "e2e": {"value": cpu["value"], "unit": "moves/s",
                                   "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}))
         return
+    print(json.dumps(smooth_record(args)))
+
+
+def _cpu_plain_pool(cores: int):
+    """Independent anneals of the config-0 region, one per core at once:
+    (completed anneals, wall s)."""
+    t = time.perf_counter()
+    with mp.get_context("spawn").Pool(cores) as pool:
+        pool.map(_cpu_plain, range(42, 42 + cores))
+    return cores, time.perf_counter() - t
+
+
+def plain_record(args) -> dict:
+    """Config-0 line: the plain drop-in call with the reference CPU annealer
+    (the oracle port, bit-identical to it) beside it: one core for one
+    structure, every core for structures/s."""
+    from oracle import oracle as O
     from pmmc_gb300 import workloads as W
+    O.build()
+    mv, dt = _cpu_plain(42)
+    cores = os.cpu_count() or 1
+    done, wall = _cpu_plain_pool(cores)
     sampler = ClockSampler(0)
     sampler.start()
-    line = W.smooth(args)
+    line = W.plain(args)
     line["clocks"] = sampler.stop()
-    line["gpu_launches"] = args.steps  # one smooth_anneal_kernel launch per call
-    line["cpu_baseline"] = cpu
-    print(json.dumps(line))
+    line["gpu_launches"] = args.steps * 2
+    line["structures_per_s"] = 1e3 / line["ms_per_step"]
+    line["cpu_baseline"] = {"value": mv / dt, "unit": "moves/s", "cores": 1, "kind": "port",
+                            "sample": f"one full anneal of the region ({mv} moves, {dt:.2f} s)",
+                            "structures_per_s_all_cores": done / wall,
+                            "all_cores": f"{done} anneals (seeds 42..) on {cores} cores at "
+                                         f"once, {wall:.1f} s wall"}
+    return line
 
 
 def plain_main(args):
     """Config-0 line: the plain drop-in call beside the reference CPU
     annealer (the oracle port, bit-identical to it) on one core."""
     from oracle import oracle as O
-    from pmmc_gb300 import workloads as W
     if args.impl == "reference":
         if int(os.environ.get("RANK", "0")) != 0:
             return
@@ -503,16 +575,21 @@ def plain_main(args):
                           "e2e": {"value": v, "unit": "moves/s", "h2d_bytes_per_step": 0,
                                   "d2h_bytes_per_step": 0}}))
         return
+    print(json.dumps(plain_record(args)))
+
+
+def serve_record(args) -> dict:
+    """Serving line with the same trace through a host-core queue beside it."""
+    from pmmc_gb300 import workloads as W
+    n_req = args.requests or 5000
+    cpu = cpu_serve_baseline(n_req, args.cpu_budget)
     sampler = ClockSampler(0)
     sampler.start()
-    line = W.plain(args)
+    line = W.serve(args)
     line["clocks"] = sampler.stop()
-    line["gpu_launches"] = args.steps * 2
-    O.build()
-    mv, dt = _cpu_plain(42)
-    line["cpu_baseline"] = {"value": mv / dt, "unit": "moves/s", "cores": 1, "kind": "port",
-                            "sample": f"one full anneal of the region ({mv} moves, {dt:.2f} s)"}
-    print(json.dumps(line))
+    line["gpu_launches"] = line["saturated"]["waves"]
+    line["cpu_baseline"] = cpu
+    return line
 
 
 def serve_main(args):
@@ -532,13 +609,7 @@ def serve_main(args):
                         "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
         print(json.dumps(line))
         return
-    sampler = ClockSampler(0)
-    sampler.start()
-    line = W.serve(args)
-    line["clocks"] = sampler.stop()
-    line["gpu_launches"] = line["saturated"]["waves"]
-    line["cpu_baseline"] = cpu_serve_baseline(n_req, args.cpu_budget)
-    print(json.dumps(line))
+    print(json.dumps(serve_record(args)))
 
 
 # --------------------------------------------------------------------------
@@ -710,10 +781,24 @@ def run_gpu(args, rank, world):
             capi.arcs_anneal(ctx, x, prm, STEP, 1)
         plain_s = time.perf_counter() - t
     batch.close()
+    # ---- latency bound: the chain with the most moves, its region alone on
+    # the device (same launch choice), time per move x its moves in the pass
+    crit = max(range(len(res)), key=lambda u: res[u].moves)
+    alone = capi.ArcsBatch(ctx, [inputs[crit]], prm, [STEP], chains=1, use_graph=False,
+                           lanes=args.lanes, drawing_warp=args.drawing_warp)
+    per_move = []
+    for _ in range(3):
+        alone.run()
+        a_ms, a_moves, _ = alone.stats()
+        per_move.append(a_ms / max(a_moves, 1))
+    alone.close()
+    crit_ms = min(per_move) * res[crit].moves
     return dict(step_ms=step_ms, moves=moves_per_step, kernel_ms=kernel_ms, wall=t_wall,
                 clocks=clk, rel_err=rel_err, bad=status_bad, e2e_ms=e2e_ms,
                 e2e_moves=e2e_moves, h2d=h2d, d2h=d2h, plain_s=plain_s, n_launch=n_launch,
-                n_units=len(inputs), classes=classes)
+                n_units=len(inputs), classes=classes,
+                crit={"region_beads": int(inputs[crit].n), "moves": int(res[crit].moves),
+                      "ms_per_move_alone": min(per_move), "bound_ms": crit_ms})
 
 
 def _batch_anneal_host(ctx, inputs, prm, steps, lanes=0, drawing_warp=False):
@@ -755,7 +840,13 @@ def main():
     ap.add_argument("--resync", type=int, default=RESYNC,
                     help="FP64 energy recompute every this many moves of a chain")
     ap.add_argument("--no-plain", dest="plain", action="store_false")
-    ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--cpu-budget", type=float, default=20.0,
+                    help="seconds of CPU-baseline work per line (0: none)")
+    ap.add_argument("--cpu-share", type=int, default=8,
+                    help="default line's CPU baseline: 1 of this many equal parts of the "
+                         "ensemble's blocks")
+    ap.add_argument("--no-configs", dest="configs", action="store_false",
+                    help="default line without the sub-records of the other configurations")
     ap.add_argument("--structures", type=int, default=N_STRUCT,
                     help="ensemble size (smaller for profiling runs)")
     ap.add_argument("--milestone", type=int, default=ANNEAL["milestone_steps"],
@@ -806,50 +897,33 @@ def main():
         return
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
+    config = ensemble_config(args, world)
 
     if args.impl == "reference":
-        # the reference's own CPU annealer (bit-identical oracle restatement;
-        # the reference sources do not travel to the GPU host) on all cores
+        # the reference's own CPU annealer (the oracle's bit-identical
+        # restatement; the reference sources do not travel to the GPU host)
+        # on all host cores, over the GPU leg's own blocks
         if rank != 0:
             return
-        vals = []
-        per = max(5.0, min(args.cpu_budget, 150.0 / max(1, args.steps + args.warmup)))
-        for k in range(args.warmup + args.steps):
-            s = cpu_sample(per)
-            if k >= args.warmup:
-                vals.append(s)
-        v = (sum(s["moves"] for s in vals) / sum(s["cpu_s"] for s in vals)
-             * vals[0]["cores"])
-        line = {
-            "impl": "reference", "metric": "MC moves/s", "value": v, "unit": "moves/s",
-            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64", "data": "synthetic",
-            "config": {"workload": WORKLOAD, "sample": "blocks with the ensemble's size "
-                       "distribution, about %.0f s per step" % per},
-            "cpu_baseline": {"value": v, "unit": "moves/s", "cores": vals[0]["cores"],
-                             "kind": "port",
-                             "sample": f"{sum(s['blocks'] for s in vals)} blocks in "
-                                       f"{len(vals)} steps; a core's rate over its own "
-                                       f"blocks, all cores at once, times the cores"},
-            "e2e": {"value": v, "unit": "moves/s", "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": 0},
-        }
-        print(json.dumps(line))
+        reference_main(args, config)
         return
 
     # CPU baseline first (spawn pool, before any CUDA call in this process)
-    cpu = cpu_sample(args.cpu_budget) if rank == 0 and args.cpu_budget > 0 else None
+    cpu = (cpu_ensemble_sample(args.cpu_share)
+           if rank == 0 and args.cpu_budget > 0 else None)
     if world > 1:
         import torch
         import torch.distributed as dist
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", rank)))
         dist.init_process_group("nccl")
     r = run_gpu(args, rank, world)
-    # max over ranks (replicas: the only cross-rank step)
+    # max over ranks (replicas: the only cross-rank step), for the device
+    # time and for the end-to-end time alike
     from pmmc_gb300.replicas import combine
-    step_ms, total_moves = combine(r["step_ms"], float(r["moves"]),
-                                   device="cuda" if world > 1 else None)
+    dev = "cuda" if world > 1 else None
+    step_ms, total_moves = combine(r["step_ms"], float(r["moves"]), device=dev)
+    e2e_ms_local = min(r["e2e_ms"]) if r["e2e_ms"] else 0.0
+    e2e_ms, e2e_moves = combine(e2e_ms_local, float(r["e2e_moves"]), device=dev)
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
@@ -857,24 +931,23 @@ def main():
         return
     value = total_moves / (step_ms * 1e-3)
     structs = world * N_STRUCT / (step_ms * 1e-3)
-    e2e_ms = min(r["e2e_ms"]) if r["e2e_ms"] else None
-    e2e_val = world * r["e2e_moves"] / (e2e_ms * 1e-3) if e2e_ms else None
+    e2e_val = e2e_moves / (e2e_ms * 1e-3) if e2e_ms > 0 else None
     peak, peak_kind = measured_peaks()
     _, inputs = make_inputs(0)
     alg = algorithmic_bytes(inputs, r["moves"])
     achieved = alg / (r["step_ms"] * 1e-3) / 1e9
     traffic = traffic_per_launch()
+    from pmmc_gb300 import workloads as W
+    deg = sum(int(x.row_ptr[-1]) for x in inputs) / sum(x.n for x in inputs)
+    sm_mhz = r["clocks"].get("sm_mhz") or 2070.0
     line = {
         "metric": "MC moves/s", "value": value, "unit": "moves/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": step_ms,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD, "structures": N_STRUCT * world,
-                   "blocks_per_structure": N_BLOCKS, "regions": r["n_units"] * world,
-                   "moves_per_step": total_moves, "fp64_resync_every": args.resync,
-                   "l2": "256 MB buffer written between timed steps",
-                   "parallelism": f"replicas x{world}",
-                   "launch_classes": [{"lanes": la, "chains_per_cta": w, "items": it,
+        "config": config,
+        "moves_per_step": total_moves,
+        "launch": {"launch_classes": [{"lanes": la, "chains_per_cta": w, "items": it,
                                        "arcs_in_smem": nb, "drawing_warp": dw}
                                       for la, w, it, nb, dw in r["classes"]],
                    "tuning": "autotuned" if args.lanes == -1 else f"lanes={args.lanes}"},
@@ -887,7 +960,19 @@ def main():
                      "frac": achieved / peak, "traffic": traffic,
                      "peak_source": peak_kind,
                      "note": "serial Metropolis chains: one warp per chain, latency-bound; "
-                             "HBM carries only the one-time staging"},
+                             "HBM carries only the one-time staging (roofline_smem: the "
+                             "per-move basis; latency_bound: the critical chain)"},
+        # per move: 2 x deg pair terms (deg = arc-list entries per bead of the
+        # ensemble), each a 16-byte position and an 8-byte arc entry, ~15 FLOP
+        "roofline_smem": W._smem_roofline(value / world, 2 * deg * 24.0, 2 * deg * 15.0,
+                                          sm_mhz),
+        "latency_bound": {"critical_region_beads": r["crit"]["region_beads"],
+                          "critical_chain_moves": r["crit"]["moves"],
+                          "ms_per_move_alone": r["crit"]["ms_per_move_alone"],
+                          "bound_ms": r["crit"]["bound_ms"],
+                          "frac": r["crit"]["bound_ms"] / r["step_ms"],
+                          "note": "the chain with the most moves, its region annealed alone: "
+                                  "no pass can be shorter than its moves x time per move"},
         "clocks": r["clocks"],
         "gpu_launches": r["n_launch"] * args.steps,
     }
@@ -895,14 +980,99 @@ def main():
         line["plain_structures_per_s"] = 1.0 / r["plain_s"]
         line["batched_over_plain"] = structs / world / (1.0 / r["plain_s"])
     if cpu:
+        mps = total_moves / world / N_STRUCT   # moves per structure (this arm)
         line["cpu_baseline"] = {"value": cpu["moves_per_s"], "unit": "moves/s",
                                 "cores": cpu["cores"], "kind": "port",
-                                "sample": f"{cpu['blocks']} blocks of the ensemble's size "
-                                          f"distribution, {cpu['wall_s']:.1f} s wall; a "
-                                          f"core's rate over its own blocks, all cores at "
-                                          f"once, times the cores",
-                                "wall_moves_per_s": cpu["wall_moves_per_s"]}
+                                "sample": f"1 of {cpu['share']} equal parts of the ensemble's "
+                                          f"own blocks ({cpu['blocks']} blocks, same size "
+                                          f"distribution) on {cpu['cores']} cores at once, "
+                                          f"largest first: completed moves / "
+                                          f"{cpu['wall_s']:.1f} s wall",
+                                "structures_per_s": cpu["moves_per_s"] / mps}
+    if rank == 0 and world == 1 and args.configs:
+        line["configs"] = config_records(args)
     print(json.dumps(line))
+
+
+def ensemble_config(args, world):
+    """The workload as both arms state it (same dictionary)."""
+    return {"workload": WORKLOAD, "structures": N_STRUCT * world,
+            "blocks_per_structure": N_BLOCKS, "regions": N_STRUCT * N_BLOCKS * world,
+            "block_seeds": "structure s: sizes from seed 10000 + s, block b from 1000 s + b",
+            "fp64_resync_every": args.resync,
+            "l2": "GPU leg: a 256 MB buffer is written between timed steps (L2 is 129 MB)",
+            "parallelism": f"replicas x{world}"}
+
+
+def reference_main(args, config):
+    """The reference arm on the GPU leg's own ensemble: its 1536 blocks split
+    into warmup + steps parts of the same size distribution; the warm-up
+    parts run untimed, the timed parts as one pass of a process pool over
+    every host core, largest block first.  Wall-clock moves/s and
+    structures/s."""
+    from oracle import oracle as O
+    O.build()
+    cores = os.cpu_count() or 1
+    shares = size_shares(ensemble_blocks(0), args.warmup + args.steps)
+    warm = [b for p in shares[:args.warmup] for b in p]
+    timed = [b for p in shares[args.warmup:] for b in p]
+    with mp.get_context("spawn").Pool(cores) as pool:
+        if warm:
+            cpu_anneal_blocks(pool, warm)
+        moves, wall, cpu_s = cpu_anneal_blocks(pool, timed)
+    v = moves / wall
+    structs = len(timed) / N_BLOCKS / wall
+    line = {
+        "impl": "reference", "metric": "MC moves/s", "value": v, "unit": "moves/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": wall / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic", "config": config,
+        "moves_per_step": moves / args.steps,
+        "structures_per_s": structs,
+        "cpu_baseline": {"value": v, "unit": "moves/s", "cores": cores, "kind": "port",
+                         "sample": f"the ensemble's {len(timed)} timed blocks ({args.steps} of "
+                                   f"{args.warmup + args.steps} equal parts of its "
+                                   f"{len(timed) + len(warm)} blocks) on {cores} cores, "
+                                   f"{wall:.1f} s wall ({cpu_s:.0f} CPU s)",
+                         "structures_per_s": structs},
+        "e2e": {"value": v, "unit": "moves/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+
+
+def config_records(args) -> dict:
+    """The other configurations beside the default line, each with its value,
+    roofline, e2e through the host-buffer C call and its CPU baseline timed
+    on this host's cores in the same run: 0 plain (one 256-bead region),
+    1 heatmap (one 2048-bead chain, 100k moves; the two-maps-per-SM batch as
+    the HBM-bound form), 3 genome smoothing (20k sweeps), 4 serving (5000
+    requests at 200/s)."""
+    out = {}
+    budget = max(5.0, min(args.cpu_budget, 15.0))
+
+    def ns(**kw):
+        base = dict(steps=3, warmup=1, moves=0, requests=0, n=0, maps=0, impl="ours",
+                    cpu_budget=budget)
+        base.update(kw)
+        return argparse.Namespace(**base)
+
+    def timed(name, fn):
+        t = time.perf_counter()
+        try:
+            rec = fn()
+        except Exception as e:  # a failing sub-record must not lose the main line
+            rec = {"error": f"{type(e).__name__}: {e}"}
+        rec["record_wall_s"] = time.perf_counter() - t
+        out[name] = rec
+
+    timed("0_plain", lambda: plain_record(ns(steps=5, warmup=2)))
+    timed("1_heatmap", lambda: heatmap_record(ns(), 1))
+    timed("1_heatmap_batch", lambda: heatmap_record(ns(), 0))
+    timed("3_smooth", lambda: smooth_record(ns()))
+    timed("4_serve", lambda: serve_record(ns()))
+    return out
 
 
 if __name__ == "__main__":

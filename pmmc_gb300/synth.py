@@ -210,21 +210,26 @@ def smooth_genome(total_beads: int = 300_000, seed: int = 3) -> list[SmoothChain
     return [smooth_chain(int(s), seed=seed * 1000 + c) for c, s in enumerate(sizes)]
 
 
-def arcs_ensemble(n_structures: int = 64, n_blocks: int = 24, min_size: int = 32,
-                  max_size: int = 2048, arcs_per_bead: float = 1.5,
-                  seeds=None) -> list[list[ArcsRegion]]:
-    """structures x blocks arc regions; block sizes log-uniform in
-    [min_size, max_size]; structure s is generated from seed s."""
+def ensemble_block_specs(n_structures: int = 64, n_blocks: int = 24, min_size: int = 32,
+                         max_size: int = 2048, seeds=None) -> list[list[tuple[int, int]]]:
+    """(beads, region seed) of every block: structures x blocks, block sizes
+    log-uniform in [min_size, max_size], structure s drawn from seed s."""
     out = []
     seeds = list(range(n_structures)) if seeds is None else list(seeds)
     for s in seeds:
         rng = np.random.default_rng(10_000 + s)
-        blocks = []
-        for b in range(n_blocks):
-            size = int(round(np.exp(rng.uniform(np.log(min_size), np.log(max_size)))))
-            blocks.append(arcs_region(size, seed=s * 1000 + b, arcs_per_bead=arcs_per_bead))
-        out.append(blocks)
+        out.append([(int(round(np.exp(rng.uniform(np.log(min_size), np.log(max_size))))),
+                     s * 1000 + b) for b in range(n_blocks)])
     return out
+
+
+def arcs_ensemble(n_structures: int = 64, n_blocks: int = 24, min_size: int = 32,
+                  max_size: int = 2048, arcs_per_bead: float = 1.5,
+                  seeds=None) -> list[list[ArcsRegion]]:
+    """structures x blocks arc regions (ensemble_block_specs); block (s, b)
+    is arcs_region(size, seed=1000 s + b)."""
+    return [[arcs_region(n, seed=seed, arcs_per_bead=arcs_per_bead) for n, seed in blocks]
+            for blocks in ensemble_block_specs(n_structures, n_blocks, min_size, max_size, seeds)]
 
 
 def freq_memo(count_a: float, count_scale: float, count_shift: float,

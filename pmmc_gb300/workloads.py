@@ -70,6 +70,33 @@ def _traffic(kernel: str, workload: str):
     return None
 
 
+def smem_peak_gbs(sm_mhz: float = 2070.0, sms: int = 152) -> float:
+    """Nominal shared-memory bandwidth of the device: 128 bytes per clock per
+    SM (no measured figure exists for it)."""
+    return 128.0 * sms * sm_mhz * 1e6 / 1e9
+
+
+def fp32_peak_tflops(sm_mhz: float = 2070.0, sms: int = 152) -> float:
+    """Nominal FP32 rate: 128 FMA lanes per SM, 2 FLOP per FMA."""
+    return 2.0 * 128.0 * sms * sm_mhz * 1e6 / 1e12
+
+
+def _smem_roofline(moves_per_s: float, bytes_per_move: float, flop_per_move: float,
+                   sm_mhz: float = 2070.0) -> dict:
+    """Shared-memory and FP32 roofline of an in-SMEM annealing kernel, on the
+    algorithmic bytes and FLOP of one move, against nominal device peaks."""
+    smem = moves_per_s * bytes_per_move / 1e9
+    flops = moves_per_s * flop_per_move / 1e12
+    return {"bound": "smem", "achieved": smem, "peak": smem_peak_gbs(sm_mhz), "unit": "GB/s",
+            "frac": smem / smem_peak_gbs(sm_mhz), "traffic": None,
+            "peak_source": "nominal (128 B/clk/SM, 152 SMs, 2070 MHz)",
+            "algorithmic_bytes_per_move": bytes_per_move,
+            "fp32": {"achieved": flops, "peak": fp32_peak_tflops(sm_mhz), "unit": "TFLOP/s",
+                     "frac": flops / fp32_peak_tflops(sm_mhz),
+                     "algorithmic_flop_per_move": flop_per_move,
+                     "peak_source": "nominal (128 FMA/clk/SM)"}}
+
+
 HEATMAP_ANNEAL = dict(max_temp=5.0, dt_temp=0.9999, milestone_steps=100_000, improvement=0.99)
 
 
@@ -95,14 +122,18 @@ def heatmap(args, n_maps):
     moves = args.moves or (100_000 if n_maps == 1 else 20_000)
     prm = capi.default_params(capi.LEVEL_HEATMAP, schedule=capi.SCHEDULE_CPU, max_moves=moves,
                               **HEATMAP_ANNEAL)
-    times, total = [], 0
+    times, walls, total = [], [], 0
     for k in range(args.warmup + args.steps):
         ctx.set_seed(7)
+        t0 = time.perf_counter()
         out, res, ms, _ = capi.heatmap_batch_anneal(ctx, inputs, prm, [1.0] * len(inputs))
+        wall = time.perf_counter() - t0
         if k >= args.warmup:
             times.append(ms)
+            walls.append(wall)
             total = sum(r.moves for r in res)
     ms = float(np.mean(times))
+    wall = float(np.median(walls))
     row_bytes = 4 * 2048
     # one launch reads each move's row once and each map twice in full (the
     # FP64 start and end scores)
@@ -122,6 +153,11 @@ def heatmap(args, n_maps):
                      "frac": achieved / peak, "traffic": traffic, "peak_source": kind,
                      "algorithmic_bytes_per_move": row_bytes,
                      "algorithmic_bytes_per_launch": alg},
+        # pmmc_heatmap_batch_anneal with host arrays: the reciprocal map is
+        # packed and checked on the host, copied up, annealed, copied back
+        "e2e": {"value": total / wall, "unit": "moves/s", "ms_per_step": wall * 1e3,
+                "h2d_bytes_per_step": int(sum(4 * (x.n * x.n + 3 * x.n) for x in inputs)),
+                "d2h_bytes_per_step": int(sum(12 * x.n + 56 for x in inputs))},
     }
     return line
 
@@ -150,15 +186,23 @@ def smooth(args):
     sweeps = args.moves or 20_000
     prm = capi.default_params(capi.LEVEL_SMOOTH, schedule=capi.SCHEDULE_CPU, resync_every=1000,
                               **SMOOTH_ANNEAL)
-    times, total = [], 0
+    times, walls, total = [], [], 0
     for k in range(args.warmup + args.steps):
         ctx.set_seed(3)
         # each region: sweeps x its free beads
+        t0 = time.perf_counter()
         out, res, ms = _smooth_run(ctx, segs, prm, sweeps)
+        wall = time.perf_counter() - t0
         if k >= args.warmup:
             times.append(ms)
+            walls.append(wall)
             total = sum(r.moves for r in res)
     ms = float(np.mean(times))
+    wall = float(np.median(walls))
+    beads = sum(x.n for x in segs)
+    # per move: two bonds and three angles read five beads (16 B each) and
+    # take ~80 FLOP (the smoothing energy of a move)
+    sm = _smem_roofline(total / (ms * 1e-3), 80.0, 80.0)
     line = {
         "metric": "MC moves/s", "value": total / (ms * 1e-3), "unit": "moves/s", "n_gpus": 1,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms,
@@ -167,6 +211,10 @@ def smooth(args):
         "config": {"workload": f"genome_smoothing_{len(segs)}regions_{free}free_beads_"
                                f"{sweeps}sweeps", "moves_per_step": total},
         "final_energy_rel_error_max": max(r.rel_error for r in res),
+        "roofline": sm,
+        "e2e": {"value": total / wall, "unit": "moves/s", "ms_per_step": wall * 1e3,
+                "h2d_bytes_per_step": int(beads * (12 + 4 + 1) + len(segs) * 80),
+                "d2h_bytes_per_step": int(beads * 12 + len(segs) * 56)},
     }
     return line
 
@@ -278,6 +326,8 @@ def serve(args) -> dict:
                              "latency_ms_mean": float(ol_lat.mean()),
                              "waves": ol_st["waves"], "running_peak": ol_st["running_peak"]},
         "final_energy_rel_error_max": max(sat_err, ol_err),
+        # per move as the plain region: 2 x deg pair terms, deg = 3.125
+        "roofline": _smem_roofline(sat_moves / sat_wall, 2 * 3.125 * 24.0, 2 * 3.125 * 15.0),
         "e2e": {"value": n_req / sat_wall, "unit": "structures/s",
                 "h2d_bytes_per_step": None, "d2h_bytes_per_step": None,
                 "note": "host arrays in, host results out, through pmmc_server_*"},
@@ -325,6 +375,12 @@ def plain(args) -> dict:
         "config": {"workload": "arcs_plain_256beads_400arcs_seed42_T0=5_cool0.9999_"
                                "milestone50k_thr0.99", "call": "pmmc_arcs_anneal"},
         "forms": out,
+        # per move: 2 x deg pair terms (deg = 800 / 256 arc-list entries per
+        # bead), each a 16-byte position and an 8-byte arc entry, ~15 FLOP;
+        # one serial chain runs on one SM of the device
+        "roofline": dict(_smem_roofline(one["chain_moves_per_s"], 2 * 3.125 * 24.0,
+                                        2 * 3.125 * 15.0),
+                         note="one serial chain on one of 152 SMs: latency-bound"),
         "e2e": {"value": one["chain_moves_per_s"], "unit": "moves/s",
                 "h2d_bytes_per_step": int(r.pos.nbytes + rp.nbytes + col.nbytes + tgt.nbytes),
                 "d2h_bytes_per_step": int(r.pos.nbytes)},

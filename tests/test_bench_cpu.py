@@ -38,9 +38,32 @@ def check_line(lines, unit):
 
 
 def test_reference_arm_ensemble():
-    d = check_line(run_bench("--impl", "reference", "--steps", "1", "--warmup", "0"),
-                   "moves/s")
+    """The reference arm anneals the GPU leg's own blocks (here a 2-structure
+    ensemble) and states the same config dictionary the GPU leg states."""
+    import argparse
+    sys.path.insert(0, ROOT)
+    import bench
+    d = check_line(run_bench("--impl", "reference", "--steps", "2", "--warmup", "1",
+                             "--structures", "2"), "moves/s")
     assert d["metric"] == "MC moves/s" and d["higher_is_better"] is True
+    bench.set_workload(2, bench.ANNEAL["milestone_steps"])
+    want = bench.ensemble_config(argparse.Namespace(resync=bench.RESYNC), 1)
+    bench.set_workload(64, bench.ANNEAL["milestone_steps"])
+    assert d["config"] == want
+    assert d["config"]["regions"] == 48 and d["config"]["fp64_resync_every"] == 1000
+    assert d["structures_per_s"] > 0 and d["steps"] == 2
+
+
+def test_size_shares_keep_the_distribution():
+    sys.path.insert(0, ROOT)
+    import bench
+    bench.set_workload(64, bench.ANNEAL["milestone_steps"])
+    blocks = bench.ensemble_blocks(0)
+    assert len(blocks) == 64 * 24
+    parts = bench.size_shares(blocks, 8)
+    assert sorted(b for p in parts for b in p) == sorted(blocks)
+    means = [sum(n for n, _ in p) / len(p) for p in parts]
+    assert max(means) / min(means) < 1.1
 
 
 @pytest.mark.parametrize("workload,unit", [("targets", "arcs/s"), ("smooth", "moves/s"),
