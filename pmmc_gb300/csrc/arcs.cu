@@ -66,6 +66,17 @@ __device__ __forceinline__ float fast_len(float ax, float ay, float az, float4 b
   return ref_len(__fsub_rn(ax, b.x), __fsub_rn(ay, b.y), __fsub_rn(az, b.z));
 }
 
+// 1/t for a target t >= 1e-6: the approximate reciprocal refined by one
+// Newton-Raphson step, r' = r + r (1 - t r), which leaves it within about half
+// an ulp of the exact reciprocal (Newton's method for f(r) = 1/r - t).  One
+// special-function operation and two fused multiply-adds, where the
+// correctly rounded library reciprocal costs several times that.
+__device__ __forceinline__ float recip_nr(float t) {
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(t));
+  return fmaf(r, fmaf(-t, r, 1.0f), r);
+}
+
 // Spring term of one arc: ((len - t) / t)^2 * k, with 1/t precomputed.
 __device__ __forceinline__ float spring_fast(float len, float t, float it, float ks,
                                              float kq) {
@@ -361,8 +372,7 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
     size_t off = (size_t)kMoveBufBytes + (size_t)n * 16 + (size_t)(n + 1) * 4 + (size_t)n * 4;
     off = (off + 7) & ~(size_t)7;
     int2 *snb = reinterpret_cast<int2 *>(wbase + off);
-    float *sinv = reinterpret_cast<float *>(wbase + off + (size_t)U.nnz * 8);
-    if (NB_SMEM) off += (size_t)U.nnz * 12;
+    if (NB_SMEM) off += (size_t)U.nnz * 8;
     const bool has_mov = U.mov_off >= 0;
     const bool mov_smem = has_mov && off + (size_t)U.n_mov * 4 <= (size_t)smem_per_warp;
     int *smov = reinterpret_cast<int *>(wbase + off);
@@ -434,10 +444,7 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
     for (int i = lane; i <= n; i += 32) srp[i] = row_ptr[U.rp_off + i];
     for (int i = lane; i < n; i += 32) smask[i] = 0u;
     if (NB_SMEM) {
-      for (int e = lane; e < U.nnz; e += 32) {
-        snb[e] = nbr[U.nbr_off + e];
-        sinv[e] = inv_t[U.nbr_off + e];
-      }
+      for (int e = lane; e < U.nnz; e += 32) snb[e] = nbr[U.nbr_off + e];
     }
     if (mov_smem)
       for (int k = lane; k < U.n_mov; k += 32) smov[k] = movable[U.mov_off + k];
@@ -452,7 +459,9 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
       pair_sync(slot_w);  // staging done: the drawing warp starts
     }
     const int2 *NB = NB_SMEM ? snb : nbr + U.nbr_off;
-    const float *INV = NB_SMEM ? sinv : inv_t + U.nbr_off;
+    // reciprocal targets: the global copy for the recompute without a spring
+    // list; the window's terms derive them from the target
+    const float *INV = inv_t + U.nbr_off;
     const int *MOV = has_mov ? (mov_smem ? smov : movable + U.mov_off) : nullptr;
     const bool has_loops = U.lrp_off >= 0;
     const int *LRP = has_loops ? lrp + U.lrp_off : nullptr;
@@ -590,7 +599,8 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
             const int ek = e + k * G;
             const bool ok = ek < end;
             ent[k] = NB[ok ? ek : e];
-            iv[k] = ok ? INV[ek] : 0.0f;
+            // 1/t from the target (8 staged bytes per entry instead of 12)
+            iv[k] = ok ? recip_nr(__int_as_float(ent[k].y)) : 0.0f;
           }
 #pragma unroll
           for (int k = 0; k < UA; ++k) {
@@ -968,7 +978,7 @@ namespace pmmc {
 size_t arcs_unit_smem(int n, int nnz, int n_mov, bool has_mov) {
   size_t s = (size_t)kMoveBufBytes + (size_t)n * 16 + (size_t)(n + 1) * 4 + (size_t)n * 4;
   s = (s + 7) & ~(size_t)7;
-  s += (size_t)nnz * 12;
+  s += (size_t)nnz * 8;
   if (has_mov) s += (size_t)n_mov * 4;
   return s;
 }
