@@ -136,16 +136,11 @@ struct MoveRec {
   float dx, dy, dz;
 };
 
-// Approximate reciprocal square root and reciprocal (one special-function
-// operation each, flush-to-zero; callers keep the arguments normal).
+// Approximate reciprocal square root (one special-function operation,
+// flush-to-zero; callers keep the argument normal).
 __device__ __forceinline__ float rsqrt_approx(float s) {
   float r;
   asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(s));
-  return r;
-}
-__device__ __forceinline__ float rcp_approx(float s) {
-  float r;
-  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(s));
   return r;
 }
 
@@ -164,20 +159,21 @@ struct MoveGeo {
 };
 
 // Change of the pair term (d r - 1)^2 (r = 1/h) between a bead at p and a
-// bead that moves from o to o + delta.  With v = p - o, s_o = |v|^2,
-// t = s_n - s_o = |delta|^2 - 2 v.delta (formed directly, no cancellation)
-// and d_n - d_o = t / (d_n + d_o):
-//   (d_n r - 1)^2 - (d_o r - 1)^2 = r t (r - 2 / (d_n + d_o)).
-// r = 0 (no target, inside the diagonal band, the bead itself, another
-// chromosome block) contributes exactly 0.
+// bead that moves from o to o + delta.  With v = p - o, s_o = |v|^2 and
+// t = s_n - s_o = |delta|^2 - 2 v.delta (formed directly, no cancellation):
+//   (d_n r - 1)^2 - (d_o r - 1)^2 = r (r t - 2 (d_n - d_o)).
+// Two special-function operations per pair (one reciprocal square root per
+// length); the difference d_n - d_o costs about one ulp of d, a relative
+// error of the move's local change below 1e-8.  r = 0 (no target, inside the
+// diagonal band, the bead itself, another chromosome block) contributes
+// exactly 0.
 __device__ __forceinline__ float pair_delta(float px, float py, float pz, const MoveGeo &g,
                                             float r) {
   const float vx = px - g.ox, vy = py - g.oy, vz = pz - g.oz;
   const float so = fmaf(vx, vx, fmaf(vy, vy, vz * vz));
   const float t = fmaf(vx, g.mx, fmaf(vy, g.my, fmaf(vz, g.mz, g.dd)));
-  const float dsum = len_from_sq(so) + len_from_sq(so + t);
-  const float q = fmaf(-2.0f, rcp_approx(dsum), r);
-  return (r * t) * q;
+  const float dd = len_from_sq(so + t) - len_from_sq(so);
+  return r * fmaf(r, t, -2.0f * dd);
 }
 
 // Full score in FP64 (FP32 terms (d r - 1)^2 summed per row, rows summed in
