@@ -185,10 +185,19 @@ void pmmc_default_params(int level, pmmc_anneal_params *out);
 /* Reference dense matrix (heatmap_exp_dist_anchor.v, -1 = no arc) -> CSR
  * over both directions, keeping every off-diagonal entry >= 0.  Entry
  * (i, j) of the CSR holds dense[j*n + i] (the column the reference's local
- * score reads, LooperSolver.hpp:3262).  With col/target NULL only counts. */
+ * score reads, LooperSolver.hpp:3262); columns ascend within a row.  With
+ * col/target NULL only row_ptr and *nnz; a cap below the count returns
+ * PMMC_ERR_INVALID with *nnz set. */
 pmmc_status pmmc_arcs_dense_to_csr(int n, const float *dense, int *row_ptr,
                                    int *col, float *target, int64_t cap,
                                    int64_t *nnz);
+/* The same from the reference's own row pointers (Heatmap::v, float**;
+ * rows[j][i] = v[j][i]), read row by row with no n x n copy: what
+ * parallelMonteCarloArcs packs from heatmap_exp_dist_anchor
+ * (ParallelMonteCarloArcs.cu:789-840). */
+pmmc_status pmmc_arcs_rows_to_csr(int n, const float *const *rows, int *row_ptr,
+                                  int *col, float *target, int64_t cap,
+                                  int64_t *nnz);
 
 /* ---------------- plain drop-in entry points (host buffers) ----------- */
 /* Replaces float LooperSolver::parallelMonteCarloArcs(float step_size)

@@ -45,6 +45,7 @@ HEADER_SYMBOLS = [
     "pmmc_selftest_sqrt", "pmmc_distance_heatmap", "pmmc_distance_heatmap_device",
     "pmmc_equidistant_model", "pmmc_hcm_write", "pmmc_anchor_targets", "pmmc_stress_refine",
     "pmmc_server_cancel", "pmmc_arcs_batch_trace_chain", "pmmc_arcs_batch_chain_results",
+    "pmmc_arcs_rows_to_csr",
 ]
 
 LANES_AUTO = -1  # PMMC_LANES_AUTO: the autotuner picks lanes and warps per class

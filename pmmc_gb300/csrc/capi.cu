@@ -1,4 +1,5 @@
 // capi.cu -- context, parameters and format conversions of the C ABI.
+#include <vector>
 #include <cstring>
 
 #include "common.cuh"
@@ -99,31 +100,65 @@ extern "C" void pmmc_default_params(int level, pmmc_anneal_params *o) {
   }
 }
 
-extern "C" pmmc_status pmmc_arcs_dense_to_csr(int n, const float *dense, int *row_ptr,
-                                              int *col, float *target, int64_t cap,
-                                              int64_t *nnz) {
-  if (n < 0 || !dense || !row_ptr) return PMMC_ERR_INVALID;
+namespace {
+
+// CSR over both directions from the reference's matrix given as rows
+// (row(j)[i] = v[j][i]): entry (i, j) holds v[j][i], the column the
+// reference's local score reads (LooperSolver.hpp:3262), kept when i != j
+// and v >= 0.  Two row-major passes: the counts of every CSR row, then the
+// entries, columns in increasing order.  With col/target NULL only row_ptr
+// and the count; a capacity below the count returns PMMC_ERR_INVALID with
+// *nnz set.
+template <class RowFn>
+pmmc_status csr_from_rows(int n, RowFn row, int *row_ptr, int *col, float *target,
+                          int64_t cap, int64_t *nnz) {
+  std::vector<int64_t> cnt((size_t)n + 1, 0);
+  for (int j = 0; j < n; ++j) {
+    const float *r = row(j);
+    if (!r) return PMMC_ERR_INVALID;
+    for (int i = 0; i < n; ++i) cnt[i] += (i != j && r[i] >= 0.0f) ? 1 : 0;
+  }
   int64_t k = 0;
   row_ptr[0] = 0;
   for (int i = 0; i < n; ++i) {
-    for (int j = 0; j < n; ++j) {
-      if (j == i) continue;
-      // the local score reads the column of the moved bead: v[j][i]
-      const float v = dense[(size_t)j * n + i];
-      if (v >= 0.0f) {
-        if (col && target) {
-          if (k >= cap) return PMMC_ERR_INVALID;
-          col[k] = j;
-          target[k] = v;
-        }
-        ++k;
-      }
-    }
+    const int64_t c = cnt[i];
+    cnt[i] = k;  // cursor of row i
+    k += c;
     if (k > 0x7fffffff) return PMMC_ERR_INVALID;
     row_ptr[i + 1] = (int)k;
   }
   if (nnz) *nnz = k;
+  if (!col || !target) return PMMC_OK;
+  if (k > cap) return PMMC_ERR_INVALID;
+  for (int j = 0; j < n; ++j) {
+    const float *r = row(j);
+    for (int i = 0; i < n; ++i) {
+      const float v = r[i];
+      if (i != j && v >= 0.0f) {
+        const int64_t e = cnt[i]++;
+        col[e] = j;
+        target[e] = v;
+      }
+    }
+  }
   return PMMC_OK;
+}
+
+}  // namespace
+
+extern "C" pmmc_status pmmc_arcs_dense_to_csr(int n, const float *dense, int *row_ptr,
+                                              int *col, float *target, int64_t cap,
+                                              int64_t *nnz) {
+  if (n < 0 || !dense || !row_ptr) return PMMC_ERR_INVALID;
+  return csr_from_rows(n, [&](int j) { return dense + (size_t)j * n; }, row_ptr, col, target,
+                       cap, nnz);
+}
+
+extern "C" pmmc_status pmmc_arcs_rows_to_csr(int n, const float *const *rows, int *row_ptr,
+                                             int *col, float *target, int64_t cap,
+                                             int64_t *nnz) {
+  if (n < 0 || !rows || !row_ptr) return PMMC_ERR_INVALID;
+  return csr_from_rows(n, [&](int j) { return rows[j]; }, row_ptr, col, target, cap, nnz);
 }
 
 // ---------------------------------------------------------------------------

@@ -18,6 +18,7 @@
 // library's status message.  There is no CPU fallback.
 #include <cstdio>
 #include <cstdlib>
+#include <algorithm>
 #include <map>
 #include <mutex>
 #include <string>
@@ -102,8 +103,15 @@ float LooperSolver::parallelMonteCarloArcs(float step_size) {
   const int n = static_cast<int>(active_region.size());
   if (n <= 1) return 0.0f;
   rebuildActiveLoopMap();
-  std::vector<float> pos(3 * n), out(3 * n);
-  std::vector<unsigned char> fixed(n);
+  // host staging kept across calls (the reference caches its device buffers
+  // in gpu_cache the same way); the drop-in is called from one thread
+  static std::vector<float> pos, out, target;
+  static std::vector<unsigned char> fixed;
+  static std::vector<int> row_ptr, col;
+  static std::vector<const float *> rows;
+  pos.resize(3 * n);
+  out.resize(3 * n);
+  fixed.resize(n);
   for (int i = 0; i < n; ++i) {
     const Cluster &c = clusters[active_region[i]];
     pos[3 * i] = c.pos.x;
@@ -111,19 +119,28 @@ float LooperSolver::parallelMonteCarloArcs(float step_size) {
     pos[3 * i + 2] = c.pos.z;
     fixed[i] = c.is_fixed ? 1 : 0;
   }
-  std::vector<float> dense((size_t)n * n, -1.0f);
-  if ((int)heatmap_exp_dist_anchor.size == n)
-    for (int i = 0; i < n; ++i)
-      for (int j = 0; j < n; ++j) dense[(size_t)i * n + j] = heatmap_exp_dist_anchor.v[i][j];
-  std::vector<int> row_ptr(n + 1);
+  // the arc lists straight from the rows of heatmap_exp_dist_anchor (no
+  // n x n copy); without a matrix of the region's size every pair repels
+  row_ptr.resize(n + 1);
+  if (col.empty()) {  // non-null buffers: a short capacity reports the count
+    col.resize(1);
+    target.resize(1);
+  }
   int64_t nnz = 0;
-  check(pmmc_arcs_dense_to_csr(n, dense.data(), row_ptr.data(), nullptr, nullptr, 0, &nnz),
-        "arc lists");
-  std::vector<int> col(nnz > 0 ? nnz : 1);
-  std::vector<float> target(nnz > 0 ? nnz : 1);
-  check(pmmc_arcs_dense_to_csr(n, dense.data(), row_ptr.data(), col.data(), target.data(), nnz,
-                               &nnz),
-        "arc lists");
+  if ((int)heatmap_exp_dist_anchor.size == n) {
+    rows.assign(heatmap_exp_dist_anchor.v, heatmap_exp_dist_anchor.v + n);
+    pmmc_status st = pmmc_arcs_rows_to_csr(n, rows.data(), row_ptr.data(), col.data(),
+                                           target.data(), (int64_t)col.size(), &nnz);
+    if (st != PMMC_OK && nnz > (int64_t)col.size()) {  // grow to the count, once
+      col.resize(nnz);
+      target.resize(nnz);
+      st = pmmc_arcs_rows_to_csr(n, rows.data(), row_ptr.data(), col.data(), target.data(),
+                                 (int64_t)col.size(), &nnz);
+    }
+    check(st, "arc lists");
+  } else {
+    std::fill(row_ptr.begin(), row_ptr.end(), 0);
+  }
   std::vector<int> li, lj;
   std::vector<float> lk, lr;
   for (const auto &entry : active_loop_map) {

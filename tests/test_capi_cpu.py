@@ -42,6 +42,44 @@ def test_dense_to_csr_reads_columns(built_lib):
     np.testing.assert_array_equal(tgt, np.array([2.5, 0.0, 1.5, 0.0], np.float32))
 
 
+def test_rows_to_csr_equals_dense_to_csr(built_lib):
+    """The reference's row pointers (Heatmap::v) give the CSR of its dense
+    matrix, with no n x n copy; a short capacity reports the count."""
+    import ctypes as C
+    rng = np.random.default_rng(4)
+    n = 300
+    d = np.full((n, n), -1.0, np.float32)
+    m = rng.random((n, n)) < 0.02
+    d[m] = rng.uniform(0.0, 3.0, m.sum()).astype(np.float32)
+    d[rng.random((n, n)) < 0.003] = 0.0
+    np.fill_diagonal(d, 0.0)
+    rp, col, tgt = capi.dense_to_csr(d)
+    rows = (C.POINTER(C.c_float) * n)(*[d[j].ctypes.data_as(C.POINTER(C.c_float))
+                                        for j in range(n)])
+    rp2 = np.zeros(n + 1, np.int32)
+    nnz = C.c_int64()
+    short = np.zeros(4, np.int32), np.zeros(4, np.float32)
+    st = capi.lib().pmmc_arcs_rows_to_csr(n, rows, rp2.ctypes.data_as(C.c_void_p),
+                                          short[0].ctypes.data_as(C.c_void_p),
+                                          short[1].ctypes.data_as(C.c_void_p), C.c_int64(4),
+                                          C.byref(nnz))
+    assert st == capi.PMMC_ERR_INVALID and nnz.value == len(col)
+    col2 = np.zeros(nnz.value, np.int32)
+    tgt2 = np.zeros(nnz.value, np.float32)
+    st = capi.lib().pmmc_arcs_rows_to_csr(n, rows, rp2.ctypes.data_as(C.c_void_p),
+                                          col2.ctypes.data_as(C.c_void_p),
+                                          tgt2.ctypes.data_as(C.c_void_p), C.c_int64(nnz.value),
+                                          C.byref(nnz))
+    assert st == capi.PMMC_OK
+    np.testing.assert_array_equal(rp2, rp)
+    np.testing.assert_array_equal(col2, col)
+    np.testing.assert_array_equal(tgt2, tgt)
+    # row i lists column i of the matrix, ascending
+    for i in (0, 7, 299):
+        js = [j for j in range(n) if j != i and d[j, i] >= 0]
+        assert list(col[rp[i]:rp[i + 1]]) == js
+
+
 def test_no_device_is_an_error(built_lib):
     try:
         import torch

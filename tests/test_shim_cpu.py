@@ -8,7 +8,8 @@ import subprocess
 import pytest
 
 ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
-REF = "/root/reference/src"
+# the reference tree, as oracle/Makefile takes it (REF_ROOT, same default)
+REF = os.path.join(os.environ.get("REF_ROOT", "/root/reference"), "src")
 
 pytestmark = pytest.mark.skipif(not os.path.isdir(REF) or shutil.which("g++") is None,
                                 reason="reference headers not present")
