@@ -408,35 +408,35 @@ extern "C" pmmc_status pmmc_stress_refine(pmmc_ctx *ctx, const pmmc_stress_probl
   });
   for (int i = 0; i < n; ++i) order_out[i] = pr->active[ord[i]];
   const int n_anc = pr->n_anchors, cs = pr->first_cluster;
-  std::vector<int> anc_to_active(std::max(n_anc, 1), -1);
+  std::vector<int> slot_of_cluster(std::max(n_anc, 1), -1);
   for (int i = 0; i < n; ++i) {
     const int ci = order_out[i];
-    if (ci >= cs && ci - cs < n_anc) anc_to_active[ci - cs] = i;
+    if (ci >= cs && ci - cs < n_anc) slot_of_cluster[ci - cs] = i;
   }
   // pair targets, the first of a pair wins (:5670-5729)
-  const bool backbone_active = pr->k_stretch > 1e-6f || pr->k_squeeze > 1e-6f;
-  struct Pair {
+  const bool with_backbone = pr->k_stretch > 1e-6f || pr->k_squeeze > 1e-6f;
+  struct TargetPair {
     int i, j;
     float t;
   };
-  std::vector<Pair> pairs;
+  std::vector<TargetPair> pairs;
   std::unordered_map<uint64_t, int> seen;
   seen.reserve((size_t)(pr->n_arcs + pr->n_long) + 16);
-  auto add_pair = [&](int ai, int aj, float t) {
+  auto take_target = [&](int ai, int aj, float t) {
     if (ai == aj) return;
     if (ai > aj) std::swap(ai, aj);
-    if (backbone_active && aj - ai <= 1) return;
+    if (with_backbone && aj - ai <= 1) return;
     const uint64_t key = (uint64_t)ai * (uint64_t)n + (uint64_t)aj;
     if (seen.emplace(key, (int)pairs.size()).second) pairs.push_back({ai, aj, t});
   };
   for (int k = 0; k < pr->n_arcs; ++k) {
     const int ca = pr->arc_start[k], cb = pr->arc_end[k];
     if (ca < cs || ca - cs >= n_anc || cb < cs || cb - cs >= n_anc) continue;
-    const int ai = anc_to_active[ca - cs], aj = anc_to_active[cb - cs];
+    const int ai = slot_of_cluster[ca - cs], aj = slot_of_cluster[cb - cs];
     if (ai < 0 || aj < 0) continue;
     const float t = count_to_distance(pr->arc_score[k], pr->count_a, pr->count_scale,
                                       pr->count_shift, pr->count_base);
-    if (t > 1e-6f) add_pair(ai, aj, t);
+    if (t > 1e-6f) take_target(ai, aj, t);
   }
   // Anchor::contains, the first anchor holding pos: binary search over
   // sorted, disjoint anchors, else the reference's scan
@@ -444,7 +444,7 @@ extern "C" pmmc_status pmmc_stress_refine(pmmc_ctx *ctx, const pmmc_stress_probl
   for (int i = 1; i < n_anc && sorted; ++i)
     sorted = pr->anchor_start[i] > pr->anchor_start[i - 1] &&
              pr->anchor_start[i] > pr->anchor_end[i - 1];
-  auto pos_to_anc = [&](int pos) -> int {
+  auto anchor_at = [&](int pos) -> int {
     if (sorted) {
       const int i = (int)(std::upper_bound(pr->anchor_start, pr->anchor_start + n_anc, pos) -
                           pr->anchor_start) - 1;
@@ -455,18 +455,18 @@ extern "C" pmmc_status pmmc_stress_refine(pmmc_ctx *ctx, const pmmc_stress_probl
     return -1;
   };
   for (int k = 0; k < pr->n_long; ++k) {
-    const int ia = pos_to_anc(pr->long_start[k]), ib = pos_to_anc(pr->long_end[k]);
+    const int ia = anchor_at(pr->long_start[k]), ib = anchor_at(pr->long_end[k]);
     if (ia < 0 || ib < 0) continue;
-    const int as = anc_to_active[ia], bs = anc_to_active[ib];
+    const int as = slot_of_cluster[ia], bs = slot_of_cluster[ib];
     if (as < 0 || bs < 0) continue;
     const float t = count_to_distance(pr->long_score[k], pr->count_a, pr->count_scale,
                                       pr->count_shift, pr->count_base);
-    if (t > 1e-6f) add_pair(as, bs, t);
+    if (t > 1e-6f) take_target(as, bs, t);
   }
   r.n_pairs = (int64_t)pairs.size();
   // each anchor's slots in pair order; a pair knows its two slots
   std::vector<int> row_ptr(n + 1, 0);
-  for (const Pair &p : pairs) {
+  for (const TargetPair &p : pairs) {
     ++row_ptr[p.i + 1];
     ++row_ptr[p.j + 1];
   }
@@ -475,7 +475,7 @@ extern "C" pmmc_status pmmc_stress_refine(pmmc_ctx *ctx, const pmmc_stress_probl
   std::vector<int4> pair4(std::max<size_t>(1, pairs.size()));
   std::vector<int> slot_hi(std::max<size_t>(1, pairs.size()));
   for (size_t q = 0; q < pairs.size(); ++q) {
-    const Pair &p = pairs[q];
+    const TargetPair &p = pairs[q];
     int tb;
     memcpy(&tb, &p.t, 4);
     pair4[q] = make_int4(p.i, p.j, tb, fill[p.i]++);
