@@ -149,6 +149,14 @@ __device__ __forceinline__ void ff_add(float &hi, float &lo, float d) {
   lo = l - (hi - s);
 }
 
+// Two lanes per chain: a move's two local energies (the bead at its old and
+// at its proposed position) are evaluated side by side, one per lane, and
+// its two draws (proposal, Metropolis threshold) likewise; the lanes swap
+// their results with one shuffle and keep identical copies of the chain's
+// state.  A thread alone ran one long dependent instruction chain per move
+// with few warps to hide it.
+constexpr int kSmoothLanes = 2;
+
 template <bool SMEM>
 __global__ void __launch_bounds__(128)
 smooth_anneal_kernel(const SmoothUnit *__restrict__ units,
@@ -159,23 +167,29 @@ smooth_anneal_kernel(const SmoothUnit *__restrict__ units,
                      ChainOut *__restrict__ outs, MoveTrace *__restrict__ trace,
                      int trace_cap) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const int item = blockIdx.x * blockDim.x + threadIdx.x;
-  if (item >= n_items) return;
+  constexpr int CPW = 32 / kSmoothLanes;  // chains per warp
+  const int lane = threadIdx.x & 31;
+  const int sub = lane & (kSmoothLanes - 1);
+  const int item = (blockIdx.x * blockDim.x + threadIdx.x) / kSmoothLanes;
+  if (item >= n_items) return;  // both lanes of a chain leave together
+  const unsigned gm = ((1u << kSmoothLanes) - 1u) << (lane & ~(kSmoothLanes - 1));
   const int2 it = items[item];
   const SmoothUnit U = units[it.x];
   const int chain = it.y;
   const int n = U.n;
   const uint32_t chain_id = (uint32_t)(U.chain_base + chain);
-  // shared-memory path: the 32 chains of a warp interleave bead by bead
-  // (bead i of lane l at i * 32 + l), so that a warp's loads of any beads
-  // fall on distinct banks
-  const int st = SMEM ? 32 : 1;
+  // shared-memory path: the chains of a warp interleave bead by bead (bead i
+  // of chain c at i * CPW + c), so that the chains' loads of any beads fall
+  // on distinct banks within a quarter warp; the two lanes of a chain read
+  // the same words
+  const int st = SMEM ? CPW : 1;
   float4 *P = SMEM ? reinterpret_cast<float4 *>(smem) +
-                         (size_t)(threadIdx.x >> 5) * S.slice * 32 + (threadIdx.x & 31)
+                         (size_t)(threadIdx.x >> 5) * S.slice * CPW + (lane / kSmoothLanes)
                    : work + U.work_off + (long long)chain * n;
   const float2 *dtn = dtn_all + U.dtn_off;
   const int *MOV = U.mov_off >= 0 ? movable + U.mov_off : nullptr;
-  for (int i = 0; i < n; ++i) P[i * st] = pos0[U.pos_off + i];
+  for (int i = sub; i < n; i += kSmoothLanes) P[i * st] = pos0[U.pos_off + i];
+  __syncwarp(gm);
 
   const double E0 = smooth_full(P, st, dtn, n, S);
   // running score: float-float pair per move, widened to FP64 at milestones
@@ -189,39 +203,67 @@ smooth_anneal_kernel(const SmoothUnit *__restrict__ units,
   // milestone and recompute counters (no 64-bit division per move)
   long long next_ms = S.window > 0 ? (long long)S.window : 0x7fffffffffffffffLL;
   long long next_rs = S.resync > 0 ? (long long)S.resync : 0x7fffffffffffffffLL;
-  while (!stop) {
-    const uint4 r = philox_move(S.seed, chain_id, (uint64_t)moves, 0u);
+  // The draws of a move depend only on its index and temperature, not on the
+  // chain's state; those of the next move are made while this move is
+  // scored.  Lane 0 draws the proposal (tag 0), lane 1 the threshold (tag 1).
+  struct Draw {
+    int b;
+    float dx, dy, dz, thr;
+  };
+  auto draw = [&](long long mv, float Tm) {
+    const uint4 r = philox_move(S.seed, chain_id, (uint64_t)mv, (uint32_t)sub);
     const int k = uniform_index(r.x, U.n_mov);
-    const int b = MOV ? MOV[k] : k;
+    Draw w;
+    w.b = MOV ? MOV[k] : k;
+    w.dx = (2.0f * u01(r.y) - 1.0f) * U.step;
+    w.dy = (2.0f * u01(r.z) - 1.0f) * U.step;
+    w.dz = S.use2d ? 0.0f : (2.0f * u01(r.w) - 1.0f) * U.step;
+    w.thr = ratio_threshold(u01(r.x), Tm, S.inv_scale, S.inv_coef);
+    return w;
+  };
+  const int lead = lane & ~(kSmoothLanes - 1);
+  auto share = [&](const Draw &w) {
+    Draw o;
+    o.b = __shfl_sync(gm, w.b, lead);
+    o.dx = __shfl_sync(gm, w.dx, lead);
+    o.dy = __shfl_sync(gm, w.dy, lead);
+    o.dz = __shfl_sync(gm, w.dz, lead);
+    o.thr = __shfl_sync(gm, w.thr, lead + 1);
+    return o;
+  };
+  Draw cur = share(draw(moves, T));
+  while (!stop) {
+    const Draw nxt = draw(moves + 1, T * S.dt);  // T of the next move
+    const int b = cur.b;
+    const float ddx = cur.dx, ddy = cur.dy, ddz = cur.dz;
     const float4 ob = P[b * st];
-    const float ddx = (2.0f * u01(r.y) - 1.0f) * U.step;
-    const float ddy = (2.0f * u01(r.z) - 1.0f) * U.step;
-    const float ddz = S.use2d ? 0.0f : (2.0f * u01(r.w) - 1.0f) * U.step;
     float4 nb = ob;
     nb.x += ddx;
     nb.y += ddy;
     nb.z += ddz;
-    const float so = smooth_local(P, st, dtn, n, b, ob, S);
-    const float sn = smooth_local(P, st, dtn, n, b, nb, S);
+    // lane 0 the old local energy, lane 1 the new one
+    const float mine = smooth_local(P, st, dtn, n, b, sub ? nb : ob, S);
+    const float other = __shfl_xor_sync(gm, mine, 1);
+    const float so = sub ? other : mine;
+    const float sn = sub ? mine : other;
     const float d = sn - so;
     // strict improvement (LooperSolver.hpp:4974), else the ratio test
     bool acc = d < 0.0f;
     if (!acc && T > 0.0f) {
-      const uint4 a = philox_move(S.seed, chain_id, (uint64_t)moves, 1u);
-      const float thr = ratio_threshold(u01(a.x), T, S.inv_scale, S.inv_coef);
+      const float thr = cur.thr;
       // the reference kernel divides by max(E_prev, 1e-12)
       // (ParallelMonteCarloSmooth.cu:293-294)
       acc = (S.gpu_sched && e_hi < 1e-12f) ? d < 1e-12f * thr - e_hi
                                            : d < e_hi * (thr - 1.0f);
     }
     if (acc) {
-      P[b * st] = nb;
+      if (sub == 0) P[b * st] = nb;
       ff_add(e_hi, e_lo, d);
       ++accepted;
       ++succ;
       if (S.gpu_sched) best = fmin(best, (double)e_hi + (double)e_lo);
     }
-    if (trace != nullptr && chain_id == 0 && moves < trace_cap) {
+    if (trace != nullptr && chain_id == 0 && sub == 0 && moves < trace_cap) {
       MoveTrace tr;
       tr.bead = b;
       tr.accepted = acc ? 1 : 0;
@@ -233,6 +275,7 @@ smooth_anneal_kernel(const SmoothUnit *__restrict__ units,
       tr.pad = d;
       trace[moves] = tr;
     }
+    __syncwarp(gm);  // the accepted position is visible to both lanes
     ++moves;
     if (moves == next_rs) {
       // remove the drift of the running score (a region is small: the
@@ -253,19 +296,22 @@ smooth_anneal_kernel(const SmoothUnit *__restrict__ units,
     }
     T *= S.dt;
     if (!stop && moves >= U.cap) stop = true;
+    cur = share(nxt);
   }
-  ChainOut o;
-  o.energy = (double)e_hi + (double)e_lo;
-  o.energy_fp64 = smooth_full(P, st, dtn, n, S);
-  o.base = 0.0;
-  o.best = S.gpu_sched ? best : o.energy;
-  o.score = e_hi;
-  o.status = status;
-  o.moves = moves;
-  o.accepted = accepted;
-  outs[U.chain_base + chain] = o;
+  if (sub == 0) {
+    ChainOut o;
+    o.energy = (double)e_hi + (double)e_lo;
+    o.energy_fp64 = smooth_full(P, st, dtn, n, S);
+    o.base = 0.0;
+    o.best = S.gpu_sched ? best : o.energy;
+    o.score = e_hi;
+    o.status = status;
+    o.moves = moves;
+    o.accepted = accepted;
+    outs[U.chain_base + chain] = o;
+  }
   float *po = pos_out + U.out_off + (long long)chain * n * 3;
-  for (int i = 0; i < n; ++i) {
+  for (int i = sub; i < n; i += kSmoothLanes) {
     const float4 q = P[i * st];
     po[3 * i] = q.x;
     po[3 * i + 1] = q.y;
@@ -389,12 +435,13 @@ extern "C" pmmc_status pmmc_smooth_batch_anneal(pmmc_ctx *ctx, int n_units,
     for (int c = 0; c < chains; ++c) items.push_back(make_int2(u, c));
 
   const int threads = 128;
-  // shared-memory slices when a thread's region fits in 1 KB... 4 KB
+  // shared-memory slices when a chain's region fits in 1 KB... 4 KB
   int slice = 0;
   if (max_n <= 64) slice = max_n;
   S.slice = slice;
   const bool use_smem = slice > 0;
-  const size_t smem = use_smem ? (size_t)threads * slice * sizeof(float4) : 0;
+  const size_t smem =
+      use_smem ? (size_t)(threads / kSmoothLanes) * slice * sizeof(float4) : 0;
 
   cudaStream_t s = ctx->stream;
   DevBuf<SmoothUnit> d_units;
@@ -421,7 +468,7 @@ extern "C" pmmc_status pmmc_smooth_batch_anneal(pmmc_ctx *ctx, int n_units,
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
   const int n_items = (int)items.size();
-  const int grid = (n_items + threads - 1) / threads;
+  const int grid = (int)(((long long)n_items * kSmoothLanes + threads - 1) / threads);
   cudaEventRecord(e0, s);
   if (use_smem) {
     cudaFuncSetAttribute(smooth_anneal_kernel<true>,
