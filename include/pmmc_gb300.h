@@ -347,6 +347,19 @@ pmmc_status pmmc_smooth_batch_anneal(pmmc_ctx *ctx, int n_units,
                                      float *pos_out, pmmc_result *res,
                                      double *kernel_ms, void *trace_out,
                                      int trace_cap);
+/* Smoothing kernel choice for the context's later smoothing calls.  A region
+ * is annealed in windows of W proposals (W = 4, 8, 16 or 32 lanes of a warp
+ * per chain: the proposals of the next W moves are scored at once and
+ * resolved in order, a window closing at the first proposal that reads a
+ * bead an accepted earlier one moved), W = window_long for regions with at
+ * least long_min_free movable beads (the longest chains) and window_short
+ * for the others; a window of 0 anneals those regions one move at a time,
+ * two lanes per chain.  Every choice gives the same moves, decisions and
+ * positions.  Default: window_short 8, window_long 32, long_min_free 20.
+ * Regions whose chain does not fit a shared-memory slice always take one
+ * move at a time. */
+pmmc_status pmmc_smooth_set_window(pmmc_ctx *ctx, int window_short, int window_long,
+                                   int long_min_free);
 /* Many independent heatmap chains (distinct matrices), one CTA each.
  * trace_out (nullable) receives trace_cap records of unit 0's first moves. */
 pmmc_status pmmc_heatmap_batch_anneal(pmmc_ctx *ctx, int n_units,

@@ -45,7 +45,7 @@ HEADER_SYMBOLS = [
     "pmmc_selftest_sqrt", "pmmc_distance_heatmap", "pmmc_distance_heatmap_device",
     "pmmc_equidistant_model", "pmmc_hcm_write", "pmmc_anchor_targets", "pmmc_stress_refine",
     "pmmc_server_cancel", "pmmc_arcs_batch_trace_chain", "pmmc_arcs_batch_chain_results",
-    "pmmc_arcs_rows_to_csr",
+    "pmmc_arcs_rows_to_csr", "pmmc_smooth_set_window",
 ]
 
 LANES_AUTO = -1  # PMMC_LANES_AUTO: the autotuner picks lanes and warps per class
@@ -193,6 +193,7 @@ def lib():
         L.pmmc_last_error.argtypes = [C.c_void_p]
         L.pmmc_set_seed.argtypes = [C.c_void_p, C.c_uint64]
         L.pmmc_sm_count.argtypes = [C.c_void_p]
+        L.pmmc_smooth_set_window.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int]
         L.pmmc_arcs_batch_destroy.argtypes = [C.c_void_p]
         L.pmmc_server_create.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p,
                                          C.POINTER(C.c_void_p)]
@@ -280,6 +281,15 @@ class Context:
 
     def set_seed(self, seed: int):
         lib().pmmc_set_seed(self.h, C.c_uint64(int(seed) & (2**64 - 1)))
+
+    def set_smooth_window(self, window: int = 8, window_long: int | None = None,
+                          long_min_free: int = 16):
+        """Smoothing kernel choice (pmmc_smooth_set_window): regions with at
+        least `long_min_free` movable beads are annealed `window_long`
+        proposals at a time, the others `window` at a time (0 = one move at
+        a time).  window_long defaults to `window`."""
+        wl = window if window_long is None else window_long
+        self.check(lib().pmmc_smooth_set_window(self.h, int(window), int(wl), int(long_min_free)))
 
     @property
     def sm_count(self) -> int:

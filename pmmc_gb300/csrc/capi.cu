@@ -52,6 +52,8 @@ extern "C" pmmc_status pmmc_ctx_create(pmmc_ctx **out, int device) {
 extern "C" void pmmc_ctx_destroy(pmmc_ctx *ctx) {
   if (!ctx) return;
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  for (cudaStream_t a : ctx->aux_stream)
+    if (a) cudaStreamDestroy(a);
   delete ctx;
 }
 

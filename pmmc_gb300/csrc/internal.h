@@ -24,6 +24,14 @@ struct pmmc_ctx {
   uint64_t seed = 0;
   uint64_t calls = 0;          // advanced by every annealing call
   cudaStream_t stream = nullptr;
+  // further kernels of one call beside the first
+  cudaStream_t aux_stream[2] = {nullptr, nullptr};
+  // smoothing: slots per chain of the windowed kernel (0 = one move at a
+  // time), for regions with fewer / at least smooth_window_long_min_free
+  // movable beads
+  int smooth_window = 8;
+  int smooth_window_long = 32;
+  int smooth_window_long_min_free = 20;
   std::string last_error;
 };
 
