@@ -347,6 +347,17 @@ pmmc_status pmmc_smooth_batch_anneal(pmmc_ctx *ctx, int n_units,
                                      float *pos_out, pmmc_result *res,
                                      double *kernel_ms, void *trace_out,
                                      int trace_cap);
+/* The same with the regions packed back to back (a chromosome's beads cut
+ * at its anchors, say): region u is beads [bead_off[u], bead_off[u+1]) of
+ * pos (3 floats a bead), dist_to_next and fixed (nullable); bead_off holds
+ * n_units+1 entries. */
+pmmc_status pmmc_smooth_batch_anneal_packed(pmmc_ctx *ctx, int n_units, const int64_t *bead_off,
+                                            const float *pos, const float *dist_to_next,
+                                            const unsigned char *fixed,
+                                            const pmmc_anneal_params *prm,
+                                            const float *step_sizes, int chains, float *pos_out,
+                                            pmmc_result *res, double *kernel_ms, void *trace_out,
+                                            int trace_cap);
 /* Smoothing kernel choice for the context's later smoothing calls.  A region
  * is annealed in windows of W proposals (W = 4, 8, 16 or 32 lanes of a warp
  * per chain: the proposals of the next W moves are scored at once and

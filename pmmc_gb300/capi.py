@@ -45,7 +45,7 @@ HEADER_SYMBOLS = [
     "pmmc_selftest_sqrt", "pmmc_distance_heatmap", "pmmc_distance_heatmap_device",
     "pmmc_equidistant_model", "pmmc_hcm_write", "pmmc_anchor_targets", "pmmc_stress_refine",
     "pmmc_server_cancel", "pmmc_arcs_batch_trace_chain", "pmmc_arcs_batch_chain_results",
-    "pmmc_arcs_rows_to_csr", "pmmc_smooth_set_window",
+    "pmmc_arcs_rows_to_csr", "pmmc_smooth_set_window", "pmmc_smooth_batch_anneal_packed",
 ]
 
 LANES_AUTO = -1  # PMMC_LANES_AUTO: the autotuner picks lanes and warps per class
@@ -504,6 +504,30 @@ def smooth_batch_anneal(ctx: Context, inputs, params: AnnealParams, steps, chain
     if trace_cap:
         return out, [r for r in res], ms.value, tr
     return out, [r for r in res], ms.value
+
+
+def smooth_batch_anneal_packed(ctx: Context, bead_off, pos, dist_to_next, fixed,
+                               params: AnnealParams, steps, chains=1, trace_cap=0):
+    """Regions packed back to back (pmmc_smooth_batch_anneal_packed): region u
+    is rows [bead_off[u], bead_off[u+1]) of pos (n x 3), dist_to_next and
+    fixed.  Returns (positions n x 3 of each region's reported chain, the
+    ctypes array of results, kernel ms[, trace])."""
+    off = np.ascontiguousarray(bead_off, dtype=np.int64)
+    n_units = len(off) - 1
+    pos = _f32(pos).reshape(-1, 3)
+    dtn = _f32(dist_to_next)
+    fx = None if fixed is None else np.ascontiguousarray(fixed, dtype=np.uint8)
+    st = _f32(steps)
+    out = np.zeros_like(pos)
+    res = (Result * n_units)()
+    ms = C.c_double()
+    tr = np.zeros(max(trace_cap, 1), TRACE_DTYPE)
+    ctx.check(lib().pmmc_smooth_batch_anneal_packed(
+        ctx.h, n_units, _p(off), _p(pos), _p(dtn), _p(fx), C.byref(params), _p(st), int(chains),
+        _p(out), res, C.byref(ms), _p(tr) if trace_cap else None, int(trace_cap)))
+    if trace_cap:
+        return out, res, ms.value, tr
+    return out, res, ms.value
 
 
 def smooth_anneal(ctx: Context, inp: SmoothInput, params: AnnealParams, step: float,

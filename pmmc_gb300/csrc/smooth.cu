@@ -937,6 +937,30 @@ extern "C" pmmc_status pmmc_smooth_batch_anneal(pmmc_ctx *ctx, int n_units,
   return PMMC_OK;
 }
 
+// Regions packed back to back: region u is beads [bead_off[u], bead_off[u+1])
+// of the packed arrays.
+extern "C" pmmc_status pmmc_smooth_batch_anneal_packed(
+    pmmc_ctx *ctx, int n_units, const int64_t *bead_off, const float *pos,
+    const float *dist_to_next, const unsigned char *fixed, const pmmc_anneal_params *prm,
+    const float *step_sizes, int chains, float *pos_out, pmmc_result *res, double *kernel_ms,
+    void *trace_out, int trace_cap) {
+  if (!ctx || n_units < 1 || !bead_off || !pos || !dist_to_next)
+    return fail(ctx, PMMC_ERR_INVALID, "smooth packed batch: bad arguments");
+  std::vector<pmmc_smooth_problem> v((size_t)n_units);
+  for (int u = 0; u < n_units; ++u) {
+    const int64_t a = bead_off[u], b = bead_off[u + 1];
+    if (a < 0 || b < a || b - a > (int64_t)INT32_MAX)
+      return fail(ctx, PMMC_ERR_INVALID, "smooth packed batch: region %d spans [%lld, %lld)", u,
+                  (long long)a, (long long)b);
+    v[u].n = (int)(b - a);
+    v[u].pos = pos + 3 * a;
+    v[u].fixed = fixed ? fixed + a : nullptr;
+    v[u].dist_to_next = dist_to_next + a;
+  }
+  return pmmc_smooth_batch_anneal(ctx, n_units, v.data(), prm, step_sizes, chains, pos_out, res,
+                                  kernel_ms, trace_out, trace_cap);
+}
+
 extern "C" pmmc_status pmmc_smooth_set_window(pmmc_ctx *ctx, int window_short, int window_long,
                                               int long_min_free) {
   if (!ctx) return PMMC_ERR_INVALID;

@@ -179,19 +179,34 @@ def smooth_segments():
     return out
 
 
+def smooth_packed():
+    """The genome-smoothing regions packed back to back: (bead_off, pos,
+    dist_to_next, fixed)."""
+    segs = smooth_segments()
+    off = np.zeros(len(segs) + 1, np.int64)
+    off[1:] = np.cumsum([len(p) for p, _, _ in segs])
+    return (off, np.concatenate([p for p, _, _ in segs]).astype(np.float32),
+            np.concatenate([d for _, d, _ in segs]).astype(np.float32),
+            np.concatenate([f for _, _, f in segs]).astype(np.uint8))
+
+
 def smooth(args):
     ctx = capi.Context(0)
     segs = [capi.SmoothInput(*x) for x in smooth_segments()]
+    packed = smooth_packed()
     free = sum(int((x.fixed == 0).sum()) for x in segs)
     sweeps = args.moves or 20_000
     prm = capi.default_params(capi.LEVEL_SMOOTH, schedule=capi.SCHEDULE_CPU, resync_every=1000,
                               **SMOOTH_ANNEAL)
+    prm.max_moves = -int(sweeps)
+    steps = np.full(len(segs), 0.5, np.float32)
     times, walls, total = [], [], 0
     for k in range(args.warmup + args.steps):
         ctx.set_seed(3)
-        # each region: sweeps x its free beads
+        # each region: sweeps x its free beads; host arrays in and out
+        # through the packed entry point
         t0 = time.perf_counter()
-        out, res, ms = _smooth_run(ctx, segs, prm, sweeps)
+        out, res, ms = capi.smooth_batch_anneal_packed(ctx, *packed, prm, steps)
         wall = time.perf_counter() - t0
         if k >= args.warmup:
             times.append(ms)

@@ -127,3 +127,23 @@ def test_window_rejects_bad_size(wctx):
         wctx.set_smooth_window(8, 12)
     with pytest.raises(RuntimeError):
         wctx.set_smooth_window(8, 16, -1)
+
+
+def test_packed_batch_matches_list_form(wctx):
+    """pmmc_smooth_batch_anneal_packed (regions back to back in one set of
+    arrays) gives the list form's results."""
+    segs, _ = _genome_segments(3000, 5)
+    prm = capi.default_params(capi.LEVEL_SMOOTH, schedule=capi.SCHEDULE_CPU, max_temp=5.0,
+                              dt_temp=0.9999, milestone_steps=10**9, improvement=0.99,
+                              max_moves=-100, resync_every=1000)
+    steps = [0.5] * len(segs)
+    ref = _run(wctx, 8, 32, 20, segs, prm, steps, 9)
+    off = np.zeros(len(segs) + 1, np.int64)
+    off[1:] = np.cumsum([s.n for s in segs])
+    wctx.set_seed(9)
+    pos, res, ms = capi.smooth_batch_anneal_packed(
+        wctx, off, np.concatenate([s.pos for s in segs]), np.concatenate([s.dtn for s in segs]),
+        np.concatenate([s.fixed for s in segs]), prm, steps)
+    for u, s in enumerate(segs):
+        np.testing.assert_array_equal(pos[off[u]:off[u + 1]], ref[0][u])
+        assert res[u].energy == ref[1][u].energy and res[u].moves == ref[1][u].moves
