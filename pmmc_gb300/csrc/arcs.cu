@@ -600,7 +600,7 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
             const bool ok = ek < end;
             ent[k] = NB[ok ? ek : e];
             // 1/t from the target (8 staged bytes per entry instead of 12)
-            iv[k] = ok ? recip_nr(__int_as_float(ent[k].y)) : 0.0f;
+            iv[k] = recip_nr(__int_as_float(ent[k].y));
           }
 #pragma unroll
           for (int k = 0; k < UA; ++k) {
@@ -611,7 +611,8 @@ arcs_anneal_kernel(const ArcsUnit *__restrict__ units,
             const float n1 = spring_fast(fast_len(nx, ny, nz, q), t, iv[k], ks, kq);
             so += ok ? o1 : 0.0f;
             sn += ok ? n1 : 0.0f;
-            cm |= ok ? (smask[ent[k].x] & earlier) : 0u;
+            const unsigned mk = smask[ent[k].x];
+            cm |= ok ? (mk & earlier) : 0u;
           }
         }
         if (has_loops) {
