@@ -738,7 +738,9 @@ def run_gpu(args, rank, world):
     for _ in range(args.warmup):
         batch.run(stream.cuda_stream)
         batch.results()
-    _, moves_per_step, n_launch = batch.stats()
+    # moves and launches of a pass (from the first timed pass when there is
+    # no warm-up)
+    moves_per_step, n_launch = batch.stats()[1:] if args.warmup > 0 else (None, None)
     # ---- timed region ----
     if world > 1:
         torch.distributed.barrier()
@@ -751,7 +753,9 @@ def run_gpu(args, rank, world):
         with torch.cuda.stream(stream):
             flush_l2(l2)
         batch.run(stream.cuda_stream)
-        ms, mv, _ = batch.stats()
+        ms, mv, nl = batch.stats()
+        if moves_per_step is None:
+            moves_per_step, n_launch = mv, nl
         assert mv == moves_per_step
         kernel_ms.append(ms)
     torch.cuda.synchronize()

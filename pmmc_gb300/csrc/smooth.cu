@@ -100,6 +100,8 @@ __device__ __forceinline__ float angle_e(float4 a, float4 b, float4 c,
 // chain end reads the bead itself and its term is then dropped), so they
 // have no branches between them and schedule side by side; with a branch
 // per term a lone chain ran them one after another, ~5x the latency.
+// SPH = false leaves out the sphere term (no container: the term is 0).
+template <bool SPH = true>
 __device__ __forceinline__ float smooth_local(const float4 *P, int st, const float2 *dtn,
                                               int n, int p, float4 q,
                                               const SmoothDevParams &S) {
@@ -120,7 +122,7 @@ __device__ __forceinline__ float smooth_local(const float4 *P, int st, const flo
   s = __fadd_rn(s, l2 ? a0 : 0.0f);
   s = __fadd_rn(s, (l1 && r1) ? a1 : 0.0f);
   s = __fadd_rn(s, r2 ? a2 : 0.0f);
-  return __fadd_rn(s, sphere_penalty(q.x, q.y, q.z, S.R));
+  return SPH ? __fadd_rn(s, sphere_penalty(q.x, q.y, q.z, S.R)) : s;
 }
 
 // Exact (IEEE sqrt / division) forms for the FP64 recompute.
@@ -390,7 +392,7 @@ struct Draw {
   float dx, dy, dz, thr, T;
 };
 
-template <int W>
+template <int W, bool SPH>
 __global__ void __launch_bounds__(128, 6)
 smooth_window_kernel(const SmoothUnit *__restrict__ units,
                      const int2 *__restrict__ items, int n_items,
@@ -430,7 +432,7 @@ smooth_window_kernel(const SmoothUnit *__restrict__ units,
     }
   __syncwarp();
   if (live)
-    for (int i = g; i < n; i += W) SO[i] = smooth_local(P, 1, D, n, i, P[i], S);
+    for (int i = g; i < n; i += W) SO[i] = smooth_local<SPH>(P, 1, D, n, i, P[i], S);
 
   const double E0 = live ? smooth_full_lanes<W>(P, 1, D, n, S, g, gmask) : 0.0;
   float e_hi = (float)E0, e_lo = (float)(E0 - (double)(float)E0);
@@ -496,7 +498,7 @@ smooth_window_kernel(const SmoothUnit *__restrict__ units,
     nb.x += dx;
     nb.y += dy;
     nb.z += dz;
-    const float sn = smooth_local(P, 1, D, n, b, nb, S);
+    const float sn = smooth_local<SPH>(P, 1, D, n, b, nb, S);
     const float d = sn - so;
     // ---- resolution ----
     unsigned accm = 0u;
@@ -555,7 +557,7 @@ smooth_window_kernel(const SmoothUnit *__restrict__ units,
     for (unsigned m = accm; m != 0u; m &= m - 1u) {
       const int c = __shfl_sync(gmask, b, gb + __ffs(m) - 1);
       for (int i = c - 2 + g; i <= c + 2; i += W)
-        if (i >= 0 && i < n) SO[i] = smooth_local(P, 1, D, n, i, P[i], S);
+        if (i >= 0 && i < n) SO[i] = smooth_local<SPH>(P, 1, D, n, i, P[i], S);
     }
     if (!run) continue;
     // the next window's slot g is move moves+lend+g: this window's lane
@@ -840,10 +842,12 @@ extern "C" pmmc_status pmmc_smooth_batch_anneal(pmmc_ctx *ctx, int n_units,
       kern<<<wgrid, wt, wsm, ws>>>(d_units.p, w.d_items.p, nw, d_pos.p, d_dtn.p, d_mov.p, SW,
                                   d_out.p, d_outs.p, dtr, trace_cap);
     };
-    if (w.W == 4) launch(smooth_window_kernel<4>);
-    else if (w.W == 8) launch(smooth_window_kernel<8>);
-    else if (w.W == 16) launch(smooth_window_kernel<16>);
-    else launch(smooth_window_kernel<32>);
+    // no container: the sphere term is left out of the kernel (it is 0)
+    const bool sph = S.R > 0.0f;
+    if (w.W == 4) sph ? launch(smooth_window_kernel<4, true>) : launch(smooth_window_kernel<4, false>);
+    else if (w.W == 8) sph ? launch(smooth_window_kernel<8, true>) : launch(smooth_window_kernel<8, false>);
+    else if (w.W == 16) sph ? launch(smooth_window_kernel<16, true>) : launch(smooth_window_kernel<16, false>);
+    else sph ? launch(smooth_window_kernel<32, true>) : launch(smooth_window_kernel<32, false>);
     cudaEventCreateWithFlags(&ej[k], cudaEventDisableTiming);
     cudaEventRecord(ej[k], ws);
   }
