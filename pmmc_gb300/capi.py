@@ -297,7 +297,9 @@ class Context:
 
 
 class ArcsInput:
-    """Keeps the numpy arrays of one arc problem alive behind the C struct."""
+    """Keeps the numpy arrays of one arc problem alive behind the C struct,
+    which is built once, at construction (its pointers are into this
+    object's own arrays: change them in place, do not rebind them)."""
 
     def __init__(self, pos, row_ptr, col, target, fixed=None, loops=None):
         self.pos = _f32(pos).reshape(-1, 3)
@@ -310,6 +312,11 @@ class ArcsInput:
         self.li, self.lj = _i32(loops[0]), _i32(loops[1])
         self.lk, self.lr = _f32(loops[2]), _f32(loops[3])
         self.n = self.pos.shape[0]
+        n_l = len(self.li)
+        self._struct = ArcsProblem(self.n, _p(self.pos), _p(self.fixed), _p(self.row_ptr),
+                                   _p(self.col), _p(self.target), n_l,
+                                   _p(self.li) if n_l else None, _p(self.lj) if n_l else None,
+                                   _p(self.lk) if n_l else None, _p(self.lr) if n_l else None)
 
     @classmethod
     def from_dense(cls, pos, dense, fixed=None, loops=None):
@@ -317,11 +324,7 @@ class ArcsInput:
         return cls(pos, rp, col, tgt, fixed, loops)
 
     def struct(self) -> ArcsProblem:
-        n_l = len(self.li)
-        return ArcsProblem(self.n, _p(self.pos), _p(self.fixed), _p(self.row_ptr), _p(self.col),
-                           _p(self.target), n_l, _p(self.li) if n_l else None,
-                           _p(self.lj) if n_l else None, _p(self.lk) if n_l else None,
-                           _p(self.lr) if n_l else None)
+        return self._struct
 
 
 class ArcsBatch:
@@ -474,14 +477,18 @@ class Server:
 
 
 class SmoothInput:
+    """One smoothing region; the C struct is built once, at construction,
+    with pointers into this object's own arrays."""
+
     def __init__(self, pos, dist_to_next, fixed=None):
         self.pos = _f32(pos).reshape(-1, 3)
         self.dtn = _f32(dist_to_next)
         self.fixed = None if fixed is None else np.ascontiguousarray(fixed, dtype=np.uint8)
         self.n = self.pos.shape[0]
+        self._struct = SmoothProblem(self.n, _p(self.pos), _p(self.fixed), _p(self.dtn))
 
     def struct(self) -> SmoothProblem:
-        return SmoothProblem(self.n, _p(self.pos), _p(self.fixed), _p(self.dtn))
+        return self._struct
 
 
 def smooth_batch_anneal(ctx: Context, inputs, params: AnnealParams, steps, chains=1,
