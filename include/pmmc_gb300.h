@@ -380,6 +380,14 @@ pmmc_status pmmc_heatmap_batch_anneal(pmmc_ctx *ctx, int n_units,
                                       pmmc_result *res, double *kernel_ms,
                                       void *trace_out, int trace_cap);
 
+/* Heatmap kernel choice for the context's later heatmap calls: each chain on
+ * a thread-block cluster of `ctas` CTAs (1, 2, 4 or 8; 0 = by the batch: 8
+ * when every chain can have its own eight SMs and the maps have 512 beads
+ * or more, else 1).  In a cluster each CTA scores its slice of every row
+ * and CTA 0 takes the decisions, so one chain uses eight SMs' worth of
+ * special-function units and shared memory. */
+pmmc_status pmmc_heatmap_set_cluster(pmmc_ctx *ctx, int ctas);
+
 /* ---------------- expected-distance heatmap ---------------- */
 /* Replaces LooperSolver::createDistanceHeatmap (src/include/LooperSolver.hpp:
  * 3042-3085), which builds heatmap_dist from heatmap[level] on the host

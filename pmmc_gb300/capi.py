@@ -46,6 +46,7 @@ HEADER_SYMBOLS = [
     "pmmc_equidistant_model", "pmmc_hcm_write", "pmmc_anchor_targets", "pmmc_stress_refine",
     "pmmc_server_cancel", "pmmc_arcs_batch_trace_chain", "pmmc_arcs_batch_chain_results",
     "pmmc_arcs_rows_to_csr", "pmmc_smooth_set_window", "pmmc_smooth_batch_anneal_packed",
+    "pmmc_heatmap_set_cluster",
 ]
 
 LANES_AUTO = -1  # PMMC_LANES_AUTO: the autotuner picks lanes and warps per class
@@ -194,6 +195,7 @@ def lib():
         L.pmmc_set_seed.argtypes = [C.c_void_p, C.c_uint64]
         L.pmmc_sm_count.argtypes = [C.c_void_p]
         L.pmmc_smooth_set_window.argtypes = [C.c_void_p, C.c_int, C.c_int, C.c_int]
+        L.pmmc_heatmap_set_cluster.argtypes = [C.c_void_p, C.c_int]
         L.pmmc_arcs_batch_destroy.argtypes = [C.c_void_p]
         L.pmmc_server_create.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p,
                                          C.POINTER(C.c_void_p)]
@@ -290,6 +292,11 @@ class Context:
         a time).  window_long defaults to `window`."""
         wl = window if window_long is None else window_long
         self.check(lib().pmmc_smooth_set_window(self.h, int(window), int(wl), int(long_min_free)))
+
+    def set_heatmap_cluster(self, ctas: int = 0):
+        """Heatmap kernel choice (pmmc_heatmap_set_cluster): CTAs of the
+        thread-block cluster that runs one chain (0 = by the batch)."""
+        self.check(lib().pmmc_heatmap_set_cluster(self.h, int(ctas)))
 
     @property
     def sm_count(self) -> int:

@@ -50,6 +50,8 @@ struct HeatUnit {
   long long out_off;
   float step;
   int single;        // 1: one chromosome block (every bead's block is [0, n-1])
+  int slice;         // cluster mode: beads per CTA (a multiple of 4)
+  int pad_;
 };
 
 struct HeatDevParams {
@@ -121,6 +123,37 @@ __device__ __forceinline__ void tma_row(void *dst, const void *src, uint32_t byt
       : "memory");
 }
 
+// Thread-block cluster: this CTA's rank, the cluster-wide barrier (every
+// thread of every CTA of the cluster), and stores into another CTA's shared
+// memory at the address of the same variable there.
+__device__ __forceinline__ uint32_t cluster_rank() {
+  uint32_t r;
+  asm volatile("mov.u32 %0, %%cluster_ctarank;" : "=r"(r));
+  return r;
+}
+
+__device__ __forceinline__ void cluster_sync() {
+  asm volatile("barrier.cluster.arrive.release;\n"
+               "barrier.cluster.wait.acquire;" ::: "memory");
+}
+
+__device__ __forceinline__ uint32_t cluster_addr(const void *p, uint32_t rank) {
+  uint32_t r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(smem_u32(p)), "r"(rank));
+  return r;
+}
+
+__device__ __forceinline__ void st_cluster(uint32_t a, float v) {
+  asm volatile("st.shared::cluster.f32 [%0], %1;" ::"r"(a), "f"(v) : "memory");
+}
+__device__ __forceinline__ void st_cluster(uint32_t a, uint32_t v) {
+  asm volatile("st.shared::cluster.u32 [%0], %1;" ::"r"(a), "r"(v) : "memory");
+}
+__device__ __forceinline__ void st_cluster(uint32_t a, int v) { st_cluster(a, (uint32_t)v); }
+__device__ __forceinline__ void st_cluster(uint32_t a, double v) {
+  asm volatile("st.shared::cluster.f64 [%0], %1;" ::"r"(a), "d"(v) : "memory");
+}
+
 // float-float accumulation (Knuth two-sum) of a float increment
 __device__ __forceinline__ void ff_add(float &hi, float &lo, float d) {
   const float s = hi + d;
@@ -177,7 +210,7 @@ __device__ __forceinline__ float pair_delta(float px, float py, float pz, const 
 }
 
 // Full score in FP64 (FP32 terms (d r - 1)^2 summed per row, rows summed in
-// FP64) plus the sphere penalties of all beads (the reference adds the
+// FP64) plus the sphere penalties of all beads -- of rows and beads [m0, m1) (the reference adds the
 // boundary sum to the initial score, LooperSolver.hpp:1451-1457).  One warp
 // per row of the reciprocal targets (zero outside the bead's block, in the
 // diagonal band and where h < 1e-6); lane l takes beads i = l mod 32, so the
@@ -185,13 +218,13 @@ __device__ __forceinline__ float pair_delta(float px, float py, float pz, const 
 // issues kB loads before it computes.  The whole block calls it and every
 // thread returns the total.
 __device__ double heat_full(const HeatUnit &U, const float4 *spos, const float *rheat,
-                            const int2 *blk, double *red, float R) {
+                            const int2 *blk, double *red, float R, int m0, int m1) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = blockDim.x >> 5;
   constexpr int kB = 32;
   double acc = 0.0;
-  for (int i = threadIdx.x; i < U.n; i += blockDim.x)
+  for (int i = m0 + threadIdx.x; i < m1; i += blockDim.x)
     acc += sphere_penalty(spos[i].x, spos[i].y, spos[i].z, R);
-  for (int m = warp; m < U.n; m += nw) {
+  for (int m = m0 + warp; m < m1; m += nw) {
     const int2 r = U.single ? make_int2(0, U.n - 1) : blk[m];
     const float *row = rheat + U.heat_off + (long long)m * U.pitch;
     const float4 pm = spos[m];
@@ -255,6 +288,14 @@ constexpr size_t kHeadBytes =
 // milestone and at the move cap, so the decisions are those of one move at a
 // time.  Two CTA barriers per window; warp 0 does the serial work between
 // them (decisions, draws, row copies, the next window's plan and row waits).
+// CL > 1 (cluster mode): one chain on a cluster of CL CTAs.  CTA r scores
+// beads [r S, r S + S) of every row (S = U.slice), streams only that slice of
+// each row and keeps all positions; the CTAs send their sums and pair
+// corrections to CTA 0, which takes the decisions and sends them back; every
+// CTA then applies them and plans the next window alike (the draws are the
+// same everywhere), so all CTAs run the same windows and meet the same two
+// cluster barriers per window.
+template <int CL>
 __global__ void __launch_bounds__(kHeatMaxThreads, 1)
 heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restrict__ pos0,
                       const float *__restrict__ rheat, const int *__restrict__ movable,
@@ -262,13 +303,20 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
                       float *__restrict__ pos_out, ChainOut *__restrict__ outs,
                       MoveTrace *__restrict__ trace) {
   extern __shared__ __align__(128) unsigned char smem[];
-  const HeatUnit U = units[blockIdx.x];
+  const int chain_ix = blockIdx.x / CL;
+  const HeatUnit U = units[chain_ix];
   const int n = U.n;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int nthr = blockDim.x, nwarps = nthr >> 5;
   const int D = P.depth;  // a power of two
   const int dmask = D - 1, dshift = __ffs(D) - 1;
   const int pitch = U.pitch;
+  // this CTA's beads [s0, s1) and the floats a ring slot holds
+  const uint32_t crank = CL > 1 ? cluster_rank() : 0u;
+  const bool leader = crank == 0u;
+  const int s0 = CL > 1 ? (int)crank * U.slice : 0;
+  const int s1 = CL > 1 ? min(n, s0 + U.slice) : n;
+  const int spitch = CL > 1 ? U.slice : pitch;
   // ---- shared-memory carve ----
   unsigned char *p = smem;
   uint64_t *bars = reinterpret_cast<uint64_t *>(p);
@@ -282,13 +330,27 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
   WinPlan *plan_s = reinterpret_cast<WinPlan *>(p);
   p += sizeof(WinPlan);
   p = smem + (((p - smem) + 15) & ~(size_t)15);
+  // cluster mode: every CTA's window record (kRec floats: its sums of the
+  // kWin moves, its kWin * kWin pair corrections, its late-row flag) from
+  // every CTA, two buffers by window parity; this CTA's own record and the
+  // records' totals; every CTA's part of a full score
+  constexpr int kRec = kWin + kWin * kWin + 1;
+  constexpr int kRecP = (kRec + 3) & ~3;          // padded to whole float4s
+  float4 *g_all = reinterpret_cast<float4 *>(p);  // CTA 0: [CL][kRecP / 4]
+  float *own = reinterpret_cast<float *>(g_all + CL * (kRecP / 4));  // [kRecP]
+  float *tot = own + kRecP;                       // CTA 0: [kRec]
+  float4 *dec = reinterpret_cast<float4 *>(tot + kRecP);  // decisions from CTA 0
+  double *g_e = reinterpret_cast<double *>(dec + 1);
+  int *g_flag = reinterpret_cast<int *>(g_e + CL);  // [CL]
+  if (CL > 1) p = reinterpret_cast<unsigned char *>(g_flag + CL);
+  p = smem + (((p - smem) + 15) & ~(size_t)15);
   MoveRec *recs = reinterpret_cast<MoveRec *>(p); // ring of 128 draws
   p += 128 * sizeof(MoveRec);
   float *thrs = reinterpret_cast<float *>(p);     // ring of 128
   p += 128 * 4;
   p = smem + (((p - smem) + 127) & ~(size_t)127);
-  float *slots = reinterpret_cast<float *>(p);    // D rows of 1/h
-  p += (size_t)D * pitch * 4;
+  float *slots = reinterpret_cast<float *>(p);    // D rows (slices) of 1/h
+  p += (size_t)D * spitch * 4;
   float4 *spos = reinterpret_cast<float4 *>(p);
   p += (size_t)n * 16;
   // per-bead chromosome block (maps with boundaries) and the movable list
@@ -302,6 +364,7 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
   const float *rrow0 = rheat + U.heat_off;
 
   if (tid == 0) {
+    plan_s->pad[1] = 0;  // cluster mode: a row copy of some CTA did not land
     for (int s = 0; s < D; ++s) mbar_init(&bars[s], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -313,7 +376,16 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
     for (int k = tid; k < U.n_mov; k += nthr) smov[k] = movable[U.mov_off + k];
   __syncthreads();
 
-  const double E0 = heat_full(U, spos, rheat, blk, red, P.R);
+  // the start score: in cluster mode each CTA scores its rows and every CTA
+  // adds the CL parts in rank order (the same value everywhere)
+  double E0 = heat_full(U, spos, rheat, blk, red, P.R, s0, s1);
+  if (CL > 1) {
+    cluster_sync();  // every CTA of the cluster is running
+    if (tid < CL) st_cluster(cluster_addr(&g_e[crank], (uint32_t)tid), E0);
+    cluster_sync();
+    E0 = 0.0;
+    for (int q = 0; q < CL; ++q) E0 += g_e[q];
+  }
   double T = P.max_temp;  // temperature of the next filled move (warp 1)
   long long filled = 0;   // records exist for moves [filled - 128, filled) (warp 1)
   long long issued = 0;   // moves whose rows were requested (warp 1)
@@ -342,10 +414,16 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
       if (lane < cnt) {
         const long long k = issued + lane;
         const int b = recs[k & 127].b;
-        const int2 r = block_of(b);
-        const int st = r.x & ~3;
-        const int en = min((r.y + 4) & ~3, pitch);
-        tma_row(slots + (size_t)(k & dmask) * pitch, rrow0 + (long long)b * pitch + st,
+        int st, en;
+        if (CL > 1) {  // this CTA's slice of the row
+          st = s0;
+          en = min(s0 + spitch, pitch);
+        } else {
+          const int2 r = block_of(b);
+          st = r.x & ~3;
+          en = min((r.y + 4) & ~3, pitch);
+        }
+        tma_row(slots + (size_t)(k & dmask) * spitch, rrow0 + (long long)b * pitch + st,
                 (uint32_t)(en - st) * 4, &bars[k & dmask]);
       }
       issued += cnt;
@@ -379,7 +457,8 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
       const float4 o = spos[rec.b];
       plan_s->ga[lane] = make_float4(o.x, o.y, o.z,
                                      fmaf(rec.dx, rec.dx, fmaf(rec.dy, rec.dy, rec.dz * rec.dz)));
-      const int roff = (int)(k & dmask) * pitch - (bk.x & ~3);
+      const int roff = CL > 1 ? (int)(k & dmask) * spitch - s0
+                              : (int)(k & dmask) * pitch - (bk.x & ~3);
       plan_s->gb[lane] =
           make_float4(-2.0f * rec.dx, -2.0f * rec.dy, -2.0f * rec.dz, __int_as_float(roff));
       plan_s->bw[lane] = rec.b;
@@ -411,7 +490,9 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
   long long moves = 0, accepted = 0;
   long long next_ms = P.window;
   bool stop = cap == 0;
-  if (!stop && plan_s->timeout) {
+  // (cluster mode: late rows are gathered at the first window and stop every
+  // CTA together)
+  if (CL == 1 && !stop && plan_s->timeout) {
     status = PMMC_ERR_TIMEOUT;
     stop = true;
   }
@@ -441,7 +522,8 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
     for (int w = 0; w < kWin; ++w) part[w] = 0.0f;
     if (same) {
       const int2 r = block_of(plan_s->bw[0]);
-      for (int i = r.x + tid; i <= r.y; i += nthr) {
+      const int i1 = min(r.y, s1 - 1);
+      for (int i = max(r.x, s0) + tid; i <= i1; i += nthr) {
         const float4 pi = spos[i];
 #pragma unroll
         for (int w = 0; w < kWin; ++w)
@@ -452,7 +534,8 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
       for (int w = 0; w < kWin; ++w) {
         if (w < L) {
           const int2 r = block_of(plan_s->bw[w]);
-          for (int i = r.x + tid; i <= r.y; i += nthr) {
+          const int i1 = min(r.y, s1 - 1);
+          for (int i = max(r.x, s0) + tid; i <= i1; i += nthr) {
             const float4 pi = spos[i];
             part[w] += pair_delta(pi.x, pi.y, pi.z, g[w], slots[roff[w] + i]);
           }
@@ -466,7 +549,8 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
       if (j < w && w < L) {
         const int bw = plan_s->bw[w], bj = plan_s->bw[j];
         const int2 r = block_of(bw);
-        if (bj >= r.x && bj <= r.y) {
+        // (cluster mode: the CTA whose slice holds column bj)
+        if (bj >= r.x && bj <= r.y && bj >= s0 && bj < s1) {
           const float4 gb = plan_s->gb[w];
           const float rv = slots[__float_as_int(gb.w) + bj];
           const float4 oj = plan_s->ga[j], dj = plan_s->gb[j];
@@ -492,16 +576,77 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
       if (lane == 0) partial[warp * kWin + w] = v;
     }
     __syncthreads();
-    // ---- warp 0: decisions, draws, row copies, the next window ----
-    if (warp == 0) {
+    // draws (moves below m are done, so the records of [filled - 128,
+    // filled - 96) are free when filled <= m + 64) and the row copies that
+    // the slots freed by this window can take (warp 1)
+    auto draws_and_copies = [&]() {
+      if (filled <= m + 64) {
+        fill(filled);
+        filled += 32;
+        __syncwarp();
+      }
+      issue(min(cap, m + L + D));
+    };
+    if (CL > 1) {
+      // this CTA's record (its sums, pair corrections and late-row flag) to
+      // CTA 0, in float4 stores
+      if (warp == 0) {
+        const int wl = lane & (kWin - 1);
+        float t = 0.0f;
+        for (int k = lane >> 3; k < nwarps; k += 4) t += partial[k * kWin + wl];
+        t += __shfl_xor_sync(0xffffffffu, t, 8);
+        t += __shfl_xor_sync(0xffffffffu, t, 16);
+        if (lane < kWin) own[lane] = t;
+        if (lane == 0) {
+          own[kRec - 1] = __int_as_float(plan_s->timeout);
+          for (int v = kRec; v < kRecP; ++v) own[v] = 0.0f;
+        }
+      }
+      if (tid < kWin * kWin) own[kWin + tid] = corr[tid];
+      __syncthreads();
+      if (tid < kRecP / 4) {
+        const float4 v = reinterpret_cast<const float4 *>(own)[tid];
+        const uint32_t a4 = cluster_addr(&g_all[(int)crank * (kRecP / 4) + tid], 0);
+        asm volatile("st.shared::cluster.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(a4), "f"(v.x),
+                     "f"(v.y), "f"(v.z), "f"(v.w)
+                     : "memory");
+      }
+      cluster_sync();  // every record is at CTA 0
+      if (leader) {    // the records' totals, in rank order
+        if (tid < kRec) {
+          const float *r0 = reinterpret_cast<const float *>(g_all);
+          if (tid == kRec - 1) {
+            int late = 0;
+            for (int q = 0; q < CL; ++q) late |= __float_as_int(r0[q * kRecP + tid]);
+            tot[tid] = __int_as_float(late);
+          } else {
+            float a = 0.0f;
+            for (int q = 0; q < CL; ++q) a += r0[q * kRecP + tid];
+            tot[tid] = a;
+          }
+        }
+        __syncthreads();
+      }
+      // the draws and row copies do not depend on the decisions: they run
+      // while CTA 0 takes them
+      if (warp == 1) draws_and_copies();
+    }
+    // ---- warp 0 (of CTA 0 in cluster mode): decisions, the next window ----
+    if (warp == 0 && leader) {
       const int wl = lane & (kWin - 1);
       float t = 0.0f;
-      for (int k = lane >> 3; k < nwarps; k += 4) t += partial[k * kWin + wl];
-      t += __shfl_xor_sync(0xffffffffu, t, 8);
-      t += __shfl_xor_sync(0xffffffffu, t, 16);
       float cr[kWin];
+      if (CL == 1) {
+        for (int k = lane >> 3; k < nwarps; k += 4) t += partial[k * kWin + wl];
+        t += __shfl_xor_sync(0xffffffffu, t, 8);
+        t += __shfl_xor_sync(0xffffffffu, t, 16);
 #pragma unroll
-      for (int j = 0; j < kWin; ++j) cr[j] = corr[wl * kWin + j];
+        for (int j = 0; j < kWin; ++j) cr[j] = corr[wl * kWin + j];
+      } else {
+        t = tot[wl];
+#pragma unroll
+        for (int j = 0; j < kWin; ++j) cr[j] = tot[kWin + wl * kWin + j];
+      }
       const int ll = lane < L ? lane : 0;
       const MoveRec rec = recs[(m + ll) & 127];
       const float4 ow = spos[rec.b];
@@ -525,7 +670,7 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
           }
         }
       }
-      if (lane < L && ((accm >> lane) & 1u)) spos[rec.b] = nw;
+      if (CL == 1 && lane < L && ((accm >> lane) & 1u)) spos[rec.b] = nw;
       if (trace != nullptr && U.chain_id == 0 && lane < L && m + lane < P.trace_cap) {
         MoveTrace tr;
         tr.bead = rec.b;
@@ -539,24 +684,47 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
         trace[m + lane] = tr;
       }
       __syncwarp();
-      const long long mn = m + L;
-      if (lane == 0) {
-        plan_s->accm = accm;
-        plan_s->lend = L;
-        plan_s->pacc = pacc;
-        plan_s->timeout = 0;
+      if (CL == 1) {
+        const long long mn = m + L;
+        if (lane == 0) {
+          plan_s->accm = accm;
+          plan_s->lend = L;
+          plan_s->pacc = pacc;
+          plan_s->timeout = 0;
+        }
+        if (mn < cap) plan(mn, mn == next_ms ? next_ms + P.window : next_ms);
+      } else if (lane < CL) {  // the decisions to every CTA, one float4 each
+        const uint32_t a4 = cluster_addr(dec, (uint32_t)lane);
+        asm volatile("st.shared::cluster.v4.f32 [%0], {%1, %2, %3, %4};" ::"r"(a4),
+                     "f"(__uint_as_float(accm)), "f"(pacc), "f"(tot[kRec - 1]), "f"(0.0f)
+                     : "memory");
       }
-      if (mn < cap) plan(mn, mn == next_ms ? next_ms + P.window : next_ms);
-    } else if (warp == 1) {
-      // meanwhile: draws (moves below m are done, so the records of
-      // [filled - 128, filled - 96) are free when filled <= m + 64) and the
-      // row copies that the slots freed by this window can take
-      if (filled <= m + 64) {
-        fill(filled);
-        filled += 32;
+    } else if (CL == 1 && warp == 1) {
+      draws_and_copies();
+    }
+    if (CL > 1) {
+      cluster_sync();  // every CTA has the window's decisions
+      if (warp == 0) {
+        // apply them (every CTA keeps all positions) and plan the next window
+        const float4 dv = *dec;
+        const unsigned am = __float_as_uint(dv.x);
+        if (lane < L && ((am >> lane) & 1u)) {
+          const MoveRec rec = recs[(m + lane) & 127];
+          const float4 ow = spos[rec.b];
+          spos[rec.b] = make_float4(ow.x + rec.dx, ow.y + rec.dy, ow.z + rec.dz, 0.f);
+        }
         __syncwarp();
+        const int late = __float_as_int(dv.z);
+        if (lane == 0) {
+          plan_s->accm = am;
+          plan_s->pacc = dv.y;
+          plan_s->pad[1] = late;
+          plan_s->lend = L;
+          plan_s->timeout = 0;
+        }
+        const long long mn = m + L;
+        if (mn < cap && late == 0) plan(mn, mn == next_ms ? next_ms + P.window : next_ms);
       }
-      issue(min(cap, m + L + D));
     }
     __syncthreads();
     const unsigned accm = plan_s->accm;
@@ -576,7 +744,9 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
       succ = 0;
     }
     if (moves >= cap) stop = true;
-    if (!stop && plan_s->timeout) {  // a row copy never landed: give up on this chain
+    // a row copy never landed: give up on this chain (cluster mode: any
+    // CTA's, the same flag everywhere)
+    if (!stop && (CL == 1 ? plan_s->timeout : plan_s->pad[1])) {
       status = PMMC_ERR_TIMEOUT;
       stop = true;
     }
@@ -593,7 +763,22 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
   __syncthreads();
   if (plan_s->pad[0] != 0) status = PMMC_ERR_TIMEOUT;
   __syncthreads();
-  const double Efin = heat_full(U, spos, rheat, blk, red, P.R);
+  double Efin = heat_full(U, spos, rheat, blk, red, P.R, s0, s1);
+  if (CL > 1) {  // CTA 0 adds the parts (and any CTA's late copies)
+    if (tid == 0) {
+      st_cluster(cluster_addr(&g_e[crank], 0), Efin);
+      st_cluster(cluster_addr(&g_flag[crank], 0), status);
+    }
+    cluster_sync();  // the last access to another CTA's shared memory
+    if (leader) {
+      Efin = 0.0;
+      for (int q = 0; q < CL; ++q) {
+        Efin += g_e[q];
+        if (status == kDevOk && g_flag[q] != kDevOk) status = g_flag[q];
+      }
+    }
+  }
+  if (!leader) return;  // CTA 0 writes the chain's results
   if (tid == 0) {
     ChainOut o;
     const double E = run ? (double)e_hi + (double)e_lo : 0.0;
@@ -605,7 +790,7 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
     o.status = status;
     o.moves = moves;
     o.accepted = accepted;
-    outs[blockIdx.x] = o;
+    outs[chain_ix] = o;
   }
   float *po = pos_out + U.out_off;
   for (int i = tid; i < n; i += nthr) {
@@ -717,6 +902,27 @@ extern "C" pmmc_status pmmc_heatmap_batch_anneal(pmmc_ctx *ctx, int n_units,
     P.dtpow[l] = dp;
     dp *= (double)prm->dt_temp;
   }
+  // Cluster mode for a few chains on a large map: each chain spread over CL
+  // CTAs (one per SM), each scoring a slice of every row.
+  int CL = ctx->heatmap_cluster;
+  if (CL == 0) CL = (n_units * 8 <= ctx->sm_count && max_n >= 512) ? 8 : 1;
+  if (CL != 1 && CL != 2 && CL != 4 && CL != 8)
+    return fail(ctx, PMMC_ERR_INVALID, "heatmap: cluster of %d CTAs (1, 2, 4 or 8)", CL);
+  while (CL > 1) {  // every CTA needs beads of its own
+    bool ok = true;
+    for (const HeatUnit &U : hu) {
+      const int sl = ((U.n + CL - 1) / CL + 3) & ~3;
+      if ((long long)sl * (CL - 1) >= U.n) ok = false;
+    }
+    if (ok) break;
+    CL >>= 1;
+  }
+  int max_slice = 0;
+  if (CL > 1)
+    for (HeatUnit &U : hu) {
+      U.slice = ((U.n + CL - 1) / CL + 3) & ~3;
+      max_slice = std::max(max_slice, U.slice);
+    }
   // Shared memory: header + D row slots + per-bead arrays.  With at least two
   // chains per SM of work, two CTAs of 256 threads share an SM (one chain's
   // serial decisions overlap the other's row pass) when a ring of 8 rows
@@ -726,6 +932,7 @@ extern "C" pmmc_status pmmc_heatmap_batch_anneal(pmmc_ctx *ctx, int n_units,
   int depth = 0, ctas_per_sm = 1;
   size_t smem = 0;
   for (int mode : {2, 1}) {
+    if (CL > 1) break;
     if (mode == 2 && n_units < 2 * ctx->sm_count) continue;
     const size_t avail = mode == 2 ? std::min(ctx->smem_optin, ctx->smem_per_sm / 2 - 1024)
                                    : ctx->smem_optin;
@@ -738,6 +945,14 @@ extern "C" pmmc_status pmmc_heatmap_batch_anneal(pmmc_ctx *ctx, int n_units,
     ctas_per_sm = mode;
     smem = head + (size_t)d * row_bytes + max_bead_bytes;
     break;
+  }
+  if (CL > 1) {
+    // header with the cluster's gather area, a 16-slot ring of row slices
+    const size_t rec = (kWin + kWin * kWin + 1 + 3) & ~(size_t)3;
+    const size_t gather = ((size_t)CL * rec + 2 * rec + 4) * 4 + (size_t)CL * 12 + 256;
+    depth = 16;
+    smem = head + gather + (size_t)depth * max_slice * 4 + max_bead_bytes;
+    if (smem > ctx->smem_optin) depth = 0;
   }
   if (depth == 0)
     return fail(ctx, PMMC_ERR_INVALID, "heatmap region of %d beads does not fit shared memory", max_n);
@@ -816,10 +1031,15 @@ extern "C" pmmc_status pmmc_heatmap_batch_anneal(pmmc_ctx *ctx, int n_units,
   if (e != cudaSuccess)
     return fail(ctx, e == cudaErrorMemoryAllocation ? PMMC_ERR_NOMEM : PMMC_ERR_CUDA,
                 "heatmap upload: %s", cudaGetErrorString(e));
-  PMMC_CUDA(ctx, cudaFuncSetAttribute(heatmap_anneal_kernel,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-  PMMC_CUDA(ctx, cudaFuncSetAttribute(heatmap_anneal_kernel,
-                                      cudaFuncAttributePreferredSharedMemoryCarveout, 100));
+  auto kernel_of = [](int cl) {
+    return cl == 8 ? heatmap_anneal_kernel<8>
+                   : cl == 4 ? heatmap_anneal_kernel<4>
+                             : cl == 2 ? heatmap_anneal_kernel<2> : heatmap_anneal_kernel<1>;
+  };
+  const auto kern = kernel_of(CL);
+  PMMC_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+  PMMC_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
   cudaEvent_t e0, e1;
   cudaEventCreate(&e0);
   cudaEventCreate(&e1);
@@ -828,11 +1048,34 @@ extern "C" pmmc_status pmmc_heatmap_batch_anneal(pmmc_ctx *ctx, int n_units,
   // 256 when two chains share an SM)
   int threads = 128;
   const int max_threads = ctas_per_sm == 2 ? 256 : kHeatMaxThreads;
-  while (threads < max_threads && threads * 4 < max_n) threads *= 2;
-  heatmap_anneal_kernel<<<n_units, threads, smem, s>>>(
-      d_units.p, d_pos.p, d_rheat.p, d_mov.p, d_blk.p, P, d_out.p, d_outs.p,
-      trace_cap > 0 ? d_trace.p : nullptr);
-  e = cudaGetLastError();
+  if (CL > 1) {
+    threads = max_slice >= 256 ? 256 : 128;
+  } else {
+    while (threads < max_threads && threads * 4 < max_n) threads *= 2;
+  }
+  MoveTrace *dtr = trace_cap > 0 ? d_trace.p : nullptr;
+  if (CL == 1) {
+    heatmap_anneal_kernel<1><<<n_units, threads, smem, s>>>(d_units.p, d_pos.p, d_rheat.p,
+                                                            d_mov.p, d_blk.p, P, d_out.p,
+                                                            d_outs.p, dtr);
+    e = cudaGetLastError();
+  } else {
+    cudaLaunchConfig_t cfg{};
+    cfg.gridDim = dim3((unsigned)(n_units * CL));
+    cfg.blockDim = dim3((unsigned)threads);
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeClusterDimension;
+    attr[0].val.clusterDim.x = (unsigned)CL;
+    attr[0].val.clusterDim.y = 1;
+    attr[0].val.clusterDim.z = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    e = cudaLaunchKernelEx(&cfg, kern, (const HeatUnit *)d_units.p, (const float4 *)d_pos.p,
+                           (const float *)d_rheat.p, (const int *)d_mov.p,
+                           (const int2 *)d_blk.p, P, d_out.p, d_outs.p, dtr);
+  }
   cudaEventRecord(e1, s);
   if (e == cudaSuccess) e = cudaEventSynchronize(e1);
   if (e == cudaSuccess && kernel_ms) {
@@ -870,6 +1113,14 @@ extern "C" pmmc_status pmmc_heatmap_batch_anneal(pmmc_ctx *ctx, int n_units,
   for (auto &o : outs)
     if (o.status == PMMC_ERR_TIMEOUT)
       return fail(ctx, PMMC_ERR_TIMEOUT, "heatmap: a row copy did not complete");
+  return PMMC_OK;
+}
+
+extern "C" pmmc_status pmmc_heatmap_set_cluster(pmmc_ctx *ctx, int ctas) {
+  if (!ctx) return PMMC_ERR_INVALID;
+  if (ctas != 0 && ctas != 1 && ctas != 2 && ctas != 4 && ctas != 8)
+    return fail(ctx, PMMC_ERR_INVALID, "heatmap cluster: %d CTAs (0, 1, 2, 4 or 8)", ctas);
+  ctx->heatmap_cluster = ctas;
   return PMMC_OK;
 }
 

@@ -9,9 +9,20 @@ from parity import check_replay, ks_2samp_p
 pytestmark = pytest.mark.gpu
 
 
+@pytest.fixture
+def hctx(ctx):
+    yield ctx
+    ctx.set_heatmap_cluster(0)   # the default: chosen by the batch
+
+
+@pytest.mark.parametrize("cl", [0, 4, 8])
 @pytest.mark.parametrize("n,diag,bounds,sphere", [(128, 1, [], 0.0), (200, 2, [0, 90, 200], 0.0),
                                                   (96, 1, [], 6.0)])
-def test_heatmap_trace_parity(ctx, n, diag, bounds, sphere):
+def test_heatmap_trace_parity(hctx, n, diag, bounds, sphere, cl):
+    """cl: CTAs of the cluster that runs the chain (0 = the default, one
+    CTA at these sizes); in a cluster each CTA scores a slice of every row."""
+    ctx = hctx
+    ctx.set_heatmap_cluster(cl)
     h = synth.heatmap_region(n, seed=n, n_tads=4, tad_min=10, tad_max=30)
     fixed = np.zeros(n, np.uint8)
     fixed[[0, n // 2]] = 1
@@ -116,9 +127,13 @@ def _config1_region():
     return synth.heatmap_region(2048, seed=7)
 
 
-def test_heatmap_trace_parity_config1(ctx):
+@pytest.mark.parametrize("cl", [0, 1])
+def test_heatmap_trace_parity_config1(hctx, cl):
     """Per-move parity on the 2048-bead map, one chain: the launch the
-    single-chain workload takes (one CTA of 512 threads, 16-row ring)."""
+    single-chain workload takes (cl = 0: a cluster of 8 CTAs, each scoring
+    256 beads of every row) and one CTA of 512 threads with a 16-row ring."""
+    ctx = hctx
+    ctx.set_heatmap_cluster(cl)
     h = _config1_region()
     base = dict(max_temp=5.0, dt_temp=0.9999, milestone_steps=100_000, improvement=0.99)
     moves = 20_000
@@ -194,3 +209,10 @@ def test_heatmap_structures_match_reference_config1(ctx):
     for name, a, b in zip(("energy", "rmsd", "pearson"), ref_m, gpu_m):
         assert ks_2samp_p(a, b) > 0.01, name
         assert welch_p(a, b) > 0.01, name
+
+
+def test_heatmap_cluster_rejects_bad_size(hctx):
+    with pytest.raises(RuntimeError):
+        hctx.set_heatmap_cluster(3)
+    with pytest.raises(RuntimeError):
+        hctx.set_heatmap_cluster(16)
