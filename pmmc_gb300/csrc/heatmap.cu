@@ -522,8 +522,8 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
     for (int w = 0; w < kWin; ++w) part[w] = 0.0f;
     if (same) {
       const int2 r = block_of(plan_s->bw[0]);
-      const int i1 = min(r.y, s1 - 1);
-      for (int i = max(r.x, s0) + tid; i <= i1; i += nthr) {
+      const int i0 = CL > 1 ? max(r.x, s0) : r.x, i1 = CL > 1 ? min(r.y, s1 - 1) : r.y;
+      for (int i = i0 + tid; i <= i1; i += nthr) {
         const float4 pi = spos[i];
 #pragma unroll
         for (int w = 0; w < kWin; ++w)
@@ -534,8 +534,8 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
       for (int w = 0; w < kWin; ++w) {
         if (w < L) {
           const int2 r = block_of(plan_s->bw[w]);
-          const int i1 = min(r.y, s1 - 1);
-          for (int i = max(r.x, s0) + tid; i <= i1; i += nthr) {
+          const int i0 = CL > 1 ? max(r.x, s0) : r.x, i1 = CL > 1 ? min(r.y, s1 - 1) : r.y;
+          for (int i = i0 + tid; i <= i1; i += nthr) {
             const float4 pi = spos[i];
             part[w] += pair_delta(pi.x, pi.y, pi.z, g[w], slots[roff[w] + i]);
           }
@@ -550,7 +550,7 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
         const int bw = plan_s->bw[w], bj = plan_s->bw[j];
         const int2 r = block_of(bw);
         // (cluster mode: the CTA whose slice holds column bj)
-        if (bj >= r.x && bj <= r.y && bj >= s0 && bj < s1) {
+        if (bj >= r.x && bj <= r.y && (CL == 1 || (bj >= s0 && bj < s1))) {
           const float4 gb = plan_s->gb[w];
           const float rv = slots[__float_as_int(gb.w) + bj];
           const float4 oj = plan_s->ga[j], dj = plan_s->gb[j];
