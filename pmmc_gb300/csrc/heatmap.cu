@@ -435,7 +435,9 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
   // the ring and its rows were requested): its length, whether its beads share
   // one block, each move's geometry at the current positions, and the wait
   // for its rows.  Slots past the length repeat move 0 (scored, unused).
-  auto plan = [&](long long m0, long long nms) {
+  // with_pos = false leaves out the moved beads' old positions (cluster
+  // mode plans the rest while CTA 0 decides; plan_old_pos adds them after)
+  auto plan = [&](long long m0, long long nms, bool with_pos = true) {
     const int lim = (int)max(1ll, min((long long)min(kWin, D), min(nms, cap) - m0));
     const int b = lane < lim ? recs[(m0 + lane) & 127].b : -1 - lane;
     bool rep = false;
@@ -454,9 +456,11 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
     const unsigned diff = __ballot_sync(0xffffffffu, bk.x != bx0 || bk.y != by0);
     bool late = false;
     if (lane < kWin) {
-      const float4 o = spos[rec.b];
-      plan_s->ga[lane] = make_float4(o.x, o.y, o.z,
-                                     fmaf(rec.dx, rec.dx, fmaf(rec.dy, rec.dy, rec.dz * rec.dz)));
+      if (with_pos) {
+        const float4 o = spos[rec.b];
+        plan_s->ga[lane] = make_float4(o.x, o.y, o.z,
+                                       fmaf(rec.dx, rec.dx, fmaf(rec.dy, rec.dy, rec.dz * rec.dz)));
+      }
       const int roff = CL > 1 ? (int)(k & dmask) * spitch - s0
                               : (int)(k & dmask) * pitch - (bk.x & ~3);
       plan_s->gb[lane] =
@@ -469,6 +473,15 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
       plan_s->len = L;
       plan_s->same = diff == 0u;
       plan_s->timeout = lm != 0u;
+    }
+  };
+  auto plan_old_pos = [&](long long m0) {
+    const int L = plan_s->len;
+    if (lane < kWin) {
+      const MoveRec rec = recs[(m0 + (lane < L ? lane : 0)) & 127];
+      const float4 o = spos[rec.b];
+      plan_s->ga[lane] = make_float4(o.x, o.y, o.z,
+                                     fmaf(rec.dx, rec.dx, fmaf(rec.dy, rec.dy, rec.dz * rec.dz)));
     }
   };
 
@@ -627,9 +640,12 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
         }
         __syncthreads();
       }
-      // the draws and row copies do not depend on the decisions: they run
-      // while CTA 0 takes them
+      // the draws, the row copies and the next window's plan (all but the
+      // moved beads' old positions) do not depend on the decisions: they
+      // run while CTA 0 takes them
       if (warp == 1) draws_and_copies();
+      if (warp == 2 && m + L < cap)
+        plan(m + L, m + L == next_ms ? next_ms + P.window : next_ms, false);
     }
     // ---- warp 0 (of CTA 0 in cluster mode): decisions, the next window ----
     if (warp == 0 && leader) {
@@ -720,10 +736,9 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
           plan_s->pacc = dv.y;
           plan_s->pad[1] = late;
           plan_s->lend = L;
-          plan_s->timeout = 0;
         }
         const long long mn = m + L;
-        if (mn < cap && late == 0) plan(mn, mn == next_ms ? next_ms + P.window : next_ms);
+        if (mn < cap && late == 0) plan_old_pos(mn);
       }
     }
     __syncthreads();
