@@ -381,7 +381,8 @@ pmmc_status pmmc_heatmap_batch_anneal(pmmc_ctx *ctx, int n_units,
                                       void *trace_out, int trace_cap);
 
 /* Heatmap kernel choice for the context's later heatmap calls: each chain on
- * a thread-block cluster of `ctas` CTAs (1, 2, 4 or 8; 0 = by the batch: 8
+ * a thread-block cluster of `ctas` CTAs (1, 2, 4, 8 or 16, 16 being beyond the
+ * portable cluster size; 0 = by the batch: 8
  * when every chain can have its own eight SMs and the maps have 512 beads
  * or more, else 1).  In a cluster each CTA scores its slice of every row
  * and CTA 0 takes the decisions, so one chain uses eight SMs' worth of

@@ -921,8 +921,8 @@ extern "C" pmmc_status pmmc_heatmap_batch_anneal(pmmc_ctx *ctx, int n_units,
   // CTAs (one per SM), each scoring a slice of every row.
   int CL = ctx->heatmap_cluster;
   if (CL == 0) CL = (n_units * 8 <= ctx->sm_count && max_n >= 512) ? 8 : 1;
-  if (CL != 1 && CL != 2 && CL != 4 && CL != 8)
-    return fail(ctx, PMMC_ERR_INVALID, "heatmap: cluster of %d CTAs (1, 2, 4 or 8)", CL);
+  if (CL != 1 && CL != 2 && CL != 4 && CL != 8 && CL != 16)
+    return fail(ctx, PMMC_ERR_INVALID, "heatmap: cluster of %d CTAs (1, 2, 4, 8 or 16)", CL);
   while (CL > 1) {  // every CTA needs beads of its own
     bool ok = true;
     for (const HeatUnit &U : hu) {
@@ -1047,11 +1047,15 @@ extern "C" pmmc_status pmmc_heatmap_batch_anneal(pmmc_ctx *ctx, int n_units,
     return fail(ctx, e == cudaErrorMemoryAllocation ? PMMC_ERR_NOMEM : PMMC_ERR_CUDA,
                 "heatmap upload: %s", cudaGetErrorString(e));
   auto kernel_of = [](int cl) {
-    return cl == 8 ? heatmap_anneal_kernel<8>
-                   : cl == 4 ? heatmap_anneal_kernel<4>
-                             : cl == 2 ? heatmap_anneal_kernel<2> : heatmap_anneal_kernel<1>;
+    return cl == 16  ? heatmap_anneal_kernel<16>
+           : cl == 8 ? heatmap_anneal_kernel<8>
+           : cl == 4 ? heatmap_anneal_kernel<4>
+           : cl == 2 ? heatmap_anneal_kernel<2>
+                     : heatmap_anneal_kernel<1>;
   };
   const auto kern = kernel_of(CL);
+  if (CL > 8)  // clusters above 8 CTAs are opt-in
+    PMMC_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1));
   PMMC_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
   PMMC_CUDA(ctx, cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, 100));
@@ -1133,8 +1137,8 @@ extern "C" pmmc_status pmmc_heatmap_batch_anneal(pmmc_ctx *ctx, int n_units,
 
 extern "C" pmmc_status pmmc_heatmap_set_cluster(pmmc_ctx *ctx, int ctas) {
   if (!ctx) return PMMC_ERR_INVALID;
-  if (ctas != 0 && ctas != 1 && ctas != 2 && ctas != 4 && ctas != 8)
-    return fail(ctx, PMMC_ERR_INVALID, "heatmap cluster: %d CTAs (0, 1, 2, 4 or 8)", ctas);
+  if (ctas != 0 && ctas != 1 && ctas != 2 && ctas != 4 && ctas != 8 && ctas != 16)
+    return fail(ctx, PMMC_ERR_INVALID, "heatmap cluster: %d CTAs (0, 1, 2, 4, 8 or 16)", ctas);
   ctx->heatmap_cluster = ctas;
   return PMMC_OK;
 }
