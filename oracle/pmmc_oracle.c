@@ -92,6 +92,9 @@ typedef struct {
   const int *movable; /* philox: indices of non-fixed beads */
   int n_movable;
   float disp_u[3];    /* philox: cached displacement draws of the move */
+  int u_from_bead;    /* philox, smoothing: the Metropolis uniform is the
+                         bead draw's fractional part (one block a move) */
+  float bead_u;
 } rng_ctx;
 
 /* libc draws, common.cpp:10-18: random(range) = rand() % range,
@@ -115,7 +118,10 @@ static int draw_bead(rng_ctx *c, int size) {
   c->disp_u[0] = orc_u01(o[1]);
   c->disp_u[1] = orc_u01(o[2]);
   c->disp_u[2] = orc_u01(o[3]);
-  uint32_t k = (uint32_t)(((uint64_t)o[0] * (uint32_t)c->n_movable) >> 32);
+  const uint64_t prod = (uint64_t)o[0] * (uint32_t)c->n_movable;
+  uint32_t k = (uint32_t)(prod >> 32);
+  /* the low word: the draw's fractional part within bead k's interval */
+  c->bead_u = orc_u01((uint32_t)prod);
   return c->movable[k];
 }
 
@@ -143,6 +149,8 @@ static void draw_disp(rng_ctx *c, float max, int in2d, float d[3]) {
 static int draw_chance(rng_ctx *c, float chance) {
   if (c->r->kind == ORC_RNG_LIBC)
     return libc_uniform() < chance;
+  if (c->u_from_bead)
+    return c->bead_u < chance;
   uint32_t o[4];
   philox_block(c->r, 1u, o);
   return orc_u01(o[0]) < chance;
@@ -168,6 +176,8 @@ static void rng_begin(rng_ctx *c, orc_rng *r, int n,
   c->r = r;
   c->movable = NULL;
   c->n_movable = 0;
+  c->u_from_bead = 0;
+  c->bead_u = 0.0f;
   if (r->kind == ORC_RNG_LIBC) {
     srand((unsigned)r->seed);
   } else {
@@ -874,6 +884,7 @@ void orc_smooth_anneal(int n, float *pos, const unsigned char *fixed,
   memset(res, 0, sizeof(*res));
   rng_ctx c;
   rng_begin(&c, rng, n, fixed);
+  c.u_from_bead = 1; /* smoothing: one Philox block a move */
   int philox = rng->kind == ORC_RNG_PHILOX;
   double T = p->max_temp, dt = p->dt_temp, tp;
   double curr_structure = orc_smooth_full_score(n, pos, dist_to_next, p);
@@ -1262,7 +1273,9 @@ static void replay_core(int kind, void *ctx, local_fn fn, int n, float *pos,
     int ok = kind == 2 ? En < E : En <= E;
     uint32_t o[4];
     philox_block(&r, 1u, o);
-    float u = orc_u01(o[0]);
+    /* smoothing draws one block a move: its uniform is the bead draw's
+       fractional part */
+    float u = kind == 2 ? c.bead_u : orc_u01(o[0]);
     int test = kind == 0 ? (!gpu || (T > 0.0 && E > 0.0)) : T > 0.0;
     if (!ok && test) {
       double den = (kind == 2 && gpu && E < 1e-12) ? 1e-12 : E;

@@ -67,6 +67,15 @@ struct SmoothDevParams {
   uint64_t seed;
 };
 
+// A smoothing move draws one Philox block: x picks the bead (the high word
+// of x * n_mov) and the low word of the same product -- x's fractional part
+// within the bead's interval, uniform and independent of which bead -- is the
+// Metropolis uniform; y, z, w are the displacement.  (The other levels draw
+// the uniform from a second block, tag 1.)
+__device__ __forceinline__ uint32_t bead_fraction(uint32_t x, int n_mov) {
+  return x * (uint32_t)n_mov;
+}
+
 // Bond term with the clamped target d0 and its reciprocal precomputed:
 // ((|a - b| - d0) / d0)^2 * (stretch | squeeze).
 __device__ __forceinline__ float bond_e(float4 a, float4 b, float2 d, float ks,
@@ -256,20 +265,20 @@ smooth_anneal_kernel(const SmoothUnit *__restrict__ units,
   long long next_rs = S.resync > 0 ? (long long)S.resync : 0x7fffffffffffffffLL;
   // The draws of a move depend only on its index and temperature, not on the
   // chain's state; those of the next move are made while this move is
-  // scored.  Lane 0 draws the proposal (tag 0), lane 1 the threshold (tag 1).
+  // scored (one Philox block a move, the same on both lanes).
   struct Draw {
     int b;
     float dx, dy, dz, thr;
   };
   auto draw = [&](long long mv, float Tm) {
-    const uint4 r = philox_move(S.seed, chain_id, (uint64_t)mv, (uint32_t)sub);
+    const uint4 r = philox_move(S.seed, chain_id, (uint64_t)mv, 0u);
     const int k = uniform_index(r.x, U.n_mov);
     Draw w;
     w.b = MOV ? MOV[k] : k;
     w.dx = (2.0f * u01(r.y) - 1.0f) * U.step;
     w.dy = (2.0f * u01(r.z) - 1.0f) * U.step;
     w.dz = S.use2d ? 0.0f : (2.0f * u01(r.w) - 1.0f) * U.step;
-    w.thr = ratio_threshold(u01(r.x), Tm, S.inv_scale, S.inv_coef);
+    w.thr = ratio_threshold(u01(bead_fraction(r.x, U.n_mov)), Tm, S.inv_scale, S.inv_coef);
     return w;
   };
   const int lead = lane & ~(kSmoothLanes - 1);
@@ -455,14 +464,13 @@ smooth_window_kernel(const SmoothUnit *__restrict__ units,
   const bool has_mov = U.n_mov > 0;
   auto draw = [&](long long mv, float Tm) {
     const uint4 r = philox_move(S.seed, chain_id, (uint64_t)mv, 0u);
-    const uint4 a = philox_move(S.seed, chain_id, (uint64_t)mv, 1u);
     const int k = uniform_index(r.x, U.n_mov);
     Draw w;
     w.b = has_mov ? (MOV ? MOV[k] : k) : 0;
     w.dx = (2.0f * u01(r.y) - 1.0f) * U.step;
     w.dy = (2.0f * u01(r.z) - 1.0f) * U.step;
     w.dz = S.use2d ? 0.0f : (2.0f * u01(r.w) - 1.0f) * U.step;
-    w.thr = ratio_threshold(u01(a.x), Tm, S.inv_scale, S.inv_coef);
+    w.thr = ratio_threshold(u01(bead_fraction(r.x, U.n_mov)), Tm, S.inv_scale, S.inv_coef);
     w.T = Tm;
     return w;
   };

@@ -31,15 +31,21 @@ def _u01(x):
     return F32(x >> 8) * F32(1.0 / 16777216.0)
 
 
-def _draws(seed, chain, move, movable, step, use2d=False):
+def _draws(seed, chain, move, movable, step, use2d=False, smooth=False):
+    """The kernels' draws of a move: block tag 0 gives the bead (high word of
+    x * n_movable) and the displacement; the Metropolis uniform is block tag
+    1's first word, or for smoothing the low word of x * n_movable."""
     key = (seed & 0xFFFFFFFF, seed >> 32)
     o = O.philox((move & 0xFFFFFFFF, move >> 32, chain, 0), key)
-    a = O.philox((move & 0xFFFFFFFF, move >> 32, chain, 1), key)
-    b = movable[(int(o[0]) * len(movable)) >> 32]
+    prod = int(o[0]) * len(movable)
+    b = movable[prod >> 32]
     d = np.array([(F32(2.0) * _u01(int(o[k])) - F32(1.0)) * F32(step) for k in (1, 2, 3)],
                  np.float32)
     if use2d:
         d[2] = 0.0
+    if smooth:
+        return b, d, _u01(prod & 0xFFFFFFFF)
+    a = O.philox((move & 0xFFFFFFFF, move >> 32, chain, 1), key)
     return b, d, _u01(int(a[0]))
 
 
@@ -98,7 +104,7 @@ def py_smooth_gpu_schedule(pr, prm, step, seed, chain):
     trace = []
     while moves < cap:
         for _ in range(256):
-            b, d, u = _draws(seed, chain, moves, movable, step)
+            b, d, u = _draws(seed, chain, moves, movable, step, smooth=True)
             before = O.smooth_local(pr, prm, b, pos=pos)
             q = pos.copy()
             q[b] += d
