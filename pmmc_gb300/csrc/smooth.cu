@@ -380,14 +380,22 @@ smooth_anneal_kernel(const SmoothUnit *__restrict__ units,
   }
 }
 
+// One move's draws (windowed kernel): bead, displacement, Metropolis
+// threshold and the move's temperature.
+struct Draw {
+  int b;
+  float dx, dy, dz, thr, T;
+};
+
 // Windows of W proposals per chain, W lanes each holding one: the proposals
 // of moves m .. m+W-1 are drawn and scored at once against the positions at
 // the window's start, then resolved in order.  A proposal whose bead lies
 // within two beads of an earlier accepted proposal of the window (its local
-// score reads the moved bead) closes the window there and is drawn and
-// scored again, from the updated positions, as the first slot of the next
-// window.  The resolution takes the slots in order with the chain's own
-// float-float running score: every slot is tested against the current score
+// score reads the moved bead) closes the window there and is scored again,
+// from the updated positions, as the first slot of the next window (with the
+// same draws: they depend only on the move's index).  The resolution takes
+// the slots in order with the chain's own float-float running score: every
+// slot is tested against the current score
 // at once, the first slot that passes is accepted (the ones before it failed
 // against the score they would have seen) and the score moves on, so every
 // decision, score and position is that of the one-move-at-a-time kernel
@@ -396,11 +404,6 @@ smooth_anneal_kernel(const SmoothUnit *__restrict__ units,
 // ballot.  The local score of every bead at its current position is kept in
 // shared memory and refreshed around each accepted move, so a slot scores
 // only its proposed position.
-struct Draw {
-  int b;
-  float dx, dy, dz, thr, T;
-};
-
 template <int W, bool SPH>
 __global__ void __launch_bounds__(128, 6)
 smooth_window_kernel(const SmoothUnit *__restrict__ units,
