@@ -159,3 +159,24 @@ def test_ctypes_structs_match_header_layouts(tmp_path):
     got = [int(x) for x in subprocess.run([str(tmp_path / "layout")], capture_output=True,
                                           text=True).stdout.split()]
     assert got == want
+
+
+def test_kernel_choice_setters_need_a_context(built_lib):
+    """pmmc_smooth_set_window and pmmc_heatmap_set_cluster validate their
+    arguments on the host; a null context is refused without device work."""
+    assert built_lib.pmmc_smooth_set_window(None, 8, 32, 20) == capi.PMMC_ERR_INVALID
+    assert built_lib.pmmc_heatmap_set_cluster(None, 8) == capi.PMMC_ERR_INVALID
+
+
+def test_smooth_packed_regions_concatenate_the_segments():
+    """The packed genome-smoothing arrays (one set of arrays, regions back to
+    back) hold exactly the list form's regions, in order."""
+    from pmmc_gb300 import workloads as W
+    segs = W.smooth_segments()
+    off, pos, dtn, fixed = W.smooth_packed()
+    assert len(off) == len(segs) + 1 and off[0] == 0 and off[-1] == len(pos) == len(dtn)
+    for u in range(0, len(segs), 997):
+        p, d, f = segs[u]
+        np.testing.assert_array_equal(pos[off[u]:off[u + 1]], np.asarray(p, np.float32))
+        np.testing.assert_array_equal(dtn[off[u]:off[u + 1]], np.asarray(d, np.float32))
+        np.testing.assert_array_equal(fixed[off[u]:off[u + 1]], np.asarray(f, np.uint8))
