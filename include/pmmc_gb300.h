@@ -382,11 +382,11 @@ pmmc_status pmmc_heatmap_batch_anneal(pmmc_ctx *ctx, int n_units,
 
 /* Heatmap kernel choice for the context's later heatmap calls: each chain on
  * a thread-block cluster of `ctas` CTAs (1, 2, 4, 8 or 16, 16 being beyond the
- * portable cluster size; 0 = by the batch: 8
- * when every chain can have its own eight SMs and the maps have 512 beads
- * or more, else 1).  In a cluster each CTA scores its slice of every row
- * and CTA 0 takes the decisions, so one chain uses eight SMs' worth of
- * special-function units and shared memory. */
+ * portable cluster size; 0 = by the batch: 16 for up to 4 chains on maps of
+ * 1024 beads or more, 8 when every chain can have its own eight SMs and the
+ * maps have 512 beads or more, else 1).  In a cluster each CTA scores its
+ * slice of every row and CTA 0 takes the decisions, so one chain uses the
+ * special-function units and shared memory of several SMs. */
 pmmc_status pmmc_heatmap_set_cluster(pmmc_ctx *ctx, int ctas);
 
 /* ---------------- expected-distance heatmap ---------------- */

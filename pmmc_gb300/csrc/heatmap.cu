@@ -920,7 +920,10 @@ extern "C" pmmc_status pmmc_heatmap_batch_anneal(pmmc_ctx *ctx, int n_units,
   // Cluster mode for a few chains on a large map: each chain spread over CL
   // CTAs (one per SM), each scoring a slice of every row.
   int CL = ctx->heatmap_cluster;
-  if (CL == 0) CL = (n_units * 8 <= ctx->sm_count && max_n >= 512) ? 8 : 1;
+  if (CL == 0)  // 16 CTAs (beyond the portable size) for up to 4 chains
+    CL = (n_units <= 4 && max_n >= 1024 && 16 * n_units <= ctx->sm_count) ? 16
+         : (n_units * 8 <= ctx->sm_count && max_n >= 512)                  ? 8
+                                                                          : 1;
   if (CL != 1 && CL != 2 && CL != 4 && CL != 8 && CL != 16)
     return fail(ctx, PMMC_ERR_INVALID, "heatmap: cluster of %d CTAs (1, 2, 4, 8 or 16)", CL);
   while (CL > 1) {  // every CTA needs beads of its own

@@ -32,8 +32,8 @@ struct pmmc_ctx {
   int smooth_window = 8;
   int smooth_window_long = 32;
   int smooth_window_long_min_free = 20;
-  // heatmap: CTAs of the cluster that runs one chain (0 = by the batch: 8
-  // for a few chains on maps of 512 beads or more, else 1)
+  // heatmap: CTAs of the cluster that runs one chain (0 = by the batch: 16
+  // or 8 for a few chains on large maps, else 1)
   int heatmap_cluster = 0;
   std::string last_error;
 };

@@ -127,12 +127,12 @@ def _config1_region():
     return synth.heatmap_region(2048, seed=7)
 
 
-@pytest.mark.parametrize("cl", [0, 1, 16])
+@pytest.mark.parametrize("cl", [0, 1, 8])
 def test_heatmap_trace_parity_config1(hctx, cl):
     """Per-move parity on the 2048-bead map, one chain: the launch the
-    single-chain workload takes (cl = 0: a cluster of 8 CTAs, each scoring
-    256 beads of every row), one CTA of 512 threads with a 16-row ring, and
-    a cluster of 16 CTAs (opt-in size)."""
+    single-chain workload takes (cl = 0: a cluster of 16 CTAs, each scoring
+    128 beads of every row), one CTA of 512 threads with a 16-row ring, and
+    a cluster of 8 CTAs."""
     ctx = hctx
     ctx.set_heatmap_cluster(cl)
     h = _config1_region()
