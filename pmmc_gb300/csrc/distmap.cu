@@ -55,21 +55,6 @@ struct DistPartial {
   int pad;
 };
 
-// Upper-triangle tile t (row by row, bi <= bj) as (bi, bj): row b holds
-// nt - b tiles and starts at b*nt - b*(b-1)/2.  The grids launch only these
-// tiles (a square grid would schedule as many blocks below the diagonal that
-// do nothing).
-__device__ __forceinline__ int2 upper_tile(long long t, int nt) {
-  const double a = 2.0 * nt + 1.0;
-  int b = (int)((a - sqrt(a * a - 8.0 * (double)t)) * 0.5);
-  auto start = [nt](long long r) { return r * nt - r * (r - 1) / 2; };
-  if (b < 0) b = 0;
-  if (b > nt - 1) b = nt - 1;
-  while (b > 0 && start(b) > t) --b;
-  while (b + 1 < nt && start(b + 1) <= t) ++b;
-  return make_int2(b, b + (int)(t - start(b)));
-}
-
 // Tile blockIdx.x of the upper triangle; its partial goes to part[blockIdx.x].
 __global__ void __launch_bounds__(kTile * kRows)
 distmap_pass1(const float *__restrict__ c, int n, int nt, int diag, float scale, float power,

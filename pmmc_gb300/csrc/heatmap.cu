@@ -27,8 +27,6 @@
 // the accepted sequence is the one-move-at-a-time sequence.  The running score
 // is a float-float pair; the start and end scores are FP64 recomputes.
 #include <algorithm>
-#include <atomic>
-#include <thread>
 #include <cmath>
 #include <vector>
 
@@ -816,6 +814,77 @@ heatmap_anneal_kernel(const HeatUnit *__restrict__ units, const float4 *__restri
   }
 }
 
+constexpr int kPackTile = 32;
+
+// r = 1/h where the score of bead m reads the pair (m, i), else 0.  The
+// reciprocal is correctly rounded (the value of 1.0f / h in IEEE single).
+__device__ __forceinline__ float packed_r(float h, int m, int i, int2 b, int diag) {
+  const bool read = i >= b.x && i <= b.y && abs(i - m) >= diag && i != m && h >= 1e-6f;
+  return read ? __frcp_rn(h) : 0.0f;
+}
+
+// The device matrix from the caller's maps (n x n, row-major, back to back
+// at raw_off[u]): rows of U.pitch floats at U.heat_off holding packed_r, the
+// padding columns zero.  The same pass checks symmetry over the pairs the
+// score reads (m < i in bead m's block, i - m >= diag): h_mi and h_im must
+// both be skipped (< 1e-6) or be equal; asym[u] keeps the lowest m * n + i
+// of a pair that is not (all ones: none).  One 256-thread block per pair of
+// 32 x 32 tiles (bm, bi), bm <= bi, of one map (tile_start[u]: the first
+// block of map u): the tile and its mirror are staged in shared memory, so
+// both are read and written along rows.
+__global__ void __launch_bounds__(256)
+heat_pack_kernel(const HeatUnit *__restrict__ units, int n_units,
+                 const long long *__restrict__ tile_start, const long long *__restrict__ raw_off,
+                 const float *__restrict__ raw, const int2 *__restrict__ blk,
+                 float *__restrict__ rheat, unsigned long long *__restrict__ asym) {
+  __shared__ float A[kPackTile][kPackTile + 1];  // rows m0.., columns i0..
+  __shared__ float B[kPackTile][kPackTile + 1];  // rows i0.., columns m0..
+  const long long t = blockIdx.x;
+  int lo = 0, hi = n_units - 1;  // the last map whose first block is <= t
+  while (lo < hi) {
+    const int mid = (lo + hi + 1) >> 1;
+    if (tile_start[mid] <= t)
+      lo = mid;
+    else
+      hi = mid - 1;
+  }
+  const int u = lo;
+  const HeatUnit U = units[u];
+  const int n = U.n;
+  const int nt = (n + kPackTile - 1) / kPackTile;
+  const int2 tb = upper_tile(t - tile_start[u], nt);
+  const int m0 = tb.x * kPackTile, i0 = tb.y * kPackTile;
+  const bool on_diag = tb.x == tb.y;
+  const float *H = raw + raw_off[u];
+  float *R = rheat + U.heat_off;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  for (int r = ty; r < kPackTile; r += 8) {
+    const int m = m0 + r, i = i0 + tx;
+    A[r][tx] = (m < n && i < n) ? H[(size_t)m * n + i] : 0.0f;
+    const int m2 = i0 + r, i2 = m0 + tx;
+    if (!on_diag) B[r][tx] = (m2 < n && i2 < n) ? H[(size_t)m2 * n + i2] : 0.0f;
+  }
+  __syncthreads();
+  for (int r = ty; r < kPackTile; r += 8) {
+    const int m = m0 + r, i = i0 + tx;
+    if (m < n && i < n) {
+      const int2 b = blk[U.blk_off + m];
+      const float a = A[r][tx];
+      R[(size_t)m * U.pitch + i] = packed_r(a, m, i, b, U.diag);
+      if (i > m && i >= b.x && i <= b.y && i - m >= U.diag) {
+        const float c = on_diag ? A[tx][r] : B[tx][r];  // h_im
+        const bool ua = a >= 1e-6f, uc = c >= 1e-6f;
+        if (ua != uc || (ua && a != c)) atomicMin(&asym[u], (unsigned long long)m * n + i);
+      }
+    } else if (m < n && i < U.pitch) {
+      R[(size_t)m * U.pitch + i] = 0.0f;  // padding (the last column tile)
+    }
+    const int m2 = i0 + r, i2 = m0 + tx;
+    if (!on_diag && m2 < n && i2 < n)
+      R[(size_t)m2 * U.pitch + i2] = packed_r(B[r][tx], m2, i2, blk[U.blk_off + m2], U.diag);
+  }
+}
+
 }  // namespace pmmc
 
 using namespace pmmc;
@@ -980,75 +1049,68 @@ extern "C" pmmc_status pmmc_heatmap_batch_anneal(pmmc_ctx *ctx, int n_units,
   // The kernels read r = 1/h, rows padded to a 16-byte pitch, with r = 0
   // wherever the reference skips the pair: h < 1e-6, |i - m| < diag, i == m,
   // and i outside bead m's chromosome block (LooperSolver.hpp:3597-3611).
-  std::vector<float> hrheat((size_t)heat_floats, 0.0f);
-  // A move changes the full score by twice its local change only when the
-  // map is symmetric over the pairs the score reads (createDistanceHeatmap
-  // mirrors it, LooperSolver.hpp:3062); an asymmetric map is refused.
-  std::vector<long long> asym(n_units, -1);
-  {
-    auto pack = [&](int u) {
-      const HeatUnit &U = hu[u];
-      const pmmc_heatmap_problem &pr = units[u];
-      for (int m = 0; m < pr.n; ++m) {
-        const int2 b = hblk[(size_t)U.blk_off + m];
-        const float *src = pr.heat + (size_t)m * pr.n;
-        float *dst = &hrheat[(size_t)U.heat_off + (size_t)m * U.pitch];
-        for (int i = b.x; i <= b.y; ++i) {
-          const float h = src[i];
-          if (std::abs(i - m) >= U.diag && i != m && h >= 1e-6f) dst[i] = 1.0f / h;
-        }
-      }
-      // pairs (m, i), m < i, in 32 x 32 tiles: h_mi and h_im must both be
-      // skipped (< 1e-6) or be equal
-      const int n = pr.n;
-      const float *H = pr.heat;
-      for (int m0 = 0; m0 < n && asym[u] < 0; m0 += 32)
-        for (int i0 = m0; i0 < n && asym[u] < 0; i0 += 32)
-          for (int m = m0; m < std::min(m0 + 32, n); ++m) {
-            const int2 b = hblk[(size_t)U.blk_off + m];
-            for (int i = std::max(i0, m + 1); i < std::min(i0 + 32, n); ++i) {
-              if (i < b.x || i > b.y || i - m < U.diag) continue;
-              const float a = H[(size_t)m * n + i], c = H[(size_t)i * n + m];
-              const bool ua = a >= 1e-6f, uc = c >= 1e-6f;
-              if (ua != uc || (ua && a != c)) {
-                asym[u] = (long long)m * n + i;
-                break;
-              }
-            }
-          }
-    };
-    const int nt = (int)std::max(1u, std::min<unsigned>(std::thread::hardware_concurrency(), 32u));
-    std::vector<std::thread> pool;
-    std::atomic<int> next{0};
-    for (int t = 0; t < std::min(nt, n_units); ++t)
-      pool.emplace_back([&] {
-        for (int u = next++; u < n_units; u = next++) pack(u);
-      });
-    for (auto &th : pool) th.join();
+  // The caller's maps go to the device as they are and heat_pack_kernel
+  // writes that matrix.  A move changes the full score by twice its local
+  // change only when the map is symmetric over the pairs the score reads
+  // (createDistanceHeatmap mirrors it, LooperSolver.hpp:3062); the same pass
+  // finds an asymmetric map, which is refused.
+  std::vector<long long> tile_start((size_t)n_units + 1, 0), raw_off((size_t)n_units, 0);
+  long long raw_floats = 0;
+  for (int u = 0; u < n_units; ++u) {
+    const long long nt = (hu[u].n + kPackTile - 1) / kPackTile;
+    tile_start[u + 1] = tile_start[u] + nt * (nt + 1) / 2;
+    raw_off[u] = raw_floats;
+    raw_floats += (long long)hu[u].n * hu[u].n;
   }
-  for (int u = 0; u < n_units; ++u)
-    if (asym[u] >= 0)
-      return fail(ctx, PMMC_ERR_INVALID,
-                  "heatmap region %d: the map is not symmetric at (%lld, %lld)", u,
-                  asym[u] / units[u].n, asym[u] % units[u].n);
+  if (tile_start[n_units] > 0x7fffffffll)
+    return fail(ctx, PMMC_ERR_INVALID, "heatmap batch: too many map tiles");
   DevBuf<HeatUnit> d_units;
   DevBuf<float4> d_pos;
-  DevBuf<float> d_rheat, d_out;
+  DevBuf<float> d_rheat, d_out, d_raw;
   DevBuf<int> d_mov;
   DevBuf<int2> d_blk;
   DevBuf<ChainOut> d_outs;
   DevBuf<MoveTrace> d_trace;
+  DevBuf<long long> d_tile_start, d_raw_off;
+  DevBuf<unsigned long long> d_asym;
   cudaError_t e = d_units.upload(hu, s);
   if (e == cudaSuccess) e = d_pos.upload(hpos, s);
-  if (e == cudaSuccess) e = d_rheat.upload(hrheat, s);
   if (e == cudaSuccess) e = d_mov.upload(hmov, s);
   if (e == cudaSuccess) e = d_blk.upload(hblk, s);
+  if (e == cudaSuccess) e = d_tile_start.upload(tile_start, s);
+  if (e == cudaSuccess) e = d_raw_off.upload(raw_off, s);
+  if (e == cudaSuccess) e = d_rheat.alloc((size_t)heat_floats);
+  if (e == cudaSuccess) e = d_raw.alloc((size_t)raw_floats);
+  for (int u = 0; u < n_units && e == cudaSuccess; ++u)
+    e = cudaMemcpyAsync(d_raw.p + raw_off[u], units[u].heat,
+                        sizeof(float) * (size_t)units[u].n * units[u].n,
+                        cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = d_asym.alloc((size_t)n_units);
+  if (e == cudaSuccess)
+    e = cudaMemsetAsync(d_asym.p, 0xff, sizeof(unsigned long long) * n_units, s);
+  std::vector<unsigned long long> asym((size_t)n_units, ~0ull);
+  if (e == cudaSuccess) {
+    heat_pack_kernel<<<(unsigned)tile_start[n_units], 256, 0, s>>>(
+        d_units.p, n_units, d_tile_start.p, d_raw_off.p, d_raw.p, d_blk.p, d_rheat.p, d_asym.p);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(asym.data(), d_asym.p, sizeof(unsigned long long) * n_units,
+                        cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  d_raw.release();
   if (e == cudaSuccess) e = d_out.alloc((size_t)out_off);
   if (e == cudaSuccess) e = d_outs.alloc((size_t)n_units);
   if (e == cudaSuccess && trace_cap > 0) e = d_trace.alloc((size_t)trace_cap);
   if (e != cudaSuccess)
     return fail(ctx, e == cudaErrorMemoryAllocation ? PMMC_ERR_NOMEM : PMMC_ERR_CUDA,
                 "heatmap upload: %s", cudaGetErrorString(e));
+  for (int u = 0; u < n_units; ++u)
+    if (asym[u] != ~0ull)
+      return fail(ctx, PMMC_ERR_INVALID,
+                  "heatmap region %d: the map is not symmetric at (%lld, %lld)", u,
+                  (long long)(asym[u] / (unsigned long long)units[u].n),
+                  (long long)(asym[u] % (unsigned long long)units[u].n));
   auto kernel_of = [](int cl) {
     return cl == 16  ? heatmap_anneal_kernel<16>
            : cl == 8 ? heatmap_anneal_kernel<8>
