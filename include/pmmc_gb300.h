@@ -141,7 +141,9 @@ typedef struct pmmc_arcs_problem {
  * change, which holds only for a symmetric map: a map whose pairs (i, m)
  * inside one block and outside the diagonal band differ from (m, i) -- one
  * side below 1e-6 and the other not, or unequal values -- is refused with
- * PMMC_ERR_INVALID. */
+ * PMMC_ERR_INVALID, the message naming the region and its lowest such pair
+ * (m, i), m < i.  The maps are copied to the device as given; the check and
+ * the reciprocals the kernels read are computed there. */
 typedef struct pmmc_heatmap_problem {
   int n;
   const float *pos;            /* n*3                        */

@@ -108,11 +108,19 @@ def test_heatmap_refuses_asymmetric_map(ctx):
     bad_value[3, 40] *= 1.5
     bad_skip = h.heat.copy()
     bad_skip[50, 5] = 0.0           # one side skipped (< 1e-6), the other not
-    for heat in (bad_value, bad_skip):
+    for heat, pair in ((bad_value, "(3, 40)"), (bad_skip, "(5, 50)")):
         with pytest.raises(capi.PmmcError) as e:
             capi.heatmap_anneal(ctx, capi.HeatmapInput(h.pos, heat), prm, 1.0)
         assert e.value.status == capi.PMMC_ERR_INVALID
-        assert "not symmetric" in str(e.value)
+        assert "not symmetric" in str(e.value) and pair in str(e.value)
+    # in a batch: the region named is the asymmetric one; its lowest pair
+    both = bad_value.copy()
+    both[50, 5] = 0.0
+    good = capi.HeatmapInput(h.pos, h.heat)
+    with pytest.raises(capi.PmmcError) as e:
+        capi.heatmap_batch_anneal(ctx, [good, good, capi.HeatmapInput(h.pos, both)], prm,
+                                  [1.0] * 3)
+    assert "region 2" in str(e.value) and "(3, 40)" in str(e.value)
     unread = h.heat.copy()
     unread[7, 8] = 9.0              # inside a diagonal band of width 2
     unread[3, 40] *= 1.5            # across the block boundary at 32
