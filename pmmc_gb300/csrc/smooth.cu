@@ -707,6 +707,12 @@ extern "C" pmmc_status pmmc_smooth_batch_anneal(pmmc_ctx *ctx, int n_units,
   std::vector<int> hmov;
   long long out_off = 0, work_off = 0;
   int chain_base = 0, max_n = 0;
+  {
+    size_t beads = 0;
+    for (int u = 0; u < n_units; ++u) beads += (size_t)std::max(0, units[u].n);
+    hpos.reserve(beads);
+    hdtn.reserve(beads);
+  }
   for (int u = 0; u < n_units; ++u) {
     const pmmc_smooth_problem &pr = units[u];
     if (pr.n < 1 || !pr.pos || !pr.dist_to_next)
@@ -721,13 +727,16 @@ extern "C" pmmc_status pmmc_smooth_batch_anneal(pmmc_ctx *ctx, int n_units,
       const float d0 = pr.dist_to_next[i] < 1e-6f ? 1e-6f : pr.dist_to_next[i];
       hdtn.push_back(make_float2(d0, 1.0f / d0));
     }
-    std::vector<int> mv;
-    for (int i = 0; i < pr.n; ++i)
-      if (!pr.fixed || !pr.fixed[i]) mv.push_back(i);
-    U.n_mov = (int)mv.size();
-    if (U.n_mov < pr.n) {
+    int n_mov = pr.n;
+    if (pr.fixed) {
+      n_mov = 0;
+      for (int i = 0; i < pr.n; ++i) n_mov += pr.fixed[i] ? 0 : 1;
+    }
+    U.n_mov = n_mov;
+    if (n_mov < pr.n) {  // the movable beads' indices
       U.mov_off = (int)hmov.size();
-      hmov.insert(hmov.end(), mv.begin(), mv.end());
+      for (int i = 0; i < pr.n; ++i)
+        if (!pr.fixed[i]) hmov.push_back(i);
     } else {
       U.mov_off = -1;
     }
@@ -902,9 +911,14 @@ extern "C" pmmc_status pmmc_smooth_batch_anneal(pmmc_ctx *ctx, int n_units,
   if (trace_out && trace_cap > 0)
     PMMC_CUDA(ctx, cudaMemcpy(trace_out, d_trace.p, sizeof(MoveTrace) * trace_cap,
                               cudaMemcpyDeviceToHost));
-  // every chain's positions in one copy (one per region was a round trip each)
+  // every chain's positions in one copy (one per region was a round trip
+  // each); with one chain per region the device layout is the caller's
+  const bool direct = chains == 1;
   std::vector<float> hout;
-  if (pos_out) {
+  if (pos_out && direct) {
+    PMMC_CUDA(ctx, cudaMemcpy(pos_out, d_out.p, sizeof(float) * (size_t)out_off,
+                              cudaMemcpyDeviceToHost));
+  } else if (pos_out) {
     hout.resize((size_t)out_off);
     PMMC_CUDA(ctx, cudaMemcpy(hout.data(), d_out.p, sizeof(float) * hout.size(),
                               cudaMemcpyDeviceToHost));
@@ -923,8 +937,9 @@ extern "C" pmmc_status pmmc_smooth_batch_anneal(pmmc_ctx *ctx, int n_units,
     }
     const ChainOut &o = outs[U.chain_base + best];
     if (pos_out) {
-      std::copy_n(hout.data() + U.out_off + (long long)best * U.n * 3, (size_t)U.n * 3,
-                  pos_out + dst);
+      if (!direct)
+        std::copy_n(hout.data() + U.out_off + (long long)best * U.n * 3, (size_t)U.n * 3,
+                    pos_out + dst);
       // fixed beads are written back unchanged (ParallelMonteCarloSmooth.cu:485-491)
       const pmmc_smooth_problem &pr = units[u];
       if (pr.fixed)
