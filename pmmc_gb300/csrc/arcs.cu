@@ -1469,21 +1469,24 @@ extern "C" pmmc_status pmmc_arcs_batch_create_ex(
     return fail(ctx, PMMC_ERR_INVALID, "arcs batch: bad arguments");
   *out = nullptr;
   const int chains = opts && opts->chains_per_unit > 0 ? opts->chains_per_unit : 1;
-  // validation and packing of many regions run on several host threads
+  // validation and packing of many regions run on the context's host
+  // worker threads
   const int n_threads = n_units >= 64
       ? (int)std::max(1u, std::min(std::thread::hardware_concurrency(), 16u)) : 1;
+  if (n_threads > 1)
+    std::call_once(ctx->host_pool_once, [ctx, n_threads] {
+      ctx->host_pool = std::make_unique<pmmc::HostPool>(n_threads);
+    });
   auto parallel = [&](auto &&fn) {  // fn(first, last) over unit ranges
     if (n_threads == 1) {
       fn(0, n_units);
       return;
     }
-    std::vector<std::thread> th;
     const int per = (n_units + n_threads - 1) / n_threads;
-    for (int t = 0; t < n_threads; ++t) {
+    ctx->host_pool->run(n_threads, [&fn, per, n_units](int t) {
       const int a = t * per, z = std::min(n_units, a + per);
-      if (a < z) th.emplace_back([&fn, a, z] { fn(a, z); });
-    }
-    for (auto &x : th) x.join();
+      if (a < z) fn(a, z);
+    });
   };
   {
     std::vector<int> bad(n_threads > 1 ? n_units : 0, 0);
@@ -1527,7 +1530,8 @@ extern "C" pmmc_status pmmc_arcs_batch_create_ex(
     std::mutex mu;
     std::vector<ArcsPack> parts;
   };
-  if (!ctx->arcs_host_cache) ctx->arcs_host_cache = std::make_shared<PackCache>();
+  std::call_once(ctx->arcs_host_cache_once,
+                 [ctx] { ctx->arcs_host_cache = std::make_shared<PackCache>(); });
   PackCache &cache = *static_cast<PackCache *>(ctx->arcs_host_cache.get());
   std::lock_guard<std::mutex> pack_lock(cache.mu);
   std::vector<ArcsPack> &parts = cache.parts;

@@ -3,21 +3,98 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <condition_variable>
 #include <cstdarg>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <memory>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "pmmc_gb300.h"
 
+namespace pmmc {
+
+// Host worker threads kept for the life of a context: a call that splits
+// its host work (validating and packing many regions) hands it to the same
+// threads every time instead of starting and joining new ones, which costs
+// tens of microseconds per thread.  run(n, fn) calls fn(t) for t = 0..n-1,
+// t = 0 on the calling thread, and returns when all are done; one run at a
+// time.
+class HostPool {
+ public:
+  explicit HostPool(int size) : size_(size < 1 ? 1 : size) {
+    for (int t = 1; t < size_; ++t) th_.emplace_back([this, t] { work(t); });
+  }
+  ~HostPool() {
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      stop_ = true;
+    }
+    cv_.notify_all();
+    for (auto &t : th_) t.join();
+  }
+  HostPool(const HostPool &) = delete;
+  HostPool &operator=(const HostPool &) = delete;
+  int size() const { return size_; }
+  void run(int n, const std::function<void(int)> &fn) {
+    std::lock_guard<std::mutex> one(run_mu_);
+    n = n < 1 ? 1 : (n > size_ ? size_ : n);
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      job_ = &fn;
+      n_job_ = n;
+      pending_ = size_ - 1;
+      ++gen_;
+    }
+    cv_.notify_all();
+    fn(0);
+    std::unique_lock<std::mutex> lk(mu_);
+    done_.wait(lk, [this] { return pending_ == 0; });
+    job_ = nullptr;
+  }
+
+ private:
+  void work(int t) {
+    unsigned long long seen = 0;
+    std::unique_lock<std::mutex> lk(mu_);
+    for (;;) {
+      cv_.wait(lk, [&] { return stop_ || gen_ != seen; });
+      if (stop_) return;
+      seen = gen_;
+      const std::function<void(int)> *f = job_;
+      const int n = n_job_;
+      lk.unlock();
+      if (t < n) (*f)(t);
+      lk.lock();
+      if (--pending_ == 0) done_.notify_one();
+    }
+  }
+  const int size_;
+  std::vector<std::thread> th_;
+  std::mutex run_mu_, mu_;
+  std::condition_variable cv_, done_;
+  const std::function<void(int)> *job_ = nullptr;
+  int n_job_ = 0, pending_ = 0;
+  unsigned long long gen_ = 0;
+  bool stop_ = false;
+};
+
+}  // namespace pmmc
+
 struct pmmc_ctx {
   int device = 0;
   // host-side state a module keeps per context (e.g. packing buffers that
-  // are reused, already paged in, by the next call)
+  // are reused, already paged in, by the next call), made once
   std::shared_ptr<void> arcs_host_cache;
+  std::once_flag arcs_host_cache_once;
+  // host worker threads (made at the first call that splits its host work)
+  std::unique_ptr<pmmc::HostPool> host_pool;
+  std::once_flag host_pool_once;
   int sm_count = 0;
   size_t smem_optin = 0;       // max dynamic shared memory per block (opt-in)
   size_t smem_per_sm = 0;
