@@ -497,7 +497,8 @@ def smooth_record(args) -> dict:
     sampler.start()
     line = W.smooth(args)
     line["clocks"] = sampler.stop()
-    line["gpu_launches"] = args.steps  # one smooth_anneal_kernel launch per call
+    # the window classes' smooth_window_kernel launches, side by side
+    line["gpu_launches"] = args.steps * line.pop("kernel_launches_per_step")
     line["cpu_baseline"] = cpu
     return line
 

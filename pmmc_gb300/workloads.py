@@ -215,6 +215,14 @@ def smooth(args):
     ms = float(np.mean(times))
     wall = float(np.median(walls))
     beads = sum(x.n for x in segs)
+    # kernel launches of a call: one per non-empty class under the library's
+    # default windows (32 slots for regions with 20+ free beads, 8 for the
+    # rest; a region whose chains overflow a 200 KB slice at that window
+    # takes the one-move kernel)
+    classes = set()
+    for x in segs:
+        w = 32 if int((x.fixed == 0).sum()) >= 20 else 8
+        classes.add(w if (32 // w) * x.n * 28 <= 200 * 1024 else 0)
     # per move: two bonds and three angles read five beads (16 B each) and
     # take ~80 FLOP (the smoothing energy of a move)
     sm = _smem_roofline(total / (ms * 1e-3), 80.0, 80.0)
@@ -226,6 +234,7 @@ def smooth(args):
         "config": {"workload": f"genome_smoothing_{len(segs)}regions_{free}free_beads_"
                                f"{sweeps}sweeps", "moves_per_step": total},
         "final_energy_rel_error_max": max(r.rel_error for r in res),
+        "kernel_launches_per_step": len(classes),
         "roofline": sm,
         "e2e": {"value": total / wall, "unit": "moves/s", "ms_per_step": wall * 1e3,
                 "h2d_bytes_per_step": int(beads * (12 + 4 + 1) + len(segs) * 80),
