@@ -823,23 +823,25 @@ __device__ __forceinline__ float packed_r(float h, int m, int i, int2 b, int dia
   return read ? __frcp_rn(h) : 0.0f;
 }
 
-// The device matrix from the caller's maps (n x n, row-major, back to back
-// at raw_off[u]): rows of U.pitch floats at U.heat_off holding packed_r, the
-// padding columns zero.  The same pass checks symmetry over the pairs the
-// score reads (m < i in bead m's block, i - m >= diag): h_mi and h_im must
-// both be skipped (< 1e-6) or be equal; asym[u] keeps the lowest m * n + i
-// of a pair that is not (all ones: none).  One 256-thread block per pair of
-// 32 x 32 tiles (bm, bi), bm <= bi, of one map (tile_start[u]: the first
-// block of map u): the tile and its mirror are staged in shared memory, so
-// both are read and written along rows.
+// The device matrix from a chunk of the caller's maps (map u: n x n,
+// row-major, at raw_off[u] - raw_base of `raw`): rows of U.pitch floats at
+// U.heat_off holding packed_r, the padding columns zero.  The same pass
+// checks symmetry over the pairs the score reads (m < i in bead m's block,
+// i - m >= diag): h_mi and h_im must both be skipped (< 1e-6) or be equal;
+// asym[u] keeps the lowest m * n + i of a pair that is not (all ones: none).
+// One 256-thread block per pair of 32 x 32 tiles (bm, bi), bm <= bi, of one
+// map (map u's first block is tile_start[u] - tile_base): the tile and its
+// mirror are staged in shared memory, so both are read and written along
+// rows.
 __global__ void __launch_bounds__(256)
 heat_pack_kernel(const HeatUnit *__restrict__ units, int n_units,
-                 const long long *__restrict__ tile_start, const long long *__restrict__ raw_off,
+                 const long long *__restrict__ tile_start, long long tile_base,
+                 const long long *__restrict__ raw_off, long long raw_base,
                  const float *__restrict__ raw, const int2 *__restrict__ blk,
                  float *__restrict__ rheat, unsigned long long *__restrict__ asym) {
   __shared__ float A[kPackTile][kPackTile + 1];  // rows m0.., columns i0..
   __shared__ float B[kPackTile][kPackTile + 1];  // rows i0.., columns m0..
-  const long long t = blockIdx.x;
+  const long long t = tile_base + blockIdx.x;
   int lo = 0, hi = n_units - 1;  // the last map whose first block is <= t
   while (lo < hi) {
     const int mid = (lo + hi + 1) >> 1;
@@ -855,7 +857,7 @@ heat_pack_kernel(const HeatUnit *__restrict__ units, int n_units,
   const int2 tb = upper_tile(t - tile_start[u], nt);
   const int m0 = tb.x * kPackTile, i0 = tb.y * kPackTile;
   const bool on_diag = tb.x == tb.y;
-  const float *H = raw + raw_off[u];
+  const float *H = raw + (raw_off[u] - raw_base);
   float *R = rheat + U.heat_off;
   const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
   for (int r = ty; r < kPackTile; r += 8) {
@@ -1049,8 +1051,10 @@ extern "C" pmmc_status pmmc_heatmap_batch_anneal(pmmc_ctx *ctx, int n_units,
   // The kernels read r = 1/h, rows padded to a 16-byte pitch, with r = 0
   // wherever the reference skips the pair: h < 1e-6, |i - m| < diag, i == m,
   // and i outside bead m's chromosome block (LooperSolver.hpp:3597-3611).
-  // The caller's maps go to the device as they are and heat_pack_kernel
-  // writes that matrix.  A move changes the full score by twice its local
+  // The caller's maps go to the device as they are, in chunks of at most
+  // 256 MiB (a larger map alone) through one staging buffer, and
+  // heat_pack_kernel writes that matrix chunk by chunk (stream order keeps
+  // the next chunk's copy behind the pass that reads the buffer).  A move changes the full score by twice its local
   // change only when the map is symmetric over the pairs the score reads
   // (createDistanceHeatmap mirrors it, LooperSolver.hpp:3062); the same pass
   // finds an asymmetric map, which is refused.
@@ -1079,20 +1083,30 @@ extern "C" pmmc_status pmmc_heatmap_batch_anneal(pmmc_ctx *ctx, int n_units,
   if (e == cudaSuccess) e = d_blk.upload(hblk, s);
   if (e == cudaSuccess) e = d_tile_start.upload(tile_start, s);
   if (e == cudaSuccess) e = d_raw_off.upload(raw_off, s);
+  long long stage = 64ll << 20;  // floats (256 MiB)
+  for (int u = 0; u < n_units; ++u) stage = std::max(stage, (long long)hu[u].n * hu[u].n);
+  stage = std::min(stage, raw_floats);
   if (e == cudaSuccess) e = d_rheat.alloc((size_t)heat_floats);
-  if (e == cudaSuccess) e = d_raw.alloc((size_t)raw_floats);
-  for (int u = 0; u < n_units && e == cudaSuccess; ++u)
-    e = cudaMemcpyAsync(d_raw.p + raw_off[u], units[u].heat,
-                        sizeof(float) * (size_t)units[u].n * units[u].n,
-                        cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = d_raw.alloc((size_t)stage);
   if (e == cudaSuccess) e = d_asym.alloc((size_t)n_units);
   if (e == cudaSuccess)
     e = cudaMemsetAsync(d_asym.p, 0xff, sizeof(unsigned long long) * n_units, s);
   std::vector<unsigned long long> asym((size_t)n_units, ~0ull);
-  if (e == cudaSuccess) {
-    heat_pack_kernel<<<(unsigned)tile_start[n_units], 256, 0, s>>>(
-        d_units.p, n_units, d_tile_start.p, d_raw_off.p, d_raw.p, d_blk.p, d_rheat.p, d_asym.p);
-    e = cudaGetLastError();
+  for (int u0 = 0; u0 < n_units && e == cudaSuccess;) {
+    int u1 = u0 + 1;  // the chunk [u0, u1): whole maps within the buffer
+    while (u1 < n_units && raw_off[u1] - raw_off[u0] + (long long)hu[u1].n * hu[u1].n <= stage)
+      ++u1;
+    for (int u = u0; u < u1 && e == cudaSuccess; ++u)
+      e = cudaMemcpyAsync(d_raw.p + (raw_off[u] - raw_off[u0]), units[u].heat,
+                          sizeof(float) * (size_t)units[u].n * units[u].n,
+                          cudaMemcpyHostToDevice, s);
+    if (e == cudaSuccess) {
+      heat_pack_kernel<<<(unsigned)(tile_start[u1] - tile_start[u0]), 256, 0, s>>>(
+          d_units.p + u0, u1 - u0, d_tile_start.p + u0, tile_start[u0], d_raw_off.p + u0,
+          raw_off[u0], d_raw.p, d_blk.p, d_rheat.p, d_asym.p + u0);
+      e = cudaGetLastError();
+    }
+    u0 = u1;
   }
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(asym.data(), d_asym.p, sizeof(unsigned long long) * n_units,
