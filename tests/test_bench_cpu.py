@@ -78,3 +78,44 @@ def test_reference_arm_workloads(workload, unit):
 def test_reference_arm_other_ranks_print_nothing(workload):
     assert run_bench("--impl", "reference", "--workload", workload, "--steps", "1",
                      "--warmup", "0", rank=1) == []
+
+
+def test_smooth_line_counts_window_class_launches(monkeypatch):
+    """The genome-smoothing line claims one launch per window class it runs
+    (regions with 20+ free beads at 32 slots, the rest at 8), with the
+    library's calls replaced by fakes: the line's bookkeeping only."""
+    import argparse
+    import types
+
+    sys.path.insert(0, ROOT)
+    import bench
+    from pmmc_gb300 import capi
+
+    class FakeCtx:
+        def __init__(self, device):
+            pass
+
+        def set_seed(self, seed):
+            pass
+
+    def fake_packed(ctx, off, pos, dtn, fixed, prm, steps, *a, **k):
+        res = [types.SimpleNamespace(moves=10, rel_error=0.0) for _ in range(len(off) - 1)]
+        return pos.copy(), res, 100.0
+
+    class NoClocks:
+        def __init__(self, device):
+            pass
+
+        def start(self):
+            pass
+
+        def stop(self):
+            return {}
+
+    monkeypatch.setattr(capi, "Context", FakeCtx)
+    monkeypatch.setattr(capi, "smooth_batch_anneal_packed", fake_packed)
+    monkeypatch.setattr(bench, "smooth_cpu_baseline", lambda sweeps, budget: {"value": 1.0})
+    monkeypatch.setattr(bench, "ClockSampler", NoClocks)
+    line = bench.smooth_record(argparse.Namespace(moves=0, steps=3, warmup=1, cpu_budget=0))
+    assert line["gpu_launches"] == 2 * 3
+    assert "kernel_launches_per_step" not in line
