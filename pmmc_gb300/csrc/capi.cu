@@ -58,7 +58,7 @@ extern "C" void pmmc_ctx_destroy(pmmc_ctx *ctx) {
 }
 
 extern "C" const char *pmmc_last_error(const pmmc_ctx *ctx) {
-  return ctx ? ctx->last_error.c_str() : "";
+  return ctx ? ctx->last_error : "";
 }
 
 extern "C" void pmmc_set_seed(pmmc_ctx *ctx, uint64_t seed) {

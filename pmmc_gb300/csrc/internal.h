@@ -112,7 +112,11 @@ struct pmmc_ctx {
   // heatmap: CTAs of the cluster that runs one chain (0 = by the batch: 16
   // or 8 for a few chains on large maps, else 1)
   int heatmap_cluster = 0;
-  std::string last_error;
+  // message of the last failing call; a fixed buffer written under a lock,
+  // so failures on several host threads at once (server submits) never
+  // touch freed memory (the last byte is always the terminator)
+  char last_error[512] = {0};
+  std::mutex error_mu;
 };
 
 namespace pmmc {
@@ -149,7 +153,11 @@ inline pmmc_status fail(pmmc_ctx *ctx, pmmc_status s, const char *fmt, ...) {
     va_start(ap, fmt);
     vsnprintf(buf, sizeof(buf), fmt, ap);
     va_end(ap);
-    ctx->last_error = buf;
+    static_assert(sizeof(buf) == sizeof(ctx->last_error), "message buffer sizes");
+    const size_t len = strnlen(buf, sizeof(buf) - 1);
+    std::lock_guard<std::mutex> lk(ctx->error_mu);
+    memcpy(ctx->last_error, buf, len);
+    ctx->last_error[len] = '\0';
   }
   return s;
 }

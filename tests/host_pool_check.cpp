@@ -1,7 +1,9 @@
-// The context's host worker pool (pmmc::HostPool, pmmc_gb300/csrc/internal.h):
-// every run calls fn(t) exactly once for each t < n, on distinct threads
-// for t > 0, returns only after all have finished, and the split of a range
-// into per-thread parts covers every index once.  Built and run by
+// Host-side thread safety of a context (pmmc_gb300/csrc/internal.h).  The
+// worker pool (pmmc::HostPool): every run calls fn(t) exactly once for each
+// t < n, on distinct threads for t > 0, returns only after all have
+// finished, and the split of a range into per-thread parts covers every
+// index once.  Failure messages (pmmc::fail) recorded by many threads at
+// once leave one whole message.  Built and run by
 // tests/test_host_pool_cpu.py.
 #include <atomic>
 #include <cstdio>
@@ -49,6 +51,25 @@ int main() {
         std::printf("units %d: unit %d seen %d times\n", units, u, (int)seen[u]);
         return 1;
       }
+  }
+  // failures recorded on one context by several threads at once
+  {
+    auto *ctx = new pmmc_ctx();
+    std::vector<std::thread> th;
+    for (int t = 0; t < 8; ++t)
+      th.emplace_back([ctx, t] {
+        for (int k = 0; k < 2000; ++k)
+          pmmc::fail(ctx, PMMC_ERR_INVALID, "thread %d failure %d %s", t, k,
+                     k % 2 ? "with a longer tail to vary the length" : "");
+      });
+    for (auto &x : th) x.join();
+    int t = -1, k = -1;
+    if (std::sscanf(ctx->last_error, "thread %d failure %d", &t, &k) != 2 || t < 0 ||
+        t >= 8 || k < 0 || k >= 2000) {
+      std::printf("last message: %s\n", ctx->last_error);
+      return 1;
+    }
+    delete ctx;
   }
   std::printf("ok\n");
   return 0;
