@@ -166,7 +166,12 @@ typedef struct pmmc_ctx pmmc_ctx;
 
 /* ---------------- context ---------------- */
 /* Replaces GpuResourceCache::init / cleanup (LooperSolver.hpp:54-106,
- * ParallelMonteCarloArcs.cu:84-213): one context owns the device buffers. */
+ * ParallelMonteCarloArcs.cu:84-213): one context owns the device buffers.
+ * The calls that take a context come from one host thread at a time (they
+ * share its stream, call counter, settings and host packing buffers); the
+ * calls of a server made on it (pmmc_server_*) may come from any thread,
+ * beside them.  pmmc_last_error then holds the message of whichever failing
+ * call came last. */
 pmmc_status pmmc_ctx_create(pmmc_ctx **out, int device);
 void pmmc_ctx_destroy(pmmc_ctx *ctx);
 const char *pmmc_status_string(pmmc_status s);
